@@ -1,0 +1,370 @@
+"""Benchmark: converged 1D Kohn-Sham SCF solves per second on GB300.
+
+Workload (the batched configuration): 4096 seeded synthetic molecules, grids
+of 257/385/513 points at 0.08 bohr, 1-4 nuclei of charge 1-3 in [-3, 3] bohr,
+neutral; FP32 window-17 MLP exchange-correlation (17->16->16->1, SiLU,
+Glorot-uniform from seed 0, local convention); FP64 SCF with the five-point
+kinetic operator; 25 iterations, linear mixing alpha=0.5 decaying by 0.9,
+one mixing difference; non-interacting start computed inside the solve.
+
+A step is one batched solve of the whole batch (one kernel launch).  A solve
+counts as converged when |E_25 - E_24| < 1e-8 Ha and its status flags are
+clear.  ``value`` times the solve with inputs resident on the device; ``e2e``
+times the public API with host inputs (descriptor upload and energy/density
+download inside the timed region).  ``--impl reference`` times the
+reference algorithm (NumPy FP64 restatement: dense eigh, materialised
+Hartree kernel) on the host cores on a bounded sample.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "converged SCF solves/sec at 1e-8 Ha (batched 1D, 4096 molecules)"
+UNIT = "solves/s"
+E_CONV = 1e-8
+FP64_PEAK_TFLOPS = 1.18  # measured FP64 FMA throughput on this GB300 pool (profiles/fp64_peak.txt)
+
+
+def workload(batch_size, seed):
+    from qex_gb300.od import workloads
+
+    return workloads.batched_molecules(batch_size, seed=seed)
+
+
+def mlp_params(seed=0):
+    from qex_gb300 import networks
+
+    init_fn, xc_fn = networks.build_xc_functional(networks.WindowMLP().build_network(None),
+                                                  np.zeros(5))
+    return init_fn(seed), xc_fn
+
+
+# ---------------------------------------------------------------------------
+# CPU reference arm: the oracle (reference algorithm) on host cores
+# ---------------------------------------------------------------------------
+
+def _cpu_solve(args):
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    from oracle import ks1d as o
+
+    (n, r, z, ne, params, iters) = args
+    g = (np.arange(n) - (n - 1) / 2) * 0.08
+    xc = o.WindowMLP(params, dtype=np.float32)
+    ve = o.get_atomic_chain_potential(g, r, z, o.exponential_coulomb)
+    n0, _, _ = o.solve_noninteracting_system(ve, ne, g, 5, "dense")
+    res = o.kohn_sham(r, z, ne, iters, g, xc, o.exponential_coulomb, n0, alpha=0.5,
+                      alpha_decay=0.9, num_mixing_iterations=1, convention="local", stencil=5,
+                      method="dense")
+    e = res["total_energy"]
+    return bool(abs(e[-1] - e[-2]) < E_CONV)
+
+
+def cpu_sample(mols, params, iters, sample, cores):
+    jobs = [(m.num_grids, m.locations, m.nuclear_charges, m.num_electrons, params, iters)
+            for m in mols[:sample]]
+    ctx = mp.get_context("spawn")
+    env_old = os.environ.get("OPENBLAS_NUM_THREADS")
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    os.environ["OMP_NUM_THREADS"] = "1"
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        conv = pool.map(_cpu_solve, jobs, chunksize=1)
+    dt = time.perf_counter() - t0
+    if env_old is not None:
+        os.environ["OPENBLAS_NUM_THREADS"] = env_old
+    return dt, sum(conv), len(jobs)
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if s[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------
+# roofline tally
+# ---------------------------------------------------------------------------
+
+def fp64_flops(mols, iterations_run, stats):
+    """FP64 flops executed, tallied per code path of the kernel."""
+    total = 0.0
+    for m, it, st in zip(mols, iterations_run, stats):
+        n = m.num_grids
+        nocc = (m.num_electrons + 1) // 2
+        k = m.num_electrons // 2 + 1
+        solves, rq_vec, upd, _ = (int(x) for x in st)
+        # per SCF iteration: two Hartree scans (15 N each), v_KS assembly (5 N),
+        # energies (4 N), mixing (10 N), density (4 N nocc), XC energy sums (4 N)
+        per_iter = (30 + 5 + 4 + 10 + 4) * n + 4 * n * nocc
+        # per eigen-solve: diagonal (1 N), FP64 conversion + final normalisation (7 N k)
+        per_solve = n + 7 * n * k
+        total += float(it) * per_iter + solves * per_solve + 16.0 * n * rq_vec + 1.0 * n * upd
+    return total
+
+
+def fp32_flops_mlp(mols, iterations_run):
+    # window-17 MLP: forward 2*(17*16+16*16+16) flops, backward ~ the same again
+    fwd = 2 * (17 * 16 + 16 * 16 + 16)
+    return float(sum(float(it) * m.num_grids * (3 * fwd) for m, it in zip(mols, iterations_run)))
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+
+def run_ours(args, rank, world):
+    import torch
+
+    from qex_gb300 import _native
+    from qex_gb300.od import engine as eng
+    from qex_gb300.xc import Partial
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    _native.load()
+    mols = workload(args.batch, args.seed + rank)
+    params, xc_fn = mlp_params(0)
+    xc = Partial(xc_fn, params=params)
+    cfg = eng.SolveConfig(num_iterations=args.iters, alpha=0.5, alpha_decay=0.9,
+                          num_mixing_iterations=1, convention="local", stencil=5)
+    engine = eng.Ks1dEngine()
+    batch = eng.PackedBatch(mols)
+    records = ("energy", "gap", "converged", "final_density")
+    out = engine.allocate_outputs(batch, cfg, records)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        engine.solve(batch, xc, cfg, out=out)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    sampler.start()
+    times = []
+    launches = 0
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush.fill_(1)  # evict L2 between timed solves (outside the events)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        engine.solve(batch, xc, cfg, out=out)
+        e1.record(stream)
+        launches += engine.last_launches
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    torch.cuda.synchronize()
+    sampler.stop()
+    step_s = sum(times) / len(times)
+    energy = out["energy"].cpu().numpy()
+    status = out["status"].cpu().numpy()
+    iters_run = out["iterations_run"].cpu().numpy()
+    stats = out["stats"].cpu().numpy()
+    conv = (np.abs(energy[:, -1] - energy[:, -2]) < E_CONV) & ((status & 0xFFFF) == 0)
+    n_conv = int(conv.sum())
+
+    # ---- end-to-end through the public API with host inputs
+    host = {k: getattr(batch, k).cpu().pin_memory() for k in
+            ("num_grids", "offsets", "grid_start", "grid_spacing", "num_electrons",
+             "num_nuclei", "locations", "nuclear_charges", "order")}
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    res_host = {k: torch.empty(out[k].shape, dtype=out[k].dtype).pin_memory()
+                for k in ("energy", "final_density", "status")}
+    d2h = sum(t.numel() * t.element_size() for t in res_host.values())
+    e2e_times = []
+    for _ in range(max(2, args.steps)):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k, t in host.items():
+            getattr(batch, k).copy_(t, non_blocking=True)
+        engine.solve(batch, xc, cfg, out=out)
+        for k, t in res_host.items():
+            t.copy_(out[k], non_blocking=True)
+        stream.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_times) / len(e2e_times)
+
+    # max over ranks
+    t_step = torch.tensor([step_s, e2e_s], dtype=torch.float64, device="cuda")
+    c = torch.tensor([n_conv, args.batch], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t_step, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(c, op=torch.distributed.ReduceOp.SUM)
+    step_s, e2e_s = float(t_step[0]), float(t_step[1])
+    total_conv, total = float(c[0]), float(c[1])
+    if rank != 0:
+        return None
+
+    w64 = fp64_flops(mols, iters_run, stats)
+    w32 = fp32_flops_mlp(mols, iters_run)
+    achieved = w64 / step_s / 1e12
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        cores = host_cores()
+        sample = min(args.cpu_sample, len(mols))
+        dt, cconv, cn = cpu_sample(mols, params, args.iters, sample, cores)
+        cpu = {"value": cconv / dt, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{cn} molecules of the same workload, reference algorithm (dense "
+                         f"eigh, materialised Hartree kernel), {cconv} converged, {dt:.1f} s wall",
+               "total_solves_per_s": cn / dt}
+    line = {
+        "metric": METRIC, "value": total_conv / step_s, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded molecules, Glorot-init MLP from seed 0)",
+        "config": {"workload": f"batched 1D KS-SCF, {args.batch} molecules x {world} ranks, "
+                               f"N in {{257,385,513}}, 1-4 nuclei Z 1-3, window-17 FP32 MLP XC, "
+                               f"5-point kinetic, {args.iters} iterations",
+                   "global_batch": int(total), "l2": "flushed between timed steps (512 MB write)",
+                   "parallelism": f"replicas x{world}"},
+        "total_solves_per_s": total / step_s,
+        "converged_fraction": total_conv / total,
+        "e2e": {"value": total_conv / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
+                     "unit": "TFLOP/s", "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
+                     "peak_source": "measured FP64 FMA probe on this pool (profiles)",
+                     "fp64_flops_per_step": w64, "fp32_mlp_flops_per_step": w32},
+        "clocks": sampler.summary(),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    return line
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    mols = workload(args.batch, args.seed)
+    params, _ = mlp_params(0)
+    cores = host_cores()
+    sample = min(args.cpu_sample, len(mols))
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_sample(mols, params, args.iters, min(cores, sample), cores)
+    times, convs = [], []
+    for s in range(args.steps):
+        dt, cconv, cn = cpu_sample(mols[s * 7 % max(1, len(mols) - sample):], params, args.iters,
+                                   sample, cores)
+        times.append(dt)
+        convs.append(cconv)
+    step_s = sum(times) / len(times)
+    value = (sum(convs) / len(convs)) / step_s
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+        "data": "synthetic (seeded molecules, Glorot-init MLP from seed 0)",
+        "config": {"workload": f"batched 1D KS-SCF sample of {sample} molecules per step "
+                               f"(same generator as the GPU arm), {args.iters} iterations",
+                   "parallelism": f"{cores} host processes"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{sample} molecules per step, reference algorithm restated "
+                                   f"in NumPy FP64 (dense eigh)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--iters", type=int, default=25)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-sample", type=int, default=64)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "ours" and world > 1:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        torch.distributed.init_process_group("nccl")
+    line = run_ours(args, rank, world) if args.impl == "ours" else run_reference(args, rank, world)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    if args.impl == "ours" and world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,165 @@
+/*
+ * qex_ks1d.h -- C ABI of the GB300 1D Kohn-Sham SCF path.
+ *
+ * Every entry point works on caller-owned DEVICE buffers (row-major, batch
+ * first, float64 unless stated), takes the CUDA stream as an opaque pointer,
+ * allocates nothing and returns an int status (QEX_OK on success).  Molecules
+ * of different grid sizes are packed one after another: molecule b's grid
+ * vectors start at element grid_offsets[b] of every packed array and hold
+ * num_grids[b] values.  Per-iteration records of molecule b start at element
+ * num_iterations * grid_offsets[b] and are (num_iterations, num_grids[b]).
+ *
+ * Reference interfaces replaced (qedft, pasqal-io/qex):
+ *   qex_ks1d_solve      <- qedft/train/od/jit_scf.py:247-330
+ *                          (kohn_sham_amplitude_encoded, lax.scan form),
+ *                          qedft/train/od/scf.py:434-560 (Python-loop form),
+ *                          jax_dft jit_scf.kohn_sham as selected at
+ *                          qedft/train/od/train.py:117-121, and the
+ *                          jax.vmap batch of qedft/train/od/train.py:125.
+ *   qex_ks1d_iteration  <- qedft/train/od/jit_scf.py:89-140
+ *                          (kohn_sham_iteration_amplitude_encoded) and
+ *                          qedft/train/od/scf.py:79-177.
+ *   qex_ks1d_noninteracting <- solve_noninteracting_system as called at
+ *                          qedft/train/od/scf.py:233-250,499-504.
+ */
+#ifndef QEX_KS1D_H_
+#define QEX_KS1D_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes (returned, and per molecule in `status`). */
+#define QEX_OK 0
+#define QEX_BAD_ARG 1
+#define QEX_NOT_CONVERGED 2
+#define QEX_NUMERICAL 3
+#define QEX_OOM 4
+#define QEX_TIMEOUT 5
+#define QEX_CUDA_ERROR 6
+
+/* Per-molecule status flags OR-ed into `status` (bit 8 and up). */
+#define QEX_FLAG_DEGENERATE_FRONTIER 0x100 /* HOMO/LUMO closer than the FP32 resolution */
+#define QEX_FLAG_REFINE_CAP 0x200          /* eigenpair refinement hit its step cap */
+
+#define QEX_KS1D_MAX_EIGENPAIRS 16 /* floor(Ne/2)+1 <= 16, i.e. Ne <= 30 */
+#define QEX_MLP_WINDOW 17
+#define QEX_MLP_HIDDEN 16
+/* W1 (17x16), b1 (16), W2 (16x16), b2 (16), W3 (16), b3 (1), as x@W+b. */
+#define QEX_MLP_NUM_PARAMS (17 * 16 + 16 + 16 * 16 + 16 + 16 + 1)
+
+enum qex_interaction_kind {
+  QEX_INTERACTION_EXPONENTIAL = 0, /* a * exp(-b |d|), jax_dft exponential_coulomb */
+  QEX_INTERACTION_SOFT_COULOMB = 1 /* 1 / sqrt(d^2 + a), jax_dft soft_coulomb */
+};
+
+enum qex_xc_kind {
+  QEX_XC_NONE = 0,
+  QEX_XC_LDA_EXP_COULOMB = 1, /* exponential-Coulomb uniform-gas LDA */
+  QEX_XC_POWER = 2,           /* f(n) = coefficient * (n + shift)^power */
+  QEX_XC_WINDOW_MLP = 3       /* FP32 window-17 MLP, two SiLU layers of 16 */
+};
+
+enum qex_xc_convention {
+  QEX_XC_AMPLITUDE = 0, /* qedft: E = dx sum f, v = dE/dn (scf.py:32-76) */
+  QEX_XC_LOCAL = 1      /* jax_dft: E = dx sum f n, v = (dE/dn)/dx */
+};
+
+typedef struct qex_xc_spec {
+  int32_t kind;       /* enum qex_xc_kind */
+  int32_t convention; /* enum qex_xc_convention */
+  double coefficient, power, shift; /* QEX_XC_POWER */
+  double lda_amplitude, lda_kappa;  /* QEX_XC_LDA_EXP_COULOMB */
+  double normalization;             /* QEX_XC_WINDOW_MLP input divisor */
+  const float* mlp_params_host;     /* HOST pointer, QEX_MLP_NUM_PARAMS floats */
+} qex_xc_spec;
+
+typedef struct qex_ks1d_options {
+  int32_t stencil;     /* 3 or 5 point kinetic operator */
+  int32_t interaction; /* enum qex_interaction_kind */
+  double interaction_a, interaction_b;
+  int32_t num_iterations;
+  double alpha, alpha_decay;
+  int32_t num_mixing_iterations;
+  double density_mse_converge_tolerance;
+  int32_t convergence_rule;            /* 0: jit scan rule, 1: Python-loop rule */
+  int32_t enforce_reflection_symmetry; /* flip-average about the grid centre */
+  int32_t external_potential_given;    /* 1: read external_potential instead of nuclei */
+  int32_t max_num_grids;               /* upper bound on num_grids[b] */
+  int32_t max_num_electrons;           /* upper bound on num_electrons[b] */
+  int32_t max_nuclei;                  /* row stride of locations / nuclear_charges */
+} qex_ks1d_options;
+
+/* Molecule descriptors: all device arrays of length num_molecules (nuclei:
+ * num_molecules * max_nuclei).  The grid of molecule b is
+ * grid_start[b] + i * grid_spacing[b], i < num_grids[b]. */
+typedef struct qex_ks1d_batch {
+  int32_t num_molecules;
+  const int32_t* num_grids;
+  const int64_t* grid_offsets;
+  const double* grid_start;
+  const double* grid_spacing;
+  const int32_t* num_electrons;
+  const int32_t* num_nuclei;
+  const double* locations;
+  const double* nuclear_charges;
+  const double* external_potential; /* packed, used if external_potential_given */
+  const double* initial_density;    /* packed, or NULL: non-interacting start */
+  const int32_t* order;             /* processing order (a permutation), or NULL */
+} qex_ks1d_batch;
+
+/* Outputs; any pointer may be NULL to skip that record. */
+typedef struct qex_ks1d_outputs {
+  double* total_energy;      /* (B, iters) */
+  double* gap;               /* (B, iters) */
+  uint8_t* converged;        /* (B, iters) */
+  double* density;           /* per-iteration records (mixed density) */
+  double* hartree_potential; /* per-iteration records */
+  double* xc_potential;      /* per-iteration records */
+  double* xc_energy_density; /* per-iteration records: per-point f (or eps) */
+  double* final_density;     /* packed (sum N) */
+  double* external_potential_out; /* packed (sum N) */
+  int32_t* status;           /* (B) */
+  int32_t* iterations_run;   /* (B) iterations that did work (not skipped as converged) */
+  int32_t* stats;            /* (B, 4): eigen-solves, Rayleigh-quotient vector passes,
+                                correction updates, Sturm multisection passes */
+} qex_ks1d_outputs;
+
+/* Bytes of device workspace qex_ks1d_solve needs for this batch shape. */
+int qex_ks1d_workspace_size(const qex_ks1d_options* options, int32_t num_molecules,
+                            size_t* bytes);
+
+/* Full SCF for a batch of molecules in one launch (one warp per molecule,
+ * persistent CTAs, all iterations inside the kernel). */
+int qex_ks1d_solve(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
+                   const qex_xc_spec* xc, const qex_ks1d_outputs* outputs,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
+/* One Kohn-Sham iteration per molecule: input density (packed) and external
+ * potential (packed) -> unmixed output density, energy, v_H, v_xc, f, gap.
+ * Records are single-iteration (iters = 1). */
+int qex_ks1d_iteration(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
+                       const qex_xc_spec* xc, const double* density_in,
+                       const qex_ks1d_outputs* outputs, void* workspace,
+                       size_t workspace_bytes, void* stream);
+
+/* Non-interacting ground state of T + diag(v) for each molecule:
+ * density (packed), total eigen-energy (B) and gap (B). */
+int qex_ks1d_noninteracting(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
+                            const double* potential, double* density,
+                            double* total_eigen_energy, double* gap, int32_t* status,
+                            void* workspace, size_t workspace_bytes, void* stream);
+
+/* Library version string and the number of kernel launches the last call on
+ * this host thread issued (for launch accounting in benchmarks). */
+const char* qex_version(void);
+int qex_last_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QEX_KS1D_H_ */

@@ -1,0 +1,1450 @@
+// GB300 (sm_103a) 1D Kohn-Sham SCF: one warp per molecule, persistent CTAs,
+// every SCF iteration inside one kernel launch.
+//
+// Reference path (qedft, pasqal-io/qex): qedft/train/od/jit_scf.py:14-244 and
+// qedft/train/od/scf.py:32-560 together with the jax_dft primitives they call
+// (kinetic matrix, Hartree convolution, dense eigh, density, energies, linear
+// mixing).  The arithmetic per iteration follows qedft/train/od/jit_scf.py:26-77:
+//   v_H = Hartree(n); v_xc = XC'(n); v_KS = v_H + v_xc + v_ext;
+//   (n_out, sum eps, gap) = lowest eigenpairs of T + diag(v_KS);
+//   E = sum eps - <v_KS, n_out> + E_H[n_out] + E_xc[n_out] + <v_ext, n_out>;
+// then the mixing / convergence rules of jit_scf.py:177-208 (or scf.py:535-558).
+//
+// GB300 design (FP64 runs at 1/59 of FP32 on this part):
+//  * The dense O(N^3) eigh is replaced by a banded selected-eigenpair solver:
+//    FP32 Sturm-count multisection (32 lanes x 2 shifts per pass) brackets the
+//    lowest eigenvalues, FP32 shifted inverse iteration gives the vectors, and
+//    FP64 Newton refinement (FP64 residual, FP32 LDL^T correction solve) brings
+//    each eigenpair to FP64 accuracy with only point-parallel FP64 work and no
+//    FP64 division.  Near-degenerate clusters get an FP64 Rayleigh-Ritz.
+//  * The exponential Hartree kernel is separable: sum_j n_j r^|i-j| is two
+//    linear recurrences, computed as a chunked warp scan in O(N) FP64.
+//  * The window-MLP exchange-correlation network runs in FP32 with its weights
+//    in the kernel's constant parameter bank (broadcast operands).
+#include <cuda_runtime.h>
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "ks1d_common.cuh"
+#include "xc_device.cuh"
+#include "qex_ks1d.h"
+
+namespace qex {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Launch parameters (passed by value; lives in the constant parameter bank)
+// ---------------------------------------------------------------------------
+enum Mode { kModeScf = 0, kModeIteration = 1, kModeNonInteracting = 2 };
+
+struct Params {
+  int mode;
+  int num_molecules;
+  const int32_t* order;
+  const int32_t* num_grids;
+  const int64_t* grid_offsets;
+  const double* grid_start;
+  const double* grid_spacing;
+  const int32_t* num_electrons;
+  const int32_t* num_nuclei;
+  const double* locations;
+  const double* charges;
+  const double* vext_in;
+  const double* dens_in;
+  int max_nuclei;
+  int stencil;
+  int interaction;
+  double ia, ib;
+  int iters;
+  double alpha, alpha_decay;
+  int mixing;
+  double tol;
+  int rule;
+  int reflect;
+  int vext_given;
+  int nmax;
+  int kmax;
+  int mix_slots;
+  int xc_kind, xc_conv;
+  double xc_a, xc_p, xc_shift, lda_A, lda_kappa;
+  // outputs
+  double* o_energy;
+  double* o_gap;
+  uint8_t* o_conv;
+  double* o_dens;
+  double* o_vh;
+  double* o_vxc;
+  double* o_f;
+  double* o_final;
+  double* o_vext;
+  int32_t* o_status;
+  int32_t* o_iters;
+  int32_t* o_stats;
+  double* o_tee;
+  // workspace
+  double* ws;
+  long long stride;  // doubles per molecule
+  int* counter;
+  MlpParams mlp;
+};
+
+// Workspace vectors (each nmax doubles) per molecule.
+enum Vec { VN = 0, VEXT, VKS, VNOUT, VH, VXC, VF, VKT, VDIFF };
+__host__ __device__ inline long long vec_count(int mix_slots, int kmax) {
+  return VDIFF + mix_slots + kmax;
+}
+
+// Shared-memory layout of one warp (one molecule in flight).
+struct SmemLayout {
+  int nstr;        // FP32 per-eigenpair stride (nmax rounded to 32k+1)
+  size_t s64a, s64b, f32, small, total;
+};
+__host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax) {
+  SmemLayout L;
+  L.nstr = ((nmax + 31) / 32) * 32 + 1;
+  size_t off = 0;
+  L.s64a = off;
+  off += sizeof(double) * (nmax + 2 * kPad64);
+  L.s64b = off;
+  off += sizeof(double) * (nmax + 2 * kPad64);
+  L.f32 = off;
+  size_t xc_floats = 2 * (size_t)(nmax + 2 * kPadMlp);
+  size_t hart_floats = 2 * (size_t)nmax + 2;  // one FP64 scan vector
+  size_t eig_floats = (1 + 3 * (size_t)kmax) * L.nstr;
+  size_t f = xc_floats > eig_floats ? xc_floats : eig_floats;
+  if (hart_floats > f) f = hart_floats;
+  off += sizeof(float) * f;
+  off = (off + 15) & ~(size_t)15;
+  L.small = off;
+  // lo, hi (float x kMaxBis), sig (float x kSamples), cnt (int x kSamples),
+  // theta, resn, eigprev (double x kMaxBis), clus (int x kMaxBis), red (double x 32)
+  off += sizeof(float) * kMaxBis * 2 + sizeof(float) * kSamples + sizeof(int) * kSamples;
+  off = (off + 7) & ~(size_t)7;
+  off += sizeof(double) * kMaxBis * 3 + sizeof(int) * kMaxBis + sizeof(double) * 32;
+  L.total = (off + 127) & ~(size_t)127;
+  return L;
+}
+
+struct Smem {
+  double* s64a;  // padded FP64 staging (index kPad64 + i)
+  double* s64b;
+  float* f32;
+  float* lo;
+  float* hi;
+  float* sig;
+  int* cnt;
+  double* theta;
+  double* resn;
+  double* eigprev;
+  int* clus;
+  double* red;
+  int nstr;
+};
+
+__device__ inline Smem carve(unsigned char* base, const SmemLayout& L) {
+  Smem s;
+  s.s64a = reinterpret_cast<double*>(base + L.s64a);
+  s.s64b = reinterpret_cast<double*>(base + L.s64b);
+  s.f32 = reinterpret_cast<float*>(base + L.f32);
+  unsigned char* p = base + L.small;
+  s.lo = reinterpret_cast<float*>(p);
+  p += sizeof(float) * kMaxBis;
+  s.hi = reinterpret_cast<float*>(p);
+  p += sizeof(float) * kMaxBis;
+  s.sig = reinterpret_cast<float*>(p);
+  p += sizeof(float) * kSamples;
+  s.cnt = reinterpret_cast<int*>(p);
+  p += sizeof(int) * kSamples;
+  p = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 7) & ~(uintptr_t)7);
+  s.theta = reinterpret_cast<double*>(p);
+  p += sizeof(double) * kMaxBis;
+  s.resn = reinterpret_cast<double*>(p);
+  p += sizeof(double) * kMaxBis;
+  s.eigprev = reinterpret_cast<double*>(p);
+  p += sizeof(double) * kMaxBis;
+  s.clus = reinterpret_cast<int*>(p);
+  p += sizeof(int) * kMaxBis;
+  p = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 7) & ~(uintptr_t)7);
+  s.red = reinterpret_cast<double*>(p);
+  s.nstr = L.nstr;
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Small helpers
+// ---------------------------------------------------------------------------
+struct Stencil {
+  double c0, b1, b2;  // diagonal offset, first and second off-diagonal of T
+};
+__device__ inline Stencil make_stencil(int stencil, double dx) {
+  // T = -1/2 L / dx^2; five-point L = (-1/12, 4/3, -5/2, 4/3, -1/12)
+  // (jax_dft discrete_laplacian, used at qedft/train/od/scf.py:185-195).
+  double inv = 1.0 / (dx * dx);
+  Stencil s;
+  if (stencil == 5) {
+    s.c0 = 1.25 * inv;
+    s.b1 = -(2.0 / 3.0) * inv;
+    s.b2 = (1.0 / 24.0) * inv;
+  } else {
+    s.c0 = inv;
+    s.b1 = -0.5 * inv;
+    s.b2 = 0.0;
+  }
+  return s;
+}
+
+__device__ inline double interaction_fn(const Params& p, double d) {
+  if (p.interaction == QEX_INTERACTION_EXPONENTIAL) return p.ia * exp(-p.ib * fabs(d));
+  return 1.0 / sqrt(d * d + p.ia);
+}
+
+// Stage a global FP64 vector into a padded shared buffer (zeros outside [0,N)).
+__device__ inline void stage64(double* s, const double* g, int N, int lane) {
+  for (int i = lane; i < N + 2 * kPad64; i += kWarp) {
+    int k = i - kPad64;
+    s[i] = (k >= 0 && k < N) ? g[k] : 0.0;
+  }
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// Hartree: out_i = dx * sum_j n_j K(x_i - x_j)       (qedft/train/od/scf.py:303-308)
+// n is staged in sm.s64a (padded).  Returns sum_i n_i * out_i (warp-uniform).
+// ---------------------------------------------------------------------------
+__device__ double hartree(const Params& p, int N, double dx, const Smem& sm, double* out,
+                          const double* kt, int lane) {
+  const double* n = sm.s64a + kPad64;
+  double acc_e = 0.0;
+  if (p.interaction == QEX_INTERACTION_EXPONENTIAL) {
+    // sum_j n_j rho^|i-j| = F_i + B_i - n_i with F_i = n_i + rho F_{i-1},
+    // B_i = n_i + rho B_{i+1}: chunked affine scans across the warp.
+    const double rho = exp(-p.ib * dx);
+    double* fwd = reinterpret_cast<double*>(sm.f32);
+    const int C = (N + kWarp - 1) / kWarp;
+    const int beg = min(lane * C, N);
+    const int end = min(beg + C, N);
+    double s = 0.0, f = 1.0;
+    for (int i = beg; i < end; ++i) {
+      s = fma(s, rho, n[i]);
+      f *= rho;
+    }
+#pragma unroll
+    for (int d = 1; d < kWarp; d <<= 1) {
+      double s2 = __shfl_up_sync(kFull, s, d);
+      double f2 = __shfl_up_sync(kFull, f, d);
+      if (lane >= d) {
+        s = fma(s2, f, s);
+        f *= f2;
+      }
+    }
+    double x = __shfl_up_sync(kFull, s, 1);
+    if (lane == 0) x = 0.0;
+    for (int i = beg; i < end; ++i) {
+      x = fma(x, rho, n[i]);
+      fwd[i] = x;
+    }
+    s = 0.0;
+    f = 1.0;
+    for (int i = end - 1; i >= beg; --i) {
+      s = fma(s, rho, n[i]);
+      f *= rho;
+    }
+#pragma unroll
+    for (int d = 1; d < kWarp; d <<= 1) {
+      double s2 = __shfl_down_sync(kFull, s, d);
+      double f2 = __shfl_down_sync(kFull, f, d);
+      if (lane + d < kWarp) {
+        s = fma(s2, f, s);
+        f *= f2;
+      }
+    }
+    double y = __shfl_down_sync(kFull, s, 1);
+    if (lane == kWarp - 1) y = 0.0;
+    const double scale = p.ia * dx;
+    for (int i = end - 1; i >= beg; --i) {
+      y = fma(y, rho, n[i]);
+      double v = scale * (fwd[i] + y - n[i]);
+      out[i] = v;
+      acc_e = fma(n[i], v, acc_e);
+    }
+    __syncwarp();
+  } else {
+    // General (soft-Coulomb) kernel: direct Toeplitz sum with the kernel row
+    // kt[d] = K(d dx) tabulated once per molecule.
+    for (int i = lane; i < N; i += kWarp) {
+      double v = 0.0;
+      for (int j = 0; j < N; ++j) v = fma(n[j], kt[abs(i - j)], v);
+      v *= dx;
+      out[i] = v;
+      acc_e = fma(n[i], v, acc_e);
+    }
+    __syncwarp();
+  }
+  return warp_sum(acc_e);
+}
+
+// ---------------------------------------------------------------------------
+// Exchange-correlation
+// ---------------------------------------------------------------------------
+// Flip-average v about the grid centre in place (jax_dft
+// jit_scf._flip_and_average_on_center, qedft/train/od/jit_scf.py:76-77).
+__device__ inline void flip_avg_global(double* v, int N, int lane) {
+  for (int i = lane; i < N / 2; i += kWarp) {
+    double a = v[i], b = v[N - 1 - i];
+    double m = 0.5 * (a + b);
+    v[i] = m;
+    v[N - 1 - i] = m;
+  }
+  __syncwarp();
+}
+
+// Evaluate the XC functional on the density staged in sm.s64a.
+//   want_v: write v_xc to vout (FP64 global);  frec: per-point f record or null.
+// Returns E_xc (already multiplied by dx).  With reflect_xc the functional is
+// symmetrised (local convention, jax_dft kohn_sham_iteration): the staged
+// density must already be flip-averaged; outputs are flip-averaged here.
+__device__ double xc_eval(const Params& p, int N, double dx, const Smem& sm, bool want_v,
+                          double* vout, double* frec, bool reflect_xc, int lane) {
+  const double* n = sm.s64a + kPad64;
+  const bool local = (p.xc_conv == QEX_XC_LOCAL);
+  double e = 0.0;
+  if (p.xc_kind == QEX_XC_NONE) {
+    for (int i = lane; i < N; i += kWarp) {
+      if (want_v) vout[i] = 0.0;
+      if (frec) frec[i] = 0.0;
+    }
+    __syncwarp();
+    return 0.0;
+  }
+  if (p.xc_kind == QEX_XC_LDA_EXP_COULOMB || p.xc_kind == QEX_XC_POWER) {
+    for (int i = lane; i < N; i += kWarp) {
+      double ni = n[i], f, df;
+      if (p.xc_kind == QEX_XC_LDA_EXP_COULOMB) {
+        lda_exp_coulomb(ni, p.lda_A, p.lda_kappa, f, df);
+      } else {
+        double base = ni + p.xc_shift;
+        f = p.xc_a * pow(base, p.xc_p);
+        df = p.xc_a * p.xc_p * pow(base, p.xc_p - 1.0);
+      }
+      if (local) {
+        e = fma(f, ni, e);
+        if (want_v) vout[i] = fma(ni, df, f);
+      } else {
+        e += f;
+        if (want_v) vout[i] = dx * df;
+      }
+      if (frec) frec[i] = f;
+    }
+  } else {
+    // Window MLP: stage n / norm as FP32 with 8 zeros either side; v_xc
+    // contributions are accumulated in FP32 shared memory, one window offset
+    // at a time (distinct addresses per lane, so no atomics are needed).
+    float* n32 = sm.f32;
+    float* vacc = sm.f32 + (p.nmax + 2 * kPadMlp);
+    const float ninv = p.mlp.norm_inv;
+    for (int i = lane; i < N + 2 * kPadMlp; i += kWarp) {
+      int k = i - kPadMlp;
+      n32[i] = (k >= 0 && k < N) ? (float)n[k] * ninv : 0.0f;
+      vacc[i] = 0.0f;
+    }
+    __syncwarp();
+    const int rounds = (N + kWarp - 1) / kWarp;
+    for (int r = 0; r < rounds; ++r) {
+      const int i = r * kWarp + lane;
+      const bool act = i < N;
+      float w[QEX_MLP_WINDOW], gw[QEX_MLP_WINDOW];
+#pragma unroll
+      for (int k = 0; k < QEX_MLP_WINDOW; ++k) w[k] = act ? n32[i + k] : 0.0f;
+      float f;
+      if (want_v) {
+        f = mlp_point<true>(p.mlp, w, gw);
+      } else {
+        f = mlp_point<false>(p.mlp, w, gw);
+      }
+      double ni = act ? n[i] : 0.0;
+      if (act) {
+        if (local) {
+          e = fma((double)f, ni, e);
+        } else {
+          e += (double)f;
+        }
+        if (frec) frec[i] = (double)f;
+      }
+      if (want_v) {
+        const float up = local ? (float)ni * ninv : ninv;
+#pragma unroll
+        for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
+          if (act) vacc[i + k] += up * gw[k];
+          __syncwarp();
+        }
+        if (act && local) vacc[i + kPadMlp] += f;
+        __syncwarp();
+      }
+    }
+    if (want_v) {
+      for (int i = lane; i < N; i += kWarp) {
+        double v = (double)vacc[i + kPadMlp];
+        vout[i] = local ? v : dx * v;
+      }
+    }
+  }
+  __syncwarp();
+  if (reflect_xc) {
+    if (want_v) flip_avg_global(vout, N, lane);
+    if (frec) flip_avg_global(frec, N, lane);
+  }
+  return warp_sum(e) * dx;
+}
+
+// ---------------------------------------------------------------------------
+// Banded selected-eigenpair solver
+// ---------------------------------------------------------------------------
+__device__ inline float pseudo_random(int i, int j) {
+  unsigned h = (unsigned)i * 2654435761u ^ ((unsigned)j * 40503u + 0x9e3779b9u);
+  h ^= h >> 15;
+  h *= 2246822519u;
+  h ^= h >> 13;
+  return 0.1f + (float)(h & 0xffffu) * (1.0f / 65536.0f) - 0.5f;
+}
+
+// FP32 Sturm counts (inertia of L D L^T of H - sigma) for kShiftsPerLane shifts.
+template <int kBand>
+__device__ inline void sturm_counts(const float* a32, int N, float b1, float b2, float pivmin,
+                                    const float* sig, int* cnt) {
+  float r1[kShiftsPerLane], r2[kShiftsPerLane], u1[kShiftsPerLane];
+  int c[kShiftsPerLane];
+#pragma unroll
+  for (int s = 0; s < kShiftsPerLane; ++s) {
+    r1[s] = 0.0f;
+    r2[s] = 0.0f;
+    u1[s] = 0.0f;
+    c[s] = 0;
+  }
+  const float b2sq = b2 * b2;
+  for (int i = 0; i < N; ++i) {
+    const float a = a32[i];
+#pragma unroll
+    for (int s = 0; s < kShiftsPerLane; ++s) {
+      float d;
+      if (kBand == 2) {
+        float t = fmaf(-b2, u1[s], b1);
+        float u = t * r1[s];
+        d = fmaf(-u, t, a - sig[s]);
+        d = fmaf(-b2sq, r2[s], d);
+        u1[s] = u;
+        r2[s] = r1[s];
+      } else {
+        d = fmaf(-b1 * b1, r1[s], a - sig[s]);
+      }
+      if (fabsf(d) < pivmin) d = -pivmin;
+      c[s] += (d < 0.0f);
+      r1[s] = __fdividef(1.0f, d);
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < kShiftsPerLane; ++s) cnt[s] = c[s];
+}
+
+// L D L^T factorization of H32 - sigma (FP32), stored as r = 1/d and u.
+template <int kBand>
+__device__ inline void ldl_factor(const float* a32, int N, float b1, float b2, float sigma,
+                                  float pivmin, float* R, float* U) {
+  float r1 = 0.0f, r2 = 0.0f, u1 = 0.0f;
+  const float b2sq = b2 * b2;
+  for (int i = 0; i < N; ++i) {
+    float d, u = 0.0f;
+    if (kBand == 2) {
+      float t = fmaf(-b2, u1, b1);
+      u = t * r1;
+      d = fmaf(-u, t, a32[i] - sigma);
+      d = fmaf(-b2sq, r2, d);
+    } else {
+      u = b1 * r1;
+      d = fmaf(-u, b1, a32[i] - sigma);
+    }
+    if (fabsf(d) < pivmin) d = (d < 0.0f) ? -pivmin : pivmin;
+    float r = 1.0f / d;
+    R[i] = r;
+    U[i] = u;
+    r2 = r1;
+    r1 = r;
+    u1 = u;
+  }
+}
+
+// Solve (L D L^T) y = scale * x in place in W; returns max |y|.
+template <int kBand>
+__device__ inline float ldl_solve(int N, float b2, const float* R, const float* U, float* W,
+                                  float scale) {
+  float z1 = 0.0f, z2 = 0.0f;
+  for (int i = 0; i < N; ++i) {
+    float z = W[i] * scale - U[i] * z1;
+    if (kBand == 2 && i >= 2) z = fmaf(-b2 * R[i - 2], z2, z);
+    W[i] = z * R[i];
+    z2 = z1;
+    z1 = z;
+  }
+  float y1 = 0.0f, y2 = 0.0f, mx = 0.0f;
+  for (int i = N - 1; i >= 0; --i) {
+    float y = W[i];
+    if (i + 1 < N) y = fmaf(-U[i + 1], y1, y);
+    if (kBand == 2 && i + 2 < N) y = fmaf(-b2 * R[i], y2, y);
+    W[i] = y;
+    mx = fmaxf(mx, fabsf(y));
+    y2 = y1;
+    y1 = y;
+  }
+  return mx;
+}
+
+// Work counters of one eigen-solve (for the roofline tally of the benchmark).
+struct EigStats {
+  int solves, rq_vectors, updates, passes;
+};
+
+// Lowest K eigenpairs of T + diag(v) (v in global vks).  X: K vectors of
+// stride nmax (FP64, global), normalised to sum x^2 = 1 on exit.
+// Eigenvalues in sm.theta[0..K); sm.eigprev holds warm-start brackets.
+template <int kBand>
+__device__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, const double* vks,
+                           double* X, bool warm, double dv, const Smem& sm, int lane,
+                           EigStats& stats) {
+  stats.solves += 1;
+  const Stencil st = make_stencil(p.stencil, dx);
+  const int nstr = sm.nstr;
+  float* a32 = sm.f32;
+  float* R = a32 + nstr;  // K arrays of nstr
+  float* U = R + (size_t)p.kmax * nstr;
+  float* W = U + (size_t)p.kmax * nstr;
+  const int Kc = K + 1;
+  int flags = 0;
+
+  // --- FP32 diagonal and Gershgorin bounds
+  double amin = 1e300, amax = -1e300;
+  for (int i = lane; i < N; i += kWarp) {
+    double a = st.c0 + vks[i];
+    a32[i] = (float)a;
+    amin = fmin(amin, a);
+    amax = fmax(amax, a);
+  }
+  amin = warp_min(amin);
+  amax = warp_max(amax);
+  const double rad = 2.0 * fabs(st.b1) + 2.0 * fabs(st.b2);
+  const double hnorm = fmax(fabs(amin), fabs(amax)) + rad;
+  const float tolabs = (float)(4.0 * FLT_EPSILON * hnorm);
+  const float pivmin = (float)(1e-20 * hnorm);
+  const float glo = (float)(amin - rad) - tolabs;
+  const float ghi = (float)(amax + rad) + tolabs;
+  const float b1f = (float)st.b1, b2f = (float)st.b2;
+  __syncwarp();
+
+  // --- brackets
+  if (lane < Kc) {
+    float lo = glo, hi = ghi;
+    if (warm) {
+      double c = sm.eigprev[lane];
+      double w = dv + 4.0 * tolabs;
+      lo = fmaxf(glo, (float)(c - w));
+      hi = fminf(ghi, (float)(c + w));
+    }
+    sm.lo[lane] = lo;
+    sm.hi[lane] = hi;
+  }
+  __syncwarp();
+  if (warm) {
+    // Verify the warm brackets with one pass of counts at both ends.
+    float sg[kShiftsPerLane];
+    int cn[kShiftsPerLane];
+#pragma unroll
+    for (int s = 0; s < kShiftsPerLane; ++s) {
+      int q = lane * kShiftsPerLane + s;
+      int j = q >> 1;
+      sg[s] = (j < Kc) ? ((q & 1) ? sm.hi[j] : sm.lo[j]) : 0.0f;
+    }
+    sturm_counts<kBand>(a32, N, b1f, b2f, pivmin, sg, cn);
+#pragma unroll
+    for (int s = 0; s < kShiftsPerLane; ++s) {
+      sm.cnt[lane * kShiftsPerLane + s] = cn[s];
+    }
+    __syncwarp();
+    if (lane < Kc) {
+      int clo = sm.cnt[2 * lane], chi = sm.cnt[2 * lane + 1];
+      if (clo > lane) sm.lo[lane] = glo;
+      if (chi <= lane) sm.hi[lane] = ghi;
+    }
+    __syncwarp();
+  }
+
+  // --- multisection
+  int pass = 0;
+  for (; pass < kMaxPasses; ++pass) {
+    bool unres = false;
+    if (lane < Kc) {
+      float lo = sm.lo[lane], hi = sm.hi[lane];
+      float tol = fmaxf(tolabs, 4.0f * FLT_EPSILON * fmaxf(fabsf(lo), fabsf(hi)));
+      unres = (hi - lo) > tol;
+      if (unres && lane > 0 && sm.lo[lane - 1] == lo && sm.hi[lane - 1] == hi) unres = false;
+    }
+    unsigned mask = __ballot_sync(kFull, unres);
+    if (mask == 0u) {
+      // shared brackets that are not yet resolved are covered by their first member
+      bool any = false;
+      if (lane < Kc) {
+        float lo = sm.lo[lane], hi = sm.hi[lane];
+        float tol = fmaxf(tolabs, 4.0f * FLT_EPSILON * fmaxf(fabsf(lo), fabsf(hi)));
+        any = (hi - lo) > tol;
+      }
+      if (__ballot_sync(kFull, any) == 0u) break;
+      // only duplicates remain unresolved: treat every member as unique
+      mask = __ballot_sync(kFull, any);
+    }
+    const int u = __popc(mask);
+    const int P = kSamples / u;
+    float sg[kShiftsPerLane];
+    bool valid[kShiftsPerLane];
+#pragma unroll
+    for (int s = 0; s < kShiftsPerLane; ++s) {
+      int q = lane * kShiftsPerLane + s;
+      int k = q / P;
+      valid[s] = k < u;
+      sg[s] = 0.0f;
+      if (valid[s]) {
+        // k-th set bit of mask
+        unsigned m = mask;
+        for (int t = 0; t < k; ++t) m &= m - 1;
+        int j = __ffs(m) - 1;
+        float lo = sm.lo[j], hi = sm.hi[j];
+        int pp = q - k * P;
+        sg[s] = lo + (hi - lo) * (float)(pp + 1) / (float)(P + 1);
+      }
+    }
+    int cn[kShiftsPerLane];
+    sturm_counts<kBand>(a32, N, b1f, b2f, pivmin, sg, cn);
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < kShiftsPerLane; ++s) {
+      int q = lane * kShiftsPerLane + s;
+      sm.sig[q] = sg[s];
+      sm.cnt[q] = valid[s] ? cn[s] : -1;
+    }
+    __syncwarp();
+    if (lane < Kc) {
+      float lo = sm.lo[lane], hi = sm.hi[lane];
+      for (int q = 0; q < kSamples; ++q) {
+        int c = sm.cnt[q];
+        if (c < 0) continue;
+        float s = sm.sig[q];
+        if (c > lane) {
+          hi = fminf(hi, s);
+        } else {
+          lo = fmaxf(lo, s);
+        }
+      }
+      sm.lo[lane] = lo;
+      sm.hi[lane] = hi;
+    }
+    __syncwarp();
+  }
+
+  stats.passes += pass + (warm ? 1 : 0);
+  // --- shifts, clusters
+  const float tau = fmaxf(1e-3f, 16.0f * tolabs);
+  if (lane < Kc) sm.eigprev[lane] = 0.5 * ((double)sm.lo[lane] + (double)sm.hi[lane]);
+  __syncwarp();
+  if (lane == 0) {
+    int cid = 0;
+    sm.clus[0] = 0;
+    for (int j = 1; j < Kc; ++j) {
+      if (sm.eigprev[j] - sm.eigprev[j - 1] >= tau) ++cid;
+      sm.clus[j] = cid;
+    }
+  }
+  __syncwarp();
+  bool any_cluster = false;
+  for (int j = 1; j < K; ++j) any_cluster |= (sm.clus[j] == sm.clus[j - 1]);
+  {
+    // occupied / unoccupied boundary inside a cluster: the density (odd Ne) or
+    // the gap (even Ne) is not determined to better than the cluster width
+    const int homo = (ne - 1) / 2, lumo = ne / 2;
+    bool deg = (homo != lumo) ? (sm.clus[homo] == sm.clus[lumo])
+                              : ((homo > 0 && sm.clus[homo - 1] == sm.clus[homo]) ||
+                                 sm.clus[homo] == sm.clus[homo + 1]);
+    deg = deg || (sm.clus[K - 1] == sm.clus[K]);
+    if (deg) flags |= QEX_FLAG_DEGENERATE_FRONTIER;
+  }
+
+  // --- FP32 inverse iteration (lane j owns eigenpair j)
+  if (lane < K) {
+    float* Rj = R + (size_t)lane * nstr;
+    float* Uj = U + (size_t)lane * nstr;
+    float* Wj = W + (size_t)lane * nstr;
+    ldl_factor<kBand>(a32, N, b1f, b2f, (float)sm.eigprev[lane], pivmin, Rj, Uj);
+    const double* Xj = X + (size_t)lane * p.nmax;
+    for (int i = 0; i < N; ++i) Wj[i] = warm ? (float)Xj[i] : pseudo_random(i, lane);
+  }
+  __syncwarp();
+  const int rounds = warm ? 2 : 4;
+  float scale = 1.0f;
+  for (int r = 0; r < rounds; ++r) {
+    if (lane < K) {
+      float mx = ldl_solve<kBand>(N, b2f, R + (size_t)lane * nstr, U + (size_t)lane * nstr,
+                                  W + (size_t)lane * nstr, scale);
+      scale = (mx > 0.0f) ? 1.0f / mx : 1.0f;
+    }
+    __syncwarp();
+    if (any_cluster) {
+      // Gram-Schmidt inside clusters (point-parallel), then rescale.
+      for (int j = 1; j < K; ++j) {
+        if (sm.clus[j] != sm.clus[j - 1]) continue;
+        float sj = __shfl_sync(kFull, scale, j);
+        for (int q = j - 1; q >= 0 && sm.clus[q] == sm.clus[j]; --q) {
+          float sq = __shfl_sync(kFull, scale, q);
+          double dot = 0.0, nq = 0.0;
+          const float* Wq = W + (size_t)q * nstr;
+          float* Wj = W + (size_t)j * nstr;
+          for (int i = lane; i < N; i += kWarp) {
+            double a = (double)Wq[i] * sq, b = (double)Wj[i] * sj;
+            dot = fma(a, b, dot);
+            nq = fma(a, a, nq);
+          }
+          dot = warp_sum(dot);
+          nq = warp_sum(nq);
+          float c = (nq > 0.0) ? (float)(dot / nq) : 0.0f;
+          for (int i = lane; i < N; i += kWarp) Wj[i] = fmaf(-c * sq / sj, Wq[i], Wj[i]);
+          __syncwarp();
+        }
+      }
+    }
+  }
+  // --- FP64 vectors, normalised
+  for (int j = 0; j < K; ++j) {
+    float sj = __shfl_sync(kFull, scale, j);
+    const float* Wj = W + (size_t)j * nstr;
+    double nn = 0.0;
+    for (int i = lane; i < N; i += kWarp) {
+      double a = (double)Wj[i] * sj;
+      nn = fma(a, a, nn);
+    }
+    nn = warp_sum(nn);
+    double inv = (nn > 0.0) ? 1.0 / sqrt(nn) : 0.0;
+    double* Xj = X + (size_t)j * p.nmax;
+    for (int i = lane; i < N; i += kWarp) Xj[i] = (double)Wj[i] * sj * inv;
+  }
+  __syncwarp();
+
+  // --- FP64 Newton refinement: x <- x + (H32 - sigma)^-1 (theta x - H x)
+  // residual target: 64 ulp of the operator norm (FP64 floor is ~1 ulp * |H|)
+  const double thr = 64.0 * DBL_EPSILON * hnorm;
+  double* xs = sm.s64a + kPad64;
+  double* ys = sm.s64b + kPad64;
+  bool done_all = false;
+  int step = 0;
+  for (; step < kMaxRefineSteps; ++step) {
+    stats.rq_vectors += K;
+    for (int j = 0; j < K; ++j) {
+      const double* Xj = X + (size_t)j * p.nmax;
+      stage64(sm.s64a, Xj, N, lane);
+      double xx = 0.0, xy = 0.0;
+      for (int i = lane; i < N; i += kWarp) {
+        double x = xs[i];
+        double y = fma(st.c0 + vks[i], x, st.b1 * (xs[i - 1] + xs[i + 1]));
+        if (kBand == 2) y = fma(st.b2, xs[i - 2] + xs[i + 2], y);
+        ys[i] = y;
+        xx = fma(x, x, xx);
+        xy = fma(x, y, xy);
+      }
+      xx = warp_sum(xx);
+      xy = warp_sum(xy);
+      const double th = xy / xx;
+      double rr = 0.0;
+      float* Wj = W + (size_t)j * nstr;
+      for (int i = lane; i < N; i += kWarp) {
+        double r = fma(-th, xs[i], ys[i]);
+        rr = fma(r, r, rr);
+        Wj[i] = (float)(-r);
+      }
+      rr = warp_sum(rr);
+      if (lane == 0) {
+        sm.theta[j] = th;
+        sm.resn[j] = sqrt(rr / xx);
+      }
+      __syncwarp();
+    }
+    bool need = false;
+    if (lane < K) {
+      bool inclus = (lane > 0 && sm.clus[lane] == sm.clus[lane - 1]) ||
+                    (lane + 1 < Kc && sm.clus[lane] == sm.clus[lane + 1]);
+      need = inclus ? (step < 3) : (sm.resn[lane] > thr);
+    }
+    const unsigned nm = __ballot_sync(kFull, need);
+    if (nm == 0u) {
+      done_all = true;
+      break;
+    }
+    stats.updates += __popc(nm);
+    if (need) {
+      ldl_solve<kBand>(N, b2f, R + (size_t)lane * nstr, U + (size_t)lane * nstr,
+                       W + (size_t)lane * nstr, 1.0f);
+    }
+    __syncwarp();
+    for (int j = 0; j < K; ++j) {
+      if (!((nm >> j) & 1u)) continue;
+      double* Xj = X + (size_t)j * p.nmax;
+      const float* Wj = W + (size_t)j * nstr;
+      for (int i = lane; i < N; i += kWarp) Xj[i] += (double)Wj[i];
+    }
+    __syncwarp();
+  }
+  if (!done_all) flags |= QEX_FLAG_REFINE_CAP;
+
+  // --- Rayleigh-Ritz inside clusters (FP64)
+  if (any_cluster) {
+    int j0 = 0;
+    while (j0 < K) {
+      int j1 = j0;
+      while (j1 + 1 < K && sm.clus[j1 + 1] == sm.clus[j0]) ++j1;
+      const int s = j1 - j0 + 1;
+      if (s >= 2) {
+        // modified Gram-Schmidt
+        for (int a = j0; a <= j1; ++a) {
+          double* Xa = X + (size_t)a * p.nmax;
+          for (int b = j0; b < a; ++b) {
+            const double* Xb = X + (size_t)b * p.nmax;
+            double d = 0.0;
+            for (int i = lane; i < N; i += kWarp) d = fma(Xa[i], Xb[i], d);
+            d = warp_sum(d);
+            for (int i = lane; i < N; i += kWarp) Xa[i] = fma(-d, Xb[i], Xa[i]);
+            __syncwarp();
+          }
+          double nn = 0.0;
+          for (int i = lane; i < N; i += kWarp) nn = fma(Xa[i], Xa[i], nn);
+          nn = warp_sum(nn);
+          double inv = 1.0 / sqrt(nn);
+          for (int i = lane; i < N; i += kWarp) Xa[i] *= inv;
+          __syncwarp();
+        }
+        // projected matrix A = Xc^T H Xc  (s <= kMaxEig, stored in sm.red / f32 scratch)
+        // the FP32 work area (16-byte aligned base) is free now
+        double* A = reinterpret_cast<double*>(sm.f32);
+        double* Q = A + s * s;
+        for (int b = j0; b <= j1; ++b) {
+          stage64(sm.s64a, X + (size_t)b * p.nmax, N, lane);
+          for (int i = lane; i < N; i += kWarp) {
+            double y = fma(st.c0 + vks[i], xs[i], st.b1 * (xs[i - 1] + xs[i + 1]));
+            if (kBand == 2) y = fma(st.b2, xs[i - 2] + xs[i + 2], y);
+            ys[i] = y;
+          }
+          __syncwarp();
+          for (int a = j0; a <= b; ++a) {
+            const double* Xa = X + (size_t)a * p.nmax;
+            double d = 0.0;
+            for (int i = lane; i < N; i += kWarp) d = fma(Xa[i], ys[i], d);
+            d = warp_sum(d);
+            if (lane == 0) {
+              A[(a - j0) * s + (b - j0)] = d;
+              A[(b - j0) * s + (a - j0)] = d;
+            }
+          }
+          __syncwarp();
+        }
+        if (lane == 0) {
+          // cyclic Jacobi on the s x s projected matrix
+          for (int a = 0; a < s; ++a)
+            for (int b = 0; b < s; ++b) Q[a * s + b] = (a == b) ? 1.0 : 0.0;
+          for (int sweep = 0; sweep < 30; ++sweep) {
+            double off = 0.0;
+            for (int a = 0; a < s; ++a)
+              for (int b = a + 1; b < s; ++b) off += A[a * s + b] * A[a * s + b];
+            if (off < 1e-30) break;
+            for (int a = 0; a < s; ++a) {
+              for (int b = a + 1; b < s; ++b) {
+                double apq = A[a * s + b];
+                if (fabs(apq) < 1e-300) continue;
+                double app = A[a * s + a], aqq = A[b * s + b];
+                double tau2 = (aqq - app) / (2.0 * apq);
+                double t = (tau2 >= 0 ? 1.0 : -1.0) / (fabs(tau2) + sqrt(1.0 + tau2 * tau2));
+                double c = 1.0 / sqrt(1.0 + t * t), sn = t * c;
+                for (int k = 0; k < s; ++k) {
+                  double akp = A[k * s + a], akq = A[k * s + b];
+                  A[k * s + a] = c * akp - sn * akq;
+                  A[k * s + b] = sn * akp + c * akq;
+                }
+                for (int k = 0; k < s; ++k) {
+                  double apk = A[a * s + k], aqk = A[b * s + k];
+                  A[a * s + k] = c * apk - sn * aqk;
+                  A[b * s + k] = sn * apk + c * aqk;
+                }
+                for (int k = 0; k < s; ++k) {
+                  double qkp = Q[k * s + a], qkq = Q[k * s + b];
+                  Q[k * s + a] = c * qkp - sn * qkq;
+                  Q[k * s + b] = sn * qkp + c * qkq;
+                }
+              }
+            }
+          }
+          // sort ascending (selection sort on eigenvalues + columns)
+          for (int a = 0; a < s; ++a) {
+            int m = a;
+            for (int b = a + 1; b < s; ++b)
+              if (A[b * s + b] < A[m * s + m]) m = b;
+            if (m != a) {
+              double t = A[a * s + a];
+              A[a * s + a] = A[m * s + m];
+              A[m * s + m] = t;
+              for (int k = 0; k < s; ++k) {
+                double q = Q[k * s + a];
+                Q[k * s + a] = Q[k * s + m];
+                Q[k * s + m] = q;
+              }
+            }
+          }
+          for (int a = 0; a < s; ++a) sm.theta[j0 + a] = A[a * s + a];
+        }
+        __syncwarp();
+        // rotate X_c <- X_c Q
+        for (int i = lane; i < N; i += kWarp) {
+          double old[kMaxEig];
+          for (int a = 0; a < s; ++a) old[a] = X[(size_t)(j0 + a) * p.nmax + i];
+          for (int b = 0; b < s; ++b) {
+            double v = 0.0;
+            for (int a = 0; a < s; ++a) v = fma(old[a], Q[a * s + b], v);
+            X[(size_t)(j0 + b) * p.nmax + i] = v;
+          }
+        }
+        __syncwarp();
+      }
+      j0 = j1 + 1;
+    }
+  }
+
+  // --- final normalisation
+  for (int j = 0; j < K; ++j) {
+    double* Xj = X + (size_t)j * p.nmax;
+    double nn = 0.0;
+    for (int i = lane; i < N; i += kWarp) nn = fma(Xj[i], Xj[i], nn);
+    nn = warp_sum(nn);
+    double inv = 1.0 / sqrt(nn);
+    for (int i = lane; i < N; i += kWarp) Xj[i] *= inv;
+  }
+  // warm-start data for the next call: refined eigenvalues, bisected top one
+  if (lane < K) sm.eigprev[lane] = sm.theta[lane];
+  __syncwarp();
+  return flags;
+}
+
+// Occupation of orbital j for Ne electrons (two per orbital, last one single
+// when Ne is odd: jnp.repeat(..., 2)[:Ne], qedft/train/od/scf.py:212-213).
+__device__ inline double occupation(int j, int ne) {
+  int rem = ne - 2 * j;
+  return rem >= 2 ? 2.0 : (rem == 1 ? 1.0 : 0.0);
+}
+
+// Density, eigen-energy sum and gap from the eigenpairs.
+__device__ void density_from_orbitals(const Params& p, int N, double dx, int ne, int K,
+                                      const double* X, double* nout, const Smem& sm, double& tee,
+                                      double& gap, int lane) {
+  const int nocc = (ne + 1) / 2;
+  const double inv_dx = 1.0 / dx;
+  for (int i = lane; i < N; i += kWarp) {
+    double v = 0.0;
+    for (int j = 0; j < nocc; ++j) {
+      double x = X[(size_t)j * p.nmax + i];
+      v = fma(occupation(j, ne) * inv_dx, x * x, v);
+    }
+    nout[i] = v;
+  }
+  tee = 0.0;
+  for (int j = 0; j < nocc; ++j) tee += occupation(j, ne) * sm.theta[j];
+  // jax_dft get_gap: repeated spectrum rep[Ne] - rep[Ne-1]
+  const int lumo = ne / 2, homo = (ne - 1) / 2;
+  gap = sm.theta[lumo] - sm.theta[homo];
+  (void)K;
+  __syncwarp();
+}
+
+__device__ inline void write_stats(const Params& p, int b, const EigStats& e) {
+  if (!p.o_stats) return;
+  p.o_stats[4 * b + 0] = e.solves;
+  p.o_stats[4 * b + 1] = e.rq_vectors;
+  p.o_stats[4 * b + 2] = e.updates;
+  p.o_stats[4 * b + 3] = e.passes;
+}
+
+// ---------------------------------------------------------------------------
+// The kernel
+// ---------------------------------------------------------------------------
+template <int kBand>
+__global__ void __launch_bounds__(kWarp) ks1d_kernel(const __grid_constant__ Params p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x;
+  const SmemLayout L = smem_layout(p.nmax, p.kmax);
+  Smem sm = carve(smem_raw, L);
+
+  for (;;) {
+    int slot = 0;
+    if (lane == 0) slot = atomicAdd(p.counter, 1);
+    slot = __shfl_sync(kFull, slot, 0);
+    if (slot >= p.num_molecules) break;
+    const int b = p.order ? p.order[slot] : slot;
+
+    const int N = p.num_grids[b];
+    const long long off = p.grid_offsets[b];
+    const int ne = p.num_electrons[b];
+    const double x0 = p.grid_start[b];
+    const double dx = p.grid_spacing[b];
+    const int K = ne / 2 + 1;
+    if (N < 5 || N > p.nmax || ne < 1 || K > p.kmax || !(dx > 0.0)) {
+      if (lane == 0 && p.o_status) p.o_status[b] = QEX_BAD_ARG;
+      continue;
+    }
+    double* ws = p.ws + (long long)slot * p.stride;
+    double* vn = ws + (long long)VN * p.nmax;
+    double* vext = ws + (long long)VEXT * p.nmax;
+    double* vks = ws + (long long)VKS * p.nmax;
+    double* nout = ws + (long long)VNOUT * p.nmax;
+    double* vh = ws + (long long)VH * p.nmax;
+    double* vxc = ws + (long long)VXC * p.nmax;
+    double* vf = ws + (long long)VF * p.nmax;
+    double* kt = ws + (long long)VKT * p.nmax;
+    double* diffs = ws + (long long)VDIFF * p.nmax;
+    double* X = diffs + (long long)p.mix_slots * p.nmax;
+    int flags = 0;
+    EigStats est = {0, 0, 0, 0};
+
+    // external potential and interaction table
+    if (p.vext_given) {
+      for (int i = lane; i < N; i += kWarp) vext[i] = p.vext_in[off + i];
+    } else {
+      const int M = p.num_nuclei[b];
+      for (int i = lane; i < N; i += kWarp) {
+        double x = x0 + i * dx, v = 0.0;
+        for (int m = 0; m < M; ++m) {
+          double R = p.locations[(long long)b * p.max_nuclei + m];
+          double Z = p.charges[(long long)b * p.max_nuclei + m];
+          v -= Z * interaction_fn(p, x - R);
+        }
+        vext[i] = v;
+      }
+    }
+    if (p.interaction != QEX_INTERACTION_EXPONENTIAL) {
+      for (int d = lane; d < N; d += kWarp) kt[d] = interaction_fn(p, d * dx);
+    }
+    if (p.o_vext)
+      for (int i = lane; i < N; i += kWarp) p.o_vext[off + i] = vext[i];
+    __syncwarp();
+
+    if (p.mode == kModeNonInteracting) {
+      flags |= eigen_solve<kBand>(p, N, dx, ne, K, vext, X, false, 0.0, sm, lane, est);
+      double tee, gap;
+      density_from_orbitals(p, N, dx, ne, K, X, nout, sm, tee, gap, lane);
+      if (p.o_final)
+        for (int i = lane; i < N; i += kWarp) p.o_final[off + i] = nout[i];
+      if (lane == 0) {
+        if (p.o_tee) p.o_tee[b] = tee;
+        if (p.o_gap) p.o_gap[b] = gap;
+        if (p.o_status) p.o_status[b] = flags;
+        write_stats(p, b, est);
+      }
+      continue;
+    }
+
+    // initial density
+    bool warm = false;
+    double dv = 0.0;
+    if (p.dens_in) {
+      for (int i = lane; i < N; i += kWarp) vn[i] = p.dens_in[off + i];
+    } else {
+      flags |= eigen_solve<kBand>(p, N, dx, ne, K, vext, X, false, 0.0, sm, lane, est);
+      double tee, gap;
+      density_from_orbitals(p, N, dx, ne, K, X, vn, sm, tee, gap, lane);
+      // warm start from the non-interacting eigenpairs: v_KS differs from
+      // v_ext by v_H + v_xc, bounded below through dv in the first iteration.
+      for (int i = lane; i < N; i += kWarp) vks[i] = vext[i];
+      warm = true;
+    }
+    __syncwarp();
+
+    double alpha = p.alpha;
+    bool converged = false;
+    int active = 0;
+    double last_energy = INFINITY, last_gap = 0.0;
+    const long long rec = (long long)p.iters * off;
+    const bool reflect_xc = p.reflect && p.xc_conv == QEX_XC_LOCAL;
+    const int slots = p.mix_slots;
+
+    for (int t = 0; t < p.iters; ++t) {
+      const long long r0 = rec + (long long)t * N;
+      if (converged && p.mode == kModeScf) {
+        // converged branch: the previous state is repeated (jit_scf.py:164-166,
+        // scf.py:522-524)
+        if (lane == 0) {
+          if (p.o_energy) p.o_energy[(long long)b * p.iters + t] = last_energy;
+          if (p.o_gap) p.o_gap[(long long)b * p.iters + t] = last_gap;
+          if (p.o_conv) p.o_conv[(long long)b * p.iters + t] = 1;
+        }
+        for (int i = lane; i < N; i += kWarp) {
+          if (p.o_dens) p.o_dens[r0 + i] = vn[i];
+          if (p.o_vh) p.o_vh[r0 + i] = vh[i];
+          if (p.o_vxc) p.o_vxc[r0 + i] = vxc[i];
+          if (p.o_f) p.o_f[r0 + i] = vf[i];
+        }
+        continue;
+      }
+      const bool conv_at_start = converged;
+      if (p.mode == kModeIteration) {
+        for (int i = lane; i < N; i += kWarp) vn[i] = p.dens_in[off + i];
+        __syncwarp();
+      }
+
+      // ---- Hartree and XC on the input density
+      stage64(sm.s64a, vn, N, lane);
+      hartree(p, N, dx, sm, vh, kt, lane);
+      if (reflect_xc) {
+        for (int i = lane; i < N; i += kWarp) {
+          sm.s64a[kPad64 + i] = 0.5 * (vn[i] + vn[N - 1 - i]);
+        }
+        __syncwarp();
+      }
+      xc_eval(p, N, dx, sm, true, vxc, vf, reflect_xc, lane);
+      double dvl = 0.0;
+      for (int i = lane; i < N; i += kWarp) {
+        double v = vh[i] + vxc[i] + vext[i];
+        dvl = fmax(dvl, fabs(v - vks[i]));
+        vks[i] = v;
+      }
+      dv = warm ? warp_max(dvl) : 0.0;
+      __syncwarp();
+
+      // ---- eigen-solve and output density
+      flags |= eigen_solve<kBand>(p, N, dx, ne, K, vks, X, warm, dv, sm, lane, est);
+      warm = true;
+      double tee, gap;
+      density_from_orbitals(p, N, dx, ne, K, X, nout, sm, tee, gap, lane);
+
+      // ---- total energy on the output density (jit_scf.py:46-72)
+      double eks = 0.0, eext = 0.0;
+      for (int i = lane; i < N; i += kWarp) {
+        eks = fma(vks[i], nout[i], eks);
+        eext = fma(vext[i], nout[i], eext);
+      }
+      eks = warp_sum(eks) * dx;
+      eext = warp_sum(eext) * dx;
+      stage64(sm.s64a, nout, N, lane);
+      // Hartree of n_out into the FP64 staging buffer b (only the energy is kept)
+      const double eh = 0.5 * dx * hartree(p, N, dx, sm, sm.s64b + kPad64, kt, lane);
+      __syncwarp();
+      if (reflect_xc) {
+        for (int i = lane; i < N; i += kWarp) {
+          sm.s64a[kPad64 + i] = 0.5 * (nout[i] + nout[N - 1 - i]);
+        }
+        __syncwarp();
+      }
+      const double exc = xc_eval(p, N, dx, sm, false, nullptr, nullptr, false, lane);
+      const double energy = tee - eks + eh + exc + eext;
+      if (p.reflect) flip_avg_global(nout, N, lane);
+
+      if (p.mode == kModeIteration) {
+        if (lane == 0) {
+          if (p.o_energy) p.o_energy[b] = energy;
+          if (p.o_gap) p.o_gap[b] = gap;
+          if (p.o_status) p.o_status[b] = flags;
+          if (p.o_iters) p.o_iters[b] = 1;
+          write_stats(p, b, est);
+        }
+        for (int i = lane; i < N; i += kWarp) {
+          if (p.o_dens) p.o_dens[off + i] = nout[i];
+          if (p.o_vh) p.o_vh[off + i] = vh[i];
+          if (p.o_vxc) p.o_vxc[off + i] = vxc[i];
+          if (p.o_f) p.o_f[off + i] = vf[i];
+          if (p.o_final) p.o_final[off + i] = nout[i];
+        }
+        break;
+      }
+
+      // ---- mixing (jit_scf.py:177-181; scf.py:547-555)
+      const int slot_w = active % slots;
+      double* dslot = diffs + (long long)slot_w * p.nmax;
+      const int navg = min(active + 1, min(p.mixing, slots));
+      double mse_raw = 0.0, mse_mix = 0.0;
+      for (int i = lane; i < N; i += kWarp) {
+        double d = nout[i] - vn[i];
+        dslot[i] = d;
+        mse_raw = fma(d, d, mse_raw);
+      }
+      __syncwarp();
+      for (int i = lane; i < N; i += kWarp) {
+        double s = 0.0;
+        for (int q = 0; q < navg; ++q) {
+          int sl = (active - q) % slots;
+          if (sl < 0) sl += slots;
+          s += diffs[(long long)sl * p.nmax + i];
+        }
+        double upd = alpha * (s / navg);
+        mse_mix = fma(upd, upd, mse_mix);
+        vn[i] += upd;
+      }
+      mse_raw = warp_sum(mse_raw) / N;
+      mse_mix = warp_sum(mse_mix) / N;
+      __syncwarp();
+      ++active;
+      bool rec_conv;
+      if (p.rule == 0) {
+        rec_conv = conv_at_start;
+        converged = mse_mix < p.tol;
+        alpha *= p.alpha_decay;
+      } else {
+        converged = mse_raw < p.tol;
+        rec_conv = converged;
+        alpha *= p.alpha_decay;
+      }
+      last_energy = energy;
+      last_gap = gap;
+      if (lane == 0) {
+        if (p.o_energy) p.o_energy[(long long)b * p.iters + t] = energy;
+        if (p.o_gap) p.o_gap[(long long)b * p.iters + t] = gap;
+        if (p.o_conv) p.o_conv[(long long)b * p.iters + t] = rec_conv ? 1 : 0;
+      }
+      for (int i = lane; i < N; i += kWarp) {
+        if (p.o_dens) p.o_dens[r0 + i] = vn[i];
+        if (p.o_vh) p.o_vh[r0 + i] = vh[i];
+        if (p.o_vxc) p.o_vxc[r0 + i] = vxc[i];
+        if (p.o_f) p.o_f[r0 + i] = vf[i];
+      }
+      __syncwarp();
+    }
+    if (p.mode == kModeScf) {
+      if (p.o_final)
+        for (int i = lane; i < N; i += kWarp) p.o_final[off + i] = vn[i];
+      if (lane == 0) {
+        if (p.o_status) p.o_status[b] = flags;
+        if (p.o_iters) p.o_iters[b] = active;
+        write_stats(p, b, est);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+thread_local int g_last_launches = 0;
+
+int mix_slots_for(const qex_ks1d_options* o) {
+  int m = o->num_mixing_iterations < 1 ? 1 : o->num_mixing_iterations;
+  int it = o->num_iterations < 1 ? 1 : o->num_iterations;
+  return m < it ? m : it;
+}
+
+int check_options(const qex_ks1d_options* o) {
+  if (!o) return QEX_BAD_ARG;
+  if (o->stencil != 3 && o->stencil != 5) return QEX_BAD_ARG;
+  if (o->interaction != QEX_INTERACTION_EXPONENTIAL &&
+      o->interaction != QEX_INTERACTION_SOFT_COULOMB)
+    return QEX_BAD_ARG;
+  if (o->num_iterations < 1 || o->max_num_grids < 5 || o->max_num_electrons < 1) return QEX_BAD_ARG;
+  if (o->max_num_electrons / 2 + 1 > QEX_KS1D_MAX_EIGENPAIRS) return QEX_BAD_ARG;
+  if (o->num_mixing_iterations < 1) return QEX_BAD_ARG;
+  return QEX_OK;
+}
+
+long long stride_doubles(const qex_ks1d_options* o) {
+  int kmax = o->max_num_electrons / 2 + 1;
+  long long s = vec_count(mix_slots_for(o), kmax) * (long long)o->max_num_grids;
+  return (s + 31) / 32 * 32;
+}
+
+int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_options* o,
+                const qex_xc_spec* xc, const qex_ks1d_outputs* out, void* ws, size_t ws_bytes,
+                int num_molecules) {
+  memset(&P, 0, sizeof(P));
+  int rc = check_options(o);
+  if (rc) return rc;
+  if (!b || !xc) return QEX_BAD_ARG;
+  P.mode = mode;
+  P.num_molecules = num_molecules;
+  P.order = b->order;
+  P.num_grids = b->num_grids;
+  P.grid_offsets = b->grid_offsets;
+  P.grid_start = b->grid_start;
+  P.grid_spacing = b->grid_spacing;
+  P.num_electrons = b->num_electrons;
+  P.num_nuclei = b->num_nuclei;
+  P.locations = b->locations;
+  P.charges = b->nuclear_charges;
+  P.vext_in = b->external_potential;
+  P.dens_in = b->initial_density;
+  P.max_nuclei = o->max_nuclei;
+  P.stencil = o->stencil;
+  P.interaction = o->interaction;
+  P.ia = o->interaction_a;
+  P.ib = o->interaction_b;
+  P.iters = o->num_iterations;
+  P.alpha = o->alpha;
+  P.alpha_decay = o->alpha_decay;
+  P.mixing = o->num_mixing_iterations;
+  P.tol = o->density_mse_converge_tolerance;
+  P.rule = o->convergence_rule;
+  P.reflect = o->enforce_reflection_symmetry;
+  P.vext_given = o->external_potential_given;
+  P.nmax = o->max_num_grids;
+  P.kmax = o->max_num_electrons / 2 + 1;
+  P.mix_slots = mix_slots_for(o);
+  P.xc_kind = xc->kind;
+  P.xc_conv = xc->convention;
+  P.xc_a = xc->coefficient;
+  P.xc_p = xc->power;
+  P.xc_shift = xc->shift;
+  P.lda_A = xc->lda_amplitude;
+  P.lda_kappa = xc->lda_kappa;
+  if (xc->kind < QEX_XC_NONE || xc->kind > QEX_XC_WINDOW_MLP) return QEX_BAD_ARG;
+  if (xc->convention != QEX_XC_AMPLITUDE && xc->convention != QEX_XC_LOCAL) return QEX_BAD_ARG;
+  if (xc->kind == QEX_XC_WINDOW_MLP) {
+    if (!fill_mlp_params(P.mlp, xc)) return QEX_BAD_ARG;
+  }
+  if (out) {
+    P.o_energy = out->total_energy;
+    P.o_gap = out->gap;
+    P.o_conv = out->converged;
+    P.o_dens = out->density;
+    P.o_vh = out->hartree_potential;
+    P.o_vxc = out->xc_potential;
+    P.o_f = out->xc_energy_density;
+    P.o_final = out->final_density;
+    P.o_vext = out->external_potential_out;
+    P.o_status = out->status;
+    P.o_iters = out->iterations_run;
+    P.o_stats = out->stats;
+  }
+  size_t need = 0;
+  qex_ks1d_workspace_size(o, num_molecules, &need);
+  if (!ws || ws_bytes < need) return QEX_BAD_ARG;
+  P.counter = reinterpret_cast<int*>(ws);
+  P.ws = reinterpret_cast<double*>(static_cast<unsigned char*>(ws) + 256);
+  P.stride = stride_doubles(o);
+  if (num_molecules < 0) return QEX_BAD_ARG;
+  if (num_molecules > 0) {
+    if (!b->num_grids || !b->grid_offsets || !b->grid_start || !b->grid_spacing ||
+        !b->num_electrons)
+      return QEX_BAD_ARG;
+    if (!o->external_potential_given &&
+        (!b->num_nuclei || !b->locations || !b->nuclear_charges || o->max_nuclei < 1))
+      return QEX_BAD_ARG;
+    if (o->external_potential_given && !b->external_potential) return QEX_BAD_ARG;
+  }
+  return QEX_OK;
+}
+
+int launch(const Params& P, cudaStream_t stream) {
+  g_last_launches = 0;
+  if (P.num_molecules == 0) return QEX_OK;
+  const SmemLayout L = smem_layout(P.nmax, P.kmax);
+  const size_t smem = L.total;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return QEX_CUDA_ERROR;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int max_optin = 0;
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if ((int)smem > max_optin) return QEX_BAD_ARG;
+  cudaError_t e;
+  int per_sm = 0;
+  if (P.stencil == 5) {
+    e = cudaFuncSetAttribute(ks1d_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return QEX_CUDA_ERROR;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks1d_kernel<2>, kWarp, smem);
+  } else {
+    e = cudaFuncSetAttribute(ks1d_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return QEX_CUDA_ERROR;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks1d_kernel<1>, kWarp, smem);
+  }
+  if (per_sm < 1) per_sm = 1;
+  long long grid = (long long)sms * per_sm;
+  if (grid > P.num_molecules) grid = P.num_molecules;
+  e = cudaMemsetAsync(P.counter, 0, sizeof(int), stream);
+  if (e != cudaSuccess) return QEX_CUDA_ERROR;
+  if (P.stencil == 5) {
+    ks1d_kernel<2><<<(unsigned)grid, kWarp, smem, stream>>>(P);
+  } else {
+    ks1d_kernel<1><<<(unsigned)grid, kWarp, smem, stream>>>(P);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return QEX_CUDA_ERROR;
+  g_last_launches = 1;
+  return QEX_OK;
+}
+
+}  // namespace
+}  // namespace qex
+
+extern "C" {
+
+int qex_ks1d_workspace_size(const qex_ks1d_options* options, int32_t num_molecules,
+                            size_t* bytes) {
+  if (!bytes) return QEX_BAD_ARG;
+  *bytes = 0;
+  int rc = qex::check_options(options);
+  if (rc) return rc;
+  if (num_molecules < 0) return QEX_BAD_ARG;
+  *bytes = 256 + sizeof(double) * (size_t)qex::stride_doubles(options) * (size_t)num_molecules;
+  return QEX_OK;
+}
+
+int qex_ks1d_solve(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
+                   const qex_xc_spec* xc, const qex_ks1d_outputs* outputs, void* workspace,
+                   size_t workspace_bytes, void* stream) {
+  qex::Params P;
+  if (!batch) return QEX_BAD_ARG;
+  int rc = qex::fill_params(P, qex::kModeScf, batch, options, xc, outputs, workspace,
+                            workspace_bytes, batch->num_molecules);
+  if (rc) return rc;
+  return qex::launch(P, static_cast<cudaStream_t>(stream));
+}
+
+int qex_ks1d_iteration(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
+                       const qex_xc_spec* xc, const double* density_in,
+                       const qex_ks1d_outputs* outputs, void* workspace, size_t workspace_bytes,
+                       void* stream) {
+  if (!batch || !density_in || !options) return QEX_BAD_ARG;
+  qex_ks1d_options o = *options;
+  o.num_iterations = 1;
+  qex::Params P;
+  int rc = qex::fill_params(P, qex::kModeIteration, batch, &o, xc, outputs, workspace,
+                            workspace_bytes, batch->num_molecules);
+  if (rc) return rc;
+  P.dens_in = density_in;
+  return qex::launch(P, static_cast<cudaStream_t>(stream));
+}
+
+int qex_ks1d_noninteracting(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
+                            const double* potential, double* density, double* total_eigen_energy,
+                            double* gap, int32_t* status, void* workspace,
+                            size_t workspace_bytes, void* stream) {
+  if (!batch || !potential || !options) return QEX_BAD_ARG;
+  qex_ks1d_options o = *options;
+  o.num_iterations = 1;
+  o.external_potential_given = 1;
+  qex_ks1d_batch bb = *batch;
+  bb.external_potential = potential;
+  qex_xc_spec xc;
+  memset(&xc, 0, sizeof(xc));
+  qex_ks1d_outputs out;
+  memset(&out, 0, sizeof(out));
+  out.final_density = density;
+  out.status = status;
+  qex::Params P;
+  int rc = qex::fill_params(P, qex::kModeNonInteracting, &bb, &o, &xc, &out, workspace,
+                            workspace_bytes, bb.num_molecules);
+  if (rc) return rc;
+  P.o_tee = total_eigen_energy;
+  P.o_gap = gap;
+  return qex::launch(P, static_cast<cudaStream_t>(stream));
+}
+
+const char* qex_version(void) { return "qex_gb300 0.1 (sm_103a)"; }
+
+int qex_last_launch_count(void) { return qex::g_last_launches; }
+
+}  // extern "C"

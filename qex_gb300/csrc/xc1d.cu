@@ -1,0 +1,168 @@
+// Point-parallel evaluation of the 1D exchange-correlation functionals on
+// packed densities: per-point values f, the potential v_xc and E_xc per
+// molecule.  One CTA per molecule; any grid size.
+//
+// Reference: qedft/train/od/scf.py:32-76 (get_xc_energy_amplitude_encoded /
+// get_xc_potential_amplitude_encoded, the potential carries the factor dx) and
+// the jax_dft local convention (E = dx sum f n, v = (dE/dn)/dx).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "ks1d_common.cuh"
+#include "qex_xc1d.h"
+#include "xc_device.cuh"
+
+namespace qex {
+namespace {
+
+struct XcParams {
+  int num_molecules;
+  const int32_t* num_grids;
+  const int64_t* offsets;
+  const double* spacing;
+  const double* density;
+  double* values;
+  double* potential;
+  double* energy;
+  float* grad;  // (total points, 17) window gradients, MLP only
+  int kind, conv;
+  double a, p, shift, lda_A, lda_kappa;
+  MlpParams mlp;
+};
+
+constexpr int kThreads = 256;
+
+__device__ double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  const int w = threadIdx.x / kWarp, l = threadIdx.x % kWarp;
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x < kWarp) {
+    t = (threadIdx.x < kThreads / kWarp) ? red[threadIdx.x] : 0.0;
+    t = warp_sum(t);
+  }
+  __syncthreads();
+  return t;
+}
+
+__global__ void __launch_bounds__(kThreads) xc1d_kernel(const __grid_constant__ XcParams p) {
+  __shared__ double red[kThreads / kWarp];
+  const int b = blockIdx.x;
+  if (b >= p.num_molecules) return;
+  const int N = p.num_grids[b];
+  const long long off = p.offsets[b];
+  const double dx = p.spacing[b];
+  const double* n = p.density + off;
+  const bool local = p.conv == QEX_XC_LOCAL;
+  double e = 0.0;
+  if (p.kind == QEX_XC_WINDOW_MLP) {
+    const float ninv = p.mlp.norm_inv;
+    for (int i = threadIdx.x; i < N; i += kThreads) {
+      float w[QEX_MLP_WINDOW], gw[QEX_MLP_WINDOW];
+#pragma unroll
+      for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
+        int j = i - kPadMlp + k;
+        w[k] = (j >= 0 && j < N) ? (float)n[j] * ninv : 0.0f;
+      }
+      float f = mlp_point<true>(p.mlp, w, gw);
+      if (p.values) p.values[off + i] = (double)f;
+      e += local ? (double)f * n[i] : (double)f;
+      const float up = local ? (float)n[i] * ninv : ninv;
+#pragma unroll
+      for (int k = 0; k < QEX_MLP_WINDOW; ++k) p.grad[(off + i) * QEX_MLP_WINDOW + k] = up * gw[k];
+    }
+    __syncthreads();
+    if (p.potential) {
+      for (int j = threadIdx.x; j < N; j += kThreads) {
+        // v_j = sum over points i with window offset k = j - i + 8
+        float acc = 0.0f;
+#pragma unroll
+        for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
+          int i = j + kPadMlp - k;
+          if (i >= 0 && i < N) acc += p.grad[(off + i) * QEX_MLP_WINDOW + k];
+        }
+        double v = (double)acc;
+        if (local) v += p.values ? p.values[off + j] : 0.0;
+        p.potential[off + j] = local ? v : dx * v;
+      }
+    }
+  } else {
+    for (int i = threadIdx.x; i < N; i += kThreads) {
+      double ni = n[i], f = 0.0, df = 0.0;
+      if (p.kind == QEX_XC_LDA_EXP_COULOMB) {
+        lda_exp_coulomb(ni, p.lda_A, p.lda_kappa, f, df);
+      } else if (p.kind == QEX_XC_POWER) {
+        double base = ni + p.shift;
+        f = p.a * pow(base, p.p);
+        df = p.a * p.p * pow(base, p.p - 1.0);
+      }
+      if (p.values) p.values[off + i] = f;
+      if (local) {
+        e = fma(f, ni, e);
+        if (p.potential) p.potential[off + i] = fma(ni, df, f);
+      } else {
+        e += f;
+        if (p.potential) p.potential[off + i] = dx * df;
+      }
+    }
+  }
+  e = block_sum(e, red);
+  if (threadIdx.x == 0 && p.energy) p.energy[b] = e * dx;
+}
+
+}  // namespace
+}  // namespace qex
+
+extern "C" {
+
+int qex_xc1d_workspace_size(int64_t total_points, const qex_xc_spec* xc, size_t* bytes) {
+  if (!bytes || !xc || total_points < 0) return QEX_BAD_ARG;
+  *bytes = (xc->kind == QEX_XC_WINDOW_MLP)
+               ? sizeof(float) * QEX_MLP_WINDOW * (size_t)total_points
+               : 0;
+  return QEX_OK;
+}
+
+int qex_xc1d_eval(int32_t num_molecules, int64_t total_points, const int32_t* num_grids,
+                  const int64_t* grid_offsets, const double* grid_spacing,
+                  const qex_xc_spec* xc, const double* density,
+                  double* values, double* potential, double* energy, void* workspace,
+                  size_t workspace_bytes, void* stream) {
+  using namespace qex;
+  if (num_molecules < 0 || !xc) return QEX_BAD_ARG;
+  if (num_molecules == 0) return QEX_OK;
+  if (!num_grids || !grid_offsets || !grid_spacing || !density) return QEX_BAD_ARG;
+  if (xc->kind < QEX_XC_NONE || xc->kind > QEX_XC_WINDOW_MLP) return QEX_BAD_ARG;
+  XcParams P;
+  memset(&P, 0, sizeof(P));
+  P.num_molecules = num_molecules;
+  P.num_grids = num_grids;
+  P.offsets = grid_offsets;
+  P.spacing = grid_spacing;
+  P.density = density;
+  P.values = values;
+  P.potential = potential;
+  P.energy = energy;
+  P.kind = xc->kind;
+  P.conv = xc->convention;
+  P.a = xc->coefficient;
+  P.p = xc->power;
+  P.shift = xc->shift;
+  P.lda_A = xc->lda_amplitude;
+  P.lda_kappa = xc->lda_kappa;
+  if (xc->kind == QEX_XC_WINDOW_MLP) {
+    if (!fill_mlp_params(P.mlp, xc)) return QEX_BAD_ARG;
+    size_t need = 0;
+    qex_xc1d_workspace_size(total_points, xc, &need);
+    if (!workspace || workspace_bytes < need) return QEX_BAD_ARG;
+    P.grad = static_cast<float*>(workspace);
+    // the potential pass needs f in `values` for the local convention
+    if (P.conv == QEX_XC_LOCAL && potential && !values) return QEX_BAD_ARG;
+  }
+  xc1d_kernel<<<num_molecules, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(P);
+  return cudaGetLastError() == cudaSuccess ? QEX_OK : QEX_CUDA_ERROR;
+}
+
+}  // extern "C"
