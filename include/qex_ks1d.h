@@ -126,6 +126,9 @@ typedef struct qex_ks1d_outputs {
   int32_t* iterations_run;   /* (B) iterations that did work (not skipped as converged) */
   int32_t* stats;            /* (B, 4): eigen-solves, Rayleigh-quotient vector passes,
                                 correction updates, Sturm multisection passes */
+  int64_t* phase_cycles;     /* (B, 8): SM clock cycles per phase: Hartree, XC potential,
+                                Sturm brackets, FP32 inverse iteration, FP64 refinement,
+                                density+energy, mixing+records, whole molecule */
 } qex_ks1d_outputs;
 
 /* Bytes of device workspace qex_ks1d_solve needs for this batch shape. */

@@ -103,6 +103,7 @@ class Ks1dOutputs(ctypes.Structure):
         ("status", _c_p),
         ("iterations_run", _c_p),
         ("stats", _c_p),
+        ("phase_cycles", _c_p),
     ]
 
 

@@ -82,6 +82,7 @@ struct Params {
   int32_t* o_status;
   int32_t* o_iters;
   int32_t* o_stats;
+  long long* o_cycles;
   double* o_tee;
   // workspace
   double* ws;
@@ -122,7 +123,9 @@ __host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax) {
   // theta, resn, eigprev (double x kMaxBis), clus (int x kMaxBis), red (double x 32)
   off += sizeof(float) * kMaxBis * 2 + sizeof(float) * kSamples + sizeof(int) * kSamples;
   off = (off + 7) & ~(size_t)7;
-  off += sizeof(double) * kMaxBis * 3 + sizeof(int) * kMaxBis + sizeof(double) * 32;
+  off += sizeof(double) * kMaxBis * 3 + sizeof(int) * kMaxBis;
+  off = (off + 7) & ~(size_t)7;
+  off += sizeof(double) * 32 + sizeof(double) * 8;  // red, aux
   L.total = (off + 127) & ~(size_t)127;
   return L;
 }
@@ -140,6 +143,7 @@ struct Smem {
   double* eigprev;
   int* clus;
   double* red;
+  double* aux;
   int nstr;
 };
 
@@ -168,6 +172,8 @@ __device__ inline Smem carve(unsigned char* base, const SmemLayout& L) {
   p += sizeof(int) * kMaxBis;
   p = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 7) & ~(uintptr_t)7);
   s.red = reinterpret_cast<double*>(p);
+  p += sizeof(double) * 32;
+  s.aux = reinterpret_cast<double*>(p);
   s.nstr = L.nstr;
   return s;
 }
@@ -502,16 +508,29 @@ __device__ inline float ldl_solve(int N, float b2, const float* R, const float* 
 // Work counters of one eigen-solve (for the roofline tally of the benchmark).
 struct EigStats {
   int solves, rq_vectors, updates, passes;
+  long long cyc[8];  // clock64 cycles per phase (see write_stats)
 };
 
 // Lowest K eigenpairs of T + diag(v) (v in global vks).  X: K vectors of
 // stride nmax (FP64, global), normalised to sum x^2 = 1 on exit.
-// Eigenvalues in sm.theta[0..K); sm.eigprev holds warm-start brackets.
+// Eigenvalues in sm.theta[0..K); sm.eigprev holds the previous eigenvalues
+// (warm-start brackets), sm.aux[0] the drift bound of eigprev[K] and
+// sm.aux[1] whether the previous solve found a cluster.
+//
+// Two routes:
+//  * cold: FP32 multisection -> FP32 inverse iteration -> FP64 refinement
+//    (Rayleigh-Ritz inside near-degenerate clusters);
+//  * fast (warm start, |dv_KS| < 2% of the smallest gap, no clusters): the
+//    previous eigenvectors go straight into the FP64 refinement, the FP32
+//    factorization taken at their FP64 Rayleigh quotients.  Its result is
+//    checked against the Weyl bound |lambda_j - lambda_j^prev| <= |dv|; on
+//    failure (or a refinement cap) the cold route runs.
 template <int kBand>
 __device__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, const double* vks,
                            double* X, bool warm, double dv, const Smem& sm, int lane,
                            EigStats& stats) {
   stats.solves += 1;
+  long long tph = clock64();
   const Stencil st = make_stencil(p.stencil, dx);
   const int nstr = sm.nstr;
   float* a32 = sm.f32;
@@ -519,7 +538,6 @@ __device__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, con
   float* U = R + (size_t)p.kmax * nstr;
   float* W = U + (size_t)p.kmax * nstr;
   const int Kc = K + 1;
-  int flags = 0;
 
   // --- FP32 diagonal and Gershgorin bounds
   double amin = 1e300, amax = -1e300;
@@ -538,400 +556,464 @@ __device__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, con
   const float glo = (float)(amin - rad) - tolabs;
   const float ghi = (float)(amax + rad) + tolabs;
   const float b1f = (float)st.b1, b2f = (float)st.b2;
-  __syncwarp();
-
-  // --- brackets
-  if (lane < Kc) {
-    float lo = glo, hi = ghi;
-    if (warm) {
-      double c = sm.eigprev[lane];
-      double w = dv + 4.0 * tolabs;
-      lo = fmaxf(glo, (float)(c - w));
-      hi = fminf(ghi, (float)(c + w));
-    }
-    sm.lo[lane] = lo;
-    sm.hi[lane] = hi;
-  }
-  __syncwarp();
-  if (warm) {
-    // Verify the warm brackets with one pass of counts at both ends.
-    float sg[kShiftsPerLane];
-    int cn[kShiftsPerLane];
-#pragma unroll
-    for (int s = 0; s < kShiftsPerLane; ++s) {
-      int q = lane * kShiftsPerLane + s;
-      int j = q >> 1;
-      sg[s] = (j < Kc) ? ((q & 1) ? sm.hi[j] : sm.lo[j]) : 0.0f;
-    }
-    sturm_counts<kBand>(a32, N, b1f, b2f, pivmin, sg, cn);
-#pragma unroll
-    for (int s = 0; s < kShiftsPerLane; ++s) {
-      sm.cnt[lane * kShiftsPerLane + s] = cn[s];
-    }
-    __syncwarp();
-    if (lane < Kc) {
-      int clo = sm.cnt[2 * lane], chi = sm.cnt[2 * lane + 1];
-      if (clo > lane) sm.lo[lane] = glo;
-      if (chi <= lane) sm.hi[lane] = ghi;
-    }
-    __syncwarp();
-  }
-
-  // --- multisection
-  int pass = 0;
-  for (; pass < kMaxPasses; ++pass) {
-    bool unres = false;
-    if (lane < Kc) {
-      float lo = sm.lo[lane], hi = sm.hi[lane];
-      float tol = fmaxf(tolabs, 4.0f * FLT_EPSILON * fmaxf(fabsf(lo), fabsf(hi)));
-      unres = (hi - lo) > tol;
-      if (unres && lane > 0 && sm.lo[lane - 1] == lo && sm.hi[lane - 1] == hi) unres = false;
-    }
-    unsigned mask = __ballot_sync(kFull, unres);
-    if (mask == 0u) {
-      // shared brackets that are not yet resolved are covered by their first member
-      bool any = false;
-      if (lane < Kc) {
-        float lo = sm.lo[lane], hi = sm.hi[lane];
-        float tol = fmaxf(tolabs, 4.0f * FLT_EPSILON * fmaxf(fabsf(lo), fabsf(hi)));
-        any = (hi - lo) > tol;
-      }
-      if (__ballot_sync(kFull, any) == 0u) break;
-      // only duplicates remain unresolved: treat every member as unique
-      mask = __ballot_sync(kFull, any);
-    }
-    const int u = __popc(mask);
-    const int P = kSamples / u;
-    float sg[kShiftsPerLane];
-    bool valid[kShiftsPerLane];
-#pragma unroll
-    for (int s = 0; s < kShiftsPerLane; ++s) {
-      int q = lane * kShiftsPerLane + s;
-      int k = q / P;
-      valid[s] = k < u;
-      sg[s] = 0.0f;
-      if (valid[s]) {
-        // k-th set bit of mask
-        unsigned m = mask;
-        for (int t = 0; t < k; ++t) m &= m - 1;
-        int j = __ffs(m) - 1;
-        float lo = sm.lo[j], hi = sm.hi[j];
-        int pp = q - k * P;
-        sg[s] = lo + (hi - lo) * (float)(pp + 1) / (float)(P + 1);
-      }
-    }
-    int cn[kShiftsPerLane];
-    sturm_counts<kBand>(a32, N, b1f, b2f, pivmin, sg, cn);
-    __syncwarp();
-#pragma unroll
-    for (int s = 0; s < kShiftsPerLane; ++s) {
-      int q = lane * kShiftsPerLane + s;
-      sm.sig[q] = sg[s];
-      sm.cnt[q] = valid[s] ? cn[s] : -1;
-    }
-    __syncwarp();
-    if (lane < Kc) {
-      float lo = sm.lo[lane], hi = sm.hi[lane];
-      for (int q = 0; q < kSamples; ++q) {
-        int c = sm.cnt[q];
-        if (c < 0) continue;
-        float s = sm.sig[q];
-        if (c > lane) {
-          hi = fminf(hi, s);
-        } else {
-          lo = fmaxf(lo, s);
-        }
-      }
-      sm.lo[lane] = lo;
-      sm.hi[lane] = hi;
-    }
-    __syncwarp();
-  }
-
-  stats.passes += pass + (warm ? 1 : 0);
-  // --- shifts, clusters
   const float tau = fmaxf(1e-3f, 16.0f * tolabs);
-  if (lane < Kc) sm.eigprev[lane] = 0.5 * ((double)sm.lo[lane] + (double)sm.hi[lane]);
-  __syncwarp();
-  if (lane == 0) {
-    int cid = 0;
-    sm.clus[0] = 0;
-    for (int j = 1; j < Kc; ++j) {
-      if (sm.eigprev[j] - sm.eigprev[j - 1] >= tau) ++cid;
-      sm.clus[j] = cid;
-    }
-  }
-  __syncwarp();
-  bool any_cluster = false;
-  for (int j = 1; j < K; ++j) any_cluster |= (sm.clus[j] == sm.clus[j - 1]);
-  {
-    // occupied / unoccupied boundary inside a cluster: the density (odd Ne) or
-    // the gap (even Ne) is not determined to better than the cluster width
-    const int homo = (ne - 1) / 2, lumo = ne / 2;
-    bool deg = (homo != lumo) ? (sm.clus[homo] == sm.clus[lumo])
-                              : ((homo > 0 && sm.clus[homo - 1] == sm.clus[homo]) ||
-                                 sm.clus[homo] == sm.clus[homo + 1]);
-    deg = deg || (sm.clus[K - 1] == sm.clus[K]);
-    if (deg) flags |= QEX_FLAG_DEGENERATE_FRONTIER;
-  }
-
-  // --- FP32 inverse iteration (lane j owns eigenpair j)
-  if (lane < K) {
-    float* Rj = R + (size_t)lane * nstr;
-    float* Uj = U + (size_t)lane * nstr;
-    float* Wj = W + (size_t)lane * nstr;
-    ldl_factor<kBand>(a32, N, b1f, b2f, (float)sm.eigprev[lane], pivmin, Rj, Uj);
-    const double* Xj = X + (size_t)lane * p.nmax;
-    for (int i = 0; i < N; ++i) Wj[i] = warm ? (float)Xj[i] : pseudo_random(i, lane);
-  }
-  __syncwarp();
-  const int rounds = warm ? 2 : 4;
-  float scale = 1.0f;
-  for (int r = 0; r < rounds; ++r) {
-    if (lane < K) {
-      float mx = ldl_solve<kBand>(N, b2f, R + (size_t)lane * nstr, U + (size_t)lane * nstr,
-                                  W + (size_t)lane * nstr, scale);
-      scale = (mx > 0.0f) ? 1.0f / mx : 1.0f;
-    }
-    __syncwarp();
-    if (any_cluster) {
-      // Gram-Schmidt inside clusters (point-parallel), then rescale.
-      for (int j = 1; j < K; ++j) {
-        if (sm.clus[j] != sm.clus[j - 1]) continue;
-        float sj = __shfl_sync(kFull, scale, j);
-        for (int q = j - 1; q >= 0 && sm.clus[q] == sm.clus[j]; --q) {
-          float sq = __shfl_sync(kFull, scale, q);
-          double dot = 0.0, nq = 0.0;
-          const float* Wq = W + (size_t)q * nstr;
-          float* Wj = W + (size_t)j * nstr;
-          for (int i = lane; i < N; i += kWarp) {
-            double a = (double)Wq[i] * sq, b = (double)Wj[i] * sj;
-            dot = fma(a, b, dot);
-            nq = fma(a, a, nq);
-          }
-          dot = warp_sum(dot);
-          nq = warp_sum(nq);
-          float c = (nq > 0.0) ? (float)(dot / nq) : 0.0f;
-          for (int i = lane; i < N; i += kWarp) Wj[i] = fmaf(-c * sq / sj, Wq[i], Wj[i]);
-          __syncwarp();
-        }
-      }
-    }
-  }
-  // --- FP64 vectors, normalised
-  for (int j = 0; j < K; ++j) {
-    float sj = __shfl_sync(kFull, scale, j);
-    const float* Wj = W + (size_t)j * nstr;
-    double nn = 0.0;
-    for (int i = lane; i < N; i += kWarp) {
-      double a = (double)Wj[i] * sj;
-      nn = fma(a, a, nn);
-    }
-    nn = warp_sum(nn);
-    double inv = (nn > 0.0) ? 1.0 / sqrt(nn) : 0.0;
-    double* Xj = X + (size_t)j * p.nmax;
-    for (int i = lane; i < N; i += kWarp) Xj[i] = (double)Wj[i] * sj * inv;
-  }
-  __syncwarp();
-
-  // --- FP64 Newton refinement: x <- x + (H32 - sigma)^-1 (theta x - H x)
   // residual target: 64 ulp of the operator norm (FP64 floor is ~1 ulp * |H|)
   const double thr = 64.0 * DBL_EPSILON * hnorm;
   double* xs = sm.s64a + kPad64;
   double* ys = sm.s64b + kPad64;
-  bool done_all = false;
-  int step = 0;
-  for (; step < kMaxRefineSteps; ++step) {
-    stats.rq_vectors += K;
-    for (int j = 0; j < K; ++j) {
-      const double* Xj = X + (size_t)j * p.nmax;
-      stage64(sm.s64a, Xj, N, lane);
-      double xx = 0.0, xy = 0.0;
-      for (int i = lane; i < N; i += kWarp) {
-        double x = xs[i];
-        double y = fma(st.c0 + vks[i], x, st.b1 * (xs[i - 1] + xs[i + 1]));
-        if (kBand == 2) y = fma(st.b2, xs[i - 2] + xs[i + 2], y);
-        ys[i] = y;
-        xx = fma(x, x, xx);
-        xy = fma(x, y, xy);
+  __syncwarp();
+
+  bool fast = false;
+  if (warm && sm.aux[1] == 0.0) {
+    double gmin = 1e300;
+    for (int j = 0; j + 1 < K; ++j) gmin = fmin(gmin, sm.eigprev[j + 1] - sm.eigprev[j]);
+    gmin = fmin(gmin, sm.eigprev[K] - sm.aux[0] - sm.eigprev[K - 1]);
+    fast = (dv < 0.02 * gmin) && (gmin > (double)tau);
+  }
+
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    int flags = 0;
+    bool any_cluster = false;
+    if (fast) {
+      if (lane <= K) sm.clus[lane] = lane;
+      if (lane < K) sm.resn[lane] = sm.eigprev[lane];  // keep the previous eigenvalues
+      __syncwarp();
+    } else {
+      // ---------------- cold route: brackets
+      if (lane < Kc) {
+        float lo = glo, hi = ghi;
+        if (warm) {
+          double c = sm.eigprev[lane];
+          double w = dv + (lane == K ? sm.aux[0] : 0.0) + 4.0 * tolabs;
+          lo = fmaxf(glo, (float)(c - w));
+          hi = fminf(ghi, (float)(c + w));
+        }
+        sm.lo[lane] = lo;
+        sm.hi[lane] = hi;
       }
-      xx = warp_sum(xx);
-      xy = warp_sum(xy);
-      const double th = xy / xx;
-      double rr = 0.0;
-      float* Wj = W + (size_t)j * nstr;
-      for (int i = lane; i < N; i += kWarp) {
-        double r = fma(-th, xs[i], ys[i]);
-        rr = fma(r, r, rr);
-        Wj[i] = (float)(-r);
+      __syncwarp();
+      int pass = 0;
+      if (warm) {
+        // verify the warm brackets with one pass of counts at both ends
+        float sg[kShiftsPerLane];
+        int cn[kShiftsPerLane];
+#pragma unroll
+        for (int s = 0; s < kShiftsPerLane; ++s) {
+          int q = lane * kShiftsPerLane + s;
+          int j = q >> 1;
+          sg[s] = (j < Kc) ? ((q & 1) ? sm.hi[j] : sm.lo[j]) : 0.0f;
+        }
+        sturm_counts<kBand>(a32, N, b1f, b2f, pivmin, sg, cn);
+#pragma unroll
+        for (int s = 0; s < kShiftsPerLane; ++s) sm.cnt[lane * kShiftsPerLane + s] = cn[s];
+        __syncwarp();
+        if (lane < Kc) {
+          int clo = sm.cnt[2 * lane], chi = sm.cnt[2 * lane + 1];
+          if (clo > lane) sm.lo[lane] = glo;
+          if (chi <= lane) sm.hi[lane] = ghi;
+        }
+        __syncwarp();
+        pass = 1;
       }
-      rr = warp_sum(rr);
+      // ---------------- multisection
+      for (int it = 0; it < kMaxPasses; ++it) {
+        bool unres = false;
+        if (lane < Kc) {
+          float lo = sm.lo[lane], hi = sm.hi[lane];
+          float tol = fmaxf(tolabs, 4.0f * FLT_EPSILON * fmaxf(fabsf(lo), fabsf(hi)));
+          unres = (hi - lo) > tol;
+          if (unres && lane > 0 && sm.lo[lane - 1] == lo && sm.hi[lane - 1] == hi) unres = false;
+        }
+        unsigned mask = __ballot_sync(kFull, unres);
+        if (mask == 0u) {
+          bool any = false;
+          if (lane < Kc) {
+            float lo = sm.lo[lane], hi = sm.hi[lane];
+            float tol = fmaxf(tolabs, 4.0f * FLT_EPSILON * fmaxf(fabsf(lo), fabsf(hi)));
+            any = (hi - lo) > tol;
+          }
+          if (__ballot_sync(kFull, any) == 0u) break;
+          mask = __ballot_sync(kFull, any);
+        }
+        ++pass;
+        const int u = __popc(mask);
+        const int P = kSamples / u;
+        float sg[kShiftsPerLane];
+        bool valid[kShiftsPerLane];
+#pragma unroll
+        for (int s = 0; s < kShiftsPerLane; ++s) {
+          int q = lane * kShiftsPerLane + s;
+          int k = q / P;
+          valid[s] = k < u;
+          sg[s] = 0.0f;
+          if (valid[s]) {
+            unsigned m = mask;
+            for (int t = 0; t < k; ++t) m &= m - 1;
+            int j = __ffs(m) - 1;
+            float lo = sm.lo[j], hi = sm.hi[j];
+            int pp = q - k * P;
+            sg[s] = lo + (hi - lo) * (float)(pp + 1) / (float)(P + 1);
+          }
+        }
+        int cn[kShiftsPerLane];
+        sturm_counts<kBand>(a32, N, b1f, b2f, pivmin, sg, cn);
+        __syncwarp();
+#pragma unroll
+        for (int s = 0; s < kShiftsPerLane; ++s) {
+          int q = lane * kShiftsPerLane + s;
+          sm.sig[q] = sg[s];
+          sm.cnt[q] = valid[s] ? cn[s] : -1;
+        }
+        __syncwarp();
+        if (lane < Kc) {
+          float lo = sm.lo[lane], hi = sm.hi[lane];
+          for (int q = 0; q < kSamples; ++q) {
+            int c = sm.cnt[q];
+            if (c < 0) continue;
+            float s = sm.sig[q];
+            if (c > lane) {
+              hi = fminf(hi, s);
+            } else {
+              lo = fmaxf(lo, s);
+            }
+          }
+          sm.lo[lane] = lo;
+          sm.hi[lane] = hi;
+        }
+        __syncwarp();
+      }
+      stats.passes += pass;
+      {
+        long long t = clock64();
+        stats.cyc[2] += t - tph;
+        tph = t;
+      }
+      // ---------------- shifts, clusters
+      if (lane < Kc) sm.eigprev[lane] = 0.5 * ((double)sm.lo[lane] + (double)sm.hi[lane]);
+      __syncwarp();
       if (lane == 0) {
-        sm.theta[j] = th;
-        sm.resn[j] = sqrt(rr / xx);
+        int cid = 0;
+        sm.clus[0] = 0;
+        for (int j = 1; j < Kc; ++j) {
+          if (sm.eigprev[j] - sm.eigprev[j - 1] >= tau) ++cid;
+          sm.clus[j] = cid;
+        }
+        sm.aux[0] = 0.0;
+      }
+      __syncwarp();
+      for (int j = 1; j < K; ++j) any_cluster |= (sm.clus[j] == sm.clus[j - 1]);
+      {
+        // occupied / unoccupied boundary inside a cluster: the density (odd Ne)
+        // or the gap (even Ne) is not determined to better than the cluster width
+        const int homo = (ne - 1) / 2, lumo = ne / 2;
+        bool deg = (homo != lumo) ? (sm.clus[homo] == sm.clus[lumo])
+                                  : ((homo > 0 && sm.clus[homo - 1] == sm.clus[homo]) ||
+                                     sm.clus[homo] == sm.clus[homo + 1]);
+        deg = deg || (sm.clus[K - 1] == sm.clus[K]);
+        if (deg) flags |= QEX_FLAG_DEGENERATE_FRONTIER;
+      }
+      // ---------------- FP32 factorization and inverse iteration (lane j: pair j)
+      if (lane < K) {
+        float* Rj = R + (size_t)lane * nstr;
+        float* Uj = U + (size_t)lane * nstr;
+        float* Wj = W + (size_t)lane * nstr;
+        ldl_factor<kBand>(a32, N, b1f, b2f, (float)sm.eigprev[lane], pivmin, Rj, Uj);
+        const double* Xj = X + (size_t)lane * p.nmax;
+        for (int i = 0; i < N; ++i) Wj[i] = warm ? (float)Xj[i] : pseudo_random(i, lane);
+      }
+      __syncwarp();
+      const int rounds = warm ? 2 : 4;
+      float scale = 1.0f;
+      for (int r = 0; r < rounds; ++r) {
+        if (lane < K) {
+          float mx = ldl_solve<kBand>(N, b2f, R + (size_t)lane * nstr, U + (size_t)lane * nstr,
+                                      W + (size_t)lane * nstr, scale);
+          scale = (mx > 0.0f) ? 1.0f / mx : 1.0f;
+        }
+        __syncwarp();
+        if (any_cluster) {
+          // Gram-Schmidt inside clusters (point-parallel)
+          for (int j = 1; j < K; ++j) {
+            if (sm.clus[j] != sm.clus[j - 1]) continue;
+            float sj = __shfl_sync(kFull, scale, j);
+            for (int q = j - 1; q >= 0 && sm.clus[q] == sm.clus[j]; --q) {
+              float sq = __shfl_sync(kFull, scale, q);
+              double dot = 0.0, nq = 0.0;
+              const float* Wq = W + (size_t)q * nstr;
+              float* Wj = W + (size_t)j * nstr;
+              for (int i = lane; i < N; i += kWarp) {
+                double a = (double)Wq[i] * sq, b = (double)Wj[i] * sj;
+                dot = fma(a, b, dot);
+                nq = fma(a, a, nq);
+              }
+              dot = warp_sum(dot);
+              nq = warp_sum(nq);
+              float c = (nq > 0.0) ? (float)(dot / nq) : 0.0f;
+              for (int i = lane; i < N; i += kWarp) Wj[i] = fmaf(-c * sq / sj, Wq[i], Wj[i]);
+              __syncwarp();
+            }
+          }
+        }
+      }
+      // FP64 vectors, normalised
+      for (int j = 0; j < K; ++j) {
+        float sj = __shfl_sync(kFull, scale, j);
+        const float* Wj = W + (size_t)j * nstr;
+        double nn = 0.0;
+        for (int i = lane; i < N; i += kWarp) {
+          double a = (double)Wj[i] * sj;
+          nn = fma(a, a, nn);
+        }
+        nn = warp_sum(nn);
+        double inv = (nn > 0.0) ? 1.0 / sqrt(nn) : 0.0;
+        double* Xj = X + (size_t)j * p.nmax;
+        for (int i = lane; i < N; i += kWarp) Xj[i] = (double)Wj[i] * sj * inv;
+      }
+      __syncwarp();
+      {
+        long long t = clock64();
+        stats.cyc[3] += t - tph;
+        tph = t;
+      }
+    }
+
+    // ---------------- FP64 Newton refinement: x <- x + (H32 - sigma)^-1 (theta x - H x)
+    bool done_all = false;
+    for (int step = 0; step < kMaxRefineSteps; ++step) {
+      stats.rq_vectors += K;
+      for (int j = 0; j < K; ++j) {
+        const double* Xj = X + (size_t)j * p.nmax;
+        stage64(sm.s64a, Xj, N, lane);
+        double xx = 0.0, xy = 0.0;
+        for (int i = lane; i < N; i += kWarp) {
+          double x = xs[i];
+          double y = fma(st.c0 + vks[i], x, st.b1 * (xs[i - 1] + xs[i + 1]));
+          if (kBand == 2) y = fma(st.b2, xs[i - 2] + xs[i + 2], y);
+          ys[i] = y;
+          xx = fma(x, x, xx);
+          xy = fma(x, y, xy);
+        }
+        xx = warp_sum(xx);
+        xy = warp_sum(xy);
+        const double th = xy / xx;
+        double rr = 0.0;
+        float* Wj = W + (size_t)j * nstr;
+        for (int i = lane; i < N; i += kWarp) {
+          double r = fma(-th, xs[i], ys[i]);
+          rr = fma(r, r, rr);
+          Wj[i] = (float)(-r);
+        }
+        rr = warp_sum(rr);
+        if (lane == 0) {
+          sm.theta[j] = th;
+          sm.red[j] = sqrt(rr / xx);
+        }
+        __syncwarp();
+      }
+      if (fast && step == 0 && lane < K) {
+        ldl_factor<kBand>(a32, N, b1f, b2f, (float)sm.theta[lane], pivmin,
+                          R + (size_t)lane * nstr, U + (size_t)lane * nstr);
+      }
+      bool need = false;
+      if (lane < K) {
+        bool inclus = (lane > 0 && sm.clus[lane] == sm.clus[lane - 1]) ||
+                      (lane + 1 < Kc && sm.clus[lane] == sm.clus[lane + 1]);
+        need = inclus ? (step < 3) : (sm.red[lane] > thr);
+      }
+      const unsigned nm = __ballot_sync(kFull, need);
+      if (nm == 0u) {
+        done_all = true;
+        break;
+      }
+      stats.updates += __popc(nm);
+      if (need) {
+        ldl_solve<kBand>(N, b2f, R + (size_t)lane * nstr, U + (size_t)lane * nstr,
+                         W + (size_t)lane * nstr, 1.0f);
+      }
+      __syncwarp();
+      for (int j = 0; j < K; ++j) {
+        if (!((nm >> j) & 1u)) continue;
+        double* Xj = X + (size_t)j * p.nmax;
+        const float* Wj = W + (size_t)j * nstr;
+        for (int i = lane; i < N; i += kWarp) Xj[i] += (double)Wj[i];
       }
       __syncwarp();
     }
-    bool need = false;
-    if (lane < K) {
-      bool inclus = (lane > 0 && sm.clus[lane] == sm.clus[lane - 1]) ||
-                    (lane + 1 < Kc && sm.clus[lane] == sm.clus[lane + 1]);
-      need = inclus ? (step < 3) : (sm.resn[lane] > thr);
-    }
-    const unsigned nm = __ballot_sync(kFull, need);
-    if (nm == 0u) {
-      done_all = true;
-      break;
-    }
-    stats.updates += __popc(nm);
-    if (need) {
-      ldl_solve<kBand>(N, b2f, R + (size_t)lane * nstr, U + (size_t)lane * nstr,
-                       W + (size_t)lane * nstr, 1.0f);
-    }
-    __syncwarp();
-    for (int j = 0; j < K; ++j) {
-      if (!((nm >> j) & 1u)) continue;
-      double* Xj = X + (size_t)j * p.nmax;
-      const float* Wj = W + (size_t)j * nstr;
-      for (int i = lane; i < N; i += kWarp) Xj[i] += (double)Wj[i];
-    }
-    __syncwarp();
-  }
-  if (!done_all) flags |= QEX_FLAG_REFINE_CAP;
 
-  // --- Rayleigh-Ritz inside clusters (FP64)
-  if (any_cluster) {
-    int j0 = 0;
-    while (j0 < K) {
-      int j1 = j0;
-      while (j1 + 1 < K && sm.clus[j1 + 1] == sm.clus[j0]) ++j1;
-      const int s = j1 - j0 + 1;
-      if (s >= 2) {
-        // modified Gram-Schmidt
-        for (int a = j0; a <= j1; ++a) {
-          double* Xa = X + (size_t)a * p.nmax;
-          for (int b = j0; b < a; ++b) {
-            const double* Xb = X + (size_t)b * p.nmax;
-            double d = 0.0;
-            for (int i = lane; i < N; i += kWarp) d = fma(Xa[i], Xb[i], d);
-            d = warp_sum(d);
-            for (int i = lane; i < N; i += kWarp) Xa[i] = fma(-d, Xb[i], Xa[i]);
+    if (fast) {
+      // Weyl check: each eigenvalue moved by at most |dv| (plus rounding)
+      bool ok = done_all;
+      if (lane < K) {
+        double moved = fabs(sm.theta[lane] - sm.resn[lane]);
+        ok = ok && (moved <= dv + 1e-9 * hnorm);
+      }
+      ok = __all_sync(kFull, ok || lane >= K);
+      if (!ok) {
+        // restore the previous eigenvalues as warm brackets and take the cold route
+        if (lane < K) sm.eigprev[lane] = sm.resn[lane];
+        __syncwarp();
+        fast = false;
+        {
+          long long t = clock64();
+          stats.cyc[4] += t - tph;
+          tph = t;
+        }
+        continue;
+      }
+    }
+    if (!done_all) flags |= QEX_FLAG_REFINE_CAP;
+
+    // ---------------- Rayleigh-Ritz inside clusters (FP64); Jacobi rotations
+    // are applied to the vectors directly
+    if (any_cluster) {
+      int j0 = 0;
+      while (j0 < K) {
+        int j1 = j0;
+        while (j1 + 1 < K && sm.clus[j1 + 1] == sm.clus[j0]) ++j1;
+        const int s = j1 - j0 + 1;
+        if (s >= 2) {
+          for (int a = j0; a <= j1; ++a) {
+            double* Xa = X + (size_t)a * p.nmax;
+            for (int b = j0; b < a; ++b) {
+              const double* Xb = X + (size_t)b * p.nmax;
+              double d = 0.0;
+              for (int i = lane; i < N; i += kWarp) d = fma(Xa[i], Xb[i], d);
+              d = warp_sum(d);
+              for (int i = lane; i < N; i += kWarp) Xa[i] = fma(-d, Xb[i], Xa[i]);
+              __syncwarp();
+            }
+            double nn = 0.0;
+            for (int i = lane; i < N; i += kWarp) nn = fma(Xa[i], Xa[i], nn);
+            nn = warp_sum(nn);
+            double inv = 1.0 / sqrt(nn);
+            for (int i = lane; i < N; i += kWarp) Xa[i] *= inv;
             __syncwarp();
           }
-          double nn = 0.0;
-          for (int i = lane; i < N; i += kWarp) nn = fma(Xa[i], Xa[i], nn);
-          nn = warp_sum(nn);
-          double inv = 1.0 / sqrt(nn);
-          for (int i = lane; i < N; i += kWarp) Xa[i] *= inv;
-          __syncwarp();
-        }
-        // projected matrix A = Xc^T H Xc  (s <= kMaxEig, stored in sm.red / f32 scratch)
-        // the FP32 work area (16-byte aligned base) is free now
-        double* A = reinterpret_cast<double*>(sm.f32);
-        double* Q = A + s * s;
-        for (int b = j0; b <= j1; ++b) {
-          stage64(sm.s64a, X + (size_t)b * p.nmax, N, lane);
-          for (int i = lane; i < N; i += kWarp) {
-            double y = fma(st.c0 + vks[i], xs[i], st.b1 * (xs[i - 1] + xs[i + 1]));
-            if (kBand == 2) y = fma(st.b2, xs[i - 2] + xs[i + 2], y);
-            ys[i] = y;
-          }
-          __syncwarp();
-          for (int a = j0; a <= b; ++a) {
-            const double* Xa = X + (size_t)a * p.nmax;
-            double d = 0.0;
-            for (int i = lane; i < N; i += kWarp) d = fma(Xa[i], ys[i], d);
-            d = warp_sum(d);
-            if (lane == 0) {
-              A[(a - j0) * s + (b - j0)] = d;
-              A[(b - j0) * s + (a - j0)] = d;
+          // projected matrix in the (free) FP32 work area, 16-byte aligned
+          double* A = reinterpret_cast<double*>(sm.f32);
+          for (int b = j0; b <= j1; ++b) {
+            stage64(sm.s64a, X + (size_t)b * p.nmax, N, lane);
+            for (int i = lane; i < N; i += kWarp) {
+              double y = fma(st.c0 + vks[i], xs[i], st.b1 * (xs[i - 1] + xs[i + 1]));
+              if (kBand == 2) y = fma(st.b2, xs[i - 2] + xs[i + 2], y);
+              ys[i] = y;
             }
+            __syncwarp();
+            for (int a = j0; a <= b; ++a) {
+              const double* Xa = X + (size_t)a * p.nmax;
+              double d = 0.0;
+              for (int i = lane; i < N; i += kWarp) d = fma(Xa[i], ys[i], d);
+              d = warp_sum(d);
+              if (lane == 0) {
+                A[(a - j0) * s + (b - j0)] = d;
+                A[(b - j0) * s + (a - j0)] = d;
+              }
+            }
+            __syncwarp();
           }
-          __syncwarp();
-        }
-        if (lane == 0) {
-          // cyclic Jacobi on the s x s projected matrix
-          for (int a = 0; a < s; ++a)
-            for (int b = 0; b < s; ++b) Q[a * s + b] = (a == b) ? 1.0 : 0.0;
           for (int sweep = 0; sweep < 30; ++sweep) {
-            double off = 0.0;
-            for (int a = 0; a < s; ++a)
-              for (int b = a + 1; b < s; ++b) off += A[a * s + b] * A[a * s + b];
-            if (off < 1e-30) break;
+            if (lane == 0) {
+              double off = 0.0, dia = 0.0;
+              for (int a = 0; a < s; ++a) {
+                dia += A[a * s + a] * A[a * s + a];
+                for (int b = a + 1; b < s; ++b) off += A[a * s + b] * A[a * s + b];
+              }
+              sm.aux[2] = (off <= 1e-30 * (1.0 + dia)) ? 1.0 : 0.0;
+            }
+            __syncwarp();
+            if (sm.aux[2] != 0.0) break;
             for (int a = 0; a < s; ++a) {
               for (int b = a + 1; b < s; ++b) {
-                double apq = A[a * s + b];
-                if (fabs(apq) < 1e-300) continue;
-                double app = A[a * s + a], aqq = A[b * s + b];
-                double tau2 = (aqq - app) / (2.0 * apq);
-                double t = (tau2 >= 0 ? 1.0 : -1.0) / (fabs(tau2) + sqrt(1.0 + tau2 * tau2));
-                double c = 1.0 / sqrt(1.0 + t * t), sn = t * c;
-                for (int k = 0; k < s; ++k) {
-                  double akp = A[k * s + a], akq = A[k * s + b];
-                  A[k * s + a] = c * akp - sn * akq;
-                  A[k * s + b] = sn * akp + c * akq;
+                if (lane == 0) {
+                  double apq = A[a * s + b], c = 1.0, sn = 0.0;
+                  if (fabs(apq) > 1e-300) {
+                    double app = A[a * s + a], aqq = A[b * s + b];
+                    double tau2 = (aqq - app) / (2.0 * apq);
+                    double t = (tau2 >= 0 ? 1.0 : -1.0) / (fabs(tau2) + sqrt(1.0 + tau2 * tau2));
+                    c = 1.0 / sqrt(1.0 + t * t);
+                    sn = t * c;
+                    for (int k = 0; k < s; ++k) {
+                      double akp = A[k * s + a], akq = A[k * s + b];
+                      A[k * s + a] = c * akp - sn * akq;
+                      A[k * s + b] = sn * akp + c * akq;
+                    }
+                    for (int k = 0; k < s; ++k) {
+                      double apk = A[a * s + k], aqk = A[b * s + k];
+                      A[a * s + k] = c * apk - sn * aqk;
+                      A[b * s + k] = sn * apk + c * aqk;
+                    }
+                  }
+                  sm.aux[3] = c;
+                  sm.aux[4] = sn;
                 }
-                for (int k = 0; k < s; ++k) {
-                  double apk = A[a * s + k], aqk = A[b * s + k];
-                  A[a * s + k] = c * apk - sn * aqk;
-                  A[b * s + k] = sn * apk + c * aqk;
+                __syncwarp();
+                const double c = sm.aux[3], sn = sm.aux[4];
+                if (sn != 0.0) {
+                  double* Xa = X + (size_t)(j0 + a) * p.nmax;
+                  double* Xb = X + (size_t)(j0 + b) * p.nmax;
+                  for (int i = lane; i < N; i += kWarp) {
+                    double xa = Xa[i], xb = Xb[i];
+                    Xa[i] = c * xa - sn * xb;
+                    Xb[i] = sn * xa + c * xb;
+                  }
                 }
-                for (int k = 0; k < s; ++k) {
-                  double qkp = Q[k * s + a], qkq = Q[k * s + b];
-                  Q[k * s + a] = c * qkp - sn * qkq;
-                  Q[k * s + b] = sn * qkp + c * qkq;
-                }
+                __syncwarp();
               }
             }
           }
-          // sort ascending (selection sort on eigenvalues + columns)
+          // ascending order (swap vectors along with the diagonal)
           for (int a = 0; a < s; ++a) {
-            int m = a;
-            for (int b = a + 1; b < s; ++b)
-              if (A[b * s + b] < A[m * s + m]) m = b;
+            if (lane == 0) {
+              int m = a;
+              for (int b = a + 1; b < s; ++b)
+                if (A[b * s + b] < A[m * s + m]) m = b;
+              if (m != a) {
+                double t = A[a * s + a];
+                A[a * s + a] = A[m * s + m];
+                A[m * s + m] = t;
+              }
+              sm.aux[5] = (double)m;
+            }
+            __syncwarp();
+            const int m = (int)sm.aux[5];
             if (m != a) {
-              double t = A[a * s + a];
-              A[a * s + a] = A[m * s + m];
-              A[m * s + m] = t;
-              for (int k = 0; k < s; ++k) {
-                double q = Q[k * s + a];
-                Q[k * s + a] = Q[k * s + m];
-                Q[k * s + m] = q;
+              double* Xa = X + (size_t)(j0 + a) * p.nmax;
+              double* Xm = X + (size_t)(j0 + m) * p.nmax;
+              for (int i = lane; i < N; i += kWarp) {
+                double t = Xa[i];
+                Xa[i] = Xm[i];
+                Xm[i] = t;
               }
             }
+            __syncwarp();
           }
-          for (int a = 0; a < s; ++a) sm.theta[j0 + a] = A[a * s + a];
+          if (lane == 0)
+            for (int a = 0; a < s; ++a) sm.theta[j0 + a] = A[a * s + a];
+          __syncwarp();
         }
-        __syncwarp();
-        // rotate X_c <- X_c Q
-        for (int i = lane; i < N; i += kWarp) {
-          double old[kMaxEig];
-          for (int a = 0; a < s; ++a) old[a] = X[(size_t)(j0 + a) * p.nmax + i];
-          for (int b = 0; b < s; ++b) {
-            double v = 0.0;
-            for (int a = 0; a < s; ++a) v = fma(old[a], Q[a * s + b], v);
-            X[(size_t)(j0 + b) * p.nmax + i] = v;
-          }
-        }
-        __syncwarp();
+        j0 = j1 + 1;
       }
-      j0 = j1 + 1;
     }
-  }
 
-  // --- final normalisation
-  for (int j = 0; j < K; ++j) {
-    double* Xj = X + (size_t)j * p.nmax;
-    double nn = 0.0;
-    for (int i = lane; i < N; i += kWarp) nn = fma(Xj[i], Xj[i], nn);
-    nn = warp_sum(nn);
-    double inv = 1.0 / sqrt(nn);
-    for (int i = lane; i < N; i += kWarp) Xj[i] *= inv;
+    // ---------------- final normalisation and warm-start data
+    for (int j = 0; j < K; ++j) {
+      double* Xj = X + (size_t)j * p.nmax;
+      double nn = 0.0;
+      for (int i = lane; i < N; i += kWarp) nn = fma(Xj[i], Xj[i], nn);
+      nn = warp_sum(nn);
+      double inv = 1.0 / sqrt(nn);
+      for (int i = lane; i < N; i += kWarp) Xj[i] *= inv;
+    }
+    if (lane < K) sm.eigprev[lane] = sm.theta[lane];
+    if (lane == 0) {
+      if (fast) sm.aux[0] += dv;  // eigprev[K] is not refreshed on the fast route
+      sm.aux[1] = any_cluster ? 1.0 : 0.0;
+    }
+    __syncwarp();
+    stats.cyc[4] += clock64() - tph;
+    return flags;
   }
-  // warm-start data for the next call: refined eigenvalues, bisected top one
-  if (lane < K) sm.eigprev[lane] = sm.theta[lane];
-  __syncwarp();
-  return flags;
+  return QEX_FLAG_REFINE_CAP;
 }
 
 // Occupation of orbital j for Ne electrons (two per orbital, last one single
@@ -970,13 +1052,15 @@ __device__ inline void write_stats(const Params& p, int b, const EigStats& e) {
   p.o_stats[4 * b + 1] = e.rq_vectors;
   p.o_stats[4 * b + 2] = e.updates;
   p.o_stats[4 * b + 3] = e.passes;
+  if (p.o_cycles)
+    for (int k = 0; k < 8; ++k) p.o_cycles[8 * b + k] = e.cyc[k];
 }
 
 // ---------------------------------------------------------------------------
 // The kernel
 // ---------------------------------------------------------------------------
 template <int kBand>
-__global__ void __launch_bounds__(kWarp) ks1d_kernel(const __grid_constant__ Params p) {
+__global__ void __launch_bounds__(kWarp, 4) ks1d_kernel(const __grid_constant__ Params p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x;
   const SmemLayout L = smem_layout(p.nmax, p.kmax);
@@ -1011,7 +1095,8 @@ __global__ void __launch_bounds__(kWarp) ks1d_kernel(const __grid_constant__ Par
     double* diffs = ws + (long long)VDIFF * p.nmax;
     double* X = diffs + (long long)p.mix_slots * p.nmax;
     int flags = 0;
-    EigStats est = {0, 0, 0, 0};
+    EigStats est = {0, 0, 0, 0, {0, 0, 0, 0, 0, 0, 0, 0}};
+    long long tmol = clock64();
 
     // external potential and interaction table
     if (p.vext_given) {
@@ -1099,8 +1184,14 @@ __global__ void __launch_bounds__(kWarp) ks1d_kernel(const __grid_constant__ Par
       }
 
       // ---- Hartree and XC on the input density
+      long long tit = clock64();
       stage64(sm.s64a, vn, N, lane);
       hartree(p, N, dx, sm, vh, kt, lane);
+      {
+        long long t = clock64();
+        est.cyc[0] += t - tit;
+        tit = t;
+      }
       if (reflect_xc) {
         for (int i = lane; i < N; i += kWarp) {
           sm.s64a[kPad64 + i] = 0.5 * (vn[i] + vn[N - 1 - i]);
@@ -1116,10 +1207,15 @@ __global__ void __launch_bounds__(kWarp) ks1d_kernel(const __grid_constant__ Par
       }
       dv = warm ? warp_max(dvl) : 0.0;
       __syncwarp();
+      {
+        long long t = clock64();
+        est.cyc[1] += t - tit;
+      }
 
       // ---- eigen-solve and output density
       flags |= eigen_solve<kBand>(p, N, dx, ne, K, vks, X, warm, dv, sm, lane, est);
       warm = true;
+      tit = clock64();
       double tee, gap;
       density_from_orbitals(p, N, dx, ne, K, X, nout, sm, tee, gap, lane);
 
@@ -1144,6 +1240,11 @@ __global__ void __launch_bounds__(kWarp) ks1d_kernel(const __grid_constant__ Par
       const double exc = xc_eval(p, N, dx, sm, false, nullptr, nullptr, false, lane);
       const double energy = tee - eks + eh + exc + eext;
       if (p.reflect) flip_avg_global(nout, N, lane);
+      {
+        long long t = clock64();
+        est.cyc[5] += t - tit;
+        tit = t;
+      }
 
       if (p.mode == kModeIteration) {
         if (lane == 0) {
@@ -1213,7 +1314,9 @@ __global__ void __launch_bounds__(kWarp) ks1d_kernel(const __grid_constant__ Par
         if (p.o_f) p.o_f[r0 + i] = vf[i];
       }
       __syncwarp();
+      est.cyc[6] += clock64() - tit;
     }
+    est.cyc[7] = clock64() - tmol;
     if (p.mode == kModeScf) {
       if (p.o_final)
         for (int i = lane; i < N; i += kWarp) p.o_final[off + i] = vn[i];
@@ -1317,6 +1420,7 @@ int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_opt
     P.o_status = out->status;
     P.o_iters = out->iterations_run;
     P.o_stats = out->stats;
+    P.o_cycles = reinterpret_cast<long long*>(out->phase_cycles);
   }
   size_t need = 0;
   qex_ks1d_workspace_size(o, num_molecules, &need);

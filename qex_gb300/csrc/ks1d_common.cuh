@@ -12,7 +12,7 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWarp = 32;
 constexpr int kMaxEig = QEX_KS1D_MAX_EIGENPAIRS;  // eigenpairs computed per molecule
 constexpr int kMaxBis = kMaxEig + 1;              // eigenvalues bracketed (one extra)
-constexpr int kShiftsPerLane = 2;                 // Sturm shifts evaluated per lane per pass
+constexpr int kShiftsPerLane = 4;                 // Sturm shifts evaluated per lane per pass
 constexpr int kSamples = kWarp * kShiftsPerLane;
 constexpr int kMaxPasses = 48;
 constexpr int kMaxRefineSteps = 10;

@@ -107,11 +107,23 @@ class PackedBatch:
             nn[i] = k
         start = np.array([m.grid_start for m in self.molecules], dtype=np.float64)
         dx = np.array([m.grid_spacing for m in self.molecules], dtype=np.float64)
+        kk = ne // 2 + 1
         if sort and B:
-            cost = ng.astype(np.int64) * (ne // 2 + 1)
-            order = np.argsort(-cost, kind="stable").astype(np.int32)
+            # eigenpair count first (it sizes shared memory), then grid size
+            order = np.lexsort((-ng.astype(np.int64), -kk)).astype(np.int32)
         else:
             order = np.arange(B, dtype=np.int32)
+        self.order_host = order
+        # contiguous runs of equal eigenpair count in processing order
+        self.buckets = []
+        if sort and B:
+            ks = kk[order]
+            first = 0
+            for i in range(1, B + 1):
+                if i == B or ks[i] != ks[first]:
+                    sel = order[first:i]
+                    self.buckets.append((first, i - first, int(ne[sel].max()), int(ng[sel].max())))
+                    first = i
         dev = torch.device("cuda") if device is None else torch.device(device)
         self.device = dev
         t = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), device=dev).to(dt)
@@ -119,6 +131,7 @@ class PackedBatch:
         self.offsets = t(off, torch.int64)
         self.grid_start = t(start, torch.float64)
         self.grid_spacing = t(dx, torch.float64)
+        assert self.grid_start.numel() == B and self.grid_spacing.numel() == B
         self.num_electrons = t(ne, torch.int32)
         self.num_nuclei = t(nn, torch.int32)
         self.locations = t(loc.reshape(-1), torch.float64)
@@ -135,9 +148,10 @@ class PackedBatch:
             self.external_potential = t(np.concatenate(
                 [np.asarray(m.external_potential, np.float64) for m in self.molecules]), torch.float64)
 
-    def c_batch(self, initial_density=None, external_potential=None) -> N.Ks1dBatch:
+    def c_batch(self, initial_density=None, external_potential=None, start=0,
+                count=None) -> N.Ks1dBatch:
         b = N.Ks1dBatch()
-        b.num_molecules = self.size
+        b.num_molecules = self.size if count is None else count
         b.num_grids = N.ptr(self.num_grids)
         b.grid_offsets = N.ptr(self.offsets)
         b.grid_start = N.ptr(self.grid_start)
@@ -150,7 +164,7 @@ class PackedBatch:
         vext = external_potential if external_potential is not None else self.external_potential
         b.initial_density = N.ptr(dens)
         b.external_potential = N.ptr(vext)
-        b.order = N.ptr(self.order)
+        b.order = N.ptr(self.order) + 4 * start if self.size else None
         return b
 
     def split(self, packed, per_iteration=0):
@@ -235,6 +249,7 @@ class Ks1dEngine:
         out["status"] = torch.zeros((B,), dtype=torch.int32, device=batch.device)
         out["iterations_run"] = torch.zeros((B,), dtype=torch.int32, device=batch.device)
         out["stats"] = torch.zeros((B, 4), dtype=torch.int32, device=batch.device)
+        out["phase_cycles"] = torch.zeros((B, 8), dtype=torch.int64, device=batch.device)
         return out
 
     @staticmethod
@@ -252,30 +267,74 @@ class Ks1dEngine:
         o.status = N.ptr(out.get("status"))
         o.iterations_run = N.ptr(out.get("iterations_run"))
         o.stats = N.ptr(out.get("stats"))
+        o.phase_cycles = N.ptr(out.get("phase_cycles"))
         return o
 
     def solve(self, batch: PackedBatch, xc, cfg: SolveConfig, records=RECORD_ALL, out=None,
-              initial_density=None):
-        """Run the full SCF for every molecule of ``batch`` (one kernel launch)."""
+              initial_density=None, bucketed=True):
+        """Run the full SCF for every molecule of ``batch``.
+
+        With ``bucketed`` the batch is split into runs of equal eigenpair count
+        (shared memory per warp scales with it), launched concurrently on
+        forked streams; otherwise one launch covers the whole batch.
+        """
+        torch = N.require_cuda()
         functional, params = resolve(xc)
         vext_given = batch.external_potential is not None
-        opts = _options(cfg, batch, vext_given)
         spec, keep = functional.spec(params, _convention(cfg))
         if out is None:
             out = self.allocate_outputs(batch, cfg, records)
-        nbytes = ctypes.c_size_t()
-        N.check(self.lib.qex_ks1d_workspace_size(ctypes.byref(opts), batch.size, ctypes.byref(nbytes)),
-                "qex_ks1d_workspace_size")
-        ws = self.workspace.get(nbytes.value)
-        cb = batch.c_batch(initial_density=initial_density)
         co = self._c_outputs(out)
-        rc = self.lib.qex_ks1d_solve(ctypes.byref(cb), ctypes.byref(opts), ctypes.byref(spec),
-                                     ctypes.byref(co), ctypes.c_void_p(ws.data_ptr()),
-                                     ctypes.c_size_t(ws.numel()), self._stream())
-        N.check(rc, "qex_ks1d_solve")
-        self.last_launches = self.lib.qex_last_launch_count()
+        parts = batch.buckets if (bucketed and len(batch.buckets) > 1) else [
+            (0, batch.size, batch.max_num_electrons, batch.max_num_grids)]
+        plans = []
+        total = 0
+        for start, count, ne_max, ng_max in parts:
+            opts = _options(cfg, batch, vext_given)
+            opts.max_num_electrons = max(ne_max, 1)
+            opts.max_num_grids = max(ng_max, 5)
+            nbytes = ctypes.c_size_t()
+            N.check(self.lib.qex_ks1d_workspace_size(ctypes.byref(opts), count, ctypes.byref(nbytes)),
+                    "qex_ks1d_workspace_size")
+            aligned = (nbytes.value + 255) // 256 * 256
+            plans.append((start, count, opts, total, aligned))
+            total += aligned
+        ws = self.workspace.get(total)
+        base = ws.data_ptr()
+        cur = torch.cuda.current_stream()
+        launches = 0
+        if len(plans) == 1:
+            streams = [cur]
+        else:
+            streams = self._streams(len(plans))
+            ev = torch.cuda.Event()
+            ev.record(cur)
+            for st in streams:
+                st.wait_event(ev)
+        for (start, count, opts, off, nb), st in zip(plans, streams):
+            cb = batch.c_batch(initial_density=initial_density, start=start, count=count)
+            rc = self.lib.qex_ks1d_solve(ctypes.byref(cb), ctypes.byref(opts), ctypes.byref(spec),
+                                         ctypes.byref(co), ctypes.c_void_p(base + off),
+                                         ctypes.c_size_t(nb), ctypes.c_void_p(st.cuda_stream))
+            N.check(rc, "qex_ks1d_solve")
+            launches += self.lib.qex_last_launch_count()
+        if len(plans) > 1:
+            for st in streams:
+                e = torch.cuda.Event()
+                e.record(st)
+                cur.wait_event(e)
+            ws.record_stream(cur)
+        self.last_launches = launches
         del keep
         return out
+
+    def _streams(self, n):
+        torch = N.require_cuda()
+        pool = getattr(self, "_stream_pool", [])
+        while len(pool) < n:
+            pool.append(torch.cuda.Stream())
+        self._stream_pool = pool
+        return pool[:n]
 
     def iteration(self, batch: PackedBatch, xc, cfg: SolveConfig, density, external_potential):
         """One KS iteration per molecule (unmixed output), records of length 1."""

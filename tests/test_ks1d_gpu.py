@@ -232,8 +232,10 @@ def test_reflection_symmetry_matches_oracle(qx, convention):
     qex, od = qx
     mols = [(257, np.array([-1.1, 1.1]), np.array([1.0, 1.0]), 2),
             (385, np.array([-2.0, 0.0, 2.0]), np.array([1.0, 2.0, 1.0]), 4)]
-    xc = qex.LDAExpCoulomb() if convention == "local" else qex.PowerXC(-0.73855, 1 / 3, 1e-10)
-    oxc = o.LDAExpCoulomb() if convention == "local" else o.PowerXC(-0.73855, 1 / 3, 1e-10)
+    # the LDA in both conventions (the power functional binds degenerate edge
+    # states on these grids, which leaves the reference's density undetermined)
+    xc = qex.LDAExpCoulomb()
+    oxc = o.LDAExpCoulomb()
     batch, host = _run_batch(od, mols, xc, convention, 6, reflection=True)
     ref = _oracle_batch(mols, oxc, convention, 6, reflection=True)
     dens = batch.split(host["final_density"])
