@@ -111,7 +111,7 @@ __host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax) {
   L.s64b = off;
   off += sizeof(double) * (nmax + 2 * kPad64);
   L.f32 = off;
-  size_t xc_floats = 2 * (size_t)(nmax + 2 * kPadMlp);
+  size_t xc_floats = 2 * (size_t)(nmax + 2 * kPadMlp) + (size_t)kMlpScratch * kWarp;
   size_t hart_floats = 2 * (size_t)nmax + 2;  // one FP64 scan vector
   size_t eig_floats = (1 + 3 * (size_t)kmax) * L.nstr;
   size_t f = xc_floats > eig_floats ? xc_floats : eig_floats;
@@ -126,6 +126,8 @@ __host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax) {
   off += sizeof(double) * kMaxBis * 3 + sizeof(int) * kMaxBis;
   off = (off + 7) & ~(size_t)7;
   off += sizeof(double) * 32 + sizeof(double) * 8;  // red, aux
+  off = (off + 15) & ~(size_t)15;
+  off += sizeof(float) * kMlpFloats;  // MLP weights
   L.total = (off + 127) & ~(size_t)127;
   return L;
 }
@@ -144,6 +146,7 @@ struct Smem {
   int* clus;
   double* red;
   double* aux;
+  float* mlpw;
   int nstr;
 };
 
@@ -174,6 +177,9 @@ __device__ inline Smem carve(unsigned char* base, const SmemLayout& L) {
   s.red = reinterpret_cast<double*>(p);
   p += sizeof(double) * 32;
   s.aux = reinterpret_cast<double*>(p);
+  p += sizeof(double) * 8;
+  p = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 15) & ~(uintptr_t)15);
+  s.mlpw = reinterpret_cast<float*>(p);
   s.nstr = L.nstr;
   return s;
 }
@@ -356,18 +362,18 @@ __device__ double xc_eval(const Params& p, int N, double dx, const Smem& sm, boo
       vacc[i] = 0.0f;
     }
     __syncwarp();
+    float* scr = vacc + (p.nmax + 2 * kPadMlp) + lane;  // per-lane MLP scratch, stride 32
     const int rounds = (N + kWarp - 1) / kWarp;
     for (int r = 0; r < rounds; ++r) {
       const int i = r * kWarp + lane;
       const bool act = i < N;
-      float w[QEX_MLP_WINDOW], gw[QEX_MLP_WINDOW];
-#pragma unroll
-      for (int k = 0; k < QEX_MLP_WINDOW; ++k) w[k] = act ? n32[i + k] : 0.0f;
+      // inactive lanes evaluate a harmless all-zero window
+      const float* win = act ? (n32 + i) : (n32 + N + kPadMlp);
       float f;
       if (want_v) {
-        f = mlp_point<true>(p.mlp, w, gw);
+        f = mlp_point<true>(sm.mlpw, win, act ? 1 : 0, scr, kWarp);
       } else {
-        f = mlp_point<false>(p.mlp, w, gw);
+        f = mlp_point<false>(sm.mlpw, win, act ? 1 : 0, scr, kWarp);
       }
       double ni = act ? n[i] : 0.0;
       if (act) {
@@ -380,9 +386,9 @@ __device__ double xc_eval(const Params& p, int N, double dx, const Smem& sm, boo
       }
       if (want_v) {
         const float up = local ? (float)ni * ninv : ninv;
-#pragma unroll
+        __syncwarp();
         for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
-          if (act) vacc[i + k] += up * gw[k];
+          if (act) vacc[i + k] += up * scr[k * kWarp];
           __syncwarp();
         }
         if (act && local) vacc[i + kPadMlp] += f;
@@ -429,6 +435,7 @@ __device__ inline void sturm_counts(const float* a32, int N, float b1, float b2,
     c[s] = 0;
   }
   const float b2sq = b2 * b2;
+#pragma unroll 2
   for (int i = 0; i < N; ++i) {
     const float a = a32[i];
 #pragma unroll
@@ -459,6 +466,7 @@ __device__ inline void ldl_factor(const float* a32, int N, float b1, float b2, f
                                   float pivmin, float* R, float* U) {
   float r1 = 0.0f, r2 = 0.0f, u1 = 0.0f;
   const float b2sq = b2 * b2;
+#pragma unroll 2
   for (int i = 0; i < N; ++i) {
     float d, u = 0.0f;
     if (kBand == 2) {
@@ -471,7 +479,7 @@ __device__ inline void ldl_factor(const float* a32, int N, float b1, float b2, f
       d = fmaf(-u, b1, a32[i] - sigma);
     }
     if (fabsf(d) < pivmin) d = (d < 0.0f) ? -pivmin : pivmin;
-    float r = 1.0f / d;
+    float r = __fdividef(1.0f, d);
     R[i] = r;
     U[i] = u;
     r2 = r1;
@@ -484,19 +492,22 @@ __device__ inline void ldl_factor(const float* a32, int N, float b1, float b2, f
 template <int kBand>
 __device__ inline float ldl_solve(int N, float b2, const float* R, const float* U, float* W,
                                   float scale) {
+  // Branch-free sweeps: the couplings that reach outside [0, N) multiply a
+  // zero carry (z2, y1, y2 start at 0), so they read a clamped in-range index.
   float z1 = 0.0f, z2 = 0.0f;
+#pragma unroll 4
   for (int i = 0; i < N; ++i) {
-    float z = W[i] * scale - U[i] * z1;
-    if (kBand == 2 && i >= 2) z = fmaf(-b2 * R[i - 2], z2, z);
+    float z = fmaf(-U[i], z1, W[i] * scale);
+    if (kBand == 2) z = fmaf(-b2 * R[max(i - 2, 0)], z2, z);
     W[i] = z * R[i];
     z2 = z1;
     z1 = z;
   }
   float y1 = 0.0f, y2 = 0.0f, mx = 0.0f;
+#pragma unroll 4
   for (int i = N - 1; i >= 0; --i) {
-    float y = W[i];
-    if (i + 1 < N) y = fmaf(-U[i + 1], y1, y);
-    if (kBand == 2 && i + 2 < N) y = fmaf(-b2 * R[i], y2, y);
+    float y = fmaf(-U[min(i + 1, N - 1)], y1, W[i]);
+    if (kBand == 2) y = fmaf(-b2 * R[i], y2, y);
     W[i] = y;
     mx = fmaxf(mx, fabsf(y));
     y2 = y1;
@@ -1060,11 +1071,13 @@ __device__ inline void write_stats(const Params& p, int b, const EigStats& e) {
 // The kernel
 // ---------------------------------------------------------------------------
 template <int kBand>
-__global__ void __launch_bounds__(kWarp, 4) ks1d_kernel(const __grid_constant__ Params p) {
+__global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__ Params p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x;
   const SmemLayout L = smem_layout(p.nmax, p.kmax);
   Smem sm = carve(smem_raw, L);
+  if (p.xc_kind == QEX_XC_WINDOW_MLP) stage_mlp_weights(p.mlp, sm.mlpw, lane, kWarp);
+  __syncwarp();
 
   for (;;) {
     int slot = 0;

@@ -31,7 +31,7 @@ struct XcParams {
   MlpParams mlp;
 };
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 64;
 
 __device__ double block_sum(double v, double* red) {
   v = warp_sum(v);
@@ -49,6 +49,11 @@ __device__ double block_sum(double v, double* red) {
 
 __global__ void __launch_bounds__(kThreads) xc1d_kernel(const __grid_constant__ XcParams p) {
   __shared__ double red[kThreads / kWarp];
+  __shared__ __align__(16) float wsm[kMlpFloats];
+  __shared__ float wbuf[QEX_MLP_WINDOW * kThreads];
+  __shared__ float sbuf[kMlpScratch * kThreads];
+  if (p.kind == QEX_XC_WINDOW_MLP) stage_mlp_weights(p.mlp, wsm, threadIdx.x, kThreads);
+  __syncthreads();
   const int b = blockIdx.x;
   if (b >= p.num_molecules) return;
   const int N = p.num_grids[b];
@@ -60,18 +65,18 @@ __global__ void __launch_bounds__(kThreads) xc1d_kernel(const __grid_constant__ 
   if (p.kind == QEX_XC_WINDOW_MLP) {
     const float ninv = p.mlp.norm_inv;
     for (int i = threadIdx.x; i < N; i += kThreads) {
-      float w[QEX_MLP_WINDOW], gw[QEX_MLP_WINDOW];
 #pragma unroll
       for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
         int j = i - kPadMlp + k;
-        w[k] = (j >= 0 && j < N) ? (float)n[j] * ninv : 0.0f;
+        wbuf[k * kThreads + threadIdx.x] = (j >= 0 && j < N) ? (float)n[j] * ninv : 0.0f;
       }
-      float f = mlp_point<true>(p.mlp, w, gw);
+      float* scr = sbuf + threadIdx.x;
+      float f = mlp_point<true>(wsm, wbuf + threadIdx.x, kThreads, scr, kThreads);
       if (p.values) p.values[off + i] = (double)f;
       e += local ? (double)f * n[i] : (double)f;
       const float up = local ? (float)n[i] * ninv : ninv;
-#pragma unroll
-      for (int k = 0; k < QEX_MLP_WINDOW; ++k) p.grad[(off + i) * QEX_MLP_WINDOW + k] = up * gw[k];
+      for (int k = 0; k < QEX_MLP_WINDOW; ++k)
+        p.grad[(off + i) * QEX_MLP_WINDOW + k] = up * scr[k * kThreads];
     }
     __syncthreads();
     if (p.potential) {

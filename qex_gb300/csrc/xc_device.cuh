@@ -62,51 +62,119 @@ __device__ inline float silu_d(float z, float& d) {
 }
 
 // Window-MLP forward (and optionally input gradient) for one point.
-// w: 17 inputs already divided by the normalization.
+// W: the 577 weights in shared memory, 16-byte aligned, in MlpParams order
+// (w1 [17][16], b1, w2 [16][16], b2, w3, b3); every weight read is a
+// broadcast 16-byte load of (part of) one weight row, issued next to its use.
+// win: the 17 window inputs (already divided by the normalization), read from
+// shared memory with stride `wstride`.  scr: per-lane shared scratch of 48
+// floats at stride `ss` (hidden activations and derivatives).  With kGrad,
+// scr[k * ss] (k < 17) receives d eps / d input_k on return.
+constexpr int kMlpFloats = 580;  // 577 weights padded to 16 bytes
+constexpr int kMlpScratch = 48;
+
+__device__ inline void mlp_load4(const float* W, int off, float& a, float& b, float& c, float& d) {
+  float4 r = *reinterpret_cast<const float4*>(W + off);
+  a = r.x;
+  b = r.y;
+  c = r.z;
+  d = r.w;
+}
+
 template <bool kGrad>
-__device__ inline float mlp_point(const MlpParams& m, const float* w, float* gw) {
-  float z1[QEX_MLP_HIDDEN], d1[QEX_MLP_HIDDEN], h1[QEX_MLP_HIDDEN];
+__device__ inline float mlp_point(const float* W, const float* win, int wstride, float* scr,
+                                  int ss) {
+  float z[QEX_MLP_HIDDEN];
 #pragma unroll
-  for (int h = 0; h < QEX_MLP_HIDDEN; ++h) {
-    float z = m.b1[h];
+  for (int q = 0; q < 4; ++q) mlp_load4(W, 272 + 4 * q, z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+#pragma unroll 1
+  for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
+    const float x = win[k * wstride];
 #pragma unroll
-    for (int k = 0; k < QEX_MLP_WINDOW; ++k) z = fmaf(w[k], m.w1[k * QEX_MLP_HIDDEN + h], z);
-    z1[h] = z;
-    h1[h] = silu_d(z, d1[h]);
+    for (int q = 0; q < 4; ++q) {
+      float a, b, c, d;
+      mlp_load4(W, 16 * k + 4 * q, a, b, c, d);
+      z[4 * q] = fmaf(x, a, z[4 * q]);
+      z[4 * q + 1] = fmaf(x, b, z[4 * q + 1]);
+      z[4 * q + 2] = fmaf(x, c, z[4 * q + 2]);
+      z[4 * q + 3] = fmaf(x, d, z[4 * q + 3]);
+    }
   }
-  float d2[QEX_MLP_HIDDEN];
-  float out = m.b3;
 #pragma unroll
   for (int h = 0; h < QEX_MLP_HIDDEN; ++h) {
-    float z = m.b2[h];
+    float d;
+    scr[h * ss] = silu_d(z[h], d);  // h1
+    scr[(16 + h) * ss] = d;         // d1
+  }
 #pragma unroll
-    for (int k = 0; k < QEX_MLP_HIDDEN; ++k) z = fmaf(h1[k], m.w2[k * QEX_MLP_HIDDEN + h], z);
-    float a = silu_d(z, d2[h]);
-    out = fmaf(a, m.w3[h], out);
+  for (int q = 0; q < 4; ++q) mlp_load4(W, 544 + 4 * q, z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+#pragma unroll 1
+  for (int k = 0; k < QEX_MLP_HIDDEN; ++k) {
+    const float x = scr[k * ss];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float a, b, c, d;
+      mlp_load4(W, 288 + 16 * k + 4 * q, a, b, c, d);
+      z[4 * q] = fmaf(x, a, z[4 * q]);
+      z[4 * q + 1] = fmaf(x, b, z[4 * q + 1]);
+      z[4 * q + 2] = fmaf(x, c, z[4 * q + 2]);
+      z[4 * q + 3] = fmaf(x, d, z[4 * q + 3]);
+    }
+  }
+  float out = W[576];
+  float g2[QEX_MLP_HIDDEN];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    float w3[4];
+    mlp_load4(W, 560 + 4 * q, w3[0], w3[1], w3[2], w3[3]);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      float d;
+      float a = silu_d(z[4 * q + e], d);
+      out = fmaf(a, w3[e], out);
+      g2[4 * q + e] = w3[e] * d;
+    }
   }
   if (kGrad) {
-    float g2[QEX_MLP_HIDDEN];
-#pragma unroll
-    for (int h = 0; h < QEX_MLP_HIDDEN; ++h) g2[h] = m.w3[h] * d2[h];
-    float g1[QEX_MLP_HIDDEN];
-#pragma unroll
+#pragma unroll 1
     for (int k = 0; k < QEX_MLP_HIDDEN; ++k) {
       float a = 0.0f;
 #pragma unroll
-      for (int h = 0; h < QEX_MLP_HIDDEN; ++h) a = fmaf(m.w2[k * QEX_MLP_HIDDEN + h], g2[h], a);
-      g1[k] = a * d1[k];
+      for (int q = 0; q < 4; ++q) {
+        float r0, r1, r2, r3;
+        mlp_load4(W, 288 + 16 * k + 4 * q, r0, r1, r2, r3);
+        a = fmaf(r0, g2[4 * q], a);
+        a = fmaf(r1, g2[4 * q + 1], a);
+        a = fmaf(r2, g2[4 * q + 2], a);
+        a = fmaf(r3, g2[4 * q + 3], a);
+      }
+      scr[(32 + k) * ss] = a * scr[(16 + k) * ss];  // g1 = (W2 g2) * d1
     }
+    float g1[QEX_MLP_HIDDEN];
 #pragma unroll
+    for (int h = 0; h < QEX_MLP_HIDDEN; ++h) g1[h] = scr[(32 + h) * ss];
+#pragma unroll 1
     for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
       float a = 0.0f;
 #pragma unroll
-      for (int h = 0; h < QEX_MLP_HIDDEN; ++h) a = fmaf(m.w1[k * QEX_MLP_HIDDEN + h], g1[h], a);
-      gw[k] = a;
+      for (int q = 0; q < 4; ++q) {
+        float r0, r1, r2, r3;
+        mlp_load4(W, 16 * k + 4 * q, r0, r1, r2, r3);
+        a = fmaf(r0, g1[4 * q], a);
+        a = fmaf(r1, g1[4 * q + 1], a);
+        a = fmaf(r2, g1[4 * q + 2], a);
+        a = fmaf(r3, g1[4 * q + 3], a);
+      }
+      scr[k * ss] = a;  // h1 / d1 slots are dead here
     }
   }
   return out;
 }
 
+// Copy the weights of a by-value MlpParams into shared memory (one warp or CTA).
+__device__ inline void stage_mlp_weights(const MlpParams& m, float* dst, int tid, int nthreads) {
+  const float* src = reinterpret_cast<const float*>(&m);
+  for (int i = tid; i < kMlpFloats; i += nthreads) dst[i] = (i < 577) ? src[i] : 0.0f;
+}
 
 // Host: copy the flat HOST parameter vector of a qex_xc_spec into MlpParams.
 inline bool fill_mlp_params(MlpParams& m, const qex_xc_spec* xc) {
