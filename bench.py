@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 METRIC = "converged SCF solves/sec at 1e-8 Ha (batched 1D, 4096 molecules)"
 UNIT = "solves/s"
 E_CONV = 1e-8
-FP64_PEAK_TFLOPS = 1.18  # measured FP64 FMA throughput on this GB300 pool (profiles/fp64_peak.txt)
+FP64_PEAK_FALLBACK_TFLOPS = 1.18  # FP64 FMA throughput measured on this GB300 pool
 
 
 def workload(batch_size, seed):
@@ -268,6 +268,12 @@ def run_ours(args, rank, world):
     if rank != 0:
         return None
 
+    try:
+        peak64, peak32 = _native.measure_fma_peak()
+        peak_src = "FP64 FMA throughput measured live by qex_probe_fma_peak in this run"
+    except RuntimeError:
+        peak64, peak32 = FP64_PEAK_FALLBACK_TFLOPS, None
+        peak_src = "fallback: FP64 FMA probe measured earlier on this pool"
     w64 = fp64_flops(mols, iters_run, stats)
     w32 = fp32_flops_mlp(mols, iters_run)
     achieved = w64 / step_s / 1e12
@@ -280,6 +286,9 @@ def run_ours(args, rank, world):
                "sample": f"{cn} molecules of the same workload, reference algorithm (dense "
                          f"eigh, materialised Hartree kernel), {cconv} converged, {dt:.1f} s wall",
                "total_solves_per_s": cn / dt}
+    serving = None
+    if world == 1 and not args.no_serving:
+        serving = run_serving(args)
     line = {
         "metric": METRIC, "value": total_conv / step_s, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
@@ -295,15 +304,45 @@ def run_ours(args, rank, world):
         "e2e": {"value": total_conv / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
-                     "unit": "TFLOP/s", "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
-                     "peak_source": "measured FP64 FMA probe on this pool (profiles)",
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64,
+                     "unit": "TFLOP/s", "frac": achieved / peak64, "traffic": None,
+                     "peak_source": peak_src, "fp32_peak_tflops": peak32,
                      "fp64_flops_per_step": w64, "fp32_mlp_flops_per_step": w32},
         "clocks": sampler.summary(),
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if serving is not None:
+        line["serving"] = serving
     return line
+
+
+def run_serving(args):
+    """Served (continuous batching) vs plain one-at-a-time form on a Poisson stream of
+    plain-configuration 1D requests (513 points, H2-like, LDA, 3-point stencil, 20 iterations)."""
+    import qex_gb300
+    from qex_gb300 import serving as sv
+    from qex_gb300.od import engine as eng
+
+    cfg = eng.SolveConfig(num_iterations=20, alpha=0.5, alpha_decay=0.9, num_mixing_iterations=1,
+                          convention="local", stencil=3)
+    xc = qex_gb300.LDAExpCoulomb()
+    out = {"workload": "Poisson stream of 1D requests: 513 points, dx 0.08, unit charges at +-R, "
+                       "R ~ U[0.5,1.5], exp-Coulomb LDA, 3-point kinetic, 20 iterations"}
+    server = sv.ScfServer(xc, cfg, max_inflight=16, max_batch=1024)
+    server.serve(sv.config1_requests(sv.poisson_arrivals(500, 0.05, seed=99), seed=99))  # warm-up
+    for rate in args.serving_rates:
+        arr = sv.poisson_arrivals(rate, args.serving_seconds, seed=int(rate))
+        reqs = sv.config1_requests(arr, seed=int(rate))
+        server = sv.ScfServer(xc, cfg, max_inflight=16, max_batch=1024)
+        done = server.serve(reqs)
+        s = sv.latency_summary(done)
+        s["launches"] = server.launches
+        out[f"served_rate_{int(rate)}"] = s
+    arr = sv.poisson_arrivals(args.plain_rate, args.plain_seconds, seed=7)
+    done = sv.serve_plain(xc, cfg, sv.config1_requests(arr, seed=7))
+    out[f"plain_rate_{int(args.plain_rate)}"] = sv.latency_summary(done)
+    return out
 
 
 def run_reference(args, rank, world):
@@ -349,6 +388,11 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-rates", type=float, nargs="*", default=[1000.0, 5000.0])
+    ap.add_argument("--serving-seconds", type=float, default=1.0)
+    ap.add_argument("--plain-rate", type=float, default=50.0)
+    ap.add_argument("--plain-seconds", type=float, default=1.0)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -120,6 +120,10 @@ _SIGNATURES = {
     "qex_ks1d_noninteracting": (ctypes.c_int, [ctypes.POINTER(Ks1dBatch),
                                                ctypes.POINTER(Ks1dOptions), _c_p, _c_p, _c_p,
                                                _c_p, _c_p, _c_p, ctypes.c_size_t, _c_p]),
+    "qex_probe_workspace_size": (ctypes.c_size_t, []),
+    "qex_probe_fma_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double), _c_p, ctypes.c_size_t,
+                                          _c_p]),
     "qex_version": (ctypes.c_char_p, []),
     "qex_last_launch_count": (ctypes.c_int, []),
 }
@@ -146,6 +150,17 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
             fn.argtypes = args
         _lib = lib
         return lib
+
+
+def measure_fma_peak():
+    """(FP64, FP32) FMA throughput in TFLOP/s on the current device."""
+    torch = require_cuda()
+    lib = load()
+    ws = torch.empty(lib.qex_probe_workspace_size(), dtype=torch.uint8, device="cuda")
+    f64, f32 = ctypes.c_double(), ctypes.c_double()
+    check(lib.qex_probe_fma_peak(ctypes.byref(f64), ctypes.byref(f32), ws.data_ptr(), ws.numel(),
+                                 torch.cuda.current_stream().cuda_stream), "qex_probe_fma_peak")
+    return f64.value, f32.value
 
 
 def declared_symbols():

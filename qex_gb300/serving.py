@@ -1,0 +1,227 @@
+"""Continuous-batching SCF server (the serving configuration).
+
+Requests (1D Kohn-Sham solves of any grid size and electron count) arrive
+over time.  The server admits every pending request into a new batch as soon
+as a launch slot (a CUDA stream) and device memory are free, so batches
+launched at different times run concurrently on the GPU; each request's
+density, eigenvectors and mixing history stay in its batch's device
+workspace until the solve ends.  Admission is by device memory: a request is
+admitted only while the bytes of all in-flight batches (workspace + outputs)
+stay under ``memory_budget_bytes``.  Latency is arrival -> result on the host.
+
+The reference has no serving layer; it solves one molecule (or one vmap'd
+batch of equal-shape molecules) per call (``qedft/train/od/train.py:84-125``),
+which is what ``serve_plain`` reproduces: one request at a time.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import time
+from typing import List, Sequence
+
+import numpy as np
+
+from . import _native as N
+from .od.engine import Ks1dEngine, Molecule1D, PackedBatch, SolveConfig, _convention, _options
+from .xc import resolve
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    molecule: Molecule1D
+    arrival: float  # seconds from the start of the stream
+    start: float = float("nan")
+    finish: float = float("nan")
+    energies: np.ndarray | None = None
+    density: np.ndarray | None = None
+    status: int = 0
+
+    @property
+    def latency(self):
+        return self.finish - self.arrival
+
+
+@dataclasses.dataclass
+class _Launch:
+    requests: List[Request]
+    batch: PackedBatch
+    out: dict
+    host: dict
+    workspace: object
+    stream: object
+    event: object
+    nbytes: int
+
+
+def config1_requests(arrivals, seed: int = 0, num_grids=513, spacing=0.08) -> List[Request]:
+    """H2-like 1D requests of the plain configuration's shape (513 points,
+    dx 0.08, unit charges at +-R with R uniform in [0.5, 1.5] bohr)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i, t in enumerate(arrivals):
+        r = rng.uniform(0.5, 1.5)
+        mol = Molecule1D(num_grids=num_grids, grid_spacing=spacing, locations=[-r, r],
+                         nuclear_charges=[1.0, 1.0], num_electrons=2)
+        out.append(Request(rid=i, molecule=mol, arrival=float(t)))
+    return out
+
+
+def poisson_arrivals(rate: float, duration: float, seed: int = 0) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    n = rng.poisson(rate * duration)
+    return np.sort(rng.uniform(0.0, duration, n))
+
+
+class ScfServer:
+    """Continuous batching of 1D SCF requests over a pool of CUDA streams."""
+
+    def __init__(self, xc, cfg: SolveConfig, max_inflight: int = 16, max_batch: int = 512,
+                 memory_budget_bytes: int = 8 << 30, engine: Ks1dEngine | None = None):
+        self.torch = N.require_cuda()
+        self.xc = xc
+        self.cfg = cfg
+        self.engine = engine or Ks1dEngine()
+        self.lib = self.engine.lib
+        self.max_inflight = max_inflight
+        self.max_batch = max_batch
+        self.budget = memory_budget_bytes
+        self.streams = [self.torch.cuda.Stream() for _ in range(max_inflight)]
+        self.functional, self.params = resolve(xc)
+        self.spec, self._keep = self.functional.spec(self.params, _convention(cfg))
+        self.in_use = 0
+        self.launches = 0
+
+    def _bytes_for(self, batch: PackedBatch, opts) -> int:
+        nb = ctypes.c_size_t()
+        N.check(self.lib.qex_ks1d_workspace_size(ctypes.byref(opts), batch.size, ctypes.byref(nb)),
+                "qex_ks1d_workspace_size")
+        T = self.cfg.num_iterations
+        outputs = batch.size * T * 8 * 2 + batch.total_points * 8 + batch.size * (8 + 16 + 64)
+        return nb.value + outputs
+
+    def _launch(self, reqs: Sequence[Request], stream, now: float) -> _Launch:
+        torch = self.torch
+        with torch.cuda.stream(stream):
+            batch = PackedBatch([r.molecule for r in reqs], sort=False)
+            opts = _options(self.cfg, batch, False)
+            nbytes = self._bytes_for(batch, opts)
+            out = self.engine.allocate_outputs(batch, self.cfg, ("energy", "final_density"))
+            nb = ctypes.c_size_t()
+            self.lib.qex_ks1d_workspace_size(ctypes.byref(opts), batch.size, ctypes.byref(nb))
+            ws = torch.empty(max(nb.value, 256), dtype=torch.uint8, device="cuda")
+            cb = batch.c_batch()
+            co = self.engine._c_outputs(out)
+            rc = self.lib.qex_ks1d_solve(ctypes.byref(cb), ctypes.byref(opts), ctypes.byref(self.spec),
+                                         ctypes.byref(co), ctypes.c_void_p(ws.data_ptr()),
+                                         ctypes.c_size_t(ws.numel()),
+                                         ctypes.c_void_p(stream.cuda_stream))
+            N.check(rc, "qex_ks1d_solve")
+            host = {k: torch.empty(out[k].shape, dtype=out[k].dtype, pin_memory=True)
+                    for k in ("energy", "final_density", "status")}
+            for k, t in host.items():
+                t.copy_(out[k], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        self.launches += 1
+        for r in reqs:
+            r.start = now
+        return _Launch(list(reqs), batch, out, host, ws, stream, ev, nbytes)
+
+    def _retire(self, launch: _Launch, now: float):
+        energy = launch.host["energy"].numpy()
+        dens = launch.batch.split(launch.host["final_density"].numpy())
+        status = launch.host["status"].numpy()
+        for i, r in enumerate(launch.requests):
+            r.finish = now
+            r.energies = energy[i].copy()
+            r.density = dens[i].copy()
+            r.status = int(status[i])
+        self.in_use -= launch.nbytes
+
+    def serve(self, requests: Sequence[Request], realtime: bool = True) -> List[Request]:
+        """Serve ``requests`` (sorted by arrival) and return them completed."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        pending: List[Request] = []
+        inflight: List[_Launch] = []
+        free = list(self.streams)
+        nxt = 0
+        t0 = time.perf_counter()
+        done = 0
+        while done < len(reqs):
+            now = time.perf_counter() - t0
+            if not realtime and not pending and not inflight and nxt < len(reqs):
+                now = reqs[nxt].arrival
+            while nxt < len(reqs) and reqs[nxt].arrival <= now:
+                pending.append(reqs[nxt])
+                nxt += 1
+            for L in list(inflight):
+                if L.event.query():
+                    self._retire(L, time.perf_counter() - t0)
+                    done += len(L.requests)
+                    inflight.remove(L)
+                    free.append(L.stream)
+            while pending and free:
+                take = pending[: self.max_batch]
+                # admission by device memory: halve the batch until it fits the
+                # free budget; a single request that does not fit waits for
+                # in-flight batches to finish (or runs alone on an idle GPU)
+                while len(take) > 1 and self.in_use + self._estimate(take) > self.budget:
+                    take = take[: len(take) // 2]
+                if self.in_use + self._estimate(take) > self.budget and inflight:
+                    break
+                L = self._launch(take, free.pop(), now)
+                self.in_use += L.nbytes
+                inflight.append(L)
+                pending = pending[len(take):]
+            if realtime:
+                time.sleep(0.0002)
+        return reqs
+
+    def _estimate(self, reqs: Sequence[Request]) -> int:
+        n = sum(r.molecule.num_grids for r in reqs)
+        nmax = max(r.molecule.num_grids for r in reqs)
+        kmax = max(r.molecule.num_electrons // 2 + 1 for r in reqs)
+        slots = min(self.cfg.num_mixing_iterations, self.cfg.num_iterations)
+        per = (9 + slots + kmax) * nmax * 8
+        return len(reqs) * per + len(reqs) * self.cfg.num_iterations * 16 + n * 8
+
+
+def serve_plain(xc, cfg: SolveConfig, requests: Sequence[Request],
+                engine: Ks1dEngine | None = None) -> List[Request]:
+    """One request at a time, in arrival order (the reference's calling pattern)."""
+    torch = N.require_cuda()
+    engine = engine or Ks1dEngine()
+    reqs = sorted(requests, key=lambda r: r.arrival)
+    t0 = time.perf_counter()
+    for r in reqs:
+        now = time.perf_counter() - t0
+        if now < r.arrival:
+            time.sleep(r.arrival - now)
+        r.start = time.perf_counter() - t0
+        batch = PackedBatch([r.molecule], sort=False)
+        out = engine.solve(batch, xc, cfg, records=("energy", "final_density"))
+        energy = out["energy"].cpu().numpy()
+        r.density = out["final_density"].cpu().numpy()
+        r.status = int(out["status"].cpu().numpy()[0])
+        r.energies = energy[0]
+        r.finish = time.perf_counter() - t0
+    return reqs
+
+
+def latency_summary(reqs: Sequence[Request], duration: float | None = None) -> dict:
+    lat = np.array([r.latency for r in reqs])
+    span = duration if duration else (max(r.finish for r in reqs) - min(r.arrival for r in reqs))
+    conv = [r for r in reqs if r.energies is not None and abs(r.energies[-1] - r.energies[-2]) < 1e-8
+            and (r.status & 0xFFFF) == 0]
+    return {
+        "requests": len(reqs),
+        "converged": len(conv),
+        "solves_per_s": len(reqs) / span if span > 0 else float("nan"),
+        "converged_solves_per_s": len(conv) / span if span > 0 else float("nan"),
+        "p50_ms": float(np.percentile(lat, 50) * 1e3),
+        "p99_ms": float(np.percentile(lat, 99) * 1e3),
+        "mean_ms": float(lat.mean() * 1e3),
+    }
