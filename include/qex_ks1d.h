@@ -141,6 +141,23 @@ int qex_ks1d_solve(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
                    const qex_xc_spec* xc, const qex_ks1d_outputs* outputs,
                    void* workspace, size_t workspace_bytes, void* stream);
 
+/* qex_ks1d_solve without a workspace argument and without any allocation.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc at solve time -- code running inside another framework's device
+ * memory pool (an XLA custom call with no workspace reserved, a serving loop
+ * whose memory is budgeted up front) or a runtime that forbids allocation on
+ * its hot path.  Its scratch is a fixed 16 MiB device array inside this
+ * library; a batch whose qex_ks1d_workspace_size exceeds 16 MiB is rejected
+ * with QEX_OOM before anything is launched.  The first call on each device
+ * looks up the array's device address (cudaGetSymbolAddress), so make that
+ * first call before any stream capture.  Every call shares the one array:
+ * calls that overlap on the GPU (other streams, other host threads) race and
+ * corrupt each other's results; serialise them.  The array keeps the last
+ * call's contents; what must start at zero (the work counter) is cleared by
+ * each call. */
+int qex_ks1d_solve_static(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
+                          const qex_xc_spec* xc, const qex_ks1d_outputs* outputs, void* stream);
+
 /* One Kohn-Sham iteration per molecule: input density (packed) and external
  * potential (packed) -> unmixed output density, energy, v_H, v_xc, f, gap.
  * Records are single-iteration (iters = 1). */

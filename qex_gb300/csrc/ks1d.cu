@@ -27,6 +27,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <mutex>
+
 #include "ks1d_common.cuh"
 #include "xc_device.cuh"
 #include "qex_ks1d.h"
@@ -1496,6 +1498,37 @@ int launch(const Params& P, cudaStream_t stream) {
 }  // namespace
 }  // namespace qex
 
+// Scratch of qex_ks1d_solve_static: a fixed device array, so that callers
+// that cannot allocate device memory can still run the batched solver.  Every
+// GPU that loads this library holds these 16 MiB until the process exits.
+static constexpr size_t kStaticScratchBytes = size_t(16) << 20;
+static __device__ __align__(256) unsigned char qex_static_scratch[kStaticScratchBytes];
+
+namespace {
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_static_mutex;
+void* g_static_address[kStaticMaxDevices] = {};
+
+// Device address of the scratch array on the current device.  Host code may
+// not use the array's name as a pointer (it is a host-side stand-in), so the
+// address is looked up once per device, with that device current.
+int static_scratch_address(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return QEX_CUDA_ERROR;
+  if (dev < 0 || dev >= kStaticMaxDevices) return QEX_BAD_ARG;
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (!g_static_address[dev]) {
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, qex_static_scratch) != cudaSuccess || !ptr) {
+      return QEX_CUDA_ERROR;
+    }
+    g_static_address[dev] = ptr;
+  }
+  *out = g_static_address[dev];
+  return QEX_OK;
+}
+}  // namespace
+
 extern "C" {
 
 int qex_ks1d_workspace_size(const qex_ks1d_options* options, int32_t num_molecules,
@@ -1517,6 +1550,24 @@ int qex_ks1d_solve(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
   int rc = qex::fill_params(P, qex::kModeScf, batch, options, xc, outputs, workspace,
                             workspace_bytes, batch->num_molecules);
   if (rc) return rc;
+  return qex::launch(P, static_cast<cudaStream_t>(stream));
+}
+
+int qex_ks1d_solve_static(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
+                          const qex_xc_spec* xc, const qex_ks1d_outputs* outputs, void* stream) {
+  if (!batch) return QEX_BAD_ARG;
+  size_t need = 0;
+  int rc = qex_ks1d_workspace_size(options, batch->num_molecules, &need);
+  if (rc) return rc;
+  if (need > kStaticScratchBytes) return QEX_OOM;  // batch too large for the fixed scratch
+  void* scratch = nullptr;
+  rc = static_scratch_address(&scratch);
+  if (rc) return rc;
+  qex::Params P;
+  rc = qex::fill_params(P, qex::kModeScf, batch, options, xc, outputs, scratch,
+                        kStaticScratchBytes, batch->num_molecules);
+  if (rc) return rc;
+  // the work counter at the start of the scratch is zeroed inside launch()
   return qex::launch(P, static_cast<cudaStream_t>(stream));
 }
 
