@@ -1,0 +1,99 @@
+/*
+ * qex_td.h -- C ABI of the GB300 3D Kohn-Sham numint / generalized-eigh path.
+ *
+ * Device buffers, row-major, float64, caller-owned; opaque stream; int status
+ * (codes of qex_ks1d.h); no allocation (workspace-size queries where needed).
+ *
+ * Reference interfaces replaced (qedft, pasqal-io/qex):
+ *   qex_td_eval_ao        <- eval_gto 'GTOval_cart' as used at
+ *                            qedft/train/td/eval_gto.py:20-70 and
+ *                            qedft/train/td/scf_functions_masked.py:169-173
+ *   qex_td_rho            <- eval_rho (LDA), qedft/train/td/numint_legacy.py:351-397
+ *   qex_td_lda            <- eval_xc for the LDA exchange inside nr_rks,
+ *                            qedft/train/td/numint_legacy.py:148-164
+ *   qex_td_vxc            <- _scale_ao + _dot_ao_ao + (V + V^T),
+ *                            qedft/train/td/numint_legacy.py:161-164,337,432-456
+ *   qex_td_gen_eigh       <- generalized_eigh,
+ *                            qedft/train/td/generalized_eigensolver.py:264-330
+ *   qex_td_make_rdm1      <- make_rdm1, qedft/train/td/hf.py:303-308 and
+ *                            qedft/train/td/scf_functions_masked.py:290-303
+ *   qex_td_diis_error     <- get_diis_error, qedft/train/td/jax_diis.py:107-114
+ *   qex_td_diis_extrapolate <- update_diis_state + extrapolate_fock,
+ *                            qedft/train/td/jax_diis.py:26-104
+ *   qex_td_coulomb        <- J = einsum('ijkl,kl->ij', eri, dm),
+ *                            qedft/train/td/scf_functions_masked.py:152, with the
+ *                            ERI in factored form (ij|kl) = sum_P B_Pij B_Pkl
+ */
+#ifndef QEX_TD_H_
+#define QEX_TD_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Shells of Cartesian contracted Gaussians: shell s has centre
+ * centers[3s..3s+2], angular momentum l[s] (0 or 1), primitives
+ * [prim_offset[s], prim_offset[s+1]) of exponents / coefficients (the
+ * coefficients include the primitive normalisation) and its first AO column
+ * ao_offset[s].  ao is (G, nao). */
+int qex_td_eval_ao(int64_t num_points, const double* coords, int32_t num_shells,
+                   const double* centers, const int32_t* l, const int32_t* prim_offset,
+                   const int32_t* ao_offset, const double* exponents, const double* coefficients,
+                   int32_t nao, double* ao, void* stream);
+
+/* rho_g = sum_ij ao_gi D_ij ao_gj.  workspace: qex_td_rho_workspace_size bytes. */
+size_t qex_td_rho_workspace_size(int64_t num_points, int32_t nao);
+int qex_td_rho(int64_t num_points, int32_t nao, const double* ao, const double* dm, double* rho,
+               void* workspace, size_t workspace_bytes, void* stream);
+
+/* Slater exchange on the grid: exc_g, vrho_g, and sums[0] = sum w rho,
+ * sums[1] = sum w rho exc (deterministic). */
+size_t qex_td_lda_workspace_size(int64_t num_points);
+int qex_td_lda(int64_t num_points, const double* rho, const double* weights, double* exc,
+               double* vrho, double* sums, void* workspace, size_t workspace_bytes, void* stream);
+
+/* vmat = ao^T diag(0.5 w v) ao, then vmat + vmat^T.  workspace:
+ * qex_td_vxc_workspace_size bytes. */
+size_t qex_td_vxc_workspace_size(int64_t num_points, int32_t nao);
+int qex_td_vxc(int64_t num_points, int32_t nao, const double* ao, const double* weights,
+               const double* vrho, double* vmat, void* workspace, size_t workspace_bytes,
+               void* stream);
+
+/* Batched generalized eigenproblem A v = w S v for `batch` matrices of order n
+ * (A, S: (batch, n, n)); w (batch, n) ascending, V (batch, n, n) with the
+ * eigenvectors in columns.  status (batch): 0, or QEX_NUMERICAL when S needed
+ * the SPD shift and its eigenvalues were computed, or QEX_NOT_CONVERGED when
+ * the Jacobi sweeps hit their cap. */
+size_t qex_td_gen_eigh_workspace_size(int32_t batch, int32_t n);
+int qex_td_gen_eigh(int32_t batch, int32_t n, const double* A, const double* S, double* w,
+                    double* V, int32_t* status, void* workspace, size_t workspace_bytes,
+                    void* stream);
+
+/* D = C diag(occ) C^T for `batch` matrices (C: (batch, n, n), occ: (batch, n)). */
+int qex_td_make_rdm1(int32_t batch, int32_t n, const double* C, const double* occ, double* D,
+                     void* stream);
+
+/* e = F D S - S D F (symmetric F, D, S of order n).  workspace: n*n doubles. */
+int qex_td_diis_error(int32_t n, const double* F, const double* D, const double* S, double* err,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+/* CDIIS extrapolation over `nvec` stored (error, fock) pairs of n*n doubles
+ * (errs, focks: (nvec, n*n), oldest first): B = [[0,-1],[-1, e_i.e_j]] + 1e-14 I,
+ * solve B c = (-1, 0, ...), F = sum_i c_i F_i.  With nvec < min_vecs, F is the
+ * newest stored fock.  coeffs (optional, nvec doubles) receives c. */
+int qex_td_diis_extrapolate(int32_t n, int32_t nvec, int32_t min_vecs, const double* errs,
+                            const double* focks, double* fock_out, double* coeffs, void* stream);
+
+/* J_ij = sum_P B_Pij (sum_kl B_Pkl D_kl); factors (naux, n, n).
+ * workspace: naux doubles. */
+int qex_td_coulomb(int32_t n, int32_t naux, const double* factors, const double* dm, double* J,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QEX_TD_H_ */

@@ -1,0 +1,231 @@
+"""NumPy float64 restatement of the 3D numint / generalized-eigh / DIIS / rdm1
+SCF pieces of the reference (test oracle; the CUDA product path never imports
+this module).
+
+Each function cites the reference file:line it follows.  pyscf / pyscfad are
+not installed anywhere this project runs, so the one-electron and
+two-electron integrals come from the synthetic model of
+``synthetic_molecule`` (same inputs for the oracle and the GPU path).
+"""
+
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+SLATER_CX = 0.75 * (3.0 / math.pi) ** (1.0 / 3.0)
+
+
+# ----------------------------------------------------------------------------
+# Basis and AO values
+# ----------------------------------------------------------------------------
+
+@dataclasses.dataclass
+class Shell:
+    center: np.ndarray  # (3,)
+    l: int  # 0 (s) or 1 (p: x, y, z Cartesian)
+    exponents: np.ndarray
+    coefficients: np.ndarray  # contraction coefficients incl. primitive normalisation
+
+
+def primitive_norm(alpha, l):
+    """Normalisation of x^l exp(-alpha r^2) (one Cartesian component)."""
+    return (2.0 * alpha / math.pi) ** 0.75 * (4.0 * alpha) ** (0.5 * l)
+
+
+def nao_of(shells):
+    return sum(1 if s.l == 0 else 3 for s in shells)
+
+
+def eval_ao(shells, coords, deriv=0):
+    """AO values (G, nao) of Cartesian contracted GTOs (pyscf ``eval_gto`` with
+    'GTOval_cart', as reached from ``qedft/train/td/eval_gto.py:20-70`` and
+    ``qedft/train/td/scf_functions_masked.py:169-173``).  With deriv=1 also
+    returns the gradient (3, G, nao)."""
+    coords = np.asarray(coords, dtype=np.float64)
+    G = coords.shape[0]
+    ao = np.zeros((G, nao_of(shells)))
+    grad = np.zeros((3, G, nao_of(shells))) if deriv else None
+    k = 0
+    for s in shells:
+        d = coords - s.center[None, :]
+        r2 = np.sum(d * d, axis=1)
+        e = np.exp(-np.outer(r2, s.exponents))  # (G, nprim)
+        rad = e @ s.coefficients
+        drad = e @ (-2.0 * s.exponents * s.coefficients)  # d rad / d(r2) * 2 ... (x factor below)
+        if s.l == 0:
+            ao[:, k] = rad
+            if deriv:
+                for c in range(3):
+                    grad[c, :, k] = drad * d[:, c]
+            k += 1
+        else:
+            for c in range(3):
+                ao[:, k + c] = d[:, c] * rad
+                if deriv:
+                    for q in range(3):
+                        grad[q, :, k + c] = (rad if q == c else 0.0) + d[:, c] * drad * d[:, q]
+            k += 3
+    return (ao, grad) if deriv else ao
+
+
+# ----------------------------------------------------------------------------
+# numint (LDA)
+# ----------------------------------------------------------------------------
+
+def eval_rho(ao, dm):
+    """rho_g = sum_ij ao_gi D_ij ao_gj (``qedft/train/td/numint_legacy.py:351-397``,
+    LDA branch; ``_dot_ao_dm`` :459-471 and ``_contract_rho`` :475-481)."""
+    c0 = ao @ dm
+    return np.einsum("gi,gi->g", c0, ao)
+
+
+def lda_x(rho):
+    """Slater exchange: exc = -C rho^(1/3), vrho = 4/3 exc (libxc LDA_X, the
+    exchange part of the reference's "LDA,VWN", ``qedft/train/td/rks.py:172``)."""
+    rho = np.asarray(rho, dtype=np.float64)
+    r13 = np.cbrt(np.maximum(rho, 0.0))
+    exc = -SLATER_CX * r13
+    return exc, 4.0 / 3.0 * exc
+
+
+def nr_rks_lda(ao, weights, dm):
+    """(nelec, excsum, vmat) of ``qedft/train/td/numint_legacy.py:122-164,337``:
+    aow = 0.5 * w * vrho * ao; vmat = ao^T aow; vmat += vmat^T."""
+    rho = eval_rho(ao, dm)
+    exc, vrho = lda_x(rho)
+    den = rho * weights
+    nelec = den.sum()
+    excsum = np.dot(den, exc)
+    aow = ao * (0.5 * weights * vrho)[:, None]
+    vmat = ao.T @ aow
+    return nelec, excsum, vmat + vmat.T
+
+
+# ----------------------------------------------------------------------------
+# Generalized eigensolver
+# ----------------------------------------------------------------------------
+
+def generalized_eigh(A, B, eps=1e-12):
+    """``qedft/train/td/generalized_eigensolver.py:264-330``: symmetrise, shift B
+    if its smallest eigenvalue is below eps, Cholesky, C = L^-1 A L^-T, eigh(C),
+    V = L^-T U."""
+    import scipy.linalg as sla
+
+    A = 0.5 * (A + A.T)
+    B = 0.5 * (B + B.T)
+    lam_min = np.linalg.eigvalsh(B).min()
+    if lam_min < eps:
+        B = B + (eps - lam_min) * np.eye(B.shape[0])
+    L = np.linalg.cholesky(B)
+    Y = sla.solve_triangular(L, A, lower=True)
+    C = sla.solve_triangular(L, Y.T, lower=True).T
+    C = 0.5 * (C + C.T)
+    w, U = np.linalg.eigh(C)
+    V = sla.solve_triangular(L.T, U, lower=False)
+    return w, V
+
+
+def masked_generalized_eigh(fock, s1e, mask):
+    """``qedft/train/td/generalized_eigensolver_masked.py:19-89``."""
+    mask = np.asarray(mask, dtype=bool)
+    n = fock.shape[0]
+    m2 = mask[:, None] & mask[None, :]
+    eye = np.eye(n, dtype=bool)
+    f = np.where(m2, fock, 0.0) + np.where(~mask[:, None] & eye, 1e-12, 0.0)
+    s = np.where(m2, s1e, np.where(~mask[:, None] & eye, 1e-12, 0.0))
+    w, v = generalized_eigh(f, s)
+    key = np.where(mask, w, 1e12)  # mask indexes basis functions; reference uses it per eigenvalue slot
+    order = np.argsort(key, kind="stable")
+    w = w[order] * mask[order]
+    v = np.where(m2[:, order], v[:, order], 0.0)
+    return w, v
+
+
+# ----------------------------------------------------------------------------
+# Occupations, density matrix, DIIS, energies
+# ----------------------------------------------------------------------------
+
+def get_occ(nelectron, mo_energy):
+    """Aufbau, 2 electrons in each of the lowest Ne/2 orbitals
+    (``qedft/train/td/scf_functions_masked.py:176-186``)."""
+    e_idx = np.argsort(mo_energy, kind="stable")
+    occ_sorted = np.where(np.arange(mo_energy.size) < nelectron // 2, 2.0, 0.0)
+    occ = np.empty_like(occ_sorted)
+    occ[e_idx] = occ_sorted
+    return occ
+
+
+def make_rdm1(mo_coeff, mo_occ):
+    """D = C diag(occ) C^T (``qedft/train/td/hf.py:303-308``)."""
+    return np.einsum("ij,j,kj->ik", mo_coeff, mo_occ, mo_coeff)
+
+
+class DIIS:
+    """CDIIS restated from ``qedft/train/td/jax_diis.py:10-134``."""
+
+    def __init__(self, max_vec=8, min_vecs=2):
+        self.max_vec, self.min_vecs = max_vec, min_vecs
+        self.errs, self.focks = [], []
+
+    @staticmethod
+    def error(fock, dm, ovlp):
+        return fock @ (dm @ ovlp) - ovlp @ (dm @ fock)
+
+    def update(self, fock, dm, ovlp):
+        self.errs.append(self.error(fock, dm, ovlp).ravel())
+        self.focks.append(fock.ravel())
+        if len(self.errs) > self.max_vec:
+            self.errs = self.errs[-self.max_vec:]
+            self.focks = self.focks[-self.max_vec:]
+        n = len(self.errs)
+        if n < self.min_vecs:
+            return self.focks[-1].reshape(fock.shape)
+        B = np.zeros((n + 1, n + 1))
+        B[0, 1:] = -1.0
+        B[1:, 0] = -1.0
+        E = np.array(self.errs)
+        B[1:, 1:] = E @ E.T
+        B[np.diag_indices(n + 1)] += 1e-14
+        rhs = np.zeros(n + 1)
+        rhs[0] = -1.0
+        c = np.linalg.solve(B, rhs)[1:]
+        return (c @ np.array(self.focks)).reshape(fock.shape)
+
+
+def coulomb_lowrank(factors, dm):
+    """J_ij = sum_kl (ij|kl) D_kl with (ij|kl) = sum_P B_P,ij B_P,kl."""
+    c = np.einsum("pij,ij->p", factors, dm)
+    return np.einsum("p,pij->ij", c, factors)
+
+
+def energy_tot(dm, h1e, J, exc, e_nuc):
+    """``qedft/train/td/scf_functions_masked.py:162-166``."""
+    return float(np.einsum("ij,ji->", dm, h1e) + 0.5 * np.einsum("ij,ij->", dm, J) + exc + e_nuc)
+
+
+def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1):
+    """Fixed-cycle SCF of ``qedft/train/td/scf_functions_masked.py:907-967`` with
+    the low-rank Coulomb model and the LDA exchange."""
+    ao, w = mol.ao, mol.weights
+    s1e, h1e = mol.s1e, mol.h1e
+    e0, c0 = generalized_eigh(h1e, s1e)
+    dm = make_rdm1(c0, get_occ(mol.nelectron, e0))
+    J = coulomb_lowrank(mol.eri_factors, dm)
+    _, exc, vxc = nr_rks_lda(ao, w, dm)
+    vhf = J + vxc
+    diis = DIIS(diis_max_vec)
+    energies = []
+    for cycle in range(max_cycle):
+        fock = h1e + vhf
+        if cycle >= diis_start_cycle:
+            fock = diis.update(fock, dm, s1e)
+        mo_e, mo_c = generalized_eigh(fock, s1e)
+        dm = make_rdm1(mo_c, get_occ(mol.nelectron, mo_e))
+        J = coulomb_lowrank(mol.eri_factors, dm)
+        _, exc, vxc = nr_rks_lda(ao, w, dm)
+        vhf = J + vxc
+        energies.append(energy_tot(dm, h1e, J, exc, mol.energy_nuc))
+    return np.array(energies), dm, mo_e

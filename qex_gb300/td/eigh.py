@@ -1,0 +1,57 @@
+"""Generalized symmetric eigensolver on the GPU.
+
+``generalized_eigh`` mirrors ``qedft/train/td/generalized_eigensolver.py:264-330``
+(symmetrise, SPD shift of S when its smallest eigenvalue is below 1e-12,
+Cholesky, C = L^-1 A L^-T, eigh(C), V = L^-T U); ``masked_generalized_eigh``
+mirrors ``qedft/train/td/generalized_eigensolver_masked.py:19-89`` (padded
+diagonals 1e-12, padded slots sorted last and zeroed).  Batched: A and S may
+be (batch, n, n).
+"""
+
+from __future__ import annotations
+
+from .. import _native as N
+from . import _lib
+from .numint import _dev
+
+
+def generalized_eigh(A, B, *, eps: float = 1.0e-12, return_status: bool = False):
+    torch = N.require_cuda()
+    if eps != 1.0e-12:
+        raise NotImplementedError("the GPU solver uses the reference's eps = 1e-12")
+    L = _lib.lib()
+    A = _dev(A, torch.float64)
+    B = _dev(B, torch.float64)
+    single = A.dim() == 2
+    if single:
+        A, B = A[None], B[None]
+    batch, n, _ = A.shape
+    w = torch.empty((batch, n), dtype=torch.float64, device="cuda")
+    V = torch.empty((batch, n, n), dtype=torch.float64, device="cuda")
+    st = torch.zeros(batch, dtype=torch.int32, device="cuda")
+    ws = torch.empty(L.qex_td_gen_eigh_workspace_size(batch, n), dtype=torch.uint8, device="cuda")
+    N.check(L.qex_td_gen_eigh(batch, n, _lib.p(A), _lib.p(B), _lib.p(w), _lib.p(V), _lib.p(st),
+                              _lib.p(ws), ws.numel(), _lib.stream()), "qex_td_gen_eigh")
+    if single:
+        w, V, st = w[0], V[0], st[0]
+    return (w, V, st) if return_status else (w, V)
+
+
+def masked_generalized_eigh(fock, s1e, mask):
+    """Padded/masked solve with the reference's padding and sorting rules."""
+    torch = N.require_cuda()
+    fock = _dev(fock, torch.float64)
+    s1e = _dev(s1e, torch.float64)
+    mask = _dev(mask, torch.bool)
+    n = fock.shape[-1]
+    m2 = mask[:, None] & mask[None, :]
+    eye = torch.eye(n, dtype=torch.bool, device="cuda")
+    padd = (~mask)[:, None] & eye
+    f = torch.where(m2, fock, 0.0) + torch.where(padd, 1e-12, 0.0)
+    s = torch.where(m2, s1e, torch.where(padd, 1e-12, 0.0))
+    w, v = generalized_eigh(f, s)
+    key = torch.where(mask, w, torch.full_like(w, 1e12))
+    order = torch.sort(key, stable=True).indices
+    w = w[order] * mask[order].to(w.dtype)
+    v = torch.where(m2[:, order], v[:, order], 0.0)
+    return w, v

@@ -1,0 +1,164 @@
+"""Seeded synthetic 3D molecules with the shapes of the 3D numint configuration.
+
+pyscf is not available here, so one- and two-electron integrals come from a
+documented synthetic model built on the molecule's own grid:
+
+* atoms H/C/N/O at random positions with a minimum separation of 1.0 Angstrom;
+* basis: Cartesian contracted Gaussians, H: 2 s shells; C, N, O: 3 s + 2 p
+  shells (1-3 primitives, exponents log-uniform in [0.1, 50]);
+* grid: points drawn from Gaussian clouds around the atoms, with Monte-Carlo
+  importance weights 1 / (G p(r)) times a random factor in [0.9, 1.1]
+  (positive random weights);
+* S = ao^T W ao, T = 1/2 sum_c (d_c ao)^T W (d_c ao),
+  V = -ao^T diag(w sum_A Z_A / sqrt(|r - R_A|^2 + 0.2)) ao, h1e = T + V;
+* two-electron integrals in factored form (ij|kl) = sum_P B_Pij B_Pkl with
+  naux = 3 nao Gaussian auxiliary functions g_P on random atoms,
+  B_P = 0.3 ao^T diag(w g_P) ao;
+* E_nuc = sum_{A<B} Z_A Z_B / R_AB; an even electron count (sum Z, minus one
+  if odd).
+This is generation of inputs (host NumPy, once per molecule), not the SCF
+hot path.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+ELEMENTS = {"H": 1, "C": 6, "N": 7, "O": 8}
+ANGSTROM = 1.8897261246
+
+
+@dataclasses.dataclass
+class Shell:
+    center: np.ndarray
+    l: int
+    exponents: np.ndarray
+    coefficients: np.ndarray
+
+
+@dataclasses.dataclass
+class Molecule3D:
+    charges: np.ndarray
+    positions: np.ndarray
+    shells: list
+    coords: np.ndarray
+    weights: np.ndarray
+    nelectron: int
+    ao: np.ndarray | None = None
+    s1e: np.ndarray | None = None
+    h1e: np.ndarray | None = None
+    eri_factors: np.ndarray | None = None
+    energy_nuc: float = 0.0
+
+    @property
+    def nao(self):
+        return sum(1 if s.l == 0 else 3 for s in self.shells)
+
+    def shell_arrays(self):
+        """Flattened shell description for ``qex_td_eval_ao``."""
+        centers = np.array([s.center for s in self.shells], dtype=np.float64).reshape(-1)
+        l = np.array([s.l for s in self.shells], dtype=np.int32)
+        nprim = [len(s.exponents) for s in self.shells]
+        poff = np.zeros(len(self.shells) + 1, dtype=np.int32)
+        poff[1:] = np.cumsum(nprim)
+        aoff = np.zeros(len(self.shells), dtype=np.int32)
+        aoff[1:] = np.cumsum([1 if s.l == 0 else 3 for s in self.shells])[:-1]
+        ex = np.concatenate([s.exponents for s in self.shells]).astype(np.float64)
+        co = np.concatenate([s.coefficients for s in self.shells]).astype(np.float64)
+        return centers, l, poff, aoff, ex, co
+
+
+def _prim_norm(alpha, l):
+    return (2.0 * alpha / math.pi) ** 0.75 * (4.0 * alpha) ** (0.5 * l)
+
+
+def ao_values(shells, coords, deriv=False):
+    """Host AO values (and gradients) for the integral model."""
+    G = coords.shape[0]
+    n = sum(1 if s.l == 0 else 3 for s in shells)
+    ao = np.zeros((G, n))
+    grad = np.zeros((3, G, n)) if deriv else None
+    k = 0
+    for s in shells:
+        d = coords - s.center[None, :]
+        r2 = np.einsum("gc,gc->g", d, d)
+        e = np.exp(-np.outer(r2, s.exponents))
+        rad = e @ s.coefficients
+        drad = e @ (-2.0 * s.exponents * s.coefficients)
+        if s.l == 0:
+            ao[:, k] = rad
+            if deriv:
+                grad[:, :, k] = (drad[:, None] * d).T
+            k += 1
+        else:
+            for c in range(3):
+                ao[:, k + c] = d[:, c] * rad
+                if deriv:
+                    for q in range(3):
+                        grad[q, :, k + c] = (rad if q == c else 0.0) + d[:, c] * drad * d[:, q]
+            k += 3
+    return (ao, grad) if deriv else ao
+
+
+def synthetic_molecule(num_atoms: int, seed: int = 0, points_per_atom: int = 620,
+                       with_integrals: bool = True) -> Molecule3D:
+    rng = np.random.default_rng(seed)
+    names = rng.choice(["H", "C", "N", "O"], size=num_atoms, p=[0.4, 0.2, 0.2, 0.2])
+    Z = np.array([ELEMENTS[x] for x in names], dtype=np.float64)
+    min_sep = 1.0 * ANGSTROM
+    box = 1.6 * min_sep * max(1.0, num_atoms ** (1.0 / 3.0))
+    pos = []
+    while len(pos) < num_atoms:
+        cand = rng.uniform(-box, box, 3)
+        if all(np.linalg.norm(cand - p) >= min_sep for p in pos):
+            pos.append(cand)
+    pos = np.array(pos)
+    shells = []
+    for z, R in zip(Z, pos):
+        ls = [0, 0] if z == 1 else [0, 0, 0, 1, 1]
+        for l in ls:
+            npr = int(rng.integers(1, 4))
+            ex = np.exp(rng.uniform(math.log(0.1), math.log(50.0), npr))
+            w = rng.uniform(0.2, 1.0, npr)
+            co = w * np.array([_prim_norm(a, l) for a in ex])
+            shells.append(Shell(center=R.copy(), l=l, exponents=ex, coefficients=co))
+    G = points_per_atom * num_atoms
+    sig = 1.5
+    which = rng.integers(0, num_atoms, G)
+    coords = pos[which] + rng.normal(0.0, sig, (G, 3))
+    d2 = ((coords[:, None, :] - pos[None, :, :]) ** 2).sum(-1)
+    dens = np.exp(-0.5 * d2 / sig ** 2).mean(axis=1) / (2 * math.pi * sig ** 2) ** 1.5
+    weights = rng.uniform(0.9, 1.1, G) / (G * dens)
+    ne = int(Z.sum())
+    ne -= ne % 2
+    mol = Molecule3D(charges=Z, positions=pos, shells=shells, coords=coords, weights=weights,
+                     nelectron=ne)
+    e_nuc = 0.0
+    for a in range(num_atoms):
+        for b in range(a + 1, num_atoms):
+            e_nuc += Z[a] * Z[b] / np.linalg.norm(pos[a] - pos[b])
+    mol.energy_nuc = float(e_nuc)
+    if with_integrals:
+        ao, grad = ao_values(shells, coords, deriv=True)
+        mol.ao = ao
+        W = weights[:, None]
+        mol.s1e = ao.T @ (W * ao)
+        T = 0.5 * sum(grad[c].T @ (W * grad[c]) for c in range(3))
+        vnuc = np.zeros(G)
+        for z, R in zip(Z, pos):
+            vnuc -= z / np.sqrt(((coords - R) ** 2).sum(-1) + 0.2)
+        V = ao.T @ ((weights * vnuc)[:, None] * ao)
+        mol.h1e = T + V
+        n = ao.shape[1]
+        naux = 3 * n
+        fac = np.empty((naux, n, n))
+        for p in range(naux):
+            R = pos[rng.integers(0, num_atoms)]
+            beta = math.exp(rng.uniform(math.log(0.2), math.log(2.0)))
+            g = np.exp(-beta * ((coords - R) ** 2).sum(-1))
+            fac[p] = 0.3 * (ao.T @ ((weights * g)[:, None] * ao))
+        mol.eri_factors = fac
+    return mol
