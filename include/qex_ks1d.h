@@ -173,6 +173,25 @@ int qex_ks1d_noninteracting(const qex_ks1d_batch* batch, const qex_ks1d_options*
                             double* total_eigen_energy, double* gap, int32_t* status,
                             void* workspace, size_t workspace_bytes, void* stream);
 
+/* Reverse-mode step of one SCF iteration t (the adjoint of
+ * qedft/train/od/jit_scf.py:184-211 with the local convention, as
+ * differentiated by jax.value_and_grad at qedft/train/od/trainer.py:139-143).
+ * Inputs: the iteration's input density n_t (packed), the upstream gradient
+ * with respect to the mixed output density n_{t+1} (packed), the upstream
+ * gradient with respect to this iteration's energy (B; NULL = 0) and its
+ * mixing factor alpha_t.  Outputs: the gradient with respect to n_t (packed)
+ * and, ACCUMULATED into grad_params (B, QEX_MLP_NUM_PARAMS), the gradient
+ * with respect to the window-MLP parameters.  Window-MLP XC in the local
+ * convention, exponential interaction, one mixing difference. */
+int qex_ks1d_adjoint_workspace_size(const qex_ks1d_options* options, int32_t num_molecules,
+                                    size_t* bytes);
+int qex_ks1d_adjoint_step(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
+                          const qex_xc_spec* xc, const double* density_in,
+                          const double* grad_density_next, const double* grad_energy,
+                          double alpha, double* grad_density, double* grad_params,
+                          int32_t* status, void* workspace, size_t workspace_bytes,
+                          void* stream);
+
 /* Library version string and the number of kernel launches the last call on
  * this host thread issued (for launch accounting in benchmarks). */
 const char* qex_version(void);

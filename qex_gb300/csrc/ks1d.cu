@@ -85,6 +85,12 @@ struct Params {
   int32_t* o_iters;
   int32_t* o_stats;
   long long* o_cycles;
+  // adjoint step
+  const double* a_gnext;  // packed upstream gradient w.r.t. the mixed output density
+  const double* a_genergy;  // (B) upstream gradient w.r.t. this iteration's energy
+  double a_alpha;         // mixing factor of this iteration
+  double* a_gn;           // packed gradient w.r.t. the input density
+  double* a_gtheta;       // (B, 577) parameter gradient, accumulated
   double* o_tee;
   // workspace
   double* ws;
@@ -104,7 +110,7 @@ struct SmemLayout {
   int nstr;        // FP32 per-eigenpair stride (nmax rounded to 32k+1)
   size_t s64a, s64b, f32, small, total;
 };
-__host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax) {
+__host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax, bool adjoint = false) {
   SmemLayout L;
   L.nstr = ((nmax + 31) / 32) * 32 + 1;
   size_t off = 0;
@@ -118,6 +124,11 @@ __host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax) {
   size_t eig_floats = (1 + 3 * (size_t)kmax) * L.nstr;
   size_t f = xc_floats > eig_floats ? xc_floats : eig_floats;
   if (hart_floats > f) f = hart_floats;
+  if (adjoint) {
+    // two padded FP32 windows + an FP32 accumulator + per-lane MLP records
+    size_t adj = 3 * (size_t)(nmax + 2 * kPadMlp) + (size_t)kMlpRec * kWarp;
+    if (adj > f) f = adj;
+  }
   off += sizeof(float) * f;
   off = (off + 15) & ~(size_t)15;
   L.small = off;
@@ -1346,6 +1357,311 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
 }
 
 // ---------------------------------------------------------------------------
+// Adjoint of one SCF iteration (local convention, window-MLP XC, exponential
+// interaction, one mixing difference):
+//   n_{t+1} = (1 - a) n_t + a m_t,   m_t = sum_j occ_j phi_j^2 / dx,
+//   v_t = v_H(n_t) + v_xc(n_t; theta) + v_ext,   (phi_j, lambda_j) = eig(T + v_t),
+//   E_t = sum occ lambda - dx<v_t, m_t> + E_H(m_t) + E_xc(m_t; theta) + dx<v_ext, m_t>.
+// Reverse: gm = a gnext + gE dx (v_H(m) + v_xc(m) + v_ext - v_t)   (dE/dv_t = 0),
+//   gv = chi gm (static response: Sternheimer solves of (H - lambda_j) y = -Q(phi_j gm)
+//   in the unoccupied complement, plus occupied pairs of unequal occupation),
+//   gn = (1 - a) gnext + v_H(gv) + d/dn [v_xc(n) . gv],
+//   gtheta += gE d/dtheta E_xc(m) + d/dtheta [v_xc(n) . gv].
+// ---------------------------------------------------------------------------
+
+// FP64 banded (H - shift) x with x staged in sm.s64a, result in ys.
+template <int kBand>
+__device__ inline void banded_apply(const Stencil& st, const double* vks, double shift, int N,
+                                    const double* xs, double* ys, int lane) {
+  for (int i = lane; i < N; i += kWarp) {
+    double y = fma(st.c0 + vks[i] - shift, xs[i], st.b1 * (xs[i - 1] + xs[i + 1]));
+    if (kBand == 2) y = fma(st.b2, xs[i - 2] + xs[i + 2], y);
+    ys[i] = y;
+  }
+  __syncwarp();
+}
+
+// v <- v - sum_k (phi_k . v) phi_k over the nocc occupied orbitals (FP64, in place)
+__device__ inline void project_out(double* v, const double* X, int nmax, int nocc, int N,
+                                   int lane) {
+  for (int k = 0; k < nocc; ++k) {
+    const double* Xk = X + (size_t)k * nmax;
+    double c = 0.0;
+    for (int i = lane; i < N; i += kWarp) c = fma(Xk[i], v[i], c);
+    c = warp_sum(c);
+    for (int i = lane; i < N; i += kWarp) v[i] = fma(-c, Xk[i], v[i]);
+    __syncwarp();
+  }
+}
+
+// gv = chi gm.  Y, Bv: K vectors each (workspace).  Returns the refinement steps used.
+template <int kBand>
+__device__ int sternheimer(const Params& p, int N, double dx, int ne, const double* vks,
+                           const double* X, const double* gm, double* Y, double* Bv, double* gv,
+                           const Smem& sm, int lane) {
+  const Stencil st = make_stencil(p.stencil, dx);
+  const int nocc = (ne + 1) / 2;
+  const int nstr = sm.nstr;
+  float* a32 = sm.f32;
+  float* R = a32 + nstr;
+  float* U = R + (size_t)p.kmax * nstr;
+  float* W = U + (size_t)p.kmax * nstr;
+  double amax = 0.0;
+  for (int i = lane; i < N; i += kWarp) {
+    const double a = st.c0 + vks[i];
+    a32[i] = (float)a;
+    amax = fmax(amax, fabs(a));
+  }
+  amax = warp_max(amax);
+  const double hnorm = amax + 2.0 * fabs(st.b1) + 2.0 * fabs(st.b2);
+  const float pivmin = (float)(1e-20 * hnorm);
+  __syncwarp();
+  if (lane < nocc)
+    ldl_factor<kBand>(a32, N, (float)st.b1, (float)st.b2, (float)sm.theta[lane], pivmin,
+                      R + (size_t)lane * nstr, U + (size_t)lane * nstr);
+  // right-hand sides b_j = -Q (phi_j gm), y_j = 0
+  for (int j = 0; j < nocc; ++j) {
+    const double* Xj = X + (size_t)j * p.nmax;
+    double* Bj = Bv + (size_t)j * p.nmax;
+    for (int i = lane; i < N; i += kWarp) {
+      Bj[i] = -Xj[i] * gm[i];
+      Y[(size_t)j * p.nmax + i] = 0.0;
+    }
+    __syncwarp();
+    project_out(Bj, X, p.nmax, nocc, N, lane);
+  }
+  double* xs = sm.s64a + kPad64;
+  double* ys = sm.s64b + kPad64;
+  int steps = 0;
+  for (; steps < 12; ++steps) {
+    bool need = false;
+    for (int j = 0; j < nocc; ++j) {
+      const double* Bj = Bv + (size_t)j * p.nmax;
+      stage64(sm.s64a, Y + (size_t)j * p.nmax, N, lane);
+      banded_apply<kBand>(st, vks, sm.theta[j], N, xs, ys, lane);
+      project_out(ys, X, p.nmax, nocc, N, lane);
+      double rr = 0.0, bb = 0.0;
+      float* Wj = W + (size_t)j * nstr;
+      for (int i = lane; i < N; i += kWarp) {
+        const double r = Bj[i] - ys[i];
+        rr = fma(r, r, rr);
+        bb = fma(Bj[i], Bj[i], bb);
+        Wj[i] = (float)r;
+      }
+      rr = warp_sum(rr);
+      bb = warp_sum(bb);
+      if (lane == j) need = rr > 1e-26 * bb;
+      __syncwarp();
+    }
+    const unsigned nm = __ballot_sync(kFull, need);
+    if (nm == 0u) break;
+    if (need)
+      ldl_solve<kBand>(N, (float)st.b2, R + (size_t)lane * nstr, U + (size_t)lane * nstr,
+                       W + (size_t)lane * nstr, 1.0f);
+    __syncwarp();
+    for (int j = 0; j < nocc; ++j) {
+      if (!((nm >> j) & 1u)) continue;
+      const float* Wj = W + (size_t)j * nstr;
+      for (int i = lane; i < N; i += kWarp) ys[i] = (double)Wj[i];
+      __syncwarp();
+      project_out(ys, X, p.nmax, nocc, N, lane);
+      double* Yj = Y + (size_t)j * p.nmax;
+      for (int i = lane; i < N; i += kWarp) Yj[i] += ys[i];
+      __syncwarp();
+    }
+  }
+  // gv = sum_j (2 occ_j / dx) phi_j y_j
+  const double inv_dx = 1.0 / dx;
+  for (int i = lane; i < N; i += kWarp) {
+    double v = 0.0;
+    for (int j = 0; j < nocc; ++j)
+      v = fma(2.0 * occupation(j, ne) * inv_dx * X[(size_t)j * p.nmax + i], Y[(size_t)j * p.nmax + i], v);
+    gv[i] = v;
+  }
+  __syncwarp();
+  // occupied pairs of unequal occupation (the half-filled HOMO of odd Ne)
+  if (ne & 1) {
+    const int h = nocc - 1;
+    const double* Xh = X + (size_t)h * p.nmax;
+    for (int k = 0; k < h; ++k) {
+      const double* Xk = X + (size_t)k * p.nmax;
+      double c = 0.0;
+      for (int i = lane; i < N; i += kWarp) c = fma(Xk[i] * Xh[i], gm[i], c);
+      c = warp_sum(c);
+      const double f = 2.0 * inv_dx * (occupation(h, ne) - occupation(k, ne)) /
+                       (sm.theta[h] - sm.theta[k]) * c;
+      for (int i = lane; i < N; i += kWarp) gv[i] = fma(f * Xh[i], Xk[i], gv[i]);
+      __syncwarp();
+    }
+  }
+  return steps;
+}
+
+// One MLP pass for the adjoint over all points of the molecule.
+//   n32 / u32: padded FP32 windows (density / norm, direction / norm)
+//   ybar_i = ya[i] * yscale, dybar_i = with_tangent ? n[i] : 0
+//   xbar scattered into gacc (FP32, padded), dy added to gn (FP64) if with_tangent.
+__device__ void mlp_adjoint_pass(const Params& p, int N, const float* n32, const float* u32,
+                                 bool with_tangent, const double* ya, double yscale,
+                                 const double* nvec, float* gacc, double* gn, float* rec,
+                                 const Smem& sm, double* acc, int lane) {
+  const float ninv = p.mlp.norm_inv;
+  const int rounds = (N + kWarp - 1) / kWarp;
+  const float* zero_win = n32 + N + kPadMlp;  // 8+ zeros
+  for (int r = 0; r < rounds; ++r) {
+    const int i = r * kWarp + lane;
+    const bool act = i < N;
+    const float* win = act ? (n32 + i) : zero_win;
+    const float* twin = (act && with_tangent) ? (u32 + i) : zero_win;
+    // inactive lanes (and the tangent of a pass without one) read a single
+    // zero element with stride 0
+    const int stride = act ? 1 : 0;
+    const int tstride = (act && with_tangent) ? 1 : 0;
+    const float ybar = act ? (float)(ya[i] * yscale) : 0.0f;
+    const float dybar = (act && with_tangent) ? (float)nvec[i] : 0.0f;
+    const float dy = mlp_dual_reverse(sm.mlpw, win, stride, twin, tstride, ybar, dybar,
+                                      rec + lane, kWarp);
+    __syncwarp();
+    mlp_param_grad_round(rec, lane, acc);
+    for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
+      if (act) gacc[i + k] += rec[(147 + k) * kWarp + lane] * ninv;
+      __syncwarp();
+    }
+    if (act && with_tangent) gn[i] += (double)dy;
+    __syncwarp();
+  }
+}
+
+template <int kBand>
+__global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_constant__ Params p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x;
+  const SmemLayout L = smem_layout(p.nmax, p.kmax, true);
+  Smem sm = carve(smem_raw, L);
+  stage_mlp_weights(p.mlp, sm.mlpw, lane, kWarp);
+  __syncwarp();
+  const int slots = p.mix_slots;
+  for (;;) {
+    int slot = 0;
+    if (lane == 0) slot = atomicAdd(p.counter, 1);
+    slot = __shfl_sync(kFull, slot, 0);
+    if (slot >= p.num_molecules) break;
+    const int b = p.order ? p.order[slot] : slot;
+    const int N = p.num_grids[b];
+    const long long off = p.grid_offsets[b];
+    const int ne = p.num_electrons[b];
+    const double x0 = p.grid_start[b];
+    const double dx = p.grid_spacing[b];
+    const int K = ne / 2 + 1;
+    if (N < 5 || N > p.nmax || ne < 1 || K > p.kmax || !(dx > 0.0)) {
+      if (lane == 0 && p.o_status) p.o_status[b] = QEX_BAD_ARG;
+      continue;
+    }
+    double* ws = p.ws + (long long)slot * p.stride;
+    double* vn = ws + (long long)VN * p.nmax;
+    double* vext = ws + (long long)VEXT * p.nmax;
+    double* vks = ws + (long long)VKS * p.nmax;
+    double* nout = ws + (long long)VNOUT * p.nmax;
+    double* vh = ws + (long long)VH * p.nmax;
+    double* vxc = ws + (long long)VXC * p.nmax;
+    double* kt = ws + (long long)VKT * p.nmax;
+    double* X = ws + (long long)(VDIFF + slots) * p.nmax;
+    double* Y = X + (long long)p.kmax * p.nmax;
+    double* Bv = Y + (long long)p.kmax * p.nmax;
+    double* gm = Bv + (long long)p.kmax * p.nmax;
+    double* gv = gm + p.nmax;
+    double* gn = gv + p.nmax;
+    double* t1 = gn + p.nmax;
+    double* t2 = t1 + p.nmax;
+    // external potential
+    {
+      const int M = p.num_nuclei[b];
+      for (int i = lane; i < N; i += kWarp) {
+        double x = x0 + i * dx, v = 0.0;
+        for (int m = 0; m < M; ++m) {
+          double Rm = p.locations[(long long)b * p.max_nuclei + m];
+          double Z = p.charges[(long long)b * p.max_nuclei + m];
+          v -= Z * interaction_fn(p, x - Rm);
+        }
+        vext[i] = v;
+        vn[i] = p.dens_in[off + i];
+      }
+      __syncwarp();
+    }
+    // forward quantities at n_t
+    stage64(sm.s64a, vn, N, lane);
+    hartree(p, N, dx, sm, vh, kt, lane);
+    xc_eval(p, N, dx, sm, true, vxc, nullptr, false, lane);
+    for (int i = lane; i < N; i += kWarp) vks[i] = vh[i] + vxc[i] + vext[i];
+    __syncwarp();
+    EigStats est = {0, 0, 0, 0, {0, 0, 0, 0, 0, 0, 0, 0}};
+    int flags = eigen_solve<kBand>(p, N, dx, ne, K, vks, X, false, 0.0, sm, lane, est);
+    double tee, gap;
+    density_from_orbitals(p, N, dx, ne, K, X, nout, sm, tee, gap, lane);
+    const double gE = p.a_genergy ? p.a_genergy[b] : 0.0;
+    const double at = p.a_alpha;
+    float* n32 = sm.f32;
+    float* u32 = n32 + (p.nmax + 2 * kPadMlp);
+    float* gacc = u32 + (p.nmax + 2 * kPadMlp);
+    float* rec = gacc + (p.nmax + 2 * kPadMlp);
+    double acc[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) acc[q] = 0.0;
+    // ---- gm, and the energy's explicit parameter dependence E_xc(m_t)
+    if (gE != 0.0) {
+      stage64(sm.s64a, nout, N, lane);
+      hartree(p, N, dx, sm, t1, kt, lane);
+      xc_eval(p, N, dx, sm, true, t2, nullptr, false, lane);
+    }
+    for (int i = lane; i < N; i += kWarp) {
+      double g = at * p.a_gnext[off + i];
+      if (gE != 0.0) g += gE * dx * (t1[i] + t2[i] + vext[i] - vks[i]);
+      gm[i] = g;
+    }
+    __syncwarp();
+    if (gE != 0.0) {
+      const float ninv = p.mlp.norm_inv;
+      for (int i = lane; i < N + 2 * kPadMlp; i += kWarp) {
+        const int k = i - kPadMlp;
+        n32[i] = (k >= 0 && k < N) ? (float)nout[k] * ninv : 0.0f;
+        gacc[i] = 0.0f;
+      }
+      __syncwarp();
+      // ybar_i = gE dx m_i (local convention E_xc = dx sum eps_i m_i); no tangent
+      mlp_adjoint_pass(p, N, n32, n32, false, nout, gE * dx, nout, gacc, gn, rec, sm, acc, lane);
+    }
+    // ---- gv = chi gm
+    sternheimer<kBand>(p, N, dx, ne, vks, X, gm, Y, Bv, gv, sm, lane);
+    // ---- gn = (1 - a) gnext + v_H(gv) + d/dn[v_xc(n) . gv]
+    stage64(sm.s64a, gv, N, lane);
+    hartree(p, N, dx, sm, t1, kt, lane);
+    for (int i = lane; i < N; i += kWarp) gn[i] = (1.0 - at) * p.a_gnext[off + i] + t1[i];
+    {
+      const float ninv = p.mlp.norm_inv;
+      for (int i = lane; i < N + 2 * kPadMlp; i += kWarp) {
+        const int k = i - kPadMlp;
+        n32[i] = (k >= 0 && k < N) ? (float)vn[k] * ninv : 0.0f;
+        u32[i] = (k >= 0 && k < N) ? (float)gv[k] * ninv : 0.0f;
+        gacc[i] = 0.0f;
+      }
+      __syncwarp();
+      // local convention: v_xc(n) . u = sum_i [eps_i u_i + n_i D eps_i[u window]]
+      mlp_adjoint_pass(p, N, n32, u32, true, gv, 1.0, vn, gacc, gn, rec, sm, acc, lane);
+      for (int i = lane; i < N; i += kWarp) gn[i] += (double)gacc[i + kPadMlp];
+      __syncwarp();
+    }
+    for (int i = lane; i < N; i += kWarp) p.a_gn[off + i] = gn[i];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+      const int pidx = lane + 32 * q;
+      if (pidx < QEX_MLP_NUM_PARAMS) p.a_gtheta[(long long)b * QEX_MLP_NUM_PARAMS + pidx] += acc[q];
+    }
+    if (lane == 0 && p.o_status) p.o_status[b] = flags;
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 thread_local int g_last_launches = 0;
@@ -1368,9 +1684,11 @@ int check_options(const qex_ks1d_options* o) {
   return QEX_OK;
 }
 
-long long stride_doubles(const qex_ks1d_options* o) {
+long long stride_doubles(const qex_ks1d_options* o, bool adjoint = false) {
   int kmax = o->max_num_electrons / 2 + 1;
-  long long s = vec_count(mix_slots_for(o), kmax) * (long long)o->max_num_grids;
+  long long v = vec_count(mix_slots_for(o), kmax);
+  if (adjoint) v += 2LL * kmax + 5;  // Sternheimer solutions and right-hand sides, 5 vectors
+  long long s = v * (long long)o->max_num_grids;
   return (s + 31) / 32 * 32;
 }
 
@@ -1453,6 +1771,45 @@ int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_opt
       return QEX_BAD_ARG;
     if (o->external_potential_given && !b->external_potential) return QEX_BAD_ARG;
   }
+  return QEX_OK;
+}
+
+int launch_adjoint(const Params& P, cudaStream_t stream) {
+  g_last_launches = 0;
+  if (P.num_molecules == 0) return QEX_OK;
+  const SmemLayout L = smem_layout(P.nmax, P.kmax, true);
+  const size_t smem = L.total;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return QEX_CUDA_ERROR;
+  int sms = 0, max_optin = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if ((int)smem > max_optin) return QEX_BAD_ARG;
+  cudaError_t e;
+  int per_sm = 0;
+  if (P.stencil == 5) {
+    e = cudaFuncSetAttribute(ks1d_adjoint_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return QEX_CUDA_ERROR;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks1d_adjoint_kernel<2>, kWarp, smem);
+  } else {
+    e = cudaFuncSetAttribute(ks1d_adjoint_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return QEX_CUDA_ERROR;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks1d_adjoint_kernel<1>, kWarp, smem);
+  }
+  if (per_sm < 1) per_sm = 1;
+  long long grid = (long long)sms * per_sm;
+  if (grid > P.num_molecules) grid = P.num_molecules;
+  e = cudaMemsetAsync(P.counter, 0, sizeof(int), stream);
+  if (e != cudaSuccess) return QEX_CUDA_ERROR;
+  if (P.stencil == 5) {
+    ks1d_adjoint_kernel<2><<<(unsigned)grid, kWarp, smem, stream>>>(P);
+  } else {
+    ks1d_adjoint_kernel<1><<<(unsigned)grid, kWarp, smem, stream>>>(P);
+  }
+  if (cudaGetLastError() != cudaSuccess) return QEX_CUDA_ERROR;
+  g_last_launches = 1;
   return QEX_OK;
 }
 
@@ -1584,6 +1941,54 @@ int qex_ks1d_iteration(const qex_ks1d_batch* batch, const qex_ks1d_options* opti
   if (rc) return rc;
   P.dens_in = density_in;
   return qex::launch(P, static_cast<cudaStream_t>(stream));
+}
+
+int qex_ks1d_adjoint_workspace_size(const qex_ks1d_options* options, int32_t num_molecules,
+                                    size_t* bytes) {
+  if (!bytes) return QEX_BAD_ARG;
+  *bytes = 0;
+  int rc = qex::check_options(options);
+  if (rc) return rc;
+  if (num_molecules < 0) return QEX_BAD_ARG;
+  *bytes = 256 + sizeof(double) * (size_t)qex::stride_doubles(options, true) * (size_t)num_molecules;
+  return QEX_OK;
+}
+
+int qex_ks1d_adjoint_step(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
+                          const qex_xc_spec* xc, const double* density_in,
+                          const double* grad_density_next, const double* grad_energy,
+                          double alpha, double* grad_density, double* grad_params,
+                          int32_t* status, void* workspace, size_t workspace_bytes,
+                          void* stream) {
+  if (!batch || !options || !xc || !density_in || !grad_density_next || !grad_density ||
+      !grad_params)
+    return QEX_BAD_ARG;
+  if (xc->kind != QEX_XC_WINDOW_MLP || xc->convention != QEX_XC_LOCAL) return QEX_BAD_ARG;
+  if (options->interaction != QEX_INTERACTION_EXPONENTIAL || options->enforce_reflection_symmetry ||
+      options->external_potential_given || options->num_mixing_iterations != 1)
+    return QEX_BAD_ARG;
+  size_t need = 0;
+  int rc = qex_ks1d_adjoint_workspace_size(options, batch->num_molecules, &need);
+  if (rc) return rc;
+  if (!workspace || workspace_bytes < need) return QEX_BAD_ARG;
+  qex_ks1d_options o = *options;
+  o.num_iterations = 1;
+  qex_ks1d_outputs out;
+  memset(&out, 0, sizeof(out));
+  out.status = status;
+  qex::Params P;
+  // fill_params checks the forward workspace size, which the adjoint one exceeds
+  rc = qex::fill_params(P, qex::kModeIteration, batch, &o, xc, &out, workspace, workspace_bytes,
+                        batch->num_molecules);
+  if (rc) return rc;
+  P.stride = qex::stride_doubles(&o, true);
+  P.dens_in = density_in;
+  P.a_gnext = grad_density_next;
+  P.a_genergy = grad_energy;
+  P.a_alpha = alpha;
+  P.a_gn = grad_density;
+  P.a_gtheta = grad_params;
+  return qex::launch_adjoint(P, static_cast<cudaStream_t>(stream));
 }
 
 int qex_ks1d_noninteracting(const qex_ks1d_batch* batch, const qex_ks1d_options* options,

@@ -497,7 +497,8 @@ __device__ int jacobi(int n, double* C, double* U, int* pos, double* cs, int* pq
     }
     off = block_sum(off, red);
     dia = block_sum(dia, red);
-    if (off <= 1e-30 * dia || off == 0.0) return sweep;
+    // converged when the off-diagonal norm is 1e-14 of the diagonal (the FP64 floor is ~1e-16)
+    if (off <= 1e-28 * dia || off == 0.0) return sweep;
     for (int step = 0; step < m - 1; ++step) {
       // pairs of this round-robin step
       for (int k = threadIdx.x; k < m / 2; k += blockDim.x) {

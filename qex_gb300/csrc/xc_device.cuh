@@ -170,6 +170,189 @@ __device__ inline float mlp_point(const float* W, const float* win, int wstride,
   return out;
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint support: dual-number forward (value y and tangent dy along the input
+// direction t) followed by the reverse pass of  ybar * y + dybar * dy.
+// Per-lane shared records (stride rs) for the parameter-gradient reduction:
+//   [0,17) x   [17,34) t   [34,50) zbar1  [50,66) dzbar1  [66,82) h1
+//   [82,98) dh1  [98,114) zbar2  [114,130) dzbar2  [130,146) w3bar  [146] ybar
+//   [147,164) xbar (d/dx of the objective, not a parameter record)
+// Returns dy.
+constexpr int kMlpRec = 164;
+
+__device__ inline float silu_dd(float z, float& d1, float& d2) {
+  float s = 1.0f / (1.0f + __expf(-z));
+  d1 = s * (1.0f + z * (1.0f - s));
+  d2 = s * (1.0f - s) * (2.0f + z * (1.0f - 2.0f * s));
+  return z * s;
+}
+
+__device__ inline float mlp_dual_reverse(const float* W, const float* win, int wstride,
+                                         const float* twin, int tstride, float ybar, float dybar,
+                                         float* rec, int rs) {
+  float z[QEX_MLP_HIDDEN], dz[QEX_MLP_HIDDEN];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    mlp_load4(W, 272 + 4 * q, z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+    dz[4 * q] = dz[4 * q + 1] = dz[4 * q + 2] = dz[4 * q + 3] = 0.0f;
+  }
+#pragma unroll 1
+  for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
+    const float x = win[k * wstride], t = twin[k * tstride];
+    rec[k * rs] = x;
+    rec[(17 + k) * rs] = t;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float a, b, c, d;
+      mlp_load4(W, 16 * k + 4 * q, a, b, c, d);
+      z[4 * q] = fmaf(x, a, z[4 * q]);
+      z[4 * q + 1] = fmaf(x, b, z[4 * q + 1]);
+      z[4 * q + 2] = fmaf(x, c, z[4 * q + 2]);
+      z[4 * q + 3] = fmaf(x, d, z[4 * q + 3]);
+      dz[4 * q] = fmaf(t, a, dz[4 * q]);
+      dz[4 * q + 1] = fmaf(t, b, dz[4 * q + 1]);
+      dz[4 * q + 2] = fmaf(t, c, dz[4 * q + 2]);
+      dz[4 * q + 3] = fmaf(t, d, dz[4 * q + 3]);
+    }
+  }
+  // layer 1 activations: h1, dh1 to records; keep s1', s1'' * dz1 for the reverse
+  float s1p[QEX_MLP_HIDDEN], s1q[QEX_MLP_HIDDEN];
+#pragma unroll
+  for (int h = 0; h < QEX_MLP_HIDDEN; ++h) {
+    float d1, d2;
+    const float a = silu_dd(z[h], d1, d2);
+    rec[(66 + h) * rs] = a;
+    rec[(82 + h) * rs] = d1 * dz[h];
+    s1p[h] = d1;
+    s1q[h] = d2 * dz[h];
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    mlp_load4(W, 544 + 4 * q, z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+    dz[4 * q] = dz[4 * q + 1] = dz[4 * q + 2] = dz[4 * q + 3] = 0.0f;
+  }
+#pragma unroll 1
+  for (int k = 0; k < QEX_MLP_HIDDEN; ++k) {
+    const float x = rec[(66 + k) * rs], t = rec[(82 + k) * rs];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float a, b, c, d;
+      mlp_load4(W, 288 + 16 * k + 4 * q, a, b, c, d);
+      z[4 * q] = fmaf(x, a, z[4 * q]);
+      z[4 * q + 1] = fmaf(x, b, z[4 * q + 1]);
+      z[4 * q + 2] = fmaf(x, c, z[4 * q + 2]);
+      z[4 * q + 3] = fmaf(x, d, z[4 * q + 3]);
+      dz[4 * q] = fmaf(t, a, dz[4 * q]);
+      dz[4 * q + 1] = fmaf(t, b, dz[4 * q + 1]);
+      dz[4 * q + 2] = fmaf(t, c, dz[4 * q + 2]);
+      dz[4 * q + 3] = fmaf(t, d, dz[4 * q + 3]);
+    }
+  }
+  // layer 2, output, and the reverse of the output layer
+  float dy = 0.0f;
+  float zb2[QEX_MLP_HIDDEN], dzb2[QEX_MLP_HIDDEN];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    float w3[4];
+    mlp_load4(W, 560 + 4 * q, w3[0], w3[1], w3[2], w3[3]);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int h = 4 * q + e;
+      float d1, d2;
+      const float h2 = silu_dd(z[h], d1, d2);
+      const float dh2 = d1 * dz[h];
+      dy = fmaf(w3[e], dh2, dy);
+      rec[(130 + h) * rs] = ybar * h2 + dybar * dh2;  // w3bar
+      const float hb2 = ybar * w3[e], dhb2 = dybar * w3[e];
+      zb2[h] = hb2 * d1 + dhb2 * d2 * dz[h];
+      dzb2[h] = dhb2 * d1;
+      rec[(98 + h) * rs] = zb2[h];
+      rec[(114 + h) * rs] = dzb2[h];
+    }
+  }
+  rec[146 * rs] = ybar;
+  // reverse of layer 2: hbar1 = W2 zbar2, dhbar1 = W2 dzbar2
+#pragma unroll 1
+  for (int k = 0; k < QEX_MLP_HIDDEN; ++k) {
+    float hb = 0.0f, dhb = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float r0, r1, r2, r3;
+      mlp_load4(W, 288 + 16 * k + 4 * q, r0, r1, r2, r3);
+      hb = fmaf(r0, zb2[4 * q], hb);
+      hb = fmaf(r1, zb2[4 * q + 1], hb);
+      hb = fmaf(r2, zb2[4 * q + 2], hb);
+      hb = fmaf(r3, zb2[4 * q + 3], hb);
+      dhb = fmaf(r0, dzb2[4 * q], dhb);
+      dhb = fmaf(r1, dzb2[4 * q + 1], dhb);
+      dhb = fmaf(r2, dzb2[4 * q + 2], dhb);
+      dhb = fmaf(r3, dzb2[4 * q + 3], dhb);
+    }
+    // zbar1 = hbar1 s1' + dhbar1 s1'' dz1 ; dzbar1 = dhbar1 s1'
+    rec[(34 + k) * rs] = hb;   // temporarily hbar1
+    rec[(50 + k) * rs] = dhb;  // temporarily dhbar1
+  }
+  float zb1[QEX_MLP_HIDDEN];
+#pragma unroll
+  for (int h = 0; h < QEX_MLP_HIDDEN; ++h) {
+    const float hb = rec[(34 + h) * rs], dhb = rec[(50 + h) * rs];
+    zb1[h] = hb * s1p[h] + dhb * s1q[h];
+    rec[(34 + h) * rs] = zb1[h];
+    rec[(50 + h) * rs] = dhb * s1p[h];
+  }
+  // xbar = W1 zbar1
+#pragma unroll 1
+  for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
+    float a = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float r0, r1, r2, r3;
+      mlp_load4(W, 16 * k + 4 * q, r0, r1, r2, r3);
+      a = fmaf(r0, zb1[4 * q], a);
+      a = fmaf(r1, zb1[4 * q + 1], a);
+      a = fmaf(r2, zb1[4 * q + 2], a);
+      a = fmaf(r3, zb1[4 * q + 3], a);
+    }
+    rec[(147 + k) * rs] = a;
+  }
+  return dy;
+}
+
+// Parameter gradient of one round: sum over the 32 lanes' records, parameter p
+// handled by lane p % 32 into acc[p / 32] (FP64 accumulators).
+__device__ inline void mlp_param_grad_round(const float* recbase, int lane, double* acc) {
+  // recbase: records of lane l at recbase[f * 32 + l]
+#pragma unroll
+  for (int q = 0; q < 19; ++q) {
+    const int pidx = lane + 32 * q;
+    if (pidx >= 577) break;
+    float s = 0.0f;
+    if (pidx < 272) {
+      const int a = pidx >> 4, h = pidx & 15;
+      for (int l = 0; l < 32; ++l)
+        s += recbase[a * 32 + l] * recbase[(34 + h) * 32 + l] +
+             recbase[(17 + a) * 32 + l] * recbase[(50 + h) * 32 + l];
+    } else if (pidx < 288) {
+      const int h = pidx - 272;
+      for (int l = 0; l < 32; ++l) s += recbase[(34 + h) * 32 + l];
+    } else if (pidx < 544) {
+      const int a = (pidx - 288) >> 4, h = (pidx - 288) & 15;
+      for (int l = 0; l < 32; ++l)
+        s += recbase[(66 + a) * 32 + l] * recbase[(98 + h) * 32 + l] +
+             recbase[(82 + a) * 32 + l] * recbase[(114 + h) * 32 + l];
+    } else if (pidx < 560) {
+      const int h = pidx - 544;
+      for (int l = 0; l < 32; ++l) s += recbase[(98 + h) * 32 + l];
+    } else if (pidx < 576) {
+      const int h = pidx - 560;
+      for (int l = 0; l < 32; ++l) s += recbase[(130 + h) * 32 + l];
+    } else {
+      for (int l = 0; l < 32; ++l) s += recbase[146 * 32 + l];
+    }
+    acc[q] += (double)s;
+  }
+}
+
 // Copy the weights of a by-value MlpParams into shared memory (one warp or CTA).
 __device__ inline void stage_mlp_weights(const MlpParams& m, float* dst, int tid, int nthreads) {
   const float* src = reinterpret_cast<const float*>(&m);

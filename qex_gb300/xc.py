@@ -106,8 +106,8 @@ class WindowMLPFunctional(XCFunctional):
         return np.ascontiguousarray(flat, dtype=np.float32)
 
     @staticmethod
-    def unflatten(flat):
-        flat = np.asarray(flat, np.float32)
+    def unflatten(flat, dtype=np.float32):
+        flat = np.asarray(flat, dtype)
         i = 0
         out = []
         for fi, fo in ((N.MLP_WINDOW, N.MLP_HIDDEN), (N.MLP_HIDDEN, N.MLP_HIDDEN), (N.MLP_HIDDEN, 1)):
