@@ -163,7 +163,7 @@ def fp64_flops(mols, iterations_run, stats):
         n = m.num_grids
         nocc = (m.num_electrons + 1) // 2
         k = m.num_electrons // 2 + 1
-        solves, rq_vec, upd, _ = (int(x) for x in st)
+        solves, rq_vec, upd = (int(x) for x in st[:3])
         # per SCF iteration: two Hartree scans (15 N each), v_KS assembly (5 N),
         # energies (4 N), mixing (10 N), density (4 N nocc), XC energy sums (4 N)
         per_iter = (30 + 5 + 4 + 10 + 4) * n + 4 * n * nocc

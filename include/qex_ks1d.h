@@ -124,11 +124,16 @@ typedef struct qex_ks1d_outputs {
   double* external_potential_out; /* packed (sum N) */
   int32_t* status;           /* (B) */
   int32_t* iterations_run;   /* (B) iterations that did work (not skipped as converged) */
-  int32_t* stats;            /* (B, 4): eigen-solves, Rayleigh-quotient vector passes,
-                                correction updates, Sturm multisection passes */
-  int64_t* phase_cycles;     /* (B, 8): SM clock cycles per phase: Hartree, XC potential,
+  int32_t* stats;            /* (B, 8): eigen-solves, Rayleigh-quotient vector passes,
+                                correction updates, Sturm multisection passes,
+                                warm-route attempts, 3 reserved */
+  int64_t* phase_cycles;     /* (B, 16): SM clock cycles per phase: Hartree, XC potential,
                                 Sturm brackets, FP32 inverse iteration, FP64 refinement,
-                                density+energy, mixing+records, whole molecule */
+                                density+energy, mixing+records, whole molecule; then
+                                parts of those: start vectors, FP32 factorisation,
+                                FP32 solves (inverse iteration), Rayleigh quotients and
+                                residuals, FP32 correction solves, FP64 updates, XC
+                                energy, cluster Rayleigh-Ritz + normalisation */
 } qex_ks1d_outputs;
 
 /* Bytes of device workspace qex_ks1d_solve needs for this batch shape. */

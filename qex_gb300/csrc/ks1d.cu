@@ -95,6 +95,7 @@ struct Params {
   // workspace
   double* ws;
   long long stride;  // doubles per molecule
+  long long ruw_doubles;  // leading streamed-solve area of a molecule's workspace
   int* counter;
   MlpParams mlp;
 };
@@ -102,30 +103,48 @@ struct Params {
 // Workspace vectors (each nmax doubles) per molecule.
 enum Vec { VN = 0, VEXT, VKS, VNOUT, VH, VXC, VF, VKT, VDIFF };
 __host__ __device__ inline long long vec_count(int mix_slots, int kmax) {
-  return VDIFF + mix_slots + kmax;
+  return VDIFF + mix_slots + kmax + 2;  // eigenvectors, H x and the FP64 diagonal
 }
 
 // Shared-memory layout of one warp (one molecule in flight).
 struct SmemLayout {
   int nstr;        // FP32 per-eigenpair stride (nmax rounded to 32k+1)
-  size_t s64a, s64b, f32, small, total;
+  size_t s64a, s64b, f32, ring, small, total;
 };
+
+// Rows of the streamed-solve area (whole chunks) and its size in doubles.
+__host__ __device__ inline long long ruw_rows(int nmax) {
+  return (long long)(nmax + kChunk - 1) / kChunk * kChunk;
+}
+__host__ __device__ inline long long ruw_doubles(int nmax, int kmax) {
+  return ruw_rows(nmax) * kmax * 3 / 2;  // a float2 and a float per point and eigenpair
+}
+
 __host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax, bool adjoint = false) {
   SmemLayout L;
   L.nstr = ((nmax + 31) / 32) * 32 + 1;
   size_t off = 0;
   L.s64a = off;
   off += sizeof(double) * (nmax + 2 * kPad64);
+  // the second FP64 staging vector and the shared-memory factor arrays are
+  // used by the adjoint's Sternheimer solves only
   L.s64b = off;
-  off += sizeof(double) * (nmax + 2 * kPad64);
+  if (adjoint) off += sizeof(double) * (nmax + 2 * kPad64);
+  off = (off + 15) & ~(size_t)15;  // float4 ring and RR matrices below
   L.f32 = off;
   size_t xc_floats = 2 * (size_t)(nmax + 2 * kPadMlp) + (size_t)kMlpScratch * kWarp;
   size_t hart_floats = 2 * (size_t)nmax + 2;  // one FP64 scan vector
-  size_t eig_floats = (1 + 3 * (size_t)kmax) * L.nstr;
+  // FP32 diagonal, then the ring of the streamed solves (16-byte aligned)
+  const size_t ring_off = ((size_t)L.nstr + 3) / 4 * 4;
+  L.ring = L.f32 + sizeof(float) * ring_off;
+  size_t eig_floats = ring_off + (size_t)kRing * kChunk * kmax * 3;  // float2 + float
   size_t f = xc_floats > eig_floats ? xc_floats : eig_floats;
   if (hart_floats > f) f = hart_floats;
   if (adjoint) {
-    // two padded FP32 windows + an FP32 accumulator + per-lane MLP records
+    // Sternheimer factor arrays; two padded FP32 windows + an FP32
+    // accumulator + per-lane MLP records
+    size_t st = (1 + 3 * (size_t)kmax) * L.nstr;
+    if (st > f) f = st;
     size_t adj = 3 * (size_t)(nmax + 2 * kPadMlp) + (size_t)kMlpRec * kWarp;
     if (adj > f) f = adj;
   }
@@ -149,6 +168,7 @@ struct Smem {
   double* s64a;  // padded FP64 staging (index kPad64 + i)
   double* s64b;
   float* f32;
+  float4* ring;
   float* lo;
   float* hi;
   float* sig;
@@ -168,6 +188,7 @@ __device__ inline Smem carve(unsigned char* base, const SmemLayout& L) {
   s.s64a = reinterpret_cast<double*>(base + L.s64a);
   s.s64b = reinterpret_cast<double*>(base + L.s64b);
   s.f32 = reinterpret_cast<float*>(base + L.f32);
+  s.ring = reinterpret_cast<float4*>(base + L.ring);
   unsigned char* p = base + L.small;
   s.lo = reinterpret_cast<float*>(p);
   p += sizeof(float) * kMaxBis;
@@ -227,6 +248,7 @@ __device__ inline double interaction_fn(const Params& p, double d) {
 
 // Stage a global FP64 vector into a padded shared buffer (zeros outside [0,N)).
 __device__ inline void stage64(double* s, const double* g, int N, int lane) {
+  #pragma unroll 1
   for (int i = lane; i < N + 2 * kPad64; i += kWarp) {
     int k = i - kPad64;
     s[i] = (k >= 0 && k < N) ? g[k] : 0.0;
@@ -238,7 +260,7 @@ __device__ inline void stage64(double* s, const double* g, int N, int lane) {
 // Hartree: out_i = dx * sum_j n_j K(x_i - x_j)       (qedft/train/od/scf.py:303-308)
 // n is staged in sm.s64a (padded).  Returns sum_i n_i * out_i (warp-uniform).
 // ---------------------------------------------------------------------------
-__device__ double hartree(const Params& p, int N, double dx, const Smem& sm, double* out,
+__device__ __noinline__ double hartree(const Params& p, int N, double dx, const Smem& sm, double* out,
                           const double* kt, int lane) {
   const double* n = sm.s64a + kPad64;
   double acc_e = 0.0;
@@ -251,6 +273,7 @@ __device__ double hartree(const Params& p, int N, double dx, const Smem& sm, dou
     const int beg = min(lane * C, N);
     const int end = min(beg + C, N);
     double s = 0.0, f = 1.0;
+#pragma unroll 1
     for (int i = beg; i < end; ++i) {
       s = fma(s, rho, n[i]);
       f *= rho;
@@ -266,12 +289,14 @@ __device__ double hartree(const Params& p, int N, double dx, const Smem& sm, dou
     }
     double x = __shfl_up_sync(kFull, s, 1);
     if (lane == 0) x = 0.0;
+#pragma unroll 1
     for (int i = beg; i < end; ++i) {
       x = fma(x, rho, n[i]);
       fwd[i] = x;
     }
     s = 0.0;
     f = 1.0;
+#pragma unroll 1
     for (int i = end - 1; i >= beg; --i) {
       s = fma(s, rho, n[i]);
       f *= rho;
@@ -288,6 +313,7 @@ __device__ double hartree(const Params& p, int N, double dx, const Smem& sm, dou
     double y = __shfl_down_sync(kFull, s, 1);
     if (lane == kWarp - 1) y = 0.0;
     const double scale = p.ia * dx;
+#pragma unroll 1
     for (int i = end - 1; i >= beg; --i) {
       y = fma(y, rho, n[i]);
       double v = scale * (fwd[i] + y - n[i]);
@@ -298,8 +324,10 @@ __device__ double hartree(const Params& p, int N, double dx, const Smem& sm, dou
   } else {
     // General (soft-Coulomb) kernel: direct Toeplitz sum with the kernel row
     // kt[d] = K(d dx) tabulated once per molecule.
+    #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) {
       double v = 0.0;
+#pragma unroll 1
       for (int j = 0; j < N; ++j) v = fma(n[j], kt[abs(i - j)], v);
       v *= dx;
       out[i] = v;
@@ -316,6 +344,7 @@ __device__ double hartree(const Params& p, int N, double dx, const Smem& sm, dou
 // Flip-average v about the grid centre in place (jax_dft
 // jit_scf._flip_and_average_on_center, qedft/train/od/jit_scf.py:76-77).
 __device__ inline void flip_avg_global(double* v, int N, int lane) {
+  #pragma unroll 1
   for (int i = lane; i < N / 2; i += kWarp) {
     double a = v[i], b = v[N - 1 - i];
     double m = 0.5 * (a + b);
@@ -330,12 +359,13 @@ __device__ inline void flip_avg_global(double* v, int N, int lane) {
 // Returns E_xc (already multiplied by dx).  With reflect_xc the functional is
 // symmetrised (local convention, jax_dft kohn_sham_iteration): the staged
 // density must already be flip-averaged; outputs are flip-averaged here.
-__device__ double xc_eval(const Params& p, int N, double dx, const Smem& sm, bool want_v,
+__device__ __noinline__ double xc_eval(const Params& p, int N, double dx, const Smem& sm, bool want_v,
                           double* vout, double* frec, bool reflect_xc, int lane) {
   const double* n = sm.s64a + kPad64;
   const bool local = (p.xc_conv == QEX_XC_LOCAL);
   double e = 0.0;
   if (p.xc_kind == QEX_XC_NONE) {
+    #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) {
       if (want_v) vout[i] = 0.0;
       if (frec) frec[i] = 0.0;
@@ -344,6 +374,7 @@ __device__ double xc_eval(const Params& p, int N, double dx, const Smem& sm, boo
     return 0.0;
   }
   if (p.xc_kind == QEX_XC_LDA_EXP_COULOMB || p.xc_kind == QEX_XC_POWER) {
+    #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) {
       double ni = n[i], f, df;
       if (p.xc_kind == QEX_XC_LDA_EXP_COULOMB) {
@@ -369,6 +400,7 @@ __device__ double xc_eval(const Params& p, int N, double dx, const Smem& sm, boo
     float* n32 = sm.f32;
     float* vacc = sm.f32 + (p.nmax + 2 * kPadMlp);
     const float ninv = p.mlp.norm_inv;
+    #pragma unroll 1
     for (int i = lane; i < N + 2 * kPadMlp; i += kWarp) {
       int k = i - kPadMlp;
       n32[i] = (k >= 0 && k < N) ? (float)n[k] * ninv : 0.0f;
@@ -409,6 +441,7 @@ __device__ double xc_eval(const Params& p, int N, double dx, const Smem& sm, boo
       }
     }
     if (want_v) {
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) {
         double v = (double)vacc[i + kPadMlp];
         vout[i] = local ? v : dx * v;
@@ -529,11 +562,334 @@ __device__ inline float ldl_solve(int N, float b2, const float* R, const float* 
   return mx;
 }
 
+// ---------------------------------------------------------------------------
+// Streamed FP32 solves.  The factors and iterates of the K shifted systems live
+// in global workspace in two planes with point-major rows of kmax entries: RU
+// (float2 {r = 1/d_i, u_i}) and W (the right-hand side / solution w_i).  They
+// pass through a ring of kRing chunks of kChunk points in shared memory
+// (cp.async, kRing - 1 chunks in flight), so that the shared-memory footprint
+// of a warp does not grow with N * K.
+// ---------------------------------------------------------------------------
+__device__ inline void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int kPending>
+__device__ inline void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(kPending) : "memory");
+}
+
+// The two planes of a molecule's solve area (rows = ruw_rows(nmax)).
+struct SolveArea {
+  float2* ru;
+  float* w;
+  int kmax;
+  __device__ float& at(int i, int j) const { return w[(size_t)i * kmax + j]; }
+};
+
+// One sweep over points 0..N-1 (kFwd) or N-1..0: lanes with act call
+// step(i, ru, w) in order on their own entries (in shared memory); the chunk's
+// W entries (and RU with kStoreRU) are then written back.  RU is read only
+// with kLoadRU.  The area holds whole chunks, so every copy is in bounds.
+template <bool kFwd, bool kLoadRU, bool kStoreRU, typename Step>
+__device__ __noinline__ Step ring_sweep(SolveArea g, int N, bool act, float4* ring, int lane,
+                                        Step step) {
+  const int kmax = g.kmax;
+  const int nc = (N + kChunk - 1) / kChunk;
+  const int per = kChunk * kmax;            // entries per chunk
+  const int ru16 = per / 2, w16 = per / 4;  // 16-byte pieces per chunk and plane
+  float2* rring = reinterpret_cast<float2*>(ring);
+  float* wring = reinterpret_cast<float*>(rring + (size_t)kRing * per);
+  auto issue = [&](int k) {
+    if (k < nc) {
+      const int c = kFwd ? k : nc - 1 - k;
+      const int s = k % kRing;
+      if (kLoadRU) {
+        const float4* src = reinterpret_cast<const float4*>(g.ru + (size_t)c * per);
+        float4* dst = reinterpret_cast<float4*>(rring + (size_t)s * per);
+#pragma unroll 1
+        for (int e = lane; e < ru16; e += kWarp) cp_async16(dst + e, src + e);
+      }
+      const float4* src = reinterpret_cast<const float4*>(g.w + (size_t)c * per);
+      float4* dst = reinterpret_cast<float4*>(wring + (size_t)s * per);
+#pragma unroll 1
+      for (int e = lane; e < w16; e += kWarp) cp_async16(dst + e, src + e);
+    }
+    cp_async_commit();
+  };
+#pragma unroll 1
+  for (int k = 0; k < kRing - 1; ++k) issue(k);
+#pragma unroll 1
+  for (int k = 0; k < nc; ++k) {
+    cp_async_wait<kRing - 2>();
+    __syncwarp();
+    const int s = k % kRing;
+    float2* rs = rring + (size_t)s * per + lane;
+    float* ws = wring + (size_t)s * per + lane;
+    const int c = kFwd ? k : nc - 1 - k;
+    const int i0 = c * kChunk;
+    const int n = min(kChunk, N - i0);
+    if (act) {
+      if (kFwd) {
+#pragma unroll 4
+        for (int ii = 0; ii < n; ++ii) step(i0 + ii, rs[ii * kmax], ws[ii * kmax]);
+      } else {
+#pragma unroll 4
+        for (int ii = n - 1; ii >= 0; --ii) step(i0 + ii, rs[ii * kmax], ws[ii * kmax]);
+      }
+    }
+    __syncwarp();
+    if (kStoreRU) {
+      float4* dst = reinterpret_cast<float4*>(g.ru + (size_t)c * per);
+      const float4* src = reinterpret_cast<const float4*>(rring + (size_t)s * per);
+#pragma unroll 1
+      for (int e = lane; e < ru16; e += kWarp) dst[e] = src[e];
+    }
+    {
+      float4* dst = reinterpret_cast<float4*>(g.w + (size_t)c * per);
+      const float4* src = reinterpret_cast<const float4*>(wring + (size_t)s * per);
+#pragma unroll 1
+      for (int e = lane; e < w16; e += kWarp) dst[e] = src[e];
+    }
+    __syncwarp();
+    issue(k + kRing - 1);
+  }
+  cp_async_wait<0>();
+  __syncwarp();
+  return step;
+}
+
+__device__ inline SolveArea solve_area(double* base, int nmax, int kmax) {
+  SolveArea a;
+  a.ru = reinterpret_cast<float2*>(base);
+  a.w = reinterpret_cast<float*>(a.ru + ruw_rows(nmax) * kmax);
+  a.kmax = kmax;
+  return a;
+}
+
+// L D L^T factorisation of H32 - sigma fused with the forward substitution
+// L z = w (w overwritten by D^-1 z).
+template <int kBand>
+struct FactorForward {
+  const float* a32;
+  float b1, b2, sigma, pivmin;
+  float r1 = 0.0f, r2 = 0.0f, u1 = 0.0f, z1 = 0.0f, z2 = 0.0f;
+  __device__ void operator()(int i, float2& ru, float& w) {
+    float d, u;
+    if (kBand == 2) {
+      const float t = fmaf(-b2, u1, b1);
+      u = t * r1;
+      d = fmaf(-u, t, a32[i] - sigma);
+      d = fmaf(-b2 * b2, r2, d);
+    } else {
+      u = b1 * r1;
+      d = fmaf(-u, b1, a32[i] - sigma);
+    }
+    if (fabsf(d) < pivmin) d = (d < 0.0f) ? -pivmin : pivmin;
+    const float r = __fdividef(1.0f, d);
+    float z = fmaf(-u, z1, w);
+    if (kBand == 2) z = fmaf(-b2 * r2, z2, z);
+    ru = make_float2(r, u);
+    w = z * r;
+    r2 = r1;
+    r1 = r;
+    u1 = u;
+    z2 = z1;
+    z1 = z;
+  }
+};
+
+// Forward substitution with stored factors: w <- D^-1 L^-1 (scale w).
+template <int kBand>
+struct SolveForward {
+  float b2, scale;
+  float r1 = 0.0f, r2 = 0.0f, z1 = 0.0f, z2 = 0.0f;
+  __device__ void operator()(int, float2& ru, float& w) {
+    float z = fmaf(-ru.y, z1, w * scale);
+    if (kBand == 2) z = fmaf(-b2 * r2, z2, z);
+    w = z * ru.x;
+    r2 = r1;
+    r1 = ru.x;
+    z2 = z1;
+    z1 = z;
+  }
+};
+
+// Back substitution L^T y = w in place; tracks max |y|.
+template <int kBand>
+struct SolveBackward {
+  float b2;
+  float un = 0.0f, y1 = 0.0f, y2 = 0.0f, mx = 0.0f;
+  __device__ void operator()(int, float2& ru, float& w) {
+    float y = fmaf(-un, y1, w);
+    if (kBand == 2) y = fmaf(-b2 * ru.x, y2, y);
+    w = y;
+    mx = fmaxf(mx, fabsf(y));
+    y2 = y1;
+    y1 = y;
+    un = ru.y;
+  }
+};
+
 // Work counters of one eigen-solve (for the roofline tally of the benchmark).
 struct EigStats {
-  int solves, rq_vectors, updates, passes;
-  long long cyc[8];  // clock64 cycles per phase (see write_stats)
+  int solves, rq_vectors, updates, passes, fast;
+  long long cyc[kPhases];  // clock64 cycles per phase (see write_stats)
 };
+
+// Adds the cycles since t to phase k and restarts t.
+__device__ inline void lap(EigStats& e, long long& t, int k) {
+  const long long now = clock64();
+  e.cyc[k] += now - t;
+  t = now;
+}
+
+// Rayleigh-Ritz inside each near-degenerate cluster of eigenpairs (FP64):
+// Gram-Schmidt, projected matrix, cyclic Jacobi with the rotations applied to
+// the vectors directly, ascending order.  Updates X and sm.theta.
+template <int kBand>
+__device__ __noinline__ void cluster_rayleigh_ritz(const Params& p, int N, int K, const Stencil& st,
+                                                   const double* vks, double* X, double* YR,
+                                                   const Smem& sm, int lane) {
+  const double* xs = sm.s64a + kPad64;
+
+      int j0 = 0;
+      while (j0 < K) {
+        int j1 = j0;
+        while (j1 + 1 < K && sm.clus[j1 + 1] == sm.clus[j0]) ++j1;
+        const int s = j1 - j0 + 1;
+        if (s >= 2) {
+          for (int a = j0; a <= j1; ++a) {
+            double* Xa = X + (size_t)a * p.nmax;
+            for (int b = j0; b < a; ++b) {
+              const double* Xb = X + (size_t)b * p.nmax;
+              double d = 0.0;
+              #pragma unroll 1
+              for (int i = lane; i < N; i += kWarp) d = fma(Xa[i], Xb[i], d);
+              d = warp_sum(d);
+              #pragma unroll 1
+              for (int i = lane; i < N; i += kWarp) Xa[i] = fma(-d, Xb[i], Xa[i]);
+              __syncwarp();
+            }
+            double nn = 0.0;
+            #pragma unroll 1
+            for (int i = lane; i < N; i += kWarp) nn = fma(Xa[i], Xa[i], nn);
+            nn = warp_sum(nn);
+            double inv = 1.0 / sqrt(nn);
+            #pragma unroll 1
+            for (int i = lane; i < N; i += kWarp) Xa[i] *= inv;
+            __syncwarp();
+          }
+          // projected matrix in the (free) FP32 work area, 16-byte aligned
+          double* A = reinterpret_cast<double*>(sm.f32);
+          for (int b = j0; b <= j1; ++b) {
+            stage64(sm.s64a, X + (size_t)b * p.nmax, N, lane);
+            #pragma unroll 1
+            for (int i = lane; i < N; i += kWarp) {
+              double y = fma(st.c0 + vks[i], xs[i], st.b1 * (xs[i - 1] + xs[i + 1]));
+              if (kBand == 2) y = fma(st.b2, xs[i - 2] + xs[i + 2], y);
+              YR[i] = y;
+            }
+            __syncwarp();
+            for (int a = j0; a <= b; ++a) {
+              const double* Xa = X + (size_t)a * p.nmax;
+              double d = 0.0;
+              #pragma unroll 1
+              for (int i = lane; i < N; i += kWarp) d = fma(Xa[i], YR[i], d);
+              d = warp_sum(d);
+              if (lane == 0) {
+                A[(a - j0) * s + (b - j0)] = d;
+                A[(b - j0) * s + (a - j0)] = d;
+              }
+            }
+            __syncwarp();
+          }
+          for (int sweep = 0; sweep < 30; ++sweep) {
+            if (lane == 0) {
+              double off = 0.0, dia = 0.0;
+              for (int a = 0; a < s; ++a) {
+                dia += A[a * s + a] * A[a * s + a];
+                for (int b = a + 1; b < s; ++b) off += A[a * s + b] * A[a * s + b];
+              }
+              sm.aux[2] = (off <= 1e-30 * (1.0 + dia)) ? 1.0 : 0.0;
+            }
+            __syncwarp();
+            if (sm.aux[2] != 0.0) break;
+            for (int a = 0; a < s; ++a) {
+              for (int b = a + 1; b < s; ++b) {
+                if (lane == 0) {
+                  double apq = A[a * s + b], c = 1.0, sn = 0.0;
+                  if (fabs(apq) > 1e-300) {
+                    double app = A[a * s + a], aqq = A[b * s + b];
+                    double tau2 = (aqq - app) / (2.0 * apq);
+                    double t = (tau2 >= 0 ? 1.0 : -1.0) / (fabs(tau2) + sqrt(1.0 + tau2 * tau2));
+                    c = 1.0 / sqrt(1.0 + t * t);
+                    sn = t * c;
+                    for (int k = 0; k < s; ++k) {
+                      double akp = A[k * s + a], akq = A[k * s + b];
+                      A[k * s + a] = c * akp - sn * akq;
+                      A[k * s + b] = sn * akp + c * akq;
+                    }
+                    for (int k = 0; k < s; ++k) {
+                      double apk = A[a * s + k], aqk = A[b * s + k];
+                      A[a * s + k] = c * apk - sn * aqk;
+                      A[b * s + k] = sn * apk + c * aqk;
+                    }
+                  }
+                  sm.aux[3] = c;
+                  sm.aux[4] = sn;
+                }
+                __syncwarp();
+                const double c = sm.aux[3], sn = sm.aux[4];
+                if (sn != 0.0) {
+                  double* Xa = X + (size_t)(j0 + a) * p.nmax;
+                  double* Xb = X + (size_t)(j0 + b) * p.nmax;
+                  #pragma unroll 1
+                  for (int i = lane; i < N; i += kWarp) {
+                    double xa = Xa[i], xb = Xb[i];
+                    Xa[i] = c * xa - sn * xb;
+                    Xb[i] = sn * xa + c * xb;
+                  }
+                }
+                __syncwarp();
+              }
+            }
+          }
+          // ascending order (swap vectors along with the diagonal)
+          for (int a = 0; a < s; ++a) {
+            if (lane == 0) {
+              int m = a;
+              for (int b = a + 1; b < s; ++b)
+                if (A[b * s + b] < A[m * s + m]) m = b;
+              if (m != a) {
+                double t = A[a * s + a];
+                A[a * s + a] = A[m * s + m];
+                A[m * s + m] = t;
+              }
+              sm.aux[5] = (double)m;
+            }
+            __syncwarp();
+            const int m = (int)sm.aux[5];
+            if (m != a) {
+              double* Xa = X + (size_t)(j0 + a) * p.nmax;
+              double* Xm = X + (size_t)(j0 + m) * p.nmax;
+              #pragma unroll 1
+              for (int i = lane; i < N; i += kWarp) {
+                double t = Xa[i];
+                Xa[i] = Xm[i];
+                Xm[i] = t;
+              }
+            }
+            __syncwarp();
+          }
+          if (lane == 0)
+            for (int a = 0; a < s; ++a) sm.theta[j0 + a] = A[a * s + a];
+          __syncwarp();
+        }
+        j0 = j1 + 1;
+      }
+    }
 
 // Lowest K eigenpairs of T + diag(v) (v in global vks).  X: K vectors of
 // stride nmax (FP64, global), normalised to sum x^2 = 1 on exit.
@@ -550,29 +906,30 @@ struct EigStats {
 //    checked against the Weyl bound |lambda_j - lambda_j^prev| <= |dv|; on
 //    failure (or a refinement cap) the cold route runs.
 template <int kBand>
-__device__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, const double* vks,
-                           double* X, bool warm, double dv, const Smem& sm, int lane,
-                           EigStats& stats) {
+__device__ __noinline__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, const double* vks,
+                           double* X, SolveArea ruw, bool warm, double dv, const Smem& sm,
+                           int lane, EigStats& stats) {
+  double* YR = X + (size_t)p.kmax * p.nmax;  // H x of the vector being refined
+  double* VA = YR + p.nmax;                  // FP64 diagonal of H
   stats.solves += 1;
   long long tph = clock64();
   const Stencil st = make_stencil(p.stencil, dx);
-  const int nstr = sm.nstr;
   float* a32 = sm.f32;
-  float* R = a32 + nstr;  // K arrays of nstr
-  float* U = R + (size_t)p.kmax * nstr;
-  float* W = U + (size_t)p.kmax * nstr;
   const int Kc = K + 1;
 
-  // --- FP32 diagonal and Gershgorin bounds
-  double amin = 1e300, amax = -1e300;
+  // --- FP64 and FP32 diagonal, Gershgorin bounds (FP32: they only seed brackets)
+  float aminf = 3e38f, amaxf = -3e38f;
+#pragma unroll 1
   for (int i = lane; i < N; i += kWarp) {
-    double a = st.c0 + vks[i];
-    a32[i] = (float)a;
-    amin = fmin(amin, a);
-    amax = fmax(amax, a);
+    const double a = st.c0 + vks[i];
+    const float af = (float)a;
+    VA[i] = a;
+    a32[i] = af;
+    aminf = fminf(aminf, af);
+    amaxf = fmaxf(amaxf, af);
   }
-  amin = warp_min(amin);
-  amax = warp_max(amax);
+  const double amin = (double)warp_minf(aminf);
+  const double amax = (double)warp_maxf(amaxf);
   const double rad = 2.0 * fabs(st.b1) + 2.0 * fabs(st.b2);
   const double hnorm = fmax(fabs(amin), fabs(amax)) + rad;
   const float tolabs = (float)(4.0 * FLT_EPSILON * hnorm);
@@ -584,7 +941,6 @@ __device__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, con
   // residual target: 64 ulp of the operator norm (FP64 floor is ~1 ulp * |H|)
   const double thr = 64.0 * DBL_EPSILON * hnorm;
   double* xs = sm.s64a + kPad64;
-  double* ys = sm.s64b + kPad64;
   __syncwarp();
 
   bool fast = false;
@@ -676,7 +1032,7 @@ __device__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, con
             int j = __ffs(m) - 1;
             float lo = sm.lo[j], hi = sm.hi[j];
             int pp = q - k * P;
-            sg[s] = lo + (hi - lo) * (float)(pp + 1) / (float)(P + 1);
+            sg[s] = lo + __fdividef((hi - lo) * (float)(pp + 1), (float)(P + 1));
           }
         }
         int cn[kShiftsPerLane];
@@ -737,24 +1093,31 @@ __device__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, con
         if (deg) flags |= QEX_FLAG_DEGENERATE_FRONTIER;
       }
       // ---------------- FP32 factorization and inverse iteration (lane j: pair j)
-      if (lane < K) {
-        float* Rj = R + (size_t)lane * nstr;
-        float* Uj = U + (size_t)lane * nstr;
-        float* Wj = W + (size_t)lane * nstr;
-        ldl_factor<kBand>(a32, N, b1f, b2f, (float)sm.eigprev[lane], pivmin, Rj, Uj);
-        const double* Xj = X + (size_t)lane * p.nmax;
-        for (int i = 0; i < N; ++i) Wj[i] = warm ? (float)Xj[i] : pseudo_random(i, lane);
+      long long tsub = clock64();
+      for (int j = 0; j < K; ++j) {
+        const double* Xj = X + (size_t)j * p.nmax;
+        #pragma unroll 1
+        for (int i = lane; i < N; i += kWarp)
+          ruw.at(i, j) = warm ? (float)Xj[i] : pseudo_random(i, j);
       }
       __syncwarp();
+      lap(stats, tsub, 8);
       const int rounds = warm ? 2 : 4;
       float scale = 1.0f;
       for (int r = 0; r < rounds; ++r) {
-        if (lane < K) {
-          float mx = ldl_solve<kBand>(N, b2f, R + (size_t)lane * nstr, U + (size_t)lane * nstr,
-                                      W + (size_t)lane * nstr, scale);
-          scale = (mx > 0.0f) ? 1.0f / mx : 1.0f;
+        if (r == 0) {
+          ring_sweep<true, false, true>(
+              ruw, N, lane < K, sm.ring, lane,
+              FactorForward<kBand>{a32, b1f, b2f, lane < K ? (float)sm.eigprev[lane] : 0.0f,
+                                   pivmin});
+          lap(stats, tsub, 9);
+        } else {
+          ring_sweep<true, true, false>(ruw, N, lane < K, sm.ring, lane,
+                                        SolveForward<kBand>{b2f, scale});
         }
-        __syncwarp();
+        const SolveBackward<kBand> bk = ring_sweep<false, true, false>(
+            ruw, N, lane < K, sm.ring, lane, SolveBackward<kBand>{b2f});
+        if (lane < K) scale = (bk.mx > 0.0f) ? __fdividef(1.0f, bk.mx) : 1.0f;
         if (any_cluster) {
           // Gram-Schmidt inside clusters (point-parallel)
           for (int j = 1; j < K; ++j) {
@@ -763,35 +1126,41 @@ __device__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, con
             for (int q = j - 1; q >= 0 && sm.clus[q] == sm.clus[j]; --q) {
               float sq = __shfl_sync(kFull, scale, q);
               double dot = 0.0, nq = 0.0;
-              const float* Wq = W + (size_t)q * nstr;
-              float* Wj = W + (size_t)j * nstr;
+              #pragma unroll 1
               for (int i = lane; i < N; i += kWarp) {
-                double a = (double)Wq[i] * sq, b = (double)Wj[i] * sj;
+                double a = (double)ruw.at(i, q) * sq;
+                double b = (double)ruw.at(i, j) * sj;
                 dot = fma(a, b, dot);
                 nq = fma(a, a, nq);
               }
               dot = warp_sum(dot);
               nq = warp_sum(nq);
-              float c = (nq > 0.0) ? (float)(dot / nq) : 0.0f;
-              for (int i = lane; i < N; i += kWarp) Wj[i] = fmaf(-c * sq / sj, Wq[i], Wj[i]);
+              const float c = (nq > 0.0) ? __fdividef((float)dot, (float)nq) : 0.0f;
+              #pragma unroll 1
+              for (int i = lane; i < N; i += kWarp) {
+                float& wj = ruw.at(i, j);
+                wj = fmaf(-__fdividef(c * sq, sj), ruw.at(i, q), wj);
+              }
               __syncwarp();
             }
           }
         }
       }
+      lap(stats, tsub, 10);
       // FP64 vectors, normalised
       for (int j = 0; j < K; ++j) {
         float sj = __shfl_sync(kFull, scale, j);
-        const float* Wj = W + (size_t)j * nstr;
         double nn = 0.0;
+        #pragma unroll 1
         for (int i = lane; i < N; i += kWarp) {
-          double a = (double)Wj[i] * sj;
+          double a = (double)ruw.at(i, j) * sj;
           nn = fma(a, a, nn);
         }
         nn = warp_sum(nn);
-        double inv = (nn > 0.0) ? 1.0 / sqrt(nn) : 0.0;
+        const double inv = (nn > 0.0) ? rsqrt_nr(nn) : 0.0;
         double* Xj = X + (size_t)j * p.nmax;
-        for (int i = lane; i < N; i += kWarp) Xj[i] = (double)Wj[i] * sj * inv;
+        #pragma unroll 1
+        for (int i = lane; i < N; i += kWarp) Xj[i] = (double)ruw.at(i, j) * sj * inv;
       }
       __syncwarp();
       {
@@ -803,41 +1172,40 @@ __device__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, con
 
     // ---------------- FP64 Newton refinement: x <- x + (H32 - sigma)^-1 (theta x - H x)
     bool done_all = false;
+    long long tsub = clock64();
     for (int step = 0; step < kMaxRefineSteps; ++step) {
       stats.rq_vectors += K;
+      // Rayleigh quotient and residual of each vector: FP64 H x (the residual
+      // cancels to ~1e-14 of |H|), FP32 residual norm (3 digits suffice)
       for (int j = 0; j < K; ++j) {
-        const double* Xj = X + (size_t)j * p.nmax;
-        stage64(sm.s64a, Xj, N, lane);
+        stage64(sm.s64a, X + (size_t)j * p.nmax, N, lane);
         double xx = 0.0, xy = 0.0;
+#pragma unroll 1
         for (int i = lane; i < N; i += kWarp) {
-          double x = xs[i];
-          double y = fma(st.c0 + vks[i], x, st.b1 * (xs[i - 1] + xs[i + 1]));
+          const double x = xs[i];
+          double y = fma(VA[i], x, st.b1 * (xs[i - 1] + xs[i + 1]));
           if (kBand == 2) y = fma(st.b2, xs[i - 2] + xs[i + 2], y);
-          ys[i] = y;
+          YR[i] = y;
           xx = fma(x, x, xx);
           xy = fma(x, y, xy);
         }
-        xx = warp_sum(xx);
-        xy = warp_sum(xy);
-        const double th = xy / xx;
-        double rr = 0.0;
-        float* Wj = W + (size_t)j * nstr;
+        warp_sum2(xx, xy, lane);
+        const double th = div_nr(xy, xx);
+        float rr = 0.0f;
+#pragma unroll 1
         for (int i = lane; i < N; i += kWarp) {
-          double r = fma(-th, xs[i], ys[i]);
-          rr = fma(r, r, rr);
-          Wj[i] = (float)(-r);
+          const float r = (float)fma(-th, xs[i], YR[i]);
+          rr = fmaf(r, r, rr);
+          ruw.at(i, j) = -r;
         }
-        rr = warp_sum(rr);
+        rr = warp_sumf(rr);
         if (lane == 0) {
           sm.theta[j] = th;
-          sm.red[j] = sqrt(rr / xx);
+          sm.red[j] = (double)sqrtf(__fdividef(rr, (float)xx));
         }
         __syncwarp();
       }
-      if (fast && step == 0 && lane < K) {
-        ldl_factor<kBand>(a32, N, b1f, b2f, (float)sm.theta[lane], pivmin,
-                          R + (size_t)lane * nstr, U + (size_t)lane * nstr);
-      }
+      lap(stats, tsub, 11);
       bool need = false;
       if (lane < K) {
         bool inclus = (lane > 0 && sm.clus[lane] == sm.clus[lane - 1]) ||
@@ -850,21 +1218,30 @@ __device__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, con
         break;
       }
       stats.updates += __popc(nm);
-      if (need) {
-        ldl_solve<kBand>(N, b2f, R + (size_t)lane * nstr, U + (size_t)lane * nstr,
-                         W + (size_t)lane * nstr, 1.0f);
+      if (fast && step == 0) {
+        // fast route: factorise at the FP64 Rayleigh quotients (a vector that
+        // needs no correction now never needs one later)
+        ring_sweep<true, false, true>(
+            ruw, N, need, sm.ring, lane,
+            FactorForward<kBand>{a32, b1f, b2f, lane < K ? (float)sm.theta[lane] : 0.0f, pivmin});
+      } else {
+        ring_sweep<true, true, false>(ruw, N, need, sm.ring, lane, SolveForward<kBand>{b2f, 1.0f});
       }
-      __syncwarp();
+      ring_sweep<false, true, false>(ruw, N, need, sm.ring, lane, SolveBackward<kBand>{b2f});
+      lap(stats, tsub, 12);
       for (int j = 0; j < K; ++j) {
         if (!((nm >> j) & 1u)) continue;
         double* Xj = X + (size_t)j * p.nmax;
-        const float* Wj = W + (size_t)j * nstr;
-        for (int i = lane; i < N; i += kWarp) Xj[i] += (double)Wj[i];
+        #pragma unroll 1
+        for (int i = lane; i < N; i += kWarp) Xj[i] += (double)ruw.at(i, j);
       }
       __syncwarp();
+      lap(stats, tsub, 13);
     }
+    lap(stats, tsub, 11);
 
     if (fast) {
+      stats.fast += 1;
       // Weyl check: each eigenvalue moved by at most |dv| (plus rounding)
       bool ok = done_all;
       if (lane < K) {
@@ -889,145 +1266,21 @@ __device__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, con
 
     // ---------------- Rayleigh-Ritz inside clusters (FP64); Jacobi rotations
     // are applied to the vectors directly
-    if (any_cluster) {
-      int j0 = 0;
-      while (j0 < K) {
-        int j1 = j0;
-        while (j1 + 1 < K && sm.clus[j1 + 1] == sm.clus[j0]) ++j1;
-        const int s = j1 - j0 + 1;
-        if (s >= 2) {
-          for (int a = j0; a <= j1; ++a) {
-            double* Xa = X + (size_t)a * p.nmax;
-            for (int b = j0; b < a; ++b) {
-              const double* Xb = X + (size_t)b * p.nmax;
-              double d = 0.0;
-              for (int i = lane; i < N; i += kWarp) d = fma(Xa[i], Xb[i], d);
-              d = warp_sum(d);
-              for (int i = lane; i < N; i += kWarp) Xa[i] = fma(-d, Xb[i], Xa[i]);
-              __syncwarp();
-            }
-            double nn = 0.0;
-            for (int i = lane; i < N; i += kWarp) nn = fma(Xa[i], Xa[i], nn);
-            nn = warp_sum(nn);
-            double inv = 1.0 / sqrt(nn);
-            for (int i = lane; i < N; i += kWarp) Xa[i] *= inv;
-            __syncwarp();
-          }
-          // projected matrix in the (free) FP32 work area, 16-byte aligned
-          double* A = reinterpret_cast<double*>(sm.f32);
-          for (int b = j0; b <= j1; ++b) {
-            stage64(sm.s64a, X + (size_t)b * p.nmax, N, lane);
-            for (int i = lane; i < N; i += kWarp) {
-              double y = fma(st.c0 + vks[i], xs[i], st.b1 * (xs[i - 1] + xs[i + 1]));
-              if (kBand == 2) y = fma(st.b2, xs[i - 2] + xs[i + 2], y);
-              ys[i] = y;
-            }
-            __syncwarp();
-            for (int a = j0; a <= b; ++a) {
-              const double* Xa = X + (size_t)a * p.nmax;
-              double d = 0.0;
-              for (int i = lane; i < N; i += kWarp) d = fma(Xa[i], ys[i], d);
-              d = warp_sum(d);
-              if (lane == 0) {
-                A[(a - j0) * s + (b - j0)] = d;
-                A[(b - j0) * s + (a - j0)] = d;
-              }
-            }
-            __syncwarp();
-          }
-          for (int sweep = 0; sweep < 30; ++sweep) {
-            if (lane == 0) {
-              double off = 0.0, dia = 0.0;
-              for (int a = 0; a < s; ++a) {
-                dia += A[a * s + a] * A[a * s + a];
-                for (int b = a + 1; b < s; ++b) off += A[a * s + b] * A[a * s + b];
-              }
-              sm.aux[2] = (off <= 1e-30 * (1.0 + dia)) ? 1.0 : 0.0;
-            }
-            __syncwarp();
-            if (sm.aux[2] != 0.0) break;
-            for (int a = 0; a < s; ++a) {
-              for (int b = a + 1; b < s; ++b) {
-                if (lane == 0) {
-                  double apq = A[a * s + b], c = 1.0, sn = 0.0;
-                  if (fabs(apq) > 1e-300) {
-                    double app = A[a * s + a], aqq = A[b * s + b];
-                    double tau2 = (aqq - app) / (2.0 * apq);
-                    double t = (tau2 >= 0 ? 1.0 : -1.0) / (fabs(tau2) + sqrt(1.0 + tau2 * tau2));
-                    c = 1.0 / sqrt(1.0 + t * t);
-                    sn = t * c;
-                    for (int k = 0; k < s; ++k) {
-                      double akp = A[k * s + a], akq = A[k * s + b];
-                      A[k * s + a] = c * akp - sn * akq;
-                      A[k * s + b] = sn * akp + c * akq;
-                    }
-                    for (int k = 0; k < s; ++k) {
-                      double apk = A[a * s + k], aqk = A[b * s + k];
-                      A[a * s + k] = c * apk - sn * aqk;
-                      A[b * s + k] = sn * apk + c * aqk;
-                    }
-                  }
-                  sm.aux[3] = c;
-                  sm.aux[4] = sn;
-                }
-                __syncwarp();
-                const double c = sm.aux[3], sn = sm.aux[4];
-                if (sn != 0.0) {
-                  double* Xa = X + (size_t)(j0 + a) * p.nmax;
-                  double* Xb = X + (size_t)(j0 + b) * p.nmax;
-                  for (int i = lane; i < N; i += kWarp) {
-                    double xa = Xa[i], xb = Xb[i];
-                    Xa[i] = c * xa - sn * xb;
-                    Xb[i] = sn * xa + c * xb;
-                  }
-                }
-                __syncwarp();
-              }
-            }
-          }
-          // ascending order (swap vectors along with the diagonal)
-          for (int a = 0; a < s; ++a) {
-            if (lane == 0) {
-              int m = a;
-              for (int b = a + 1; b < s; ++b)
-                if (A[b * s + b] < A[m * s + m]) m = b;
-              if (m != a) {
-                double t = A[a * s + a];
-                A[a * s + a] = A[m * s + m];
-                A[m * s + m] = t;
-              }
-              sm.aux[5] = (double)m;
-            }
-            __syncwarp();
-            const int m = (int)sm.aux[5];
-            if (m != a) {
-              double* Xa = X + (size_t)(j0 + a) * p.nmax;
-              double* Xm = X + (size_t)(j0 + m) * p.nmax;
-              for (int i = lane; i < N; i += kWarp) {
-                double t = Xa[i];
-                Xa[i] = Xm[i];
-                Xm[i] = t;
-              }
-            }
-            __syncwarp();
-          }
-          if (lane == 0)
-            for (int a = 0; a < s; ++a) sm.theta[j0 + a] = A[a * s + a];
-          __syncwarp();
-        }
-        j0 = j1 + 1;
-      }
-    }
+    tsub = clock64();
+    if (any_cluster) cluster_rayleigh_ritz<kBand>(p, N, K, st, vks, X, YR, sm, lane);
 
     // ---------------- final normalisation and warm-start data
     for (int j = 0; j < K; ++j) {
       double* Xj = X + (size_t)j * p.nmax;
       double nn = 0.0;
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) nn = fma(Xj[i], Xj[i], nn);
       nn = warp_sum(nn);
-      double inv = 1.0 / sqrt(nn);
+      const double inv = rsqrt_nr(nn);
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) Xj[i] *= inv;
     }
+    lap(stats, tsub, 15);
     if (lane < K) sm.eigprev[lane] = sm.theta[lane];
     if (lane == 0) {
       if (fast) sm.aux[0] += dv;  // eigprev[K] is not refreshed on the fast route
@@ -1048,11 +1301,12 @@ __device__ inline double occupation(int j, int ne) {
 }
 
 // Density, eigen-energy sum and gap from the eigenpairs.
-__device__ void density_from_orbitals(const Params& p, int N, double dx, int ne, int K,
+__device__ __noinline__ void density_from_orbitals(const Params& p, int N, double dx, int ne, int K,
                                       const double* X, double* nout, const Smem& sm, double& tee,
                                       double& gap, int lane) {
   const int nocc = (ne + 1) / 2;
   const double inv_dx = 1.0 / dx;
+  #pragma unroll 1
   for (int i = lane; i < N; i += kWarp) {
     double v = 0.0;
     for (int j = 0; j < nocc; ++j) {
@@ -1072,12 +1326,13 @@ __device__ void density_from_orbitals(const Params& p, int N, double dx, int ne,
 
 __device__ inline void write_stats(const Params& p, int b, const EigStats& e) {
   if (!p.o_stats) return;
-  p.o_stats[4 * b + 0] = e.solves;
-  p.o_stats[4 * b + 1] = e.rq_vectors;
-  p.o_stats[4 * b + 2] = e.updates;
-  p.o_stats[4 * b + 3] = e.passes;
+  p.o_stats[8 * b + 0] = e.solves;
+  p.o_stats[8 * b + 1] = e.rq_vectors;
+  p.o_stats[8 * b + 2] = e.updates;
+  p.o_stats[8 * b + 3] = e.passes;
+  p.o_stats[8 * b + 4] = e.fast;
   if (p.o_cycles)
-    for (int k = 0; k < 8; ++k) p.o_cycles[8 * b + k] = e.cyc[k];
+    for (int k = 0; k < kPhases; ++k) p.o_cycles[(long long)kPhases * b + k] = e.cyc[k];
 }
 
 // ---------------------------------------------------------------------------
@@ -1109,7 +1364,9 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
       if (lane == 0 && p.o_status) p.o_status[b] = QEX_BAD_ARG;
       continue;
     }
-    double* ws = p.ws + (long long)slot * p.stride;
+    double* const slot_base = p.ws + (long long)slot * p.stride;
+    const SolveArea ruw = solve_area(slot_base, p.nmax, p.kmax);  // streamed FP32 solves
+    double* ws = slot_base + p.ruw_doubles;
     double* vn = ws + (long long)VN * p.nmax;
     double* vext = ws + (long long)VEXT * p.nmax;
     double* vks = ws + (long long)VKS * p.nmax;
@@ -1121,14 +1378,16 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
     double* diffs = ws + (long long)VDIFF * p.nmax;
     double* X = diffs + (long long)p.mix_slots * p.nmax;
     int flags = 0;
-    EigStats est = {0, 0, 0, 0, {0, 0, 0, 0, 0, 0, 0, 0}};
+    EigStats est = {};
     long long tmol = clock64();
 
     // external potential and interaction table
     if (p.vext_given) {
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) vext[i] = p.vext_in[off + i];
     } else {
       const int M = p.num_nuclei[b];
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) {
         double x = x0 + i * dx, v = 0.0;
         for (int m = 0; m < M; ++m) {
@@ -1140,17 +1399,20 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
       }
     }
     if (p.interaction != QEX_INTERACTION_EXPONENTIAL) {
+      #pragma unroll 1
       for (int d = lane; d < N; d += kWarp) kt[d] = interaction_fn(p, d * dx);
     }
     if (p.o_vext)
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) p.o_vext[off + i] = vext[i];
     __syncwarp();
 
     if (p.mode == kModeNonInteracting) {
-      flags |= eigen_solve<kBand>(p, N, dx, ne, K, vext, X, false, 0.0, sm, lane, est);
+      flags |= eigen_solve<kBand>(p, N, dx, ne, K, vext, X, ruw, false, 0.0, sm, lane, est);
       double tee, gap;
       density_from_orbitals(p, N, dx, ne, K, X, nout, sm, tee, gap, lane);
       if (p.o_final)
+        #pragma unroll 1
         for (int i = lane; i < N; i += kWarp) p.o_final[off + i] = nout[i];
       if (lane == 0) {
         if (p.o_tee) p.o_tee[b] = tee;
@@ -1165,13 +1427,15 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
     bool warm = false;
     double dv = 0.0;
     if (p.dens_in) {
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) vn[i] = p.dens_in[off + i];
     } else {
-      flags |= eigen_solve<kBand>(p, N, dx, ne, K, vext, X, false, 0.0, sm, lane, est);
+      flags |= eigen_solve<kBand>(p, N, dx, ne, K, vext, X, ruw, false, 0.0, sm, lane, est);
       double tee, gap;
       density_from_orbitals(p, N, dx, ne, K, X, vn, sm, tee, gap, lane);
       // warm start from the non-interacting eigenpairs: v_KS differs from
       // v_ext by v_H + v_xc, bounded below through dv in the first iteration.
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) vks[i] = vext[i];
       warm = true;
     }
@@ -1195,6 +1459,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
           if (p.o_gap) p.o_gap[(long long)b * p.iters + t] = last_gap;
           if (p.o_conv) p.o_conv[(long long)b * p.iters + t] = 1;
         }
+        #pragma unroll 1
         for (int i = lane; i < N; i += kWarp) {
           if (p.o_dens) p.o_dens[r0 + i] = vn[i];
           if (p.o_vh) p.o_vh[r0 + i] = vh[i];
@@ -1205,6 +1470,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
       }
       const bool conv_at_start = converged;
       if (p.mode == kModeIteration) {
+        #pragma unroll 1
         for (int i = lane; i < N; i += kWarp) vn[i] = p.dens_in[off + i];
         __syncwarp();
       }
@@ -1219,19 +1485,23 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
         tit = t;
       }
       if (reflect_xc) {
+        #pragma unroll 1
         for (int i = lane; i < N; i += kWarp) {
           sm.s64a[kPad64 + i] = 0.5 * (vn[i] + vn[N - 1 - i]);
         }
         __syncwarp();
       }
       xc_eval(p, N, dx, sm, true, vxc, vf, reflect_xc, lane);
-      double dvl = 0.0;
+      // |dv_KS|_inf in FP32, rounded up: it only sizes brackets and picks the
+      // warm route, both of which are verified
+      float dvl = 0.0f;
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) {
         double v = vh[i] + vxc[i] + vext[i];
-        dvl = fmax(dvl, fabs(v - vks[i]));
+        dvl = fmaxf(dvl, fabsf((float)(v - vks[i])));
         vks[i] = v;
       }
-      dv = warm ? warp_max(dvl) : 0.0;
+      dv = warm ? (double)warp_maxf(dvl) * (1.0 + 1e-6) : 0.0;
       __syncwarp();
       {
         long long t = clock64();
@@ -1239,7 +1509,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
       }
 
       // ---- eigen-solve and output density
-      flags |= eigen_solve<kBand>(p, N, dx, ne, K, vks, X, warm, dv, sm, lane, est);
+      flags |= eigen_solve<kBand>(p, N, dx, ne, K, vks, X, ruw, warm, dv, sm, lane, est);
       warm = true;
       tit = clock64();
       double tee, gap;
@@ -1247,6 +1517,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
 
       // ---- total energy on the output density (jit_scf.py:46-72)
       double eks = 0.0, eext = 0.0;
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) {
         eks = fma(vks[i], nout[i], eks);
         eext = fma(vext[i], nout[i], eext);
@@ -1254,16 +1525,19 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
       eks = warp_sum(eks) * dx;
       eext = warp_sum(eext) * dx;
       stage64(sm.s64a, nout, N, lane);
-      // Hartree of n_out into the FP64 staging buffer b (only the energy is kept)
-      const double eh = 0.5 * dx * hartree(p, N, dx, sm, sm.s64b + kPad64, kt, lane);
+      // Hartree of n_out into the refinement scratch (only the energy is kept)
+      const double eh = 0.5 * dx * hartree(p, N, dx, sm, X + (long long)p.kmax * p.nmax, kt, lane);
       __syncwarp();
       if (reflect_xc) {
+        #pragma unroll 1
         for (int i = lane; i < N; i += kWarp) {
           sm.s64a[kPad64 + i] = 0.5 * (nout[i] + nout[N - 1 - i]);
         }
         __syncwarp();
       }
+      long long tsub = clock64();
       const double exc = xc_eval(p, N, dx, sm, false, nullptr, nullptr, false, lane);
+      lap(est, tsub, 14);
       const double energy = tee - eks + eh + exc + eext;
       if (p.reflect) flip_avg_global(nout, N, lane);
       {
@@ -1280,6 +1554,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
           if (p.o_iters) p.o_iters[b] = 1;
           write_stats(p, b, est);
         }
+        #pragma unroll 1
         for (int i = lane; i < N; i += kWarp) {
           if (p.o_dens) p.o_dens[off + i] = nout[i];
           if (p.o_vh) p.o_vh[off + i] = vh[i];
@@ -1295,12 +1570,15 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
       double* dslot = diffs + (long long)slot_w * p.nmax;
       const int navg = min(active + 1, min(p.mixing, slots));
       double mse_raw = 0.0, mse_mix = 0.0;
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) {
         double d = nout[i] - vn[i];
         dslot[i] = d;
         mse_raw = fma(d, d, mse_raw);
       }
       __syncwarp();
+      const double coef = (navg == 1) ? alpha : div_nr(alpha, (double)navg);
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) {
         double s = 0.0;
         for (int q = 0; q < navg; ++q) {
@@ -1308,12 +1586,13 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
           if (sl < 0) sl += slots;
           s += diffs[(long long)sl * p.nmax + i];
         }
-        double upd = alpha * (s / navg);
+        const double upd = coef * s;
         mse_mix = fma(upd, upd, mse_mix);
         vn[i] += upd;
       }
-      mse_raw = warp_sum(mse_raw) / N;
-      mse_mix = warp_sum(mse_mix) / N;
+      warp_sum2(mse_raw, mse_mix, lane);
+      mse_raw = div_nr(mse_raw, (double)N);
+      mse_mix = div_nr(mse_mix, (double)N);
       __syncwarp();
       ++active;
       bool rec_conv;
@@ -1333,6 +1612,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
         if (p.o_gap) p.o_gap[(long long)b * p.iters + t] = gap;
         if (p.o_conv) p.o_conv[(long long)b * p.iters + t] = rec_conv ? 1 : 0;
       }
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) {
         if (p.o_dens) p.o_dens[r0 + i] = vn[i];
         if (p.o_vh) p.o_vh[r0 + i] = vh[i];
@@ -1345,6 +1625,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
     est.cyc[7] = clock64() - tmol;
     if (p.mode == kModeScf) {
       if (p.o_final)
+        #pragma unroll 1
         for (int i = lane; i < N; i += kWarp) p.o_final[off + i] = vn[i];
       if (lane == 0) {
         if (p.o_status) p.o_status[b] = flags;
@@ -1373,6 +1654,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
 template <int kBand>
 __device__ inline void banded_apply(const Stencil& st, const double* vks, double shift, int N,
                                     const double* xs, double* ys, int lane) {
+  #pragma unroll 1
   for (int i = lane; i < N; i += kWarp) {
     double y = fma(st.c0 + vks[i] - shift, xs[i], st.b1 * (xs[i - 1] + xs[i + 1]));
     if (kBand == 2) y = fma(st.b2, xs[i - 2] + xs[i + 2], y);
@@ -1387,8 +1669,10 @@ __device__ inline void project_out(double* v, const double* X, int nmax, int noc
   for (int k = 0; k < nocc; ++k) {
     const double* Xk = X + (size_t)k * nmax;
     double c = 0.0;
+    #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) c = fma(Xk[i], v[i], c);
     c = warp_sum(c);
+    #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) v[i] = fma(-c, Xk[i], v[i]);
     __syncwarp();
   }
@@ -1407,6 +1691,7 @@ __device__ int sternheimer(const Params& p, int N, double dx, int ne, const doub
   float* U = R + (size_t)p.kmax * nstr;
   float* W = U + (size_t)p.kmax * nstr;
   double amax = 0.0;
+  #pragma unroll 1
   for (int i = lane; i < N; i += kWarp) {
     const double a = st.c0 + vks[i];
     a32[i] = (float)a;
@@ -1423,6 +1708,7 @@ __device__ int sternheimer(const Params& p, int N, double dx, int ne, const doub
   for (int j = 0; j < nocc; ++j) {
     const double* Xj = X + (size_t)j * p.nmax;
     double* Bj = Bv + (size_t)j * p.nmax;
+    #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) {
       Bj[i] = -Xj[i] * gm[i];
       Y[(size_t)j * p.nmax + i] = 0.0;
@@ -1442,6 +1728,7 @@ __device__ int sternheimer(const Params& p, int N, double dx, int ne, const doub
       project_out(ys, X, p.nmax, nocc, N, lane);
       double rr = 0.0, bb = 0.0;
       float* Wj = W + (size_t)j * nstr;
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) {
         const double r = Bj[i] - ys[i];
         rr = fma(r, r, rr);
@@ -1462,16 +1749,19 @@ __device__ int sternheimer(const Params& p, int N, double dx, int ne, const doub
     for (int j = 0; j < nocc; ++j) {
       if (!((nm >> j) & 1u)) continue;
       const float* Wj = W + (size_t)j * nstr;
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) ys[i] = (double)Wj[i];
       __syncwarp();
       project_out(ys, X, p.nmax, nocc, N, lane);
       double* Yj = Y + (size_t)j * p.nmax;
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) Yj[i] += ys[i];
       __syncwarp();
     }
   }
   // gv = sum_j (2 occ_j / dx) phi_j y_j
   const double inv_dx = 1.0 / dx;
+  #pragma unroll 1
   for (int i = lane; i < N; i += kWarp) {
     double v = 0.0;
     for (int j = 0; j < nocc; ++j)
@@ -1486,10 +1776,12 @@ __device__ int sternheimer(const Params& p, int N, double dx, int ne, const doub
     for (int k = 0; k < h; ++k) {
       const double* Xk = X + (size_t)k * p.nmax;
       double c = 0.0;
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) c = fma(Xk[i] * Xh[i], gm[i], c);
       c = warp_sum(c);
       const double f = 2.0 * inv_dx * (occupation(h, ne) - occupation(k, ne)) /
                        (sm.theta[h] - sm.theta[k]) * c;
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) gv[i] = fma(f * Xh[i], Xk[i], gv[i]);
       __syncwarp();
     }
@@ -1557,7 +1849,9 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
       if (lane == 0 && p.o_status) p.o_status[b] = QEX_BAD_ARG;
       continue;
     }
-    double* ws = p.ws + (long long)slot * p.stride;
+    double* const slot_base = p.ws + (long long)slot * p.stride;
+    const SolveArea ruw = solve_area(slot_base, p.nmax, p.kmax);  // streamed FP32 solves
+    double* ws = slot_base + p.ruw_doubles;
     double* vn = ws + (long long)VN * p.nmax;
     double* vext = ws + (long long)VEXT * p.nmax;
     double* vks = ws + (long long)VKS * p.nmax;
@@ -1566,7 +1860,7 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
     double* vxc = ws + (long long)VXC * p.nmax;
     double* kt = ws + (long long)VKT * p.nmax;
     double* X = ws + (long long)(VDIFF + slots) * p.nmax;
-    double* Y = X + (long long)p.kmax * p.nmax;
+    double* Y = X + (long long)(p.kmax + 2) * p.nmax;  // after the forward scratch
     double* Bv = Y + (long long)p.kmax * p.nmax;
     double* gm = Bv + (long long)p.kmax * p.nmax;
     double* gv = gm + p.nmax;
@@ -1576,6 +1870,7 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
     // external potential
     {
       const int M = p.num_nuclei[b];
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) {
         double x = x0 + i * dx, v = 0.0;
         for (int m = 0; m < M; ++m) {
@@ -1592,10 +1887,11 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
     stage64(sm.s64a, vn, N, lane);
     hartree(p, N, dx, sm, vh, kt, lane);
     xc_eval(p, N, dx, sm, true, vxc, nullptr, false, lane);
+    #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) vks[i] = vh[i] + vxc[i] + vext[i];
     __syncwarp();
-    EigStats est = {0, 0, 0, 0, {0, 0, 0, 0, 0, 0, 0, 0}};
-    int flags = eigen_solve<kBand>(p, N, dx, ne, K, vks, X, false, 0.0, sm, lane, est);
+    EigStats est = {};
+    int flags = eigen_solve<kBand>(p, N, dx, ne, K, vks, X, ruw, false, 0.0, sm, lane, est);
     double tee, gap;
     density_from_orbitals(p, N, dx, ne, K, X, nout, sm, tee, gap, lane);
     const double gE = p.a_genergy ? p.a_genergy[b] : 0.0;
@@ -1613,6 +1909,7 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
       hartree(p, N, dx, sm, t1, kt, lane);
       xc_eval(p, N, dx, sm, true, t2, nullptr, false, lane);
     }
+    #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) {
       double g = at * p.a_gnext[off + i];
       if (gE != 0.0) g += gE * dx * (t1[i] + t2[i] + vext[i] - vks[i]);
@@ -1621,6 +1918,7 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
     __syncwarp();
     if (gE != 0.0) {
       const float ninv = p.mlp.norm_inv;
+      #pragma unroll 1
       for (int i = lane; i < N + 2 * kPadMlp; i += kWarp) {
         const int k = i - kPadMlp;
         n32[i] = (k >= 0 && k < N) ? (float)nout[k] * ninv : 0.0f;
@@ -1635,9 +1933,11 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
     // ---- gn = (1 - a) gnext + v_H(gv) + d/dn[v_xc(n) . gv]
     stage64(sm.s64a, gv, N, lane);
     hartree(p, N, dx, sm, t1, kt, lane);
+    #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) gn[i] = (1.0 - at) * p.a_gnext[off + i] + t1[i];
     {
       const float ninv = p.mlp.norm_inv;
+      #pragma unroll 1
       for (int i = lane; i < N + 2 * kPadMlp; i += kWarp) {
         const int k = i - kPadMlp;
         n32[i] = (k >= 0 && k < N) ? (float)vn[k] * ninv : 0.0f;
@@ -1647,9 +1947,11 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
       __syncwarp();
       // local convention: v_xc(n) . u = sum_i [eps_i u_i + n_i D eps_i[u window]]
       mlp_adjoint_pass(p, N, n32, u32, true, gv, 1.0, vn, gacc, gn, rec, sm, acc, lane);
+      #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) gn[i] += (double)gacc[i + kPadMlp];
       __syncwarp();
     }
+    #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) p.a_gn[off + i] = gn[i];
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
@@ -1688,7 +1990,7 @@ long long stride_doubles(const qex_ks1d_options* o, bool adjoint = false) {
   int kmax = o->max_num_electrons / 2 + 1;
   long long v = vec_count(mix_slots_for(o), kmax);
   if (adjoint) v += 2LL * kmax + 5;  // Sternheimer solutions and right-hand sides, 5 vectors
-  long long s = v * (long long)o->max_num_grids;
+  long long s = ruw_doubles(o->max_num_grids, kmax) + v * (long long)o->max_num_grids;
   return (s + 31) / 32 * 32;
 }
 
@@ -1758,9 +2060,11 @@ int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_opt
   size_t need = 0;
   qex_ks1d_workspace_size(o, num_molecules, &need);
   if (!ws || ws_bytes < need) return QEX_BAD_ARG;
+  if (reinterpret_cast<uintptr_t>(ws) % 16 != 0) return QEX_BAD_ARG;  // float4 solve area
   P.counter = reinterpret_cast<int*>(ws);
   P.ws = reinterpret_cast<double*>(static_cast<unsigned char*>(ws) + 256);
   P.stride = stride_doubles(o);
+  P.ruw_doubles = ruw_doubles(o->max_num_grids, o->max_num_electrons / 2 + 1);
   if (num_molecules < 0) return QEX_BAD_ARG;
   if (num_molecules > 0) {
     if (!b->num_grids || !b->grid_offsets || !b->grid_start || !b->grid_spacing ||

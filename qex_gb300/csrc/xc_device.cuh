@@ -56,7 +56,7 @@ __device__ inline void lda_exp_coulomb(double n, double A, double kappa, double&
 }
 
 __device__ inline float silu_d(float z, float& d) {
-  float s = 1.0f / (1.0f + __expf(-z));
+  float s = __fdividef(1.0f, 1.0f + __expf(-z));  // 0 when exp(-z) overflows: silu -> 0
   d = s * (1.0f + z * (1.0f - s));
   return z * s;
 }
@@ -66,11 +66,11 @@ __device__ inline float silu_d(float z, float& d) {
 // (w1 [17][16], b1, w2 [16][16], b2, w3, b3); every weight read is a
 // broadcast 16-byte load of (part of) one weight row, issued next to its use.
 // win: the 17 window inputs (already divided by the normalization), read from
-// shared memory with stride `wstride`.  scr: per-lane shared scratch of 48
+// shared memory with stride `wstride`.  scr: per-lane shared scratch of 32
 // floats at stride `ss` (hidden activations and derivatives).  With kGrad,
 // scr[k * ss] (k < 17) receives d eps / d input_k on return.
 constexpr int kMlpFloats = 580;  // 577 weights padded to 16 bytes
-constexpr int kMlpScratch = 48;
+constexpr int kMlpScratch = 32;  // h1, then d1 (overwritten in place by g1)
 
 __device__ inline void mlp_load4(const float* W, int off, float& a, float& b, float& c, float& d) {
   float4 r = *reinterpret_cast<const float4*>(W + off);
@@ -147,11 +147,11 @@ __device__ inline float mlp_point(const float* W, const float* win, int wstride,
         a = fmaf(r2, g2[4 * q + 2], a);
         a = fmaf(r3, g2[4 * q + 3], a);
       }
-      scr[(32 + k) * ss] = a * scr[(16 + k) * ss];  // g1 = (W2 g2) * d1
+      scr[(16 + k) * ss] = a * scr[(16 + k) * ss];  // g1 = (W2 g2) * d1, over d1
     }
     float g1[QEX_MLP_HIDDEN];
 #pragma unroll
-    for (int h = 0; h < QEX_MLP_HIDDEN; ++h) g1[h] = scr[(32 + h) * ss];
+    for (int h = 0; h < QEX_MLP_HIDDEN; ++h) g1[h] = scr[(16 + h) * ss];
 #pragma unroll 1
     for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
       float a = 0.0f;
@@ -181,7 +181,7 @@ __device__ inline float mlp_point(const float* W, const float* win, int wstride,
 constexpr int kMlpRec = 164;
 
 __device__ inline float silu_dd(float z, float& d1, float& d2) {
-  float s = 1.0f / (1.0f + __expf(-z));
+  float s = __fdividef(1.0f, 1.0f + __expf(-z));  // 0 when exp(-z) overflows: silu -> 0
   d1 = s * (1.0f + z * (1.0f - s));
   d2 = s * (1.0f - s) * (2.0f + z * (1.0f - 2.0f * s));
   return z * s;

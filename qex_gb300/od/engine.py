@@ -248,8 +248,8 @@ class Ks1dEngine:
             out["external_potential"] = torch.empty((P,), **f64)
         out["status"] = torch.zeros((B,), dtype=torch.int32, device=batch.device)
         out["iterations_run"] = torch.zeros((B,), dtype=torch.int32, device=batch.device)
-        out["stats"] = torch.zeros((B, 4), dtype=torch.int32, device=batch.device)
-        out["phase_cycles"] = torch.zeros((B, 8), dtype=torch.int64, device=batch.device)
+        out["stats"] = torch.zeros((B, 8), dtype=torch.int32, device=batch.device)
+        out["phase_cycles"] = torch.zeros((B, 16), dtype=torch.int64, device=batch.device)
         return out
 
     @staticmethod
