@@ -248,11 +248,16 @@ __device__ inline double interaction_fn(const Params& p, double d) {
 
 // Stage a global FP64 vector into a padded shared buffer (zeros outside [0,N)).
 __device__ inline void stage64(double* s, const double* g, int N, int lane) {
-  #pragma unroll 1
-  for (int i = lane; i < N + 2 * kPad64; i += kWarp) {
-    int k = i - kPad64;
-    s[i] = (k >= 0 && k < N) ? g[k] : 0.0;
+  // zero padding either side; the interior by asynchronous copies, all in
+  // flight at once (one memory latency per vector)
+  if (lane < kPad64) {
+    s[lane] = 0.0;
+    s[N + kPad64 + lane] = 0.0;
   }
+#pragma unroll 1
+  for (int i = lane; i < N; i += kWarp) cp_async8(s + kPad64 + i, g + i);
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncwarp();
 }
 
@@ -570,15 +575,6 @@ __device__ inline float ldl_solve(int N, float b2, const float* R, const float* 
 // (cp.async, kRing - 1 chunks in flight), so that the shared-memory footprint
 // of a warp does not grow with N * K.
 // ---------------------------------------------------------------------------
-__device__ inline void cp_async16(void* smem, const void* gmem) {
-  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int kPending>
-__device__ inline void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(kPending) : "memory");
-}
 
 // The two planes of a molecule's solve area (rows = ruw_rows(nmax)).
 struct SolveArea {
@@ -900,7 +896,7 @@ __device__ __noinline__ void cluster_rayleigh_ritz(const Params& p, int N, int K
 // Two routes:
 //  * cold: FP32 multisection -> FP32 inverse iteration -> FP64 refinement
 //    (Rayleigh-Ritz inside near-degenerate clusters);
-//  * fast (warm start, |dv_KS| < 2% of the smallest gap, no clusters): the
+//  * fast (warm start, |dv_KS| < kFastGap x the smallest gap, no clusters): the
 //    previous eigenvectors go straight into the FP64 refinement, the FP32
 //    factorization taken at their FP64 Rayleigh quotients.  Its result is
 //    checked against the Weyl bound |lambda_j - lambda_j^prev| <= |dv|; on
@@ -948,7 +944,7 @@ __device__ __noinline__ int eigen_solve(const Params& p, int N, double dx, int n
     double gmin = 1e300;
     for (int j = 0; j + 1 < K; ++j) gmin = fmin(gmin, sm.eigprev[j + 1] - sm.eigprev[j]);
     gmin = fmin(gmin, sm.eigprev[K] - sm.aux[0] - sm.eigprev[K - 1]);
-    fast = (dv < 0.02 * gmin) && (gmin > (double)tau);
+    fast = (dv < kFastGap * gmin) && (gmin > (double)tau);
   }
 
   for (int attempt = 0; attempt < 2; ++attempt) {
@@ -1173,6 +1169,9 @@ __device__ __noinline__ int eigen_solve(const Params& p, int N, double dx, int n
     // ---------------- FP64 Newton refinement: x <- x + (H32 - sigma)^-1 (theta x - H x)
     bool done_all = false;
     long long tsub = clock64();
+    // shift of each lane's current factorisation, and the last residual
+    float sig_cur = (!fast && lane < K) ? (float)sm.eigprev[lane] : 0.0f;
+    double red_prev = 1e300;
     for (int step = 0; step < kMaxRefineSteps; ++step) {
       stats.rq_vectors += K;
       // Rayleigh quotient and residual of each vector: FP64 H x (the residual
@@ -1218,12 +1217,15 @@ __device__ __noinline__ int eigen_solve(const Params& p, int N, double dx, int n
         break;
       }
       stats.updates += __popc(nm);
-      if (fast && step == 0) {
-        // fast route: factorise at the FP64 Rayleigh quotients (a vector that
-        // needs no correction now never needs one later)
-        ring_sweep<true, false, true>(
-            ruw, N, need, sm.ring, lane,
-            FactorForward<kBand>{a32, b1f, b2f, lane < K ? (float)sm.theta[lane] : 0.0f, pivmin});
+      // factorise at the FP64 Rayleigh quotient on the fast route's first step
+      // and wherever the last correction gained less than two digits (a vector
+      // that needs no correction now never needs one later)
+      const bool refac = need && ((fast && step == 0) || (step > 0 && sm.red[lane] > 1e-2 * red_prev));
+      if (lane < K) red_prev = sm.red[lane];
+      if (refac) sig_cur = (float)sm.theta[lane];
+      if (__any_sync(kFull, refac)) {
+        ring_sweep<true, false, true>(ruw, N, need, sm.ring, lane,
+                                      FactorForward<kBand>{a32, b1f, b2f, sig_cur, pivmin});
       } else {
         ring_sweep<true, true, false>(ruw, N, need, sm.ring, lane, SolveForward<kBand>{b2f, 1.0f});
       }
@@ -1305,15 +1307,21 @@ __device__ __noinline__ void density_from_orbitals(const Params& p, int N, doubl
                                       const double* X, double* nout, const Smem& sm, double& tee,
                                       double& gap, int lane) {
   const int nocc = (ne + 1) / 2;
-  const double inv_dx = 1.0 / dx;
-  #pragma unroll 1
+  const int nfull = ne / 2;  // doubly occupied; with odd ne, orbital nfull holds one
+  const double inv_dx = recip_nr(dx);
+#pragma unroll 2
   for (int i = lane; i < N; i += kWarp) {
     double v = 0.0;
-    for (int j = 0; j < nocc; ++j) {
-      double x = X[(size_t)j * p.nmax + i];
-      v = fma(occupation(j, ne) * inv_dx, x * x, v);
+    for (int j = 0; j < nfull; ++j) {
+      const double x = X[(size_t)j * p.nmax + i];
+      v = fma(x, x, v);
     }
-    nout[i] = v;
+    v += v;
+    if (nfull < nocc) {
+      const double x = X[(size_t)nfull * p.nmax + i];
+      v = fma(x, x, v);
+    }
+    nout[i] = v * inv_dx;
   }
   tee = 0.0;
   for (int j = 0; j < nocc; ++j) tee += occupation(j, ne) * sm.theta[j];

@@ -17,6 +17,9 @@ constexpr int kSamples = kWarp * kShiftsPerLane;
 constexpr int kMaxPasses = 48;
 constexpr int kMaxRefineSteps = 10;
 constexpr int kPhases = 16;  // phase timers per molecule
+// Warm route when |dv_KS| < kFastGap * (smallest gap): below 1/2 the Weyl
+// intervals of neighbouring eigenvalues are disjoint, which the check needs.
+constexpr double kFastGap = 0.25;
 constexpr int kChunk = 16;   // points per chunk of the streamed FP32 solves
 constexpr int kRing = 6;     // chunks in the shared-memory ring (kRing - 1 in flight)
 constexpr int kPad64 = 2;   // zero padding either side of the FP64 staging vector
@@ -64,6 +67,24 @@ __device__ __forceinline__ void warp_sum2(double& a, double& b, int lane) {
   for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
   a = __shfl_sync(kFull, v, 0);
   b = __shfl_sync(kFull, v, 16);
+}
+
+// Asynchronous global -> shared copies (sm_80+ cp.async); the caller commits
+// and waits on groups.
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int kPending>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(kPending) : "memory");
 }
 
 // FP64 reciprocal, quotient and inverse square root by Newton's iteration
