@@ -157,19 +157,22 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 
 def fp64_flops(mols, iterations_run, stats):
-    """FP64 flops executed, tallied per code path of the kernel."""
+    """FP64 flops executed, tallied per code path of the kernel (an FMA is 2)."""
     total = 0.0
     for m, it, st in zip(mols, iterations_run, stats):
         n = m.num_grids
         nocc = (m.num_electrons + 1) // 2
         k = m.num_electrons // 2 + 1
         solves, rq_vec, upd = (int(x) for x in st[:3])
-        # per SCF iteration: two Hartree scans (15 N each), v_KS assembly (5 N),
-        # energies (4 N), mixing (10 N), density (4 N nocc), XC energy sums (4 N)
-        per_iter = (30 + 5 + 4 + 10 + 4) * n + 4 * n * nocc
-        # per eigen-solve: diagonal (1 N), FP64 conversion + final normalisation (7 N k)
-        per_solve = n + 7 * n * k
-        total += float(it) * per_iter + solves * per_solve + 16.0 * n * rq_vec + 1.0 * n * upd
+        # per SCF iteration: two Hartree scans (15 N each), v_KS assembly and
+        # drift (4 N), energies (4 N), mixing (8 N), density (2 N nocc + 2 N),
+        # XC energy sum (2 N)
+        per_iter = (30 + 4 + 4 + 8 + 2 + 2) * n + 2 * n * nocc
+        # per eigen-solve: FP64 diagonal (1 N), normalisations (~5 N per vector)
+        per_solve = n + 5 * n * k
+        # per Rayleigh-quotient pass: H x (7 N), x.x and x.Hx (4 N), residual (2 N);
+        # per correction: x += w (1 N)
+        total += float(it) * per_iter + solves * per_solve + 13.0 * n * rq_vec + 1.0 * n * upd
     return total
 
 
