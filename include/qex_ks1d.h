@@ -91,6 +91,10 @@ typedef struct qex_ks1d_options {
   int32_t max_num_grids;               /* upper bound on num_grids[b] */
   int32_t max_num_electrons;           /* upper bound on num_electrons[b] */
   int32_t max_nuclei;                  /* row stride of locations / nuclear_charges */
+  int32_t solve_planes; /* FP32 solve planes: 0 automatic (resident when the batch fits in
+                           one wave of resident warps), 1 resident in shared memory,
+                           2 streamed through a shared-memory ring (more warps per SM;
+                           for large batches, or several batches launched concurrently) */
 } qex_ks1d_options;
 
 /* Molecule descriptors: all device arrays of length num_molecules (nuclei:

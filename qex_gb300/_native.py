@@ -69,6 +69,7 @@ class Ks1dOptions(ctypes.Structure):
         ("max_num_grids", ctypes.c_int32),
         ("max_num_electrons", ctypes.c_int32),
         ("max_nuclei", ctypes.c_int32),
+        ("solve_planes", ctypes.c_int32),
     ]
 
 

@@ -96,6 +96,7 @@ struct Params {
   double* ws;
   long long stride;  // doubles per molecule
   long long ruw_doubles;  // leading streamed-solve area of a molecule's workspace
+  int planes;             // qex_ks1d_options.solve_planes
   int* counter;
   MlpParams mlp;
 };
@@ -120,7 +121,10 @@ __host__ __device__ inline long long ruw_doubles(int nmax, int kmax) {
   return ruw_rows(nmax) * kmax * 3 / 2;  // a float2 and a float per point and eigenpair
 }
 
-__host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax, bool adjoint = false) {
+// resident: the FP32 solve planes live in shared memory (small batches, where
+// occupancy is not limited by shared memory) instead of streaming through the ring.
+__host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax, bool adjoint = false,
+                                                  bool resident = false) {
   SmemLayout L;
   L.nstr = ((nmax + 31) / 32) * 32 + 1;
   size_t off = 0;
@@ -137,7 +141,7 @@ __host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax, bool adjoi
   // FP32 diagonal, then the ring of the streamed solves (16-byte aligned)
   const size_t ring_off = ((size_t)L.nstr + 3) / 4 * 4;
   L.ring = L.f32 + sizeof(float) * ring_off;
-  size_t eig_floats = ring_off + (size_t)kRing * kChunk * kmax * 3;  // float2 + float
+  size_t eig_floats = ring_off + (size_t)(resident ? ruw_rows(nmax) : kRing * kChunk) * kmax * 3;
   size_t f = xc_floats > eig_floats ? xc_floats : eig_floats;
   if (hart_floats > f) f = hart_floats;
   if (adjoint) {
@@ -588,10 +592,26 @@ struct SolveArea {
 // step(i, ru, w) in order on their own entries (in shared memory); the chunk's
 // W entries (and RU with kStoreRU) are then written back.  RU is read only
 // with kLoadRU.  The area holds whole chunks, so every copy is in bounds.
-template <bool kFwd, bool kLoadRU, bool kStoreRU, typename Step>
+template <bool kFwd, bool kLoadRU, bool kStoreRU, bool kRes, typename Step>
 __device__ __noinline__ Step ring_sweep(SolveArea g, int N, bool act, float4* ring, int lane,
                                         Step step) {
   const int kmax = g.kmax;
+  if (kRes) {
+    // planes resident in shared memory: sweep them in place
+    if (act) {
+      float2* rs = g.ru + lane;
+      float* ws = g.w + lane;
+      if (kFwd) {
+#pragma unroll 4
+        for (int i = 0; i < N; ++i) step(i, rs[(size_t)i * kmax], ws[(size_t)i * kmax]);
+      } else {
+#pragma unroll 4
+        for (int i = N - 1; i >= 0; --i) step(i, rs[(size_t)i * kmax], ws[(size_t)i * kmax]);
+      }
+    }
+    __syncwarp();
+    return step;
+  }
   const int nc = (N + kChunk - 1) / kChunk;
   const int per = kChunk * kmax;            // entries per chunk
   const int ru16 = per / 2, w16 = per / 4;  // 16-byte pieces per chunk and plane
@@ -901,7 +921,7 @@ __device__ __noinline__ void cluster_rayleigh_ritz(const Params& p, int N, int K
 //    factorization taken at their FP64 Rayleigh quotients.  Its result is
 //    checked against the Weyl bound |lambda_j - lambda_j^prev| <= |dv|; on
 //    failure (or a refinement cap) the cold route runs.
-template <int kBand>
+template <int kBand, bool kRes>
 __device__ __noinline__ int eigen_solve(const Params& p, int N, double dx, int ne, int K, const double* vks,
                            double* X, SolveArea ruw, bool warm, double dv, const Smem& sm,
                            int lane, EigStats& stats) {
@@ -1102,16 +1122,16 @@ __device__ __noinline__ int eigen_solve(const Params& p, int N, double dx, int n
       float scale = 1.0f;
       for (int r = 0; r < rounds; ++r) {
         if (r == 0) {
-          ring_sweep<true, false, true>(
+          ring_sweep<true, false, true, kRes>(
               ruw, N, lane < K, sm.ring, lane,
               FactorForward<kBand>{a32, b1f, b2f, lane < K ? (float)sm.eigprev[lane] : 0.0f,
                                    pivmin});
           lap(stats, tsub, 9);
         } else {
-          ring_sweep<true, true, false>(ruw, N, lane < K, sm.ring, lane,
+          ring_sweep<true, true, false, kRes>(ruw, N, lane < K, sm.ring, lane,
                                         SolveForward<kBand>{b2f, scale});
         }
-        const SolveBackward<kBand> bk = ring_sweep<false, true, false>(
+        const SolveBackward<kBand> bk = ring_sweep<false, true, false, kRes>(
             ruw, N, lane < K, sm.ring, lane, SolveBackward<kBand>{b2f});
         if (lane < K) scale = (bk.mx > 0.0f) ? __fdividef(1.0f, bk.mx) : 1.0f;
         if (any_cluster) {
@@ -1224,12 +1244,12 @@ __device__ __noinline__ int eigen_solve(const Params& p, int N, double dx, int n
       if (lane < K) red_prev = sm.red[lane];
       if (refac) sig_cur = (float)sm.theta[lane];
       if (__any_sync(kFull, refac)) {
-        ring_sweep<true, false, true>(ruw, N, need, sm.ring, lane,
+        ring_sweep<true, false, true, kRes>(ruw, N, need, sm.ring, lane,
                                       FactorForward<kBand>{a32, b1f, b2f, sig_cur, pivmin});
       } else {
-        ring_sweep<true, true, false>(ruw, N, need, sm.ring, lane, SolveForward<kBand>{b2f, 1.0f});
+        ring_sweep<true, true, false, kRes>(ruw, N, need, sm.ring, lane, SolveForward<kBand>{b2f, 1.0f});
       }
-      ring_sweep<false, true, false>(ruw, N, need, sm.ring, lane, SolveBackward<kBand>{b2f});
+      ring_sweep<false, true, false, kRes>(ruw, N, need, sm.ring, lane, SolveBackward<kBand>{b2f});
       lap(stats, tsub, 12);
       for (int j = 0; j < K; ++j) {
         if (!((nm >> j) & 1u)) continue;
@@ -1309,7 +1329,7 @@ __device__ __noinline__ void density_from_orbitals(const Params& p, int N, doubl
   const int nocc = (ne + 1) / 2;
   const int nfull = ne / 2;  // doubly occupied; with odd ne, orbital nfull holds one
   const double inv_dx = recip_nr(dx);
-#pragma unroll 2
+#pragma unroll 1
   for (int i = lane; i < N; i += kWarp) {
     double v = 0.0;
     for (int j = 0; j < nfull; ++j) {
@@ -1346,11 +1366,11 @@ __device__ inline void write_stats(const Params& p, int b, const EigStats& e) {
 // ---------------------------------------------------------------------------
 // The kernel
 // ---------------------------------------------------------------------------
-template <int kBand>
+template <int kBand, bool kRes>
 __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__ Params p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x;
-  const SmemLayout L = smem_layout(p.nmax, p.kmax);
+  const SmemLayout L = smem_layout(p.nmax, p.kmax, false, kRes);
   Smem sm = carve(smem_raw, L);
   if (p.xc_kind == QEX_XC_WINDOW_MLP) stage_mlp_weights(p.mlp, sm.mlpw, lane, kWarp);
   __syncwarp();
@@ -1373,7 +1393,8 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
       continue;
     }
     double* const slot_base = p.ws + (long long)slot * p.stride;
-    const SolveArea ruw = solve_area(slot_base, p.nmax, p.kmax);  // streamed FP32 solves
+    const SolveArea ruw = kRes ? solve_area(reinterpret_cast<double*>(sm.ring), p.nmax, p.kmax)
+                               : solve_area(slot_base, p.nmax, p.kmax);  // FP32 solve planes
     double* ws = slot_base + p.ruw_doubles;
     double* vn = ws + (long long)VN * p.nmax;
     double* vext = ws + (long long)VEXT * p.nmax;
@@ -1416,7 +1437,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
     __syncwarp();
 
     if (p.mode == kModeNonInteracting) {
-      flags |= eigen_solve<kBand>(p, N, dx, ne, K, vext, X, ruw, false, 0.0, sm, lane, est);
+      flags |= eigen_solve<kBand, kRes>(p, N, dx, ne, K, vext, X, ruw, false, 0.0, sm, lane, est);
       double tee, gap;
       density_from_orbitals(p, N, dx, ne, K, X, nout, sm, tee, gap, lane);
       if (p.o_final)
@@ -1438,7 +1459,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
       #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) vn[i] = p.dens_in[off + i];
     } else {
-      flags |= eigen_solve<kBand>(p, N, dx, ne, K, vext, X, ruw, false, 0.0, sm, lane, est);
+      flags |= eigen_solve<kBand, kRes>(p, N, dx, ne, K, vext, X, ruw, false, 0.0, sm, lane, est);
       double tee, gap;
       density_from_orbitals(p, N, dx, ne, K, X, vn, sm, tee, gap, lane);
       // warm start from the non-interacting eigenpairs: v_KS differs from
@@ -1517,7 +1538,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
       }
 
       // ---- eigen-solve and output density
-      flags |= eigen_solve<kBand>(p, N, dx, ne, K, vks, X, ruw, warm, dv, sm, lane, est);
+      flags |= eigen_solve<kBand, kRes>(p, N, dx, ne, K, vks, X, ruw, warm, dv, sm, lane, est);
       warm = true;
       tit = clock64();
       double tee, gap;
@@ -1899,7 +1920,7 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
     for (int i = lane; i < N; i += kWarp) vks[i] = vh[i] + vxc[i] + vext[i];
     __syncwarp();
     EigStats est = {};
-    int flags = eigen_solve<kBand>(p, N, dx, ne, K, vks, X, ruw, false, 0.0, sm, lane, est);
+    int flags = eigen_solve<kBand, false>(p, N, dx, ne, K, vks, X, ruw, false, 0.0, sm, lane, est);
     double tee, gap;
     density_from_orbitals(p, N, dx, ne, K, X, nout, sm, tee, gap, lane);
     const double gE = p.a_genergy ? p.a_genergy[b] : 0.0;
@@ -1991,6 +2012,7 @@ int check_options(const qex_ks1d_options* o) {
   if (o->num_iterations < 1 || o->max_num_grids < 5 || o->max_num_electrons < 1) return QEX_BAD_ARG;
   if (o->max_num_electrons / 2 + 1 > QEX_KS1D_MAX_EIGENPAIRS) return QEX_BAD_ARG;
   if (o->num_mixing_iterations < 1) return QEX_BAD_ARG;
+  if (o->solve_planes < 0 || o->solve_planes > 2) return QEX_BAD_ARG;
   return QEX_OK;
 }
 
@@ -2073,6 +2095,7 @@ int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_opt
   P.ws = reinterpret_cast<double*>(static_cast<unsigned char*>(ws) + 256);
   P.stride = stride_doubles(o);
   P.ruw_doubles = ruw_doubles(o->max_num_grids, o->max_num_electrons / 2 + 1);
+  P.planes = o->solve_planes;
   if (num_molecules < 0) return QEX_BAD_ARG;
   if (num_molecules > 0) {
     if (!b->num_grids || !b->grid_offsets || !b->grid_start || !b->grid_spacing ||
@@ -2125,43 +2148,57 @@ int launch_adjoint(const Params& P, cudaStream_t stream) {
   return QEX_OK;
 }
 
-int launch(const Params& P, cudaStream_t stream) {
-  g_last_launches = 0;
-  if (P.num_molecules == 0) return QEX_OK;
-  const SmemLayout L = smem_layout(P.nmax, P.kmax);
-  const size_t smem = L.total;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return QEX_CUDA_ERROR;
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int max_optin = 0;
-  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if ((int)smem > max_optin) return QEX_BAD_ARG;
-  cudaError_t e;
-  int per_sm = 0;
-  if (P.stencil == 5) {
-    e = cudaFuncSetAttribute(ks1d_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return QEX_CUDA_ERROR;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks1d_kernel<2>, kWarp, smem);
-  } else {
-    e = cudaFuncSetAttribute(ks1d_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return QEX_CUDA_ERROR;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks1d_kernel<1>, kWarp, smem);
-  }
-  if (per_sm < 1) per_sm = 1;
+template <int kBand, bool kRes>
+int launch_variant(const Params& P, cudaStream_t stream, size_t smem, int per_sm, int sms) {
+  cudaError_t e =
+      cudaFuncSetAttribute(ks1d_kernel<kBand, kRes>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return QEX_CUDA_ERROR;
   long long grid = (long long)sms * per_sm;
   if (grid > P.num_molecules) grid = P.num_molecules;
   e = cudaMemsetAsync(P.counter, 0, sizeof(int), stream);
   if (e != cudaSuccess) return QEX_CUDA_ERROR;
-  if (P.stencil == 5) {
-    ks1d_kernel<2><<<(unsigned)grid, kWarp, smem, stream>>>(P);
-  } else {
-    ks1d_kernel<1><<<(unsigned)grid, kWarp, smem, stream>>>(P);
-  }
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return QEX_CUDA_ERROR;
+  ks1d_kernel<kBand, kRes><<<(unsigned)grid, kWarp, smem, stream>>>(P);
+  if (cudaGetLastError() != cudaSuccess) return QEX_CUDA_ERROR;
   g_last_launches = 1;
   return QEX_OK;
+}
+
+template <int kBand, bool kRes>
+int blocks_per_sm(size_t smem) {
+  int per_sm = 0;
+  if (cudaFuncSetAttribute(ks1d_kernel<kBand, kRes>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks1d_kernel<kBand, kRes>, kWarp, smem);
+  return per_sm;
+}
+
+// Picks the solve-plane placement: resident in shared memory when the whole
+// batch fits in one wave of resident warps (lowest latency), streamed through
+// the ring otherwise (a small shared-memory footprint, so more warps per SM).
+int launch(const Params& P, cudaStream_t stream) {
+  g_last_launches = 0;
+  if (P.num_molecules == 0) return QEX_OK;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return QEX_CUDA_ERROR;
+  int sms = 0, max_optin = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t smem_s = smem_layout(P.nmax, P.kmax, false, false).total;
+  const size_t smem_r = smem_layout(P.nmax, P.kmax, false, true).total;
+  const bool band2 = (P.stencil == 5);
+  if (P.planes != 2 && (int)smem_r <= max_optin) {
+    const int per_r = band2 ? blocks_per_sm<2, true>(smem_r) : blocks_per_sm<1, true>(smem_r);
+    if (per_r >= 1 && (P.planes == 1 || (long long)P.num_molecules <= (long long)sms * per_r)) {
+      return band2 ? launch_variant<2, true>(P, stream, smem_r, per_r, sms)
+                   : launch_variant<1, true>(P, stream, smem_r, per_r, sms);
+    }
+  }
+  if (P.planes == 1 || (int)smem_s > max_optin) return QEX_BAD_ARG;
+  int per_s = band2 ? blocks_per_sm<2, false>(smem_s) : blocks_per_sm<1, false>(smem_s);
+  if (per_s < 1) per_s = 1;
+  return band2 ? launch_variant<2, false>(P, stream, smem_s, per_s, sms)
+               : launch_variant<1, false>(P, stream, smem_s, per_s, sms);
 }
 
 }  // namespace

@@ -271,12 +271,14 @@ class Ks1dEngine:
         return o
 
     def solve(self, batch: PackedBatch, xc, cfg: SolveConfig, records=RECORD_ALL, out=None,
-              initial_density=None, bucketed=True):
+              initial_density=None, bucketed=True, planes=None):
         """Run the full SCF for every molecule of ``batch``.
 
         With ``bucketed`` the batch is split into runs of equal eigenpair count
         (shared memory per warp scales with it), launched concurrently on
         forked streams; otherwise one launch covers the whole batch.
+        ``planes`` overrides the placement of the FP32 solve planes
+        (``qex_ks1d_options.solve_planes``: 1 resident, 2 streamed).
         """
         torch = N.require_cuda()
         functional, params = resolve(xc)
@@ -289,10 +291,16 @@ class Ks1dEngine:
             (0, batch.size, batch.max_num_electrons, batch.max_num_grids)]
         plans = []
         total = 0
+        # concurrent launches share the SMs: past one molecule per SM, stream
+        # the FP32 solve planes (small shared-memory footprint, more warps per SM)
+        sms = torch.cuda.get_device_properties(batch.device).multi_processor_count
+        if planes is None:
+            planes = 2 if (len(parts) > 1 and batch.size > sms) else 0
         for start, count, ne_max, ng_max in parts:
             opts = _options(cfg, batch, vext_given)
             opts.max_num_electrons = max(ne_max, 1)
             opts.max_num_grids = max(ng_max, 5)
+            opts.solve_planes = planes
             nbytes = ctypes.c_size_t()
             N.check(self.lib.qex_ks1d_workspace_size(ctypes.byref(opts), count, ctypes.byref(nbytes)),
                     "qex_ks1d_workspace_size")

@@ -255,6 +255,39 @@ def test_molecule_alone_equals_molecule_in_batch(qx):
         np.testing.assert_array_equal(alone["energy"][0], full["energy"][i])
 
 
+def test_streamed_solve_planes_match_resident(qx):
+    # A batch larger than one wave of resident warps streams the FP32 solve
+    # planes through the shared-memory ring; the same molecules solved alone
+    # keep them resident in shared memory.  Both orders of work are the same.
+    qex, od = qx
+    base = _random_molecules(21, 8, grid_choices=(257,), max_nuclei=2, max_z=2)
+    mols = base * 256  # 2048 molecules: more than 12 resident warps on each SM
+    batch, full = _run_batch(od, mols, qex.LDAExpCoulomb(), "local", 6)
+    small, alone = _run_batch(od, base, qex.LDAExpCoulomb(), "local", 6)
+    np.testing.assert_allclose(full["energy"][:8], alone["energy"], rtol=0, atol=1e-11)
+    np.testing.assert_allclose(full["energy"][-8:], alone["energy"], rtol=0, atol=1e-11)
+    d_full = batch.split(full["final_density"])[:8]
+    d_alone = small.split(alone["final_density"])
+    for a, b in zip(d_full, d_alone):
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-11)
+
+
+@pytest.mark.parametrize("stencil", [3, 5])
+def test_resident_and_streamed_planes_agree(qx, stencil):
+    qex, od = qx
+    mols = _random_molecules(31 + stencil, 6)
+    ms = [od.Molecule1D(num_grids=n, grid_spacing=0.08, locations=r, nuclear_charges=z,
+                        num_electrons=ne) for n, r, z, ne in mols]
+    batch = od.PackedBatch(ms)
+    cfg = od.SolveConfig(num_iterations=8, convention="local", stencil=stencil)
+    eng = od.engine.default_engine()
+    res = [eng.solve(batch, qex.LDAExpCoulomb(), cfg, planes=pl) for pl in (1, 2)]
+    np.testing.assert_allclose(res[0]["energy"].cpu().numpy(), res[1]["energy"].cpu().numpy(),
+                               rtol=0, atol=1e-11)
+    np.testing.assert_allclose(res[0]["final_density"].cpu().numpy(),
+                               res[1]["final_density"].cpu().numpy(), rtol=0, atol=1e-11)
+
+
 def test_xc_eval_known_answer_on_gpu(qx):
     qex, od = qx
     grids = np.linspace(-5, 5, 10001)
