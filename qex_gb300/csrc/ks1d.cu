@@ -383,15 +383,20 @@ __device__ __noinline__ double xc_eval(const Params& p, int N, double dx, const 
     return 0.0;
   }
   if (p.xc_kind == QEX_XC_LDA_EXP_COULOMB || p.xc_kind == QEX_XC_POWER) {
+    const LdaConsts lc = lda_consts(p.lda_A, p.lda_kappa);
     #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) {
-      double ni = n[i], f, df;
+      double ni = n[i], f, df = 0.0;
       if (p.xc_kind == QEX_XC_LDA_EXP_COULOMB) {
-        lda_exp_coulomb(ni, p.lda_A, p.lda_kappa, f, df);
+        if (want_v) {
+          lda_exp_coulomb<true>(ni, lc, f, df);
+        } else {
+          lda_exp_coulomb<false>(ni, lc, f, df);
+        }
       } else {
         double base = ni + p.xc_shift;
         f = p.xc_a * pow(base, p.xc_p);
-        df = p.xc_a * p.xc_p * pow(base, p.xc_p - 1.0);
+        if (want_v) df = p.xc_a * p.xc_p * pow(base, p.xc_p - 1.0);
       }
       if (local) {
         e = fma(f, ni, e);

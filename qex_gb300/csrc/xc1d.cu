@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(kThreads) xc1d_kernel(const __grid_constant__ 
     for (int i = threadIdx.x; i < N; i += kThreads) {
       double ni = n[i], f = 0.0, df = 0.0;
       if (p.kind == QEX_XC_LDA_EXP_COULOMB) {
-        lda_exp_coulomb(ni, p.lda_A, p.lda_kappa, f, df);
+        lda_exp_coulomb<true>(ni, lda_consts(p.lda_A, p.lda_kappa), f, df);
       } else if (p.kind == QEX_XC_POWER) {
         double base = ni + p.shift;
         f = p.a * pow(base, p.p);

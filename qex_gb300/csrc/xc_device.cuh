@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include "qex_ks1d.h"
+#include "ks1d_common.cuh"
 
 namespace qex {
 
@@ -21,38 +22,70 @@ struct MlpParams {
   float norm_inv;
 };
 
-__device__ inline void lda_exp_coulomb(double n, double A, double kappa, double& eps,
-                                       double& deps_dn) {
-  // Exponential-Coulomb uniform-gas LDA (jax_dft xc.py, called at
-  // qedft/train/od/eval.py:79; published fit of Baker et al., PRB 91, 235141).
+// Exponential-Coulomb uniform-gas LDA (jax_dft xc.py, called at
+// qedft/train/od/eval.py:79; published fit of Baker et al., PRB 91, 235141).
+// Constants hoisted per call site; kDeriv adds d eps / d n.  Divisions are
+// Newton reciprocals (ks1d_common.cuh) wherever the argument is inside the
+// FP32 normal range, the exact operations otherwise (density tails).
+struct LdaConsts {
+  double pik;   // pi / kappa
+  double ax;    // A / (2 pi)
+  double ma_pi; // -A / pi
+  double c3;    // pi kappa^2 / A
+};
+
+__device__ inline LdaConsts lda_consts(double A, double kappa) {
   const double pi = 3.141592653589793;
-  const double y = pi * n / kappa;
-  const double ax = A / (2.0 * pi);
-  double ex, dex;
+  return LdaConsts{pi / kappa, A / (2.0 * pi), -A / pi, pi * kappa * kappa / A};
+}
+
+// IEEE division kept out of line (rarely taken fallbacks stay small).
+__device__ __noinline__ inline double div_exact(double a, double b) { return a / b; }
+
+template <bool kDeriv>
+__device__ inline void lda_exp_coulomb(double n, const LdaConsts& c, double& eps,
+                                       double& deps_dn) {
+  const double y = c.pik * n;
+  double ex, dex = 0.0;
   if (y > 1e-15) {
-    double l = log1p(y * y);
-    ex = ax * (l / y - 2.0 * atan(y));
-    dex = -ax * l / (y * y);
+    const double l = log1p(y * y);
+    const double iy = (y > 1e-30 && y < 1e30) ? recip_nr(y) : div_exact(1.0, y);
+    ex = c.ax * fma(l, iy, -2.0 * atan(y));
+    if (kDeriv) dex = -c.ax * l * iy * iy;
   } else {
-    ex = ax * (-y + y * y * y / 6.0);
-    dex = ax * (-1.0 + 0.5 * y * y);
+    ex = c.ax * (-y + y * y * y / 6.0);
+    if (kDeriv) dex = c.ax * (-1.0 + 0.5 * y * y);
   }
-  double ec, dec;
+  double ec, dec = 0.0;
   if (y > 0.0) {
     const double sy = sqrt(y);
-    const double c3 = pi * kappa * kappa / A;
-    const double P = 2.0 - 1.00077 * sy + 6.26099 * y - 11.9041 * y * sy + 9.62614 * y * y -
-                     1.48334 * y * y * sy + c3 * y * y * y;
-    const double dP = -0.5 * 1.00077 / sy + 6.26099 - 1.5 * 11.9041 * sy + 2.0 * 9.62614 * y -
-                      2.5 * 1.48334 * y * sy + 3.0 * c3 * y * y;
-    ec = -A * y / pi / P;
-    dec = -A / pi * (P - y * dP) / (P * P);
+    // P(s), s = sqrt(y): 2 - 1.00077 s + 6.26099 s^2 - 11.9041 s^3 + 9.62614 s^4
+    //                    - 1.48334 s^5 + c3 s^6
+    const double P =
+        fma(sy, fma(sy, fma(sy, fma(sy, fma(sy, fma(sy, c.c3, -1.48334), 9.62614), -11.9041),
+                            6.26099),
+                    -1.00077),
+            2.0);
+    const double iP = (P > 1e-30 && P < 1e30) ? recip_nr(P) : div_exact(1.0, P);
+    ec = c.ma_pi * y * iP;
+    if (kDeriv) {
+      // dP/dy = (dP/ds) / (2 s)
+      const double dPds =
+          fma(sy,
+              fma(sy, fma(sy, fma(sy, fma(sy, 6.0 * c.c3, -5.0 * 1.48334), 4.0 * 9.62614),
+                          -3.0 * 11.9041),
+                  2.0 * 6.26099),
+              -1.00077);
+      const double isy = (sy > 1e-30 && sy < 1e30) ? recip_nr(sy) : div_exact(1.0, sy);
+      const double dP = 0.5 * dPds * isy;
+      dec = c.ma_pi * (P - y * dP) * iP * iP;
+    }
   } else {
     ec = 0.0;
-    dec = -A / pi / 2.0;
+    if (kDeriv) dec = c.ma_pi / 2.0;
   }
   eps = ex + ec;
-  deps_dn = (dex + dec) * (pi / kappa);
+  if (kDeriv) deps_dn = (dex + dec) * c.pik;
 }
 
 __device__ inline float silu_d(float z, float& d) {
