@@ -10,6 +10,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "ks1d_common.cuh"
 #include "qex_ks1d.h"
 #include "qex_td.h"
 
@@ -19,7 +20,18 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kTile = 64;      // GEMM tile (rows x cols)
 constexpr int kTileK = 16;     // GEMM k-step
 constexpr int kThreads = 256;  // 16 x 16 threads, 4 x 4 outputs each
-constexpr int kVxcChunk = 2048;
+constexpr int kVxcCtas = 304;  // target CTAs of one Vxc product (2 per SM)
+
+// Grid points per Vxc chunk: enough chunks that the upper tiles times the
+// chunks fill the GPU (FP64 issues slowly on one SM), at least one k-step.
+long long vxc_chunk_len(long long G, int nao) {
+  const long long tiles = (nao + kTile - 1) / kTile;
+  const long long upper = tiles * (tiles + 1) / 2;
+  long long chunks = (kVxcCtas + upper - 1) / upper;
+  long long len = (G + chunks - 1) / chunks;
+  len = (len + kTileK - 1) / kTileK * kTileK;
+  return len < kTileK ? kTileK : len;
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -206,15 +218,16 @@ __global__ void __launch_bounds__(kThreads) vxc_kernel(long long G, int n,
                                                        const double* __restrict__ ao,
                                                        const double* __restrict__ w,
                                                        const double* __restrict__ v,
-                                                       double* __restrict__ part) {
+                                                       double* __restrict__ part,
+                                                       long long chunk) {
   const int ti = blockIdx.x, tj = blockIdx.y;
   if (ti > tj) return;
   __shared__ double As[kTileK][kTile + 1];
   __shared__ double Bs[kTileK][kTile + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int r0 = ti * kTile, c0 = tj * kTile;
-  const long long g0 = (long long)blockIdx.z * kVxcChunk;
-  const long long g1 = min(G, g0 + kVxcChunk);
+  const long long g0 = (long long)blockIdx.z * chunk;
+  const long long g1 = min(G, g0 + chunk);
   double acc[4][4] = {};
   for (long long gk = g0; gk < g1; gk += kTileK) {
     for (int e = threadIdx.x; e < kTile * kTileK; e += kThreads) {
@@ -512,11 +525,21 @@ __device__ int jacobi(int n, double* C, double* U, int* pos, double* cs, int* pq
         if (q < n) {
           const double apq = C[(long long)p * n + q];
           if (apq != 0.0) {
+            // rotation angle in FP32 (it need not annihilate a_pq exactly: the
+            // sweeps converge all the same), made orthogonal in FP64
             const double app = C[(long long)p * n + p], aqq = C[(long long)q * n + q];
-            const double th = (aqq - app) / (2.0 * apq);
-            const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(1.0 + th * th));
-            c = 1.0 / sqrt(1.0 + t * t);
-            s = t * c;
+            const float th = __fdividef((float)(aqq - app), 2.0f * (float)apq);
+            const float t = (fabsf(th) < 1e18f)
+                                ? copysignf(1.0f, th) / (fabsf(th) + sqrtf(fmaf(th, th, 1.0f)))
+                                : 0.0f;
+            if (t != 0.0f) {
+              const float cf = rsqrtf(fmaf(t, t, 1.0f));
+              c = (double)cf;
+              s = (double)(t * cf);
+              const double nrm = qex::rsqrt_nr(fma(c, c, s * s));
+              c *= nrm;
+              s *= nrm;
+            }
           }
         }
         cs[2 * k] = c;
@@ -742,7 +765,8 @@ int qex_td_lda(int64_t num_points, const double* rho, const double* weights, dou
 
 size_t qex_td_vxc_workspace_size(int64_t num_points, int32_t nao) {
   if (num_points < 0 || nao < 1) return 0;
-  const long long chunks = (num_points + kVxcChunk - 1) / kVxcChunk;
+  const long long len = vxc_chunk_len(num_points, nao);
+  const long long chunks = (num_points + len - 1) / len;
   return sizeof(double) * (size_t)(chunks < 1 ? 1 : chunks) * (size_t)nao * (size_t)nao;
 }
 
@@ -753,14 +777,15 @@ int qex_td_vxc(int64_t num_points, int32_t nao, const double* ao, const double* 
   if (!ao || !weights || !vrho || !vmat || !workspace) return QEX_BAD_ARG;
   if (workspace_bytes < qex_td_vxc_workspace_size(num_points, nao)) return QEX_BAD_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  long long chunks = (num_points + kVxcChunk - 1) / kVxcChunk;
+  const long long len = vxc_chunk_len(num_points, nao);
+  long long chunks = (num_points + len - 1) / len;
   if (chunks < 1) chunks = 1;
   if (chunks > 65535) return QEX_BAD_ARG;
   double* part = static_cast<double*>(workspace);
   const int tiles = (nao + kTile - 1) / kTile;
   if (num_points == 0) cudaMemsetAsync(part, 0, sizeof(double) * (size_t)nao * nao, s);
   vxc_kernel<<<dim3(tiles, tiles, (unsigned)chunks), kThreads, 0, s>>>(num_points, nao, ao, weights,
-                                                                       vrho, part);
+                                                                       vrho, part, len);
   vxc_sum_kernel<<<grid_for((long long)nao * nao, kThreads), kThreads, 0, s>>>(nao, (int)chunks,
                                                                                part, vmat);
   return cudaGetLastError() == cudaSuccess ? QEX_OK : QEX_CUDA_ERROR;

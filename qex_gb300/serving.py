@@ -1,13 +1,17 @@
 """Continuous-batching SCF server (the serving configuration).
 
-Requests (1D Kohn-Sham solves of any grid size and electron count) arrive
-over time.  The server admits every pending request into a new batch as soon
-as a launch slot (a CUDA stream) and device memory are free, so batches
-launched at different times run concurrently on the GPU; each request's
-density, eigenvectors and mixing history stay in its batch's device
-workspace until the solve ends.  Admission is by device memory: a request is
-admitted only while the bytes of all in-flight batches (workspace + outputs)
-stay under ``memory_budget_bytes``.  Latency is arrival -> result on the host.
+Requests arrive over time: 1D Kohn-Sham solves of any grid size and electron
+count, and 3D SCF solves (numint LDA + DIIS) of resident molecules.  The
+server admits every pending 1D request into a new batch as soon as a launch
+slot (a CUDA stream) and device memory are free, so batches launched at
+different times run concurrently on the GPU; each request's density,
+eigenvectors and mixing history stay in its batch's device workspace until
+the solve ends.  A 3D request replays its molecule's captured SCF graph
+(``qex_gb300.td.graph.CapturedScf``: integrals, density matrix and DIIS
+history resident on the device) on a free stream.  Admission is by device
+memory: a 1D batch is admitted only while the bytes of all in-flight batches
+(workspace + outputs) plus the resident 3D graphs stay under
+``memory_budget_bytes``.  Latency is arrival -> result on the host.
 
 The reference has no serving layer; it solves one molecule (or one vmap'd
 batch of equal-shape molecules) per call (``qedft/train/od/train.py:84-125``),
@@ -31,13 +35,18 @@ from .xc import resolve
 @dataclasses.dataclass
 class Request:
     rid: int
-    molecule: Molecule1D
+    molecule: Molecule1D | None  # 1D request
     arrival: float  # seconds from the start of the stream
     start: float = float("nan")
     finish: float = float("nan")
     energies: np.ndarray | None = None
     density: np.ndarray | None = None
     status: int = 0
+    graph3d: object = None  # 3D request: key of a resident CapturedScf
+
+    @property
+    def is3d(self):
+        return self.graph3d is not None
 
     @property
     def latency(self):
@@ -47,13 +56,14 @@ class Request:
 @dataclasses.dataclass
 class _Launch:
     requests: List[Request]
-    batch: PackedBatch
-    out: dict
+    batch: PackedBatch | None
+    out: dict | None
     host: dict
     workspace: object
     stream: object
     event: object
     nbytes: int
+    graph3d: object = None
 
 
 def config1_requests(arrivals, seed: int = 0, num_grids=513, spacing=0.08) -> List[Request]:
@@ -79,7 +89,8 @@ class ScfServer:
     """Continuous batching of 1D SCF requests over a pool of CUDA streams."""
 
     def __init__(self, xc, cfg: SolveConfig, max_inflight: int = 16, max_batch: int = 512,
-                 memory_budget_bytes: int = 8 << 30, engine: Ks1dEngine | None = None):
+                 memory_budget_bytes: int = 8 << 30, engine: Ks1dEngine | None = None,
+                 graphs3d: dict | None = None):
         self.torch = N.require_cuda()
         self.xc = xc
         self.cfg = cfg
@@ -91,6 +102,10 @@ class ScfServer:
         self.streams = [self.torch.cuda.Stream() for _ in range(max_inflight)]
         self.functional, self.params = resolve(xc)
         self.spec, self._keep = self.functional.spec(self.params, _convention(cfg))
+        # resident 3D molecules (captured SCF graphs) hold their memory throughout
+        self.graphs3d = dict(graphs3d or {})
+        self.resident = sum(g.nbytes for g in self.graphs3d.values())
+        self.busy3d = set()
         self.in_use = 0
         self.launches = 0
 
@@ -130,7 +145,30 @@ class ScfServer:
             r.start = now
         return _Launch(list(reqs), batch, out, host, ws, stream, ev, nbytes)
 
+    def _launch3d(self, req: Request, stream, now: float) -> _Launch:
+        torch = self.torch
+        g = self.graphs3d[req.graph3d]
+        with torch.cuda.stream(stream):
+            res = g.replay()
+            host = {"energy": torch.empty(res.energies.shape, dtype=torch.float64, pin_memory=True),
+                    "status": torch.empty(res.status.shape, dtype=torch.int32, pin_memory=True)}
+            host["energy"].copy_(res.energies, non_blocking=True)
+            host["status"].copy_(res.status, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        self.busy3d.add(req.graph3d)
+        self.launches += 1
+        req.start = now
+        return _Launch([req], None, None, host, None, stream, ev, 0, graph3d=req.graph3d)
+
     def _retire(self, launch: _Launch, now: float):
+        if launch.graph3d is not None:
+            r = launch.requests[0]
+            r.finish = now
+            r.energies = launch.host["energy"].numpy().copy()
+            r.status = int(np.bitwise_or.reduce(launch.host["status"].numpy()))
+            self.busy3d.discard(launch.graph3d)
+            return
         energy = launch.host["energy"].numpy()
         dens = launch.batch.split(launch.host["final_density"].numpy())
         status = launch.host["status"].numpy()
@@ -163,19 +201,31 @@ class ScfServer:
                     done += len(L.requests)
                     inflight.remove(L)
                     free.append(L.stream)
-            while pending and free:
-                take = pending[: self.max_batch]
+            # 3D requests: a replay of the molecule's graph on a free stream
+            # (one replay of a graph at a time: its results are static tensors)
+            for r in [q for q in pending if q.is3d]:
+                if not free:
+                    break
+                if r.graph3d in self.busy3d:
+                    continue
+                inflight.append(self._launch3d(r, free.pop(), now))
+                pending.remove(r)
+            while free and any(not q.is3d for q in pending):
+                p1d = [q for q in pending if not q.is3d]
+                take = p1d[: self.max_batch]
                 # admission by device memory: halve the batch until it fits the
                 # free budget; a single request that does not fit waits for
                 # in-flight batches to finish (or runs alone on an idle GPU)
-                while len(take) > 1 and self.in_use + self._estimate(take) > self.budget:
+                base = self.in_use + self.resident
+                while len(take) > 1 and base + self._estimate(take) > self.budget:
                     take = take[: len(take) // 2]
-                if self.in_use + self._estimate(take) > self.budget and inflight:
+                if base + self._estimate(take) > self.budget and inflight:
                     break
                 L = self._launch(take, free.pop(), now)
                 self.in_use += L.nbytes
                 inflight.append(L)
-                pending = pending[len(take):]
+                taken = set(id(q) for q in take)
+                pending = [q for q in pending if id(q) not in taken]
             if realtime:
                 time.sleep(0.0002)
         return reqs
@@ -185,13 +235,17 @@ class ScfServer:
         nmax = max(r.molecule.num_grids for r in reqs)
         kmax = max(r.molecule.num_electrons // 2 + 1 for r in reqs)
         slots = min(self.cfg.num_mixing_iterations, self.cfg.num_iterations)
-        per = (9 + slots + kmax) * nmax * 8
+        # FP64 vectors + the FP32 solve planes of one molecule (ks1d.cu workspace)
+        per = (9 + slots + kmax + 2) * nmax * 8 + -(-nmax // 16) * 16 * kmax * 12
         return len(reqs) * per + len(reqs) * self.cfg.num_iterations * 16 + n * 8
 
 
 def serve_plain(xc, cfg: SolveConfig, requests: Sequence[Request],
-                engine: Ks1dEngine | None = None) -> List[Request]:
-    """One request at a time, in arrival order (the reference's calling pattern)."""
+                engine: Ks1dEngine | None = None, molecules3d: dict | None = None,
+                max_cycle: int = 30) -> List[Request]:
+    """One request at a time, in arrival order (the reference's calling pattern):
+    1D requests through the engine, 3D requests through ``td.scf.run_scf`` (kernel
+    launches from the host, no graph) on the molecule in ``molecules3d``."""
     torch = N.require_cuda()
     engine = engine or Ks1dEngine()
     reqs = sorted(requests, key=lambda r: r.arrival)
@@ -201,6 +255,14 @@ def serve_plain(xc, cfg: SolveConfig, requests: Sequence[Request],
         if now < r.arrival:
             time.sleep(r.arrival - now)
         r.start = time.perf_counter() - t0
+        if r.is3d:
+            from .td.scf import run_scf
+
+            res = run_scf(molecules3d[r.graph3d], max_cycle)
+            r.energies = res.energies.cpu().numpy()
+            r.status = int(np.bitwise_or.reduce(res.status.cpu().numpy()))
+            r.finish = time.perf_counter() - t0
+            continue
         batch = PackedBatch([r.molecule], sort=False)
         out = engine.solve(batch, xc, cfg, records=("energy", "final_density"))
         energy = out["energy"].cpu().numpy()
@@ -211,7 +273,34 @@ def serve_plain(xc, cfg: SolveConfig, requests: Sequence[Request],
     return reqs
 
 
+def mixed_requests(arrivals, keys3d: Sequence, frac3d: float = 0.2, seed: int = 0,
+                   num_grids=513, spacing=0.08) -> List[Request]:
+    """Config-5 stream: a fraction ``frac3d`` of 3D requests (uniform over the
+    resident molecules ``keys3d``), the rest config-1-shaped 1D requests."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i, t in enumerate(arrivals):
+        if keys3d and rng.uniform() < frac3d:
+            out.append(Request(rid=i, molecule=None, arrival=float(t),
+                               graph3d=keys3d[int(rng.integers(len(keys3d)))]))
+        else:
+            r = rng.uniform(0.5, 1.5)
+            mol = Molecule1D(num_grids=num_grids, grid_spacing=spacing, locations=[-r, r],
+                             nuclear_charges=[1.0, 1.0], num_electrons=2)
+            out.append(Request(rid=i, molecule=mol, arrival=float(t)))
+    return out
+
+
 def latency_summary(reqs: Sequence[Request], duration: float | None = None) -> dict:
+    out = _summary(reqs, duration)
+    if any(r.is3d for r in reqs) and not all(r.is3d for r in reqs):
+        span = out["span_s"]
+        out["1d"] = _summary([r for r in reqs if not r.is3d], span)
+        out["3d"] = _summary([r for r in reqs if r.is3d], span)
+    return out
+
+
+def _summary(reqs: Sequence[Request], duration: float | None = None) -> dict:
     lat = np.array([r.latency for r in reqs])
     span = duration if duration else (max(r.finish for r in reqs) - min(r.arrival for r in reqs))
     conv = [r for r in reqs if r.energies is not None and abs(r.energies[-1] - r.energies[-2]) < 1e-8
@@ -224,4 +313,5 @@ def latency_summary(reqs: Sequence[Request], duration: float | None = None) -> d
         "p50_ms": float(np.percentile(lat, 50) * 1e3),
         "p99_ms": float(np.percentile(lat, 99) * 1e3),
         "mean_ms": float(lat.mean() * 1e3),
+        "span_s": float(span),
     }

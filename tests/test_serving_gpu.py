@@ -67,3 +67,39 @@ def test_plain_form_matches_served(srv):
     served = serving.ScfServer(qex.LDAExpCoulomb(), cfg).serve(reqs)
     for a, b in zip(plain, served):
         np.testing.assert_array_equal(a.energies, b.energies)
+
+
+def test_mixed_1d_3d_stream_equals_alone(srv):
+    # config-5 shape: 1D requests batched, 3D requests replaying their resident
+    # molecule's captured SCF graph; every result equals the request solved alone
+    qex, serving, eng, cfg = srv
+    from qex_gb300.td import graph, scf, workloads
+
+    mols3 = {"a": workloads.synthetic_molecule(2, seed=0),
+             "b": workloads.synthetic_molecule(3, seed=1)}
+    graphs = {k: graph.CapturedScf(m, max_cycle=12) for k, m in mols3.items()}
+    reqs = serving.mixed_requests(serving.poisson_arrivals(300.0, 0.1, seed=7), list(mols3),
+                                  frac3d=0.3, seed=7)
+    server = serving.ScfServer(qex.LDAExpCoulomb(), cfg, max_inflight=4, max_batch=16,
+                               graphs3d=graphs)
+    done = server.serve(reqs, realtime=False)
+    three = [r for r in done if r.is3d]
+    one = [r for r in done if not r.is3d]
+    assert three and one
+    alone = {k: scf.run_scf(m, max_cycle=12) for k, m in mols3.items()}
+    for r in three:
+        np.testing.assert_array_equal(r.energies, alone[r.graph3d].energies.cpu().numpy())
+        assert r.status == 0
+    engine = eng.Ks1dEngine()
+    for r in one[:4]:
+        a = engine.solve(eng.PackedBatch([r.molecule]), qex.LDAExpCoulomb(), cfg,
+                         records=("energy", "final_density"))
+        np.testing.assert_array_equal(a["energy"].cpu().numpy()[0], r.energies)
+    s = serving.latency_summary(done)
+    assert s["3d"]["requests"] == len(three) and s["1d"]["requests"] == len(one)
+    # the plain one-at-a-time form gives the same 3D energies (no graph)
+    plain = serving.serve_plain(qex.LDAExpCoulomb(), cfg,
+                                [serving.Request(r.rid, None, r.arrival, graph3d=r.graph3d)
+                                 for r in three[:2]], molecules3d=mols3, max_cycle=12)
+    for a, b in zip(plain, three[:2]):
+        np.testing.assert_array_equal(a.energies, b.energies)
