@@ -345,6 +345,41 @@ def run_serving(args):
     arr = sv.poisson_arrivals(args.plain_rate, args.plain_seconds, seed=7)
     done = sv.serve_plain(xc, cfg, sv.config1_requests(arr, seed=7))
     out[f"plain_rate_{int(args.plain_rate)}"] = sv.latency_summary(done)
+    if args.mix_rates:
+        out["mix"] = run_serving_mix(args, xc, cfg)
+    return out
+
+
+def run_serving_mix(args, xc, cfg):
+    """Config-5 mix: 80% plain-configuration 1D requests, 20% 3D SCF requests
+    (numint LDA + factored Coulomb + DIIS, 30 cycles) over a pool of resident
+    synthetic molecules, each replaying its captured CUDA graph; beside it the
+    plain one-at-a-time form (3D through host-launched kernels)."""
+    from qex_gb300 import serving as sv
+    from qex_gb300.td import graph, workloads
+
+    pool = {f"m{na}_{sd}": workloads.synthetic_molecule(na, seed=sd)
+            for na, sd in ((1, 11), (2, 12), (3, 13), (4, 14))}
+    graphs = {k: graph.CapturedScf(m, max_cycle=30) for k, m in pool.items()}
+    out = {"workload": "Poisson stream, 80% 1D requests as above, 20% 3D SCF requests over "
+                       "4 resident synthetic molecules (nao " +
+                       ",".join(str(m.nao) for m in pool.values()) + "), LDA exchange, "
+                       "factored Coulomb, DIIS, 30 cycles",
+           "resident_3d_bytes": int(sum(g.nbytes for g in graphs.values()))}
+    keys = list(pool)
+    for rate in args.mix_rates:
+        arr = sv.poisson_arrivals(rate, args.serving_seconds, seed=int(rate) + 1)
+        reqs = sv.mixed_requests(arr, keys, frac3d=0.2, seed=int(rate) + 1)
+        server = sv.ScfServer(xc, cfg, max_inflight=16, max_batch=1024, graphs3d=graphs)
+        done = server.serve(reqs)
+        s = sv.latency_summary(done)
+        s["launches"] = server.launches
+        out[f"served_rate_{int(rate)}"] = s
+    rate = min(args.mix_rates)
+    arr = sv.poisson_arrivals(rate, args.plain_seconds, seed=17)
+    done = sv.serve_plain(xc, cfg, sv.mixed_requests(arr, keys, frac3d=0.2, seed=17),
+                          molecules3d=pool, max_cycle=30)
+    out[f"plain_rate_{int(rate)}"] = sv.latency_summary(done)
     return out
 
 
@@ -394,6 +429,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serving-rates", type=float, nargs="*", default=[1000.0, 5000.0])
     ap.add_argument("--serving-seconds", type=float, default=1.0)
+    ap.add_argument("--mix-rates", type=float, nargs="*", default=[100.0, 200.0])
     ap.add_argument("--plain-rate", type=float, default=50.0)
     ap.add_argument("--plain-seconds", type=float, default=1.0)
     args = ap.parse_args()

@@ -20,6 +20,8 @@
  *   qex_td_diis_error     <- get_diis_error, qedft/train/td/jax_diis.py:107-114
  *   qex_td_diis_extrapolate <- update_diis_state + extrapolate_fock,
  *                            qedft/train/td/jax_diis.py:26-104
+ *   qex_td_nn_xc          <- get_exc_and_vrho, qedft/train/td/xc.py:12-47 (local MLP of
+ *                            qedft/train/td/trainer_legacy_no_jit.py:56-62, 98-107)
  *   qex_td_coulomb        <- J = einsum('ijkl,kl->ij', eri, dm),
  *                            qedft/train/td/scf_functions_masked.py:152, with the
  *                            ERI in factored form (ij|kl) = sum_P B_Pij B_Pkl
@@ -91,6 +93,19 @@ int qex_td_diis_extrapolate(int32_t n, int32_t nvec, int32_t min_vecs, const dou
  * workspace: naux doubles. */
 int qex_td_coulomb(int32_t n, int32_t naux, const double* factors, const double* dm, double* J,
                    void* workspace, size_t workspace_bytes, void* stream);
+
+/* Neural XC on the grid: replaces get_exc_and_vrho (qedft/train/td/xc.py:12-47)
+ * with the local MLP of qedft/train/td/trainer_legacy_no_jit.py:56-62, 98-107
+ * (features [H, H, 1], gelu (tanh form), output -scale * swish).  rho, exc, vrho:
+ * (num_points) FP64 device; params: FP32 device, w1 (H), b1 (H), W2 (H x H,
+ * row = input unit), b2 (H), w3 (H), b3 (1).  exc_g = network(rho_g),
+ * vrho_g = d exc_g / d rho_g; the network runs in FP32.  With weights (else
+ * null, and sums null), sums = (sum w rho, sum w rho exc) in FP64 as nr_rks
+ * accumulates them (qedft/train/td/numint_legacy.py:148-160). */
+size_t qex_td_nn_xc_workspace_size(int64_t num_points, int32_t hidden);
+int qex_td_nn_xc(int64_t num_points, int32_t hidden, const double* rho, const double* weights,
+                 const float* params, double scale, double* exc, double* vrho, double* sums,
+                 void* workspace, size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

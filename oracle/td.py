@@ -105,6 +105,60 @@ def nr_rks_lda(ao, weights, dm):
 
 
 # ----------------------------------------------------------------------------
+# Neural XC (local MLP)
+# ----------------------------------------------------------------------------
+def _gelu(x):
+    """flax/jax gelu, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3)))."""
+    c = x.dtype.type(np.sqrt(2.0 / np.pi))
+    a = x.dtype.type(0.044715)
+    half = x.dtype.type(0.5)
+    one = x.dtype.type(1.0)
+    t = np.tanh(c * (x + a * x ** 3))
+    d = half * (one + t) + half * x * (one - t * t) * c * (one + x.dtype.type(3.0) * a * x * x)
+    return half * x * (one + t), d
+
+
+def nn_xc_local(flat, rho, scale=1e-2, dtype=np.float64):
+    """(exc, vrho) of ``get_exc_and_vrho`` (``qedft/train/td/xc.py:12-47``) for the
+    local MLP of ``qedft/train/td/trainer_legacy_no_jit.py:56-62, 98-107``:
+    exc_g = -scale swish(w3 . gelu(gelu(rho_g w1 + b1) W2 + b2) + b3) and
+    vrho_g = d exc_g / d rho_g (the vjp with ones of a per-point map), evaluated
+    in ``dtype``.  ``flat`` = (w1, b1, W2 (in, out), b2, w3, b3)."""
+    flat = np.asarray(flat, dtype)
+    H = int(round((-3 + np.sqrt(9 + 4 * (flat.size - 1))) / 2))
+    w1, b1 = flat[:H], flat[H:2 * H]
+    W2 = flat[2 * H:2 * H + H * H].reshape(H, H)
+    o = 2 * H + H * H
+    b2, w3, b3 = flat[o:o + H], flat[o + H:o + 2 * H], flat[o + 2 * H]
+    x = np.asarray(rho, dtype)[:, None]
+    h1, d1 = _gelu(x * w1[None, :] + b1[None, :])
+    z2 = h1 @ W2 + b2[None, :]
+    h2, d2 = _gelu(z2)
+    z3 = h2 @ w3 + b3
+    sg = 1 / (1 + np.exp(-z3))
+    s = dtype(scale)
+    exc = -s * z3 * sg
+    dz3 = -s * sg * (1 + z3 * (1 - sg))
+    dz2 = (dz3[:, None] * w3[None, :]) * d2
+    dh1 = dz2 @ W2.T
+    vrho = (dh1 * d1) @ w1
+    return exc, vrho
+
+
+def nr_rks_nn(ao, weights, dm, flat, scale=1e-2, dtype=np.float64):
+    """``nr_rks_lda`` with the neural functional in place of the LDA exchange."""
+    rho = eval_rho(ao, dm)
+    exc, vrho = nn_xc_local(flat, rho, scale, dtype)
+    exc, vrho = np.asarray(exc, np.float64), np.asarray(vrho, np.float64)
+    den = rho * weights
+    nelec = den.sum()
+    excsum = np.dot(den, exc)
+    aow = ao * (0.5 * weights * vrho)[:, None]
+    vmat = ao.T @ aow
+    return nelec, excsum, vmat + vmat.T
+
+
+# ----------------------------------------------------------------------------
 # Generalized eigensolver
 # ----------------------------------------------------------------------------
 
@@ -206,15 +260,21 @@ def energy_tot(dm, h1e, J, exc, e_nuc):
     return float(np.einsum("ij,ji->", dm, h1e) + 0.5 * np.einsum("ij,ij->", dm, J) + exc + e_nuc)
 
 
-def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1):
+def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, nn=None):
     """Fixed-cycle SCF of ``qedft/train/td/scf_functions_masked.py:907-967`` with
-    the low-rank Coulomb model and the LDA exchange."""
+    the low-rank Coulomb model and the LDA exchange, or with ``nn = (flat,
+    scale, dtype)`` the neural functional."""
     ao, w = mol.ao, mol.weights
+    if nn is None:
+        rks = nr_rks_lda
+    else:
+        def rks(ao, w, dm):
+            return nr_rks_nn(ao, w, dm, *nn)
     s1e, h1e = mol.s1e, mol.h1e
     e0, c0 = generalized_eigh(h1e, s1e)
     dm = make_rdm1(c0, get_occ(mol.nelectron, e0))
     J = coulomb_lowrank(mol.eri_factors, dm)
-    _, exc, vxc = nr_rks_lda(ao, w, dm)
+    _, exc, vxc = rks(ao, w, dm)
     vhf = J + vxc
     diis = DIIS(diis_max_vec)
     energies = []
@@ -225,7 +285,7 @@ def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1):
         mo_e, mo_c = generalized_eigh(fock, s1e)
         dm = make_rdm1(mo_c, get_occ(mol.nelectron, mo_e))
         J = coulomb_lowrank(mol.eri_factors, dm)
-        _, exc, vxc = nr_rks_lda(ao, w, dm)
+        _, exc, vxc = rks(ao, w, dm)
         vhf = J + vxc
         energies.append(energy_tot(dm, h1e, J, exc, mol.energy_nuc))
     return np.array(energies), dm, mo_e

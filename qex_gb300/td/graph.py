@@ -52,7 +52,7 @@ class DeviceMolecule3D:
 class CapturedScf:
     """One molecule's ``run_scf(max_cycle)`` captured as a CUDA graph."""
 
-    def __init__(self, mol, max_cycle: int = 30):
+    def __init__(self, mol, max_cycle: int = 30, xc="LDA"):
         torch = N.require_cuda()
         self.max_cycle = max_cycle
         self.mol = mol if isinstance(mol, DeviceMolecule3D) else DeviceMolecule3D.from_host(mol)
@@ -61,12 +61,12 @@ class CapturedScf:
         side = torch.cuda.Stream()
         side.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(side):
-            run_scf(self.mol, max_cycle)
+            run_scf(self.mol, max_cycle, xc=xc)
         torch.cuda.current_stream().wait_stream(side)
         torch.cuda.synchronize()
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
-            self.result: ScfResult = run_scf(self.mol, max_cycle)
+            self.result: ScfResult = run_scf(self.mol, max_cycle, xc=xc)
         torch.cuda.synchronize()
         # device bytes held while resident: inputs + the graph's private pool
         self.nbytes = self.mol.nbytes() + max(torch.cuda.memory_allocated() - before, 0)

@@ -66,6 +66,75 @@ def eval_xc_lda(rho, weights):
     return exc, vrho, sums[0], sums[1]
 
 
+class NeuralXC:
+    """Local neural XC functional of the 3D path (qedft/train/td/trainer_legacy_no_jit.py:98-107:
+    MLP features [H, H, 1], gelu hidden layers, output -scale * swish; evaluated per grid
+    point as in :56-62).  ``params`` is the flax parameter tree
+    ``{"Dense_0": {"kernel": (1, H), "bias": (H,)}, "Dense_1": ..., "Dense_2": ...}`` or
+    the flat FP32 vector (w1, b1, W2, b2, w3, b3)."""
+
+    def __init__(self, params, scale=1e-2):
+        import numpy as np
+
+        self.scale = float(scale)
+        if isinstance(params, dict):
+            d0, d1, d2 = params["Dense_0"], params["Dense_1"], params["Dense_2"]
+            flat = np.concatenate([np.ravel(d0["kernel"]), np.ravel(d0["bias"]),
+                                   np.ravel(d1["kernel"]), np.ravel(d1["bias"]),
+                                   np.ravel(d2["kernel"]), np.ravel(d2["bias"])])
+            self.hidden = int(np.shape(d0["bias"])[0])
+        else:
+            flat = np.ravel(np.asarray(params))
+            self.hidden = int(round((-3 + (9 + 4 * (flat.size - 1)) ** 0.5) / 2))
+        if flat.size != self.hidden * self.hidden + 4 * self.hidden + 1:
+            raise ValueError(f"parameter vector of {flat.size} floats does not fit [H, H, 1]")
+        self.flat = np.ascontiguousarray(flat, dtype=np.float32)
+        self._dev = None
+
+    @staticmethod
+    def init(hidden=512, seed=0):
+        """flax-style initialisation: lecun-normal kernels, zero biases."""
+        import numpy as np
+
+        rng = np.random.default_rng(seed)
+
+        def dense(fi, fo):
+            return {"kernel": rng.normal(0.0, 1.0 / np.sqrt(fi), (fi, fo)).astype(np.float32),
+                    "bias": np.zeros(fo, np.float32)}
+
+        return {"Dense_0": dense(1, hidden), "Dense_1": dense(hidden, hidden),
+                "Dense_2": dense(hidden, 1)}
+
+    def device_params(self):
+        torch = N.require_cuda()
+        if self._dev is None:
+            self._dev = torch.as_tensor(self.flat, device="cuda")
+        return self._dev
+
+
+def eval_xc_nn(rho, functional: NeuralXC, weights=None):
+    """(exc, vrho) = (network(rho), d network / d rho) per grid point, as
+    ``get_exc_and_vrho`` (qedft/train/td/xc.py:12-47) returns them; with
+    ``weights`` also (nelec, excsum) = (sum w rho, sum w rho exc)."""
+    torch = N.require_cuda()
+    L = _lib.lib()
+    rho = _dev(rho, torch.float64)
+    G = rho.shape[0]
+    exc = torch.empty_like(rho)
+    vrho = torch.empty_like(rho)
+    H = functional.hidden
+    w = None if weights is None else _dev(weights, torch.float64)
+    sums = None if w is None else torch.empty(2, dtype=torch.float64, device="cuda")
+    ws = torch.empty(max(L.qex_td_nn_xc_workspace_size(G, H), 256), dtype=torch.uint8,
+                     device="cuda")
+    N.check(L.qex_td_nn_xc(G, H, _lib.p(rho), _lib.p(w), _lib.p(functional.device_params()),
+                           functional.scale, _lib.p(exc), _lib.p(vrho), _lib.p(sums),
+                           _lib.p(ws), ws.numel(), _lib.stream()), "qex_td_nn_xc")
+    if w is None:
+        return exc, vrho
+    return exc, vrho, sums[0], sums[1]
+
+
 def vxc_matrix(ao, weights, vrho):
     """ao^T diag(0.5 w v) ao + its transpose."""
     torch = N.require_cuda()
@@ -81,9 +150,14 @@ def vxc_matrix(ao, weights, vrho):
 
 
 def nr_rks(ao, weights, dm, xc_code="LDA"):
-    """(nelec, excsum, vmat) for the LDA exchange (``numint_legacy.py:122-164,337``)."""
-    if xc_code.upper() not in ("LDA", "LDA_X", "SLATER"):
-        raise NotImplementedError(f"xc_code {xc_code!r}: the GPU path implements the LDA exchange")
+    """(nelec, excsum, vmat) (``numint_legacy.py:122-164,337``) for the LDA exchange
+    or, with a ``NeuralXC`` as ``xc_code``, the neural functional (``xc.py:57-87``)."""
     rho = eval_rho(ao, dm)
+    if isinstance(xc_code, NeuralXC):
+        exc, vrho, nelec, excsum = eval_xc_nn(rho, xc_code, weights)
+        return nelec, excsum, vxc_matrix(ao, weights, vrho)
+    if xc_code.upper() not in ("LDA", "LDA_X", "SLATER"):
+        raise NotImplementedError(f"xc_code {xc_code!r}: the GPU path implements the LDA exchange "
+                                  "and the neural functional")
     exc, vrho, nelec, excsum = eval_xc_lda(rho, weights)
     return nelec, excsum, vxc_matrix(ao, weights, vrho)

@@ -17,7 +17,7 @@ import numpy as np
 from .. import _native as N
 from . import _lib
 from .eigh import generalized_eigh
-from .numint import _dev, eval_rho, eval_xc_lda, vxc_matrix
+from .numint import _dev, nr_rks
 
 
 def get_occ(nelectron, mo_energy):
@@ -113,8 +113,9 @@ def energy_tot(dm, h1e, J, excsum, energy_nuc):
     return (dm * h1e.T).sum() + 0.5 * (dm * J).sum() + excsum + energy_nuc
 
 
-def run_scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, diis_min_vecs=2):
-    """Fixed-cycle SCF for one synthetic molecule (LDA exchange, factored Coulomb)."""
+def run_scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, diis_min_vecs=2, xc="LDA"):
+    """Fixed-cycle SCF for one synthetic molecule (factored Coulomb; the LDA
+    exchange, or a ``numint.NeuralXC`` functional as ``xc``)."""
     torch = N.require_cuda()
     ao = _dev(mol.ao, torch.float64)
     w = _dev(mol.weights, torch.float64)
@@ -127,9 +128,8 @@ def run_scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, diis_min_vecs
 
     def veff(dm):
         J = coulomb(fac, dm)
-        rho = eval_rho(ao, dm)
-        _, vrho, _, excsum = eval_xc_lda(rho, w)
-        return J + vxc_matrix(ao, w, vrho), J, excsum
+        _, excsum, vmat = nr_rks(ao, w, dm, xc)
+        return J + vmat, J, excsum
 
     vhf, J, exc = veff(dm)
     diis = DIIS(n, diis_max_vec, diis_min_vecs)

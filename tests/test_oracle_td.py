@@ -86,3 +86,21 @@ def test_synthetic_scf_converges():
     assert abs(e[-1] - e[-2]) < 1e-8
     # electron count on the grid matches the trace of D S
     assert abs(np.trace(dm @ m.s1e) - m.nelectron) < 1e-8
+
+
+def test_nn_xc_oracle_is_its_own_derivative():
+    # vrho is d exc / d rho of the per-point network (the vjp with ones of
+    # qedft/train/td/xc.py:12-47): central differences in FP64
+    rng = np.random.default_rng(11)
+    H = 24
+    flat = rng.normal(0.0, 0.4, H * H + 4 * H + 1)
+    rho = rng.uniform(0.0, 3.0, 80)
+    exc, vrho = o.nn_xc_local(flat, rho, scale=1e-2)
+    h = 1e-6
+    ep, _ = o.nn_xc_local(flat, rho + h)
+    em, _ = o.nn_xc_local(flat, rho - h)
+    np.testing.assert_allclose((ep - em) / (2 * h), vrho, rtol=0, atol=1e-9 * np.abs(vrho).max())
+    # the FP32 evaluation stays within FP32 rounding of the FP64 one
+    e32, v32 = o.nn_xc_local(flat, rho, scale=1e-2, dtype=np.float32)
+    np.testing.assert_allclose(e32, exc, rtol=0, atol=1e-6 * np.abs(exc).max())
+    np.testing.assert_allclose(v32, vrho, rtol=0, atol=1e-5 * np.abs(vrho).max())

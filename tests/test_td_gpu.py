@@ -158,3 +158,37 @@ def test_scf_matches_oracle(td, mols):
         # quadratic in its error): compare it at 1e-6 of its largest element
         np.testing.assert_allclose(_host(res.dm), dm_ref, rtol=0, atol=1e-6 * np.abs(dm_ref).max())
         assert (_host(res.status) == 0).all()
+
+
+def test_nn_xc_matches_oracle(td):
+    torch, eigh, numint, scf, W = td
+    rng = np.random.default_rng(12)
+    params = numint.NeuralXC.init(hidden=96, seed=3)
+    # non-zero biases so that every term of the chain rule is exercised
+    params["Dense_0"]["bias"] = rng.normal(0, 0.3, 96).astype(np.float32)
+    params["Dense_1"]["bias"] = rng.normal(0, 0.3, 96).astype(np.float32)
+    params["Dense_2"]["bias"] = np.array([0.2], np.float32)
+    f = numint.NeuralXC(params, scale=1e-2)
+    rho = rng.uniform(0.0, 2.0, 3001)
+    w = rng.uniform(0.5, 1.5, rho.size)
+    exc, vrho, nelec, excsum = numint.eval_xc_nn(rho, f, w)
+    e64, v64 = o.nn_xc_local(f.flat, rho, 1e-2, np.float64)
+    # FP32 network: errors of FP32 rounding against the FP64 evaluation
+    np.testing.assert_allclose(_host(exc), e64, rtol=0, atol=2e-6 * np.abs(e64).max())
+    np.testing.assert_allclose(_host(vrho), v64, rtol=0, atol=2e-5 * np.abs(v64).max())
+    assert abs(float(nelec) - np.dot(w, rho)) < 1e-10 * np.dot(w, rho)
+    assert abs(float(excsum) - np.dot(w * rho, _host(exc))) < 1e-12 * abs(np.dot(w * rho, _host(exc)))
+
+
+def test_scf_with_nn_xc_matches_oracle(td, mols):
+    torch, eigh, numint, scf, W = td
+    params = numint.NeuralXC.init(hidden=64, seed=5)
+    f = numint.NeuralXC(params, scale=1e-2)
+    m = mols[1]
+    res = scf.run_scf(m, max_cycle=12, xc=f)
+    e_ref, dm_ref, _ = o.scf(m, max_cycle=12, nn=(f.flat, 1e-2, np.float64))
+    e = _host(res.energies)
+    # the FP32 network perturbs v_xc at ~1e-7 relative; DIIS carries it along
+    np.testing.assert_allclose(e, e_ref, atol=1e-5, rtol=0)
+    assert abs(e[-1] - e_ref[-1]) < 1e-7
+    assert (_host(res.status) == 0).all()
