@@ -1,0 +1,455 @@
+// Mixed-precision generalized symmetric eigensolver A x = lambda S x (FP64
+// results) for the 3D SCF.
+//
+// GB300 issues FP64 at 1/64 of its FP32 rate, and a one-CTA FP64 Jacobi is
+// bound by that pipe on one SM.  So:
+//   1. FP32, one CTA per matrix, everything in shared memory: Cholesky S = L L^T,
+//      C = L^-1 A L^-T, cyclic Jacobi C = U diag U^T, X = L^-T U.
+//   2. FP64 refinement of X (Ogita & Aishima's iterative refinement for the
+//      symmetric eigenproblem, in its generalized form): R = I - X^T S X,
+//      T = X^T A X, lambda_i = t_ii / (1 - r_ii),
+//      e_ij = (t_ij + lambda_j r_ij) / (lambda_j - lambda_i) when the two
+//      eigenvalues are further apart than delta = 2 (|T - D|_F + |A|_F |R|_F),
+//      else r_ij / 2; X <- X + X E.  Each step squares the error (FP32 ~1e-7 ->
+//      ~1e-13 -> the FP64 floor), so two steps follow the FP32 solve.  The
+//      products are batched split-K FP64 GEMMs over many CTAs.
+//   3. Ascending order (stable), eigenvectors in columns.
+// Matrices whose FP32 Cholesky fails (S not numerically SPD) keep the FP64
+// path of td.cu, which applies the reference's shift
+// (qedft/train/td/generalized_eigensolver.py:264-330).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "qex_ks1d.h"
+
+namespace qex_mp {
+
+constexpr int kThreads = 512;
+constexpr int kMaxSweeps32 = 24;
+constexpr int kT = 32;      // GEMM tile
+constexpr int kKC = 16;     // split-K chunk (one shared-memory stage)
+constexpr int kGThreads = 256;
+
+__device__ inline float block_sumf(float v, float* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float s = 0.0f;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
+  __syncthreads();
+  return s;
+}
+
+__device__ inline double block_sum(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
+  __syncthreads();
+  return s;
+}
+
+// Stage 1: FP32 solve in shared memory.  X (n x n, FP64) receives L^-T U;
+// ok[b] = 1 on success, 0 when the FP32 Cholesky of S fails.
+__global__ void __launch_bounds__(kThreads) eigh32_kernel(int n, const double* __restrict__ A,
+                                                          const double* __restrict__ S,
+                                                          double* __restrict__ X,
+                                                          int* __restrict__ ok) {
+  extern __shared__ float sm[];
+  const int b = blockIdx.x;
+  const long long nn = (long long)n * n;
+  const int m = (n + 1) & ~1;
+  float* L = sm;
+  float* C = L + nn;
+  float* U = C + nn;
+  float* cs = U + nn;                                // 2 * (m / 2)
+  int* pos = reinterpret_cast<int*>(cs + m);         // m
+  int* pq = pos + m;                                 // m
+  float* red = reinterpret_cast<float*>(pq + m);     // 32
+  float* piv = red + 32;                             // 1
+  const double* Ab = A + b * nn;
+  const double* Sb = S + b * nn;
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    C[e] = (float)(0.5 * (Ab[e] + Ab[(long long)j * n + i]));
+    L[e] = (float)(0.5 * (Sb[e] + Sb[(long long)j * n + i]));
+  }
+  __syncthreads();
+  // Cholesky (right-looking), lower triangle of L
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      const float d = L[(long long)k * n + k];
+      piv[0] = d;
+      L[(long long)k * n + k] = d > 0.0f ? sqrtf(d) : 0.0f;
+    }
+    __syncthreads();
+    if (!(piv[0] > 0.0f)) {
+      if (threadIdx.x == 0) ok[b] = 0;
+      return;
+    }
+    const float inv = 1.0f / L[(long long)k * n + k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) L[(long long)i * n + k] *= inv;
+    __syncthreads();
+    const int r = n - k - 1;
+    for (long long e = threadIdx.x; e < (long long)r * r; e += blockDim.x) {
+      const int i = k + 1 + (int)(e / r), j = k + 1 + (int)(e % r);
+      if (j <= i) L[(long long)i * n + j] -= L[(long long)i * n + k] * L[(long long)j * n + k];
+    }
+    __syncthreads();
+  }
+  // C <- L^-1 C (column j per thread), then C <- C L^-T (row r per thread)
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    for (int i = 0; i < n; ++i) {
+      float s = C[(long long)i * n + j];
+      for (int k = 0; k < i; ++k) s = fmaf(-L[(long long)i * n + k], C[(long long)k * n + j], s);
+      C[(long long)i * n + j] = s / L[(long long)i * n + i];
+    }
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    for (int i = 0; i < n; ++i) {
+      float s = C[(long long)r * n + i];
+      for (int k = 0; k < i; ++k) s = fmaf(-L[(long long)i * n + k], C[(long long)r * n + k], s);
+      C[(long long)r * n + i] = s / L[(long long)i * n + i];
+    }
+  }
+  __syncthreads();
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    if (j > i) {
+      const float v = 0.5f * (C[e] + C[(long long)j * n + i]);
+      C[e] = v;
+      C[(long long)j * n + i] = v;
+    }
+    U[e] = (i == j) ? 1.0f : 0.0f;
+  }
+  for (int i = threadIdx.x; i < m; i += blockDim.x) pos[i] = i;
+  __syncthreads();
+  // parallel cyclic Jacobi (round-robin pairs), FP32
+  for (int sweep = 0; sweep < kMaxSweeps32; ++sweep) {
+    float off = 0.0f, dia = 0.0f;
+    for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+      const int i = (int)(e / n), j = (int)(e % n);
+      const float v = C[e];
+      if (i == j) {
+        dia = fmaf(v, v, dia);
+      } else {
+        off = fmaf(v, v, off);
+      }
+    }
+    off = block_sumf(off, red);
+    dia = block_sumf(dia, red);
+    // FP32 floor: the off-diagonal at ~1e-6 of the diagonal (the FP64
+    // refinement takes it from there)
+    if (off <= 1e-12f * dia || off == 0.0f) break;
+    for (int step = 0; step < m - 1; ++step) {
+      for (int k = threadIdx.x; k < m / 2; k += blockDim.x) {
+        int p = pos[k], q = pos[m - 1 - k];
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
+        }
+        float c = 1.0f, s = 0.0f;
+        if (q < n) {
+          const float apq = C[(long long)p * n + q];
+          if (apq != 0.0f) {
+            const float th = (C[(long long)q * n + q] - C[(long long)p * n + p]) / (2.0f * apq);
+            const float t = (fabsf(th) < 1e18f)
+                                ? copysignf(1.0f, th) / (fabsf(th) + sqrtf(fmaf(th, th, 1.0f)))
+                                : 0.0f;
+            c = rsqrtf(fmaf(t, t, 1.0f));
+            s = t * c;
+          }
+        }
+        cs[2 * k] = c;
+        cs[2 * k + 1] = s;
+        pq[2 * k] = p;
+        pq[2 * k + 1] = q;
+      }
+      __syncthreads();
+      for (long long e = threadIdx.x; e < (long long)(m / 2) * n; e += blockDim.x) {
+        const int k = (int)(e / n), j = (int)(e % n);
+        const float s = cs[2 * k + 1];
+        if (s == 0.0f) continue;
+        const float c = cs[2 * k];
+        const int p = pq[2 * k], q = pq[2 * k + 1];
+        const float xp = C[(long long)p * n + j], xq = C[(long long)q * n + j];
+        C[(long long)p * n + j] = c * xp - s * xq;
+        C[(long long)q * n + j] = s * xp + c * xq;
+      }
+      __syncthreads();
+      for (long long e = threadIdx.x; e < (long long)(m / 2) * n; e += blockDim.x) {
+        const int k = (int)(e / n), i = (int)(e % n);
+        const float s = cs[2 * k + 1];
+        if (s == 0.0f) continue;
+        const float c = cs[2 * k];
+        const int p = pq[2 * k], q = pq[2 * k + 1];
+        float xp = C[(long long)i * n + p], xq = C[(long long)i * n + q];
+        C[(long long)i * n + p] = c * xp - s * xq;
+        C[(long long)i * n + q] = s * xp + c * xq;
+        xp = U[(long long)i * n + p];
+        xq = U[(long long)i * n + q];
+        U[(long long)i * n + p] = c * xp - s * xq;
+        U[(long long)i * n + q] = s * xp + c * xq;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const int last = pos[m - 1];
+        for (int i = m - 1; i > 1; --i) pos[i] = pos[i - 1];
+        pos[1] = last;
+      }
+      __syncthreads();
+    }
+  }
+  // X = L^-T U: column j solves L^T x = u_j (back substitution)
+  double* Xb = X + b * nn;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    for (int i = n - 1; i >= 0; --i) {
+      float s = U[(long long)i * n + j];
+      for (int k = i + 1; k < n; ++k) s = fmaf(-L[(long long)k * n + i], U[(long long)k * n + j], s);
+      U[(long long)i * n + j] = s / L[(long long)i * n + i];
+    }
+  }
+  __syncthreads();
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) Xb[e] = (double)U[e];
+  if (threadIdx.x == 0) ok[b] = 1;
+}
+
+// Batched split-K FP64 GEMM partials: P[b][kc] = op(A_b)[:, kc chunk] B_b[kc chunk, :]
+// (n x n, op = transpose with kTA).  grid (tiles, tiles, batch * ksplit).
+template <bool kTA>
+__global__ void __launch_bounds__(kGThreads) gemm_part_kernel(int n, int ksplit,
+                                                              const double* __restrict__ A,
+                                                              const double* __restrict__ B,
+                                                              double* __restrict__ P) {
+  __shared__ double As[kKC][kT + 1];
+  __shared__ double Bs[kKC][kT + 1];
+  const long long nn = (long long)n * n;
+  const int b = blockIdx.z / ksplit, kc = blockIdx.z % ksplit;
+  const int r0 = blockIdx.y * kT, c0 = blockIdx.x * kT;
+  const int k0 = kc * kKC;
+  const double* Ab = A + b * nn;
+  const double* Bb = B + b * nn;
+  for (int e = threadIdx.x; e < kKC * kT; e += kGThreads) {
+    const int k = e / kT, c = e % kT;
+    const int kk = k0 + k;
+    double a = 0.0, v = 0.0;
+    if (kk < n) {
+      if (r0 + c < n) a = kTA ? Ab[(long long)kk * n + r0 + c] : Ab[(long long)(r0 + c) * n + kk];
+      if (c0 + c < n) v = Bb[(long long)kk * n + c0 + c];
+    }
+    As[k][c] = a;
+    Bs[k][c] = v;
+  }
+  __syncthreads();
+  // 16 x 16 threads, 2 x 2 outputs each
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[2][2] = {};
+#pragma unroll
+  for (int k = 0; k < kKC; ++k) {
+    const double a0 = As[k][ty * 2], a1 = As[k][ty * 2 + 1];
+    const double b0 = Bs[k][tx * 2], b1 = Bs[k][tx * 2 + 1];
+    acc[0][0] = fma(a0, b0, acc[0][0]);
+    acc[0][1] = fma(a0, b1, acc[0][1]);
+    acc[1][0] = fma(a1, b0, acc[1][0]);
+    acc[1][1] = fma(a1, b1, acc[1][1]);
+  }
+  double* Pb = P + ((long long)b * ksplit + kc) * nn;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int r = r0 + ty * 2 + i, c = c0 + tx * 2 + j;
+      if (r < n && c < n) Pb[(long long)r * n + c] = acc[i][j];
+    }
+}
+
+// C_b = base + sign * sum_kc P[b][kc] (fixed order).  base: kIdentity -> I,
+// else the matrix `base` (may be null: 0).
+__global__ void gemm_sum_kernel(int batch, int n, int ksplit, const double* __restrict__ P,
+                                const double* base, bool identity, double sign, double* C) {
+  const long long nn = (long long)n * n;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < batch * nn;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long b = e / nn, o = e % nn;
+    double s = 0.0;
+    for (int kc = 0; kc < ksplit; ++kc) s += P[(b * ksplit + kc) * nn + o];
+    double v = identity ? ((o / n == o % n) ? 1.0 : 0.0) : (base ? base[e] : 0.0);
+    C[e] = fma(sign, s, v);
+  }
+}
+
+// As = (A + A^T)/2, Ss = (S + S^T)/2 for every matrix of the batch.
+__global__ void sym_kernel(int batch, int n, const double* __restrict__ A,
+                           const double* __restrict__ S, double* __restrict__ As,
+                           double* __restrict__ Ss) {
+  const long long nn = (long long)n * n;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < batch * nn;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long b = e / nn, o = e % nn;
+    const long long t = b * nn + (o % n) * n + o / n;
+    As[e] = 0.5 * (A[e] + A[t]);
+    Ss[e] = 0.5 * (S[e] + S[t]);
+  }
+}
+
+// Refinement step: lambda_i = t_ii / (1 - r_ii), delta, correction E.
+__global__ void __launch_bounds__(kThreads) refine_update_kernel(int n, const double* __restrict__ A,
+                                                                 const double* __restrict__ R,
+                                                                 const double* __restrict__ T,
+                                                                 double* __restrict__ E,
+                                                                 double* __restrict__ lam) {
+  __shared__ double red[kThreads / 32];
+  const int b = blockIdx.x;
+  const long long nn = (long long)n * n;
+  const double* Ab = A + b * nn;
+  const double* Rb = R + b * nn;
+  const double* Tb = T + b * nn;
+  double* Eb = E + b * nn;
+  double* lb = lam + (long long)b * n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    lb[i] = Tb[(long long)i * n + i] / (1.0 - Rb[(long long)i * n + i]);
+  }
+  __syncthreads();
+  double od = 0.0, an = 0.0, rn = 0.0;
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    const double d = Tb[e] - (i == j ? lb[i] : 0.0);
+    od = fma(d, d, od);
+    an = fma(Ab[e], Ab[e], an);
+    rn = fma(Rb[e], Rb[e], rn);
+  }
+  od = block_sum(od, red);
+  an = block_sum(an, red);
+  rn = block_sum(rn, red);
+  // Frobenius norms bound the 2-norms of Ogita and Aishima's threshold
+  const double delta = 2.0 * (sqrt(od) + sqrt(an) * sqrt(rn));
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    double v;
+    if (i == j) {
+      v = 0.5 * Rb[e];
+    } else {
+      const double gap = lb[j] - lb[i];
+      v = (fabs(gap) > delta) ? (Tb[e] + lb[j] * Rb[e]) / gap : 0.5 * Rb[e];
+    }
+    Eb[e] = v;
+  }
+}
+
+// Ascending (stable) order: w[b][rank_i] = lambda_i, V[b][:, rank_i] = X[:, i].
+__global__ void sort_out_kernel(int n, const double* __restrict__ lam,
+                                const double* __restrict__ X, const int* __restrict__ ok,
+                                double* __restrict__ w, double* __restrict__ V,
+                                int32_t* __restrict__ status) {
+  extern __shared__ int rank[];
+  const int b = blockIdx.x;
+  if (!ok[b]) return;
+  const long long nn = (long long)n * n;
+  const double* lb = lam + (long long)b * n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double li = lb[i];
+    int r = 0;
+    for (int j = 0; j < n; ++j) r += (lb[j] < li) || (lb[j] == li && j < i);
+    rank[i] = r;
+    w[(long long)b * n + r] = li;
+  }
+  __syncthreads();
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    V[b * nn + (long long)i * n + rank[j]] = X[b * nn + e];
+  }
+  if (threadIdx.x == 0 && status) status[b] = 0;
+}
+
+}  // namespace qex_mp
+
+namespace qex_mp_host {
+
+using namespace qex_mp;
+
+constexpr int kMaxN = 128;  // 3 n^2 FP32 matrices in shared memory
+
+int ksplit_of(int n) { return (n + kKC - 1) / kKC; }
+
+// Doubles of the mixed-precision area per matrix: As, Ss, X, X', T, R, E
+// (7 n^2), split-K partials (ksplit n^2), lambda (n), the ok flag (1).
+long long area_doubles(int n) {
+  const long long nn = (long long)n * n;
+  return (7 + ksplit_of(n)) * nn + n + 1;
+}
+
+size_t smem32(int n) {
+  const int m = (n + 1) & ~1;
+  return sizeof(float) * (3 * (size_t)n * n + 3 * (size_t)m + 33);
+}
+
+void gemm(cudaStream_t s, int batch, int n, bool ta, const double* A, const double* B, double* P,
+          const double* base, bool identity, double sign, double* C) {
+  const int ks = ksplit_of(n);
+  const int tiles = (n + kT - 1) / kT;
+  const dim3 grid(tiles, tiles, (unsigned)(batch * ks));
+  if (ta) {
+    gemm_part_kernel<true><<<grid, kGThreads, 0, s>>>(n, ks, A, B, P);
+  } else {
+    gemm_part_kernel<false><<<grid, kGThreads, 0, s>>>(n, ks, A, B, P);
+  }
+  const long long work = (long long)batch * n * n;
+  const int blocks = (int)((work + 255) / 256 < 4096 ? (work + 255) / 256 : 4096);
+  gemm_sum_kernel<<<blocks, 256, 0, s>>>(batch, n, ks, P, base, identity, sign, C);
+}
+
+}  // namespace qex_mp_host
+
+// Host entry used by qex_td_gen_eigh: runs the mixed-precision solver on the
+// batch and leaves ok[b] = 0 for matrices that need the FP64 path.  Returns
+// false when n is beyond the shared-memory solver (then nothing was launched).
+bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double* w, double* V,
+                     int32_t* status, double* area, int* ok_out, cudaStream_t s) {
+  using namespace qex_mp_host;
+  if (n > kMaxN) return false;
+  const long long nn = (long long)n * n;
+  const long long per = (long long)batch * nn;
+  double* As = area;
+  double* Ss = As + per;
+  double* X = Ss + per;
+  double* X2 = X + per;
+  double* T = X2 + per;
+  double* R = T + per;
+  double* E = R + per;
+  double* P = E + per;
+  double* lam = P + (long long)ksplit_of(n) * per;
+  int* ok = ok_out;
+  const int eb = (int)((per + 255) / 256 < 4096 ? (per + 255) / 256 : 4096);
+  sym_kernel<<<eb, 256, 0, s>>>(batch, n, A, S, As, Ss);
+  const size_t sm = smem32(n);
+  cudaFuncSetAttribute(eigh32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  eigh32_kernel<<<batch, kThreads, sm, s>>>(n, As, Ss, X, ok);
+  for (int it = 0; it < 2; ++it) {
+    gemm(s, batch, n, false, Ss, X, P, nullptr, false, 1.0, T);   // T = S X
+    gemm(s, batch, n, true, X, T, P, nullptr, true, -1.0, R);     // R = I - X^T S X
+    gemm(s, batch, n, false, As, X, P, nullptr, false, 1.0, T);   // T = A X
+    gemm(s, batch, n, true, X, T, P, nullptr, false, 1.0, E);     // E <- X^T A X
+    // move X^T A X into T and build the correction in E
+    cudaMemcpyAsync(T, E, sizeof(double) * per, cudaMemcpyDeviceToDevice, s);
+    refine_update_kernel<<<batch, kThreads, 0, s>>>(n, As, R, T, E, lam);
+    gemm(s, batch, n, false, X, E, P, X, false, 1.0, X2);         // X' = X + X E
+    double* t = X;
+    X = X2;
+    X2 = t;
+  }
+  sort_out_kernel<<<batch, 256, sizeof(int) * n, s>>>(n, lam, X, ok, w, V, status);
+  return true;
+}
+
+// Doubles of mixed-precision workspace per matrix (0 when n is beyond it).
+long long qex_mp_area_doubles(int n) {
+  return n <= qex_mp_host::kMaxN ? qex_mp_host::area_doubles(n) : 0;
+}

@@ -14,6 +14,11 @@
 #include "qex_ks1d.h"
 #include "qex_td.h"
 
+// Mixed-precision generalized eigensolver (eigh_mp.cu).
+bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double* w, double* V,
+                     int32_t* status, double* area, int* ok_out, cudaStream_t s);
+long long qex_mp_area_doubles(int n);
+
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
@@ -593,7 +598,9 @@ __global__ void __launch_bounds__(kEighThreads) gen_eigh_kernel(int n, const dou
                                                                 double* __restrict__ w,
                                                                 double* __restrict__ V,
                                                                 int* __restrict__ status,
-                                                                double* __restrict__ ws) {
+                                                                double* __restrict__ ws,
+                                                                const int* __restrict__ done) {
+  if (done && done[blockIdx.x]) return;  // solved by the mixed-precision path
   __shared__ double red[kEighThreads / 32];
   __shared__ double flag[2];
   extern __shared__ double dyn[];  // cs (2 * m/2), pos (m), pq (m) ints
@@ -793,7 +800,9 @@ int qex_td_vxc(int64_t num_points, int32_t nao, const double* ao, const double* 
 
 size_t qex_td_gen_eigh_workspace_size(int32_t batch, int32_t n) {
   if (batch < 0 || n < 1) return 0;
-  return sizeof(double) * 3 * (size_t)n * n * (size_t)batch;
+  // FP64 path (L, C, U), then the mixed-precision area and its ok flags
+  return sizeof(double) * (3 * (size_t)n * n + (size_t)qex_mp_area_doubles(n)) * (size_t)batch +
+         sizeof(int) * (size_t)batch;
 }
 
 int qex_td_gen_eigh(int32_t batch, int32_t n, const double* A, const double* S, double* w,
@@ -805,8 +814,15 @@ int qex_td_gen_eigh(int32_t batch, int32_t n, const double* A, const double* S, 
   if (workspace_bytes < qex_td_gen_eigh_workspace_size(batch, n)) return QEX_BAD_ARG;
   const int m = (n + 1) & ~1;
   const size_t smem = sizeof(double) * m + sizeof(int) * (3 * m + 2);
-  gen_eigh_kernel<<<batch, kEighThreads, smem, static_cast<cudaStream_t>(stream)>>>(
-      n, A, S, w, V, status, static_cast<double*>(workspace));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  double* fp64_ws = static_cast<double*>(workspace);
+  double* area = fp64_ws + 3 * (size_t)n * n * (size_t)batch;
+  int* ok = reinterpret_cast<int*>(area + (size_t)qex_mp_area_doubles(n) * (size_t)batch);
+  // FP32 solve + FP64 refinement; the FP64 Jacobi path takes the matrices it
+  // leaves (S not numerically SPD, or n beyond its shared memory)
+  const bool mp = qex_mp_gen_eigh(batch, n, A, S, w, V, status, area, ok, s);
+  gen_eigh_kernel<<<batch, kEighThreads, smem, s>>>(n, A, S, w, V, status, fp64_ws,
+                                                    mp ? ok : nullptr);
   return cudaGetLastError() == cudaSuccess ? QEX_OK : QEX_CUDA_ERROR;
 }
 
