@@ -156,6 +156,12 @@ class ClockSampler:
 # roofline tally
 # ---------------------------------------------------------------------------
 
+# DRAM bytes per molecule of a 25-iteration batched solve: 419.2 MB read +
+# written by the 950-molecule K=4 bucket launch under ncu (FP32 solve planes
+# and workspace vectors evicted from L2)
+DRAM_BYTES_PER_MOLECULE = 419.2e6 / 950
+
+
 def fp64_flops(mols, iterations_run, stats):
     """FP64 flops executed, tallied per code path of the kernel (an FMA is 2)."""
     total = 0.0
@@ -308,7 +314,11 @@ def run_ours(args, rank, world):
                 "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s},
         "gpu_launches": int(launches),
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64,
-                     "unit": "TFLOP/s", "frac": achieved / peak64, "traffic": None,
+                     "unit": "TFLOP/s", "frac": achieved / peak64,
+                     "traffic": int(DRAM_BYTES_PER_MOLECULE * args.batch),
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu "
+                                       "capture of the K=4 bucket launch (950 molecules, 25 "
+                                       "iterations), per molecule, times the step's molecules",
                      "peak_source": peak_src, "fp32_peak_tflops": peak32,
                      "fp64_flops_per_step": w64, "fp32_mlp_flops_per_step": w32},
         "clocks": sampler.summary(),

@@ -305,7 +305,8 @@ __global__ void __launch_bounds__(kThreads) refine_update_kernel(int n, const do
                                                                  const double* __restrict__ R,
                                                                  const double* __restrict__ T,
                                                                  double* __restrict__ E,
-                                                                 double* __restrict__ lam) {
+                                                                 double* __restrict__ lam,
+                                                                 int* __restrict__ ok, int check) {
   __shared__ double red[kThreads / 32];
   const int b = blockIdx.x;
   const long long nn = (long long)n * n;
@@ -331,6 +332,10 @@ __global__ void __launch_bounds__(kThreads) refine_update_kernel(int n, const do
   rn = block_sum(rn, red);
   // Frobenius norms bound the 2-norms of Ogita and Aishima's threshold
   const double delta = 2.0 * (sqrt(od) + sqrt(an) * sqrt(rn));
+  // second step: the once-refined X must already be accurate to ~1e-7 (it is
+  // unless S is too ill-conditioned for the FP32 solve); otherwise hand the
+  // matrix to the FP64 path
+  if (check && threadIdx.x == 0 && !(rn <= 1e-14 && od <= 1e-14 * an)) ok[b] = 0;
   for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
     const int i = (int)(e / n), j = (int)(e % n);
     double v;
@@ -439,7 +444,7 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     gemm(s, batch, n, true, X, T, P, nullptr, false, 1.0, E);     // E <- X^T A X
     // move X^T A X into T and build the correction in E
     cudaMemcpyAsync(T, E, sizeof(double) * per, cudaMemcpyDeviceToDevice, s);
-    refine_update_kernel<<<batch, kThreads, 0, s>>>(n, As, R, T, E, lam);
+    refine_update_kernel<<<batch, kThreads, 0, s>>>(n, As, R, T, E, lam, ok, it == 1);
     gemm(s, batch, n, false, X, E, P, X, false, 1.0, X2);         // X' = X + X E
     double* t = X;
     X = X2;
