@@ -10,9 +10,10 @@
 //      T = X^T A X, lambda_i = t_ii / (1 - r_ii),
 //      e_ij = (t_ij + lambda_j r_ij) / (lambda_j - lambda_i) when the two
 //      eigenvalues are further apart than delta = 2 (|T - D|_F + |A|_F |R|_F),
-//      else r_ij / 2; X <- X + X E.  Each step squares the error (FP32 ~1e-7 ->
-//      ~1e-13 -> the FP64 floor), so two steps follow the FP32 solve.  The
-//      products are batched split-K FP64 GEMMs over many CTAs.
+//      else r_ij / 2; X <- X + X E.  Each step squares the error (FP32 ~1e-7
+//      times the conditioning of S -> its square -> the FP64 floor); three
+//      steps follow the FP32 solve, the last one checked.  The products are
+//      batched split-K FP64 GEMMs over many CTAs.
 //   3. Ascending order (stable), eigenvectors in columns.
 // Matrices whose FP32 Cholesky fails (S not numerically SPD) keep the FP64
 // path of td.cu, which applies the reference's shift
@@ -30,6 +31,7 @@ constexpr int kMaxSweeps32 = 24;
 constexpr int kT = 32;      // GEMM tile
 constexpr int kKC = 16;     // split-K chunk (one shared-memory stage)
 constexpr int kGThreads = 256;
+constexpr int kRefineSteps = 3;  // FP32 start -> two squarings -> checked final step
 
 __device__ inline float block_sumf(float v, float* red) {
 #pragma unroll
@@ -332,9 +334,9 @@ __global__ void __launch_bounds__(kThreads) refine_update_kernel(int n, const do
   rn = block_sum(rn, red);
   // Frobenius norms bound the 2-norms of Ogita and Aishima's threshold
   const double delta = 2.0 * (sqrt(od) + sqrt(an) * sqrt(rn));
-  // second step: the once-refined X must already be accurate to ~1e-7 (it is
-  // unless S is too ill-conditioned for the FP32 solve); otherwise hand the
-  // matrix to the FP64 path
+  // last step: the X it refines must already be accurate to ~1e-7 (it is
+  // unless S is too ill-conditioned for the FP32 solve), so that this step
+  // reaches the FP64 floor; otherwise hand the matrix to the FP64 path
   if (check && threadIdx.x == 0 && !(rn <= 1e-14 && od <= 1e-14 * an)) ok[b] = 0;
   for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
     const int i = (int)(e / n), j = (int)(e % n);
@@ -437,14 +439,14 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
   const size_t sm = smem32(n);
   cudaFuncSetAttribute(eigh32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   eigh32_kernel<<<batch, kThreads, sm, s>>>(n, As, Ss, X, ok);
-  for (int it = 0; it < 2; ++it) {
+  for (int it = 0; it < kRefineSteps; ++it) {
     gemm(s, batch, n, false, Ss, X, P, nullptr, false, 1.0, T);   // T = S X
     gemm(s, batch, n, true, X, T, P, nullptr, true, -1.0, R);     // R = I - X^T S X
     gemm(s, batch, n, false, As, X, P, nullptr, false, 1.0, T);   // T = A X
     gemm(s, batch, n, true, X, T, P, nullptr, false, 1.0, E);     // E <- X^T A X
     // move X^T A X into T and build the correction in E
     cudaMemcpyAsync(T, E, sizeof(double) * per, cudaMemcpyDeviceToDevice, s);
-    refine_update_kernel<<<batch, kThreads, 0, s>>>(n, As, R, T, E, lam, ok, it == 1);
+    refine_update_kernel<<<batch, kThreads, 0, s>>>(n, As, R, T, E, lam, ok, it == kRefineSteps - 1);
     gemm(s, batch, n, false, X, E, P, X, false, 1.0, X2);         // X' = X + X E
     double* t = X;
     X = X2;
