@@ -217,12 +217,21 @@ class Workspace:
 
 
 class Ks1dEngine:
-    """Owns a workspace and runs batched solves on the current torch stream."""
+    """Owns a workspace and runs batched solves on the current torch stream.
 
-    def __init__(self):
+    With ``autotune`` the launch plan (eigenpair-count runs or one launch,
+    resident or streamed FP32 solve planes) of each new batch shape is chosen
+    by timing the candidates on the batch (``qex_gb300.od.autotune``)."""
+
+    def __init__(self, autotune: bool = False):
         self.lib = N.load()
         self.workspace = Workspace()
         self.last_launches = 0
+        self.tuner = None
+        if autotune:
+            from .autotune import PlanTuner
+
+            self.tuner = PlanTuner()
 
     def _stream(self):
         torch = N.require_cuda()
@@ -271,7 +280,7 @@ class Ks1dEngine:
         return o
 
     def solve(self, batch: PackedBatch, xc, cfg: SolveConfig, records=RECORD_ALL, out=None,
-              initial_density=None, bucketed=True, planes=None):
+              initial_density=None, bucketed=True, planes=None, tune=True):
         """Run the full SCF for every molecule of ``batch``.
 
         With ``bucketed`` the batch is split into runs of equal eigenpair count
@@ -282,6 +291,9 @@ class Ks1dEngine:
         """
         torch = N.require_cuda()
         functional, params = resolve(xc)
+        if self.tuner is not None and tune and planes is None and bucketed:
+            plan = self.tuner.plan(self, batch, xc, cfg, functional.kind)
+            bucketed, planes = plan.bucketed, plan.planes
         vext_given = batch.external_potential is not None
         spec, keep = functional.spec(params, _convention(cfg))
         if out is None:

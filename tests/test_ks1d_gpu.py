@@ -311,3 +311,21 @@ def test_bad_arguments_fail_loudly(qx):
     cfg = od.SolveConfig(num_iterations=2, stencil=4)
     with pytest.raises(RuntimeError):
         od.engine.default_engine().solve(batch, qex.LDAExpCoulomb(), cfg)
+
+
+def test_autotuned_launch_plan_gives_the_same_results(qx):
+    qex, od = qx
+    mols = _random_molecules(41, 24)
+    ms = [od.Molecule1D(num_grids=n, grid_spacing=0.08, locations=r, nuclear_charges=z,
+                        num_electrons=ne) for n, r, z, ne in mols]
+    batch = od.PackedBatch(ms)
+    cfg = od.SolveConfig(num_iterations=6, convention="local", stencil=5)
+    tuned = od.engine.Ks1dEngine(autotune=True)
+    a = tuned.solve(batch, qex.LDAExpCoulomb(), cfg, records=("energy", "final_density"))
+    assert len(tuned.tuner.cache) == 1 and len(next(iter(tuned.tuner.timings.values()))) >= 2
+    b = od.engine.Ks1dEngine().solve(batch, qex.LDAExpCoulomb(), cfg,
+                                     records=("energy", "final_density"))
+    np.testing.assert_allclose(a["energy"].cpu().numpy(), b["energy"].cpu().numpy(), rtol=0,
+                               atol=1e-11)
+    np.testing.assert_allclose(a["final_density"].cpu().numpy(),
+                               b["final_density"].cpu().numpy(), rtol=0, atol=1e-11)
