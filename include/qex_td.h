@@ -22,6 +22,7 @@
  *                            qedft/train/td/jax_diis.py:26-104
  *   qex_td_nn_xc          <- get_exc_and_vrho, qedft/train/td/xc.py:12-47 (local MLP of
  *                            qedft/train/td/trainer_legacy_no_jit.py:56-62, 98-107)
+ *   qex_td_nn_xc_global   <- exc_and_vrho_global, qedft/train/td/trainer_legacy_no_jit.py:46-53
  *   qex_td_coulomb        <- J = einsum('ijkl,kl->ij', eri, dm),
  *                            qedft/train/td/scf_functions_masked.py:152, with the
  *                            ERI in factored form (ij|kl) = sum_P B_Pij B_Pkl
@@ -106,6 +107,18 @@ size_t qex_td_nn_xc_workspace_size(int64_t num_points, int32_t hidden);
 int qex_td_nn_xc(int64_t num_points, int32_t hidden, const double* rho, const double* weights,
                  const float* params, double scale, double* exc, double* vrho, double* sums,
                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* Global neural XC: replaces exc_and_vrho_global (qedft/train/td/
+ * trainer_legacy_no_jit.py:46-53) as consumed by the NN-AmplitudeEncoding
+ * xctype of nr_rks (qedft/train/td/numint_legacy.py:311-333): the density vector
+ * is one input of the MLP [H, H, 1] (W1: (num_points, H) row-major, then b1,
+ * W2 (H x H), b2, w3, b3; FP32 device), exc = sum of its output (scalar),
+ * vrho = d exc / d rho (num_points, FP64 device).  sums = (sum w rho, exc).
+ * hidden <= 1024. */
+size_t qex_td_nn_xc_global_workspace_size(int64_t num_points, int32_t hidden);
+int qex_td_nn_xc_global(int64_t num_points, int32_t hidden, const double* rho,
+                        const double* weights, const float* params, double scale, double* vrho,
+                        double* sums, void* workspace, size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

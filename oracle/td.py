@@ -145,13 +145,45 @@ def nn_xc_local(flat, rho, scale=1e-2, dtype=np.float64):
     return exc, vrho
 
 
-def nr_rks_nn(ao, weights, dm, flat, scale=1e-2, dtype=np.float64):
-    """``nr_rks_lda`` with the neural functional in place of the LDA exchange."""
+def nn_xc_global(flat, rho, hidden, scale=1e-2, dtype=np.float64):
+    """(exc, vrho) of ``exc_and_vrho_global`` (``qedft/train/td/trainer_legacy_no_jit.py:46-53``):
+    the density vector (G) is one input of the MLP [H, H, 1]; exc is the scalar sum of
+    its output, vrho = d exc / d rho.  ``flat`` = (W1 (G, H), b1, W2, b2, w3, b3)."""
+    flat = np.asarray(flat, dtype)
+    x = np.asarray(rho, dtype)
+    G, H = x.size, int(hidden)
+    W1 = flat[:G * H].reshape(G, H)
+    o = G * H
+    b1 = flat[o:o + H]
+    W2 = flat[o + H:o + H + H * H].reshape(H, H)
+    o += H + H * H
+    b2, w3, b3 = flat[o:o + H], flat[o + H:o + 2 * H], flat[o + 2 * H]
+    h1, d1 = _gelu(x @ W1 + b1)
+    h2, d2 = _gelu(h1 @ W2 + b2)
+    z3 = h2 @ w3 + b3
+    sg = 1 / (1 + np.exp(-z3))
+    s = dtype(scale)
+    exc = -s * z3 * sg
+    dz3 = -s * sg * (1 + z3 * (1 - sg))
+    dz2 = dz3 * w3 * d2
+    dz1 = (W2 @ dz2) * d1
+    return exc, W1 @ dz1
+
+
+def nr_rks_nn(ao, weights, dm, flat, scale=1e-2, dtype=np.float64, hidden=None):
+    """``nr_rks_lda`` with the neural functional in place of the LDA exchange: the
+    local network (exc per point), or with ``hidden`` the global network, whose
+    scalar output is added as the XC energy (``numint_legacy.py:311-333``)."""
     rho = eval_rho(ao, dm)
-    exc, vrho = nn_xc_local(flat, rho, scale, dtype)
-    exc, vrho = np.asarray(exc, np.float64), np.asarray(vrho, np.float64)
     den = rho * weights
     nelec = den.sum()
+    if hidden is not None:
+        exc, vrho = nn_xc_global(flat, rho, hidden, scale, dtype)
+        aow = ao * (0.5 * weights * np.asarray(vrho, np.float64))[:, None]
+        vmat = ao.T @ aow
+        return nelec, float(exc), vmat + vmat.T
+    exc, vrho = nn_xc_local(flat, rho, scale, dtype)
+    exc, vrho = np.asarray(exc, np.float64), np.asarray(vrho, np.float64)
     excsum = np.dot(den, exc)
     aow = ao * (0.5 * weights * vrho)[:, None]
     vmat = ao.T @ aow

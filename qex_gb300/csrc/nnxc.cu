@@ -313,3 +313,172 @@ int qex_td_nn_xc(int64_t num_points, int32_t hidden, const double* rho, const do
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Global network (qedft/train/td/trainer_legacy_no_jit.py:46-53 with the MLP of
+// :98-107, consumed as the "NN-AmplitudeEncoding" xctype of
+// qedft/train/td/numint_legacy.py:311-333): the whole density vector is one
+// input, exc = sum network(rho) is a scalar and vrho = d exc / d rho (G).
+// Layer 1 is a G x H GEMV (W1 row-major (G, H)), so the first and last kernels
+// stream W1 from memory coalesced; the H-wide middle runs in one CTA.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kGChunk = 128;   // grid points per z1 partial
+constexpr int kGlobThreads = 256;
+constexpr int kMaxHidden = 1024;
+
+struct GlobView {
+  const float* W1;  // G x H
+  const float* b1;
+  const float* W2;  // H x H
+  const float* b2;
+  const float* w3;
+  const float* b3;
+};
+
+__device__ __forceinline__ GlobView glob_view(const float* p, long long G, int H) {
+  GlobView v;
+  v.W1 = p;
+  v.b1 = p + (size_t)G * H;
+  v.W2 = v.b1 + H;
+  v.b2 = v.W2 + (size_t)H * H;
+  v.w3 = v.b2 + H;
+  v.b3 = v.w3 + H;
+  return v;
+}
+
+// part[c][h] = sum over chunk c of rho_g W1[g][h]
+__global__ void __launch_bounds__(kGlobThreads) glob_z1_kernel(long long G, int H,
+                                                               const double* rho,
+                                                               const float* params, float* part) {
+  const GlobView net = glob_view(params, G, H);
+  const int h = blockIdx.y * kGlobThreads + threadIdx.x;
+  const long long g0 = (long long)blockIdx.x * kGChunk;
+  if (h >= H) return;
+  float acc = 0.0f;
+  const long long g1 = min(G, g0 + kGChunk);
+  for (long long g = g0; g < g1; ++g) acc = fmaf((float)rho[g], net.W1[(size_t)g * H + h], acc);
+  part[(size_t)blockIdx.x * H + h] = acc;
+}
+
+// One CTA: z1, h1 = gelu, z2, h2, z3, out and the backward to dz1 (global),
+// exc sum into sums[1].
+__global__ void __launch_bounds__(kMaxHidden) glob_mid_kernel(long long G, int H, int nchunks,
+                                                              const float* params,
+                                                              const float* part, float scale,
+                                                              float* dz1, double* sums) {
+  const GlobView net = glob_view(params, G, H);
+  __shared__ float h1[kMaxHidden], d1[kMaxHidden], dz2[kMaxHidden];
+  __shared__ float red[32];
+  const int h = threadIdx.x;
+  if (h < H) {
+    float z = net.b1[h];
+    for (int c = 0; c < nchunks; ++c) z += part[(size_t)c * H + h];
+    float d;
+    h1[h] = gelu_f(z, d);
+    d1[h] = d;
+  }
+  __syncthreads();
+  float d2 = 0.0f, contrib = 0.0f;
+  if (h < H) {
+    float z = net.b2[h];
+    for (int k = 0; k < H; ++k) z = fmaf(h1[k], net.W2[(size_t)k * H + h], z);
+    const float a = gelu_f(z, d2);
+    contrib = a * net.w3[h];
+  }
+  // z3 = sum_h h2 w3 + b3 (fixed-order block reduction)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
+  if ((h & 31) == 0) red[h >> 5] = contrib;
+  __syncthreads();
+  float z3 = net.b3[0];
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) z3 += red[i];
+  const float sg = 1.0f / (1.0f + expf(-z3));
+  const float dz3 = -scale * sg * fmaf(z3, 1.0f - sg, 1.0f);
+  if (h < H) dz2[h] = dz3 * net.w3[h] * d2;
+  __syncthreads();
+  if (h < H) {
+    float s = 0.0f;
+    for (int j = 0; j < H; ++j) s = fmaf(net.W2[(size_t)h * H + j], dz2[j], s);
+    dz1[h] = s * d1[h];
+  }
+  if (h == 0) sums[1] = (double)(-scale * z3 * sg);
+}
+
+// vrho[g] = sum_h W1[g][h] dz1[h] (one warp per grid point); sums[0] partials.
+__global__ void __launch_bounds__(kGlobThreads) glob_vrho_kernel(long long G, int H,
+                                                                 const double* rho,
+                                                                 const double* w,
+                                                                 const float* params,
+                                                                 const float* dz1, double* vrho,
+                                                                 double* ne_part) {
+  const GlobView net = glob_view(params, G, H);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int wpb = kGlobThreads / 32;
+  double ne = 0.0;
+  for (long long g = (long long)blockIdx.x * wpb + wid; g < G; g += (long long)gridDim.x * wpb) {
+    float s = 0.0f;
+    for (int h = lane; h < H; h += 32) s = fmaf(net.W1[(size_t)g * H + h], dz1[h], s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      vrho[g] = (double)s;
+      if (w) ne += w[g] * rho[g];
+    }
+  }
+  __shared__ double red[kGlobThreads / 32];
+  if (lane == 0) red[wid] = ne;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0;
+    for (int i = 0; i < wpb; ++i) a += red[i];
+    ne_part[blockIdx.x] = a;
+  }
+}
+
+__global__ void glob_sum_kernel(int nblocks, const double* part, double* sums) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double a = 0.0;
+    for (int i = 0; i < nblocks; ++i) a += part[i];
+    sums[0] = a;
+  }
+}
+
+constexpr int kGlobVrhoBlocks = 1024;
+
+}  // namespace
+
+extern "C" {
+
+size_t qex_td_nn_xc_global_workspace_size(int64_t num_points, int32_t hidden) {
+  if (num_points < 1 || hidden < 1 || hidden > kMaxHidden) return 0;
+  const size_t chunks = (size_t)((num_points + kGChunk - 1) / kGChunk);
+  return sizeof(float) * (chunks * (size_t)hidden + (size_t)hidden) +
+         sizeof(double) * kGlobVrhoBlocks + 256;
+}
+
+int qex_td_nn_xc_global(int64_t num_points, int32_t hidden, const double* rho,
+                        const double* weights, const float* params, double scale, double* vrho,
+                        double* sums, void* workspace, size_t workspace_bytes, void* stream) {
+  if (num_points < 1 || hidden < 1 || hidden > kMaxHidden) return QEX_BAD_ARG;
+  if (!rho || !weights || !params || !vrho || !sums || !workspace) return QEX_BAD_ARG;
+  if (workspace_bytes < qex_td_nn_xc_global_workspace_size(num_points, hidden)) return QEX_BAD_ARG;
+  const long long G = num_points;
+  const int chunks = (int)((G + kGChunk - 1) / kGChunk);
+  if (chunks > 0x7fffffff) return QEX_BAD_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  double* ne_part = static_cast<double*>(workspace);
+  float* part = reinterpret_cast<float*>(ne_part + kGlobVrhoBlocks);
+  float* dz1 = part + (size_t)chunks * hidden;
+  glob_z1_kernel<<<dim3((unsigned)chunks, (hidden + kGlobThreads - 1) / kGlobThreads), kGlobThreads,
+                   0, s>>>(G, hidden, rho, params, part);
+  const int mt = ((hidden + 31) / 32) * 32;
+  glob_mid_kernel<<<1, mt, 0, s>>>(G, hidden, chunks, params, part, (float)scale, dz1, sums);
+  const int vb = (int)((G + 7) / 8 < kGlobVrhoBlocks ? (G + 7) / 8 : kGlobVrhoBlocks);
+  glob_vrho_kernel<<<vb, kGlobThreads, 0, s>>>(G, hidden, rho, weights, params, dz1, vrho, ne_part);
+  glob_sum_kernel<<<1, 32, 0, s>>>(vb, ne_part, sums);
+  return cudaGetLastError() == cudaSuccess ? QEX_OK : QEX_CUDA_ERROR;
+}
+
+}  // extern "C"

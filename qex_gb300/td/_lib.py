@@ -26,6 +26,9 @@ SIGNATURES = {
     "qex_td_diis_extrapolate": (ctypes.c_int, [_i32, _i32, _i32, _v, _v, _v, _v, _v]),
     "qex_td_coulomb": (ctypes.c_int, [_i32, _i32, _v, _v, _v, _v, _sz, _v]),
     "qex_td_nn_xc_workspace_size": (_sz, [_i64, _i32]),
+    "qex_td_nn_xc_global_workspace_size": (_sz, [_i64, _i32]),
+    "qex_td_nn_xc_global": (ctypes.c_int, [_i64, _i32, _v, _v, _v, ctypes.c_double, _v, _v, _v,
+                                           _sz, _v]),
     "qex_td_nn_xc": (ctypes.c_int, [_i64, _i32, _v, _v, _v, ctypes.c_double, _v, _v, _v, _v,
                                     _sz, _v]),
 }

@@ -67,33 +67,43 @@ def eval_xc_lda(rho, weights):
 
 
 class NeuralXC:
-    """Local neural XC functional of the 3D path (qedft/train/td/trainer_legacy_no_jit.py:98-107:
-    MLP features [H, H, 1], gelu hidden layers, output -scale * swish; evaluated per grid
-    point as in :56-62).  ``params`` is the flax parameter tree
-    ``{"Dense_0": {"kernel": (1, H), "bias": (H,)}, "Dense_1": ..., "Dense_2": ...}`` or
-    the flat FP32 vector (w1, b1, W2, b2, w3, b3)."""
+    """Neural XC functional of the 3D path (qedft/train/td/trainer_legacy_no_jit.py:98-107:
+    MLP features [H, H, 1], gelu hidden layers, output -scale * swish).  Local form
+    (Dense_0 kernel (1, H)): evaluated per grid point (:56-62), exc per point.  Global
+    form (Dense_0 kernel (G, H)): the density vector is one input (:46-53), exc is the
+    scalar sum of the output.  ``params`` is the flax parameter tree
+    ``{"Dense_0": {"kernel": (in, H), "bias": (H,)}, "Dense_1": ..., "Dense_2": ...}`` or,
+    for the local form, the flat FP32 vector (w1, b1, W2, b2, w3, b3)."""
 
     def __init__(self, params, scale=1e-2):
         import numpy as np
 
         self.scale = float(scale)
+        self.inputs = 1
         if isinstance(params, dict):
             d0, d1, d2 = params["Dense_0"], params["Dense_1"], params["Dense_2"]
             flat = np.concatenate([np.ravel(d0["kernel"]), np.ravel(d0["bias"]),
                                    np.ravel(d1["kernel"]), np.ravel(d1["bias"]),
                                    np.ravel(d2["kernel"]), np.ravel(d2["bias"])])
             self.hidden = int(np.shape(d0["bias"])[0])
+            self.inputs = int(np.shape(d0["kernel"])[0])
         else:
             flat = np.ravel(np.asarray(params))
             self.hidden = int(round((-3 + (9 + 4 * (flat.size - 1)) ** 0.5) / 2))
-        if flat.size != self.hidden * self.hidden + 4 * self.hidden + 1:
+        H = self.hidden
+        if flat.size != H * H + (2 + self.inputs + 1) * H + 1:
             raise ValueError(f"parameter vector of {flat.size} floats does not fit [H, H, 1]")
         self.flat = np.ascontiguousarray(flat, dtype=np.float32)
         self._dev = None
 
+    @property
+    def is_global(self):
+        return self.inputs > 1
+
     @staticmethod
-    def init(hidden=512, seed=0):
-        """flax-style initialisation: lecun-normal kernels, zero biases."""
+    def init(hidden=512, seed=0, inputs=1):
+        """flax-style initialisation: lecun-normal kernels, zero biases; ``inputs`` =
+        1 for the local form, the number of grid points for the global form."""
         import numpy as np
 
         rng = np.random.default_rng(seed)
@@ -102,7 +112,7 @@ class NeuralXC:
             return {"kernel": rng.normal(0.0, 1.0 / np.sqrt(fi), (fi, fo)).astype(np.float32),
                     "bias": np.zeros(fo, np.float32)}
 
-        return {"Dense_0": dense(1, hidden), "Dense_1": dense(hidden, hidden),
+        return {"Dense_0": dense(inputs, hidden), "Dense_1": dense(hidden, hidden),
                 "Dense_2": dense(hidden, 1)}
 
     def device_params(self):
@@ -120,10 +130,25 @@ def eval_xc_nn(rho, functional: NeuralXC, weights=None):
     L = _lib.lib()
     rho = _dev(rho, torch.float64)
     G = rho.shape[0]
-    exc = torch.empty_like(rho)
-    vrho = torch.empty_like(rho)
     H = functional.hidden
     w = None if weights is None else _dev(weights, torch.float64)
+    if functional.is_global:
+        # exc is one number (the network's summed output); nr_rks adds it as excsum
+        if functional.inputs != G:
+            raise ValueError(f"global network over {functional.inputs} points, grid has {G}")
+        if w is None:
+            raise ValueError("the global network needs the grid weights")
+        vrho = torch.empty_like(rho)
+        sums = torch.empty(2, dtype=torch.float64, device="cuda")
+        ws = torch.empty(max(L.qex_td_nn_xc_global_workspace_size(G, H), 256), dtype=torch.uint8,
+                         device="cuda")
+        N.check(L.qex_td_nn_xc_global(G, H, _lib.p(rho), _lib.p(w),
+                                      _lib.p(functional.device_params()), functional.scale,
+                                      _lib.p(vrho), _lib.p(sums), _lib.p(ws), ws.numel(),
+                                      _lib.stream()), "qex_td_nn_xc_global")
+        return None, vrho, sums[0], sums[1]
+    exc = torch.empty_like(rho)
+    vrho = torch.empty_like(rho)
     sums = None if w is None else torch.empty(2, dtype=torch.float64, device="cuda")
     ws = torch.empty(max(L.qex_td_nn_xc_workspace_size(G, H), 256), dtype=torch.uint8,
                      device="cuda")

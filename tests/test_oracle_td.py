@@ -104,3 +104,17 @@ def test_nn_xc_oracle_is_its_own_derivative():
     e32, v32 = o.nn_xc_local(flat, rho, scale=1e-2, dtype=np.float32)
     np.testing.assert_allclose(e32, exc, rtol=0, atol=1e-6 * np.abs(exc).max())
     np.testing.assert_allclose(v32, vrho, rtol=0, atol=1e-5 * np.abs(vrho).max())
+
+
+def test_nn_xc_global_oracle_is_its_own_derivative():
+    # exc_and_vrho_global (qedft/train/td/trainer_legacy_no_jit.py:46-53): the
+    # density vector is one input; vrho = d exc / d rho by central differences
+    rng = np.random.default_rng(13)
+    G, H = 40, 12
+    flat = rng.normal(0.0, 0.3, G * H + H * H + 3 * H + 1)
+    rho = rng.uniform(0.0, 2.0, G)
+    exc, vrho = o.nn_xc_global(flat, rho, H)
+    h = 1e-6
+    fd = np.array([(o.nn_xc_global(flat, rho + h * e, H)[0] - o.nn_xc_global(flat, rho - h * e, H)[0])
+                   / (2 * h) for e in np.eye(G)])
+    np.testing.assert_allclose(fd, vrho, rtol=0, atol=1e-9 * np.abs(vrho).max())

@@ -192,3 +192,27 @@ def test_scf_with_nn_xc_matches_oracle(td, mols):
     np.testing.assert_allclose(e, e_ref, atol=1e-5, rtol=0)
     assert abs(e[-1] - e_ref[-1]) < 1e-7
     assert (_host(res.status) == 0).all()
+
+
+def test_nn_xc_global_matches_oracle(td, mols):
+    torch, eigh, numint, scf, W = td
+    m = mols[0]
+    G = m.weights.size
+    rng = np.random.default_rng(14)
+    params = numint.NeuralXC.init(hidden=64, seed=6, inputs=G)
+    params["Dense_0"]["bias"] = rng.normal(0, 0.3, 64).astype(np.float32)
+    params["Dense_2"]["bias"] = np.array([-0.1], np.float32)
+    f = numint.NeuralXC(params, scale=1e-2)
+    assert f.is_global
+    rho = rng.uniform(0.0, 1.0, G)
+    exc, vrho, nelec, excsum = numint.eval_xc_nn(rho, f, m.weights)
+    assert exc is None
+    e_ref, v_ref = o.nn_xc_global(f.flat, rho, 64, 1e-2, np.float64)
+    # FP32 network, G-long first-layer sums
+    assert abs(float(excsum) - e_ref) < 1e-5 * max(abs(e_ref), 1e-3)
+    np.testing.assert_allclose(_host(vrho), v_ref, rtol=0, atol=1e-4 * np.abs(v_ref).max())
+    assert abs(float(nelec) - np.dot(m.weights, rho)) < 1e-10 * np.dot(m.weights, rho)
+    # the SCF with the global functional follows the oracle's
+    res = scf.run_scf(m, max_cycle=10, xc=f)
+    e_scf, _, _ = o.scf(m, max_cycle=10, nn=(f.flat, 1e-2, np.float64, 64))
+    np.testing.assert_allclose(_host(res.energies), e_scf, atol=1e-5, rtol=0)
