@@ -60,6 +60,12 @@ int qex_td_lda(int64_t num_points, const double* rho, const double* weights, dou
 
 /* vmat = ao^T diag(0.5 w v) ao, then vmat + vmat^T.  workspace:
  * qex_td_vxc_workspace_size bytes. */
+/* Slater exchange + VWN correlation (paramagnetic fit 5): the reference's
+ * default "LDA,VWN" (qedft/train/td/rks.py:172).  Same arguments as qex_td_lda. */
+int qex_td_lda_vwn(int64_t num_points, const double* rho, const double* weights, double* exc,
+                   double* vrho, double* sums, void* workspace, size_t workspace_bytes,
+                   void* stream);
+
 size_t qex_td_vxc_workspace_size(int64_t num_points, int32_t nao);
 int qex_td_vxc(int64_t num_points, int32_t nao, const double* ao, const double* weights,
                const double* vrho, double* vmat, void* workspace, size_t workspace_bytes,

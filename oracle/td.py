@@ -91,11 +91,39 @@ def lda_x(rho):
     return exc, 4.0 / 3.0 * exc
 
 
-def nr_rks_lda(ao, weights, dm):
+def vwn5_c(rho):
+    """VWN correlation, paramagnetic fit 5 (Vosko, Wilk, Nusair, Can. J. Phys. 58,
+    1200 (1980); libxc's "VWN" in the reference's "LDA,VWN", ``rks.py:172``):
+    (eps_c, v_c = d(rho eps_c)/d rho) in Hartree."""
+    rho = np.asarray(rho, dtype=np.float64)
+    A, b, c, x0 = 0.0310907, 3.72744, 12.9352, -0.10498
+    ok = rho > 1e-30
+    r = np.where(ok, rho, 1.0)
+    rs = np.cbrt(3.0 / (4.0 * np.pi * r))
+    x = np.sqrt(rs)
+    X = x * x + b * x + c
+    X0 = x0 * x0 + b * x0 + c
+    Q = np.sqrt(4.0 * c - b * b)
+    t = 2.0 * x + b
+    at = np.arctan(Q / t)
+    f = b * x0 / X0
+    eps = A * (np.log(x * x / X) + 2.0 * b / Q * at
+               - f * (np.log((x - x0) ** 2 / X) + 2.0 * (b + 2.0 * x0) / Q * at))
+    den = t * t + Q * Q
+    de_dx = A * (2.0 / x - t / X - 4.0 * b / den
+                 - f * (2.0 / (x - x0) - t / X - 4.0 * (b + 2.0 * x0) / den))
+    v = eps - x / 6.0 * de_dx
+    return np.where(ok, eps, 0.0), np.where(ok, v, 0.0)
+
+
+def nr_rks_lda(ao, weights, dm, vwn=False):
     """(nelec, excsum, vmat) of ``qedft/train/td/numint_legacy.py:122-164,337``:
     aow = 0.5 * w * vrho * ao; vmat = ao^T aow; vmat += vmat^T."""
     rho = eval_rho(ao, dm)
     exc, vrho = lda_x(rho)
+    if vwn:
+        ec, vc = vwn5_c(rho)
+        exc, vrho = exc + ec, vrho + vc
     den = rho * weights
     nelec = den.sum()
     excsum = np.dot(den, exc)
@@ -292,13 +320,14 @@ def energy_tot(dm, h1e, J, exc, e_nuc):
     return float(np.einsum("ij,ji->", dm, h1e) + 0.5 * np.einsum("ij,ij->", dm, J) + exc + e_nuc)
 
 
-def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, nn=None):
+def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, nn=None, vwn=False):
     """Fixed-cycle SCF of ``qedft/train/td/scf_functions_masked.py:907-967`` with
     the low-rank Coulomb model and the LDA exchange, or with ``nn = (flat,
     scale, dtype)`` the neural functional."""
     ao, w = mol.ao, mol.weights
     if nn is None:
-        rks = nr_rks_lda
+        def rks(ao, w, dm):
+            return nr_rks_lda(ao, w, dm, vwn=vwn)
     else:
         def rks(ao, w, dm):
             return nr_rks_nn(ao, w, dm, *nn)

@@ -176,8 +176,36 @@ __global__ void sum_parts_kernel(long long G, int nparts, const double* __restri
 }
 
 // ---------------------------------------------------------------------------
-// LDA (Slater) exchange on the grid
+// LDA on the grid: Slater exchange, optionally with the VWN correlation of the
+// reference's default "LDA,VWN" (qedft/train/td/rks.py:172; libxc's VWN is the
+// paramagnetic fit 5 of Vosko, Wilk and Nusair, Can. J. Phys. 58, 1200 (1980)).
 // ---------------------------------------------------------------------------
+// eps_c and v_c = d(rho eps_c)/d rho at density r, in Hartree.
+__device__ inline void vwn5_c(double r, double& eps, double& v) {
+  if (!(r > 1e-30)) {
+    eps = 0.0;
+    v = 0.0;
+    return;
+  }
+  const double A = 0.0310907, b = 3.72744, c = 12.9352, x0 = -0.10498;
+  const double pi = 3.141592653589793;
+  const double rs = cbrt(3.0 / (4.0 * pi * r));
+  const double x = sqrt(rs);
+  const double X = x * x + b * x + c;
+  const double X0 = x0 * x0 + b * x0 + c;
+  const double Q = sqrt(4.0 * c - b * b);
+  const double t = 2.0 * x + b;
+  const double at = atan(Q / t);
+  const double f = b * x0 / X0;
+  eps = A * (log(x * x / X) + 2.0 * b / Q * at -
+             f * (log((x - x0) * (x - x0) / X) + 2.0 * (b + 2.0 * x0) / Q * at));
+  const double den = t * t + Q * Q;
+  const double de_dx = A * (2.0 / x - t / X - 4.0 * b / den -
+                            f * (2.0 / (x - x0) - t / X - 4.0 * (b + 2.0 * x0) / den));
+  v = eps - x / 6.0 * de_dx;
+}
+
+template <bool kVwn>
 __global__ void __launch_bounds__(kThreads) lda_kernel(long long G, const double* __restrict__ rho,
                                                        const double* __restrict__ w,
                                                        double* __restrict__ exc,
@@ -189,9 +217,16 @@ __global__ void __launch_bounds__(kThreads) lda_kernel(long long G, const double
   for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < G;
        g += (long long)gridDim.x * blockDim.x) {
     const double r = rho[g];
-    const double e = -cx * cbrt(fmax(r, 0.0));
+    double e = -cx * cbrt(fmax(r, 0.0));
+    double v = (4.0 / 3.0) * e;
+    if (kVwn) {
+      double ec, vc;
+      vwn5_c(r, ec, vc);
+      e += ec;
+      v += vc;
+    }
     if (exc) exc[g] = e;
-    if (vrho) vrho[g] = (4.0 / 3.0) * e;
+    if (vrho) vrho[g] = v;
     const double den = r * w[g];
     s0 += den;
     s1 = fma(den, e, s1);
@@ -756,7 +791,8 @@ size_t qex_td_lda_workspace_size(int64_t num_points) {
   return sizeof(double) * 2 * 1024;
 }
 
-int qex_td_lda(int64_t num_points, const double* rho, const double* weights, double* exc,
+namespace {
+int lda_launch(bool vwn, int64_t num_points, const double* rho, const double* weights, double* exc,
                double* vrho, double* sums, void* workspace, size_t workspace_bytes, void* stream) {
   if (num_points < 0) return QEX_BAD_ARG;
   if (!rho || !weights || !sums || !workspace) return QEX_BAD_ARG;
@@ -765,9 +801,27 @@ int qex_td_lda(int64_t num_points, const double* rho, const double* weights, dou
   int blocks = grid_for(num_points, kThreads);
   if (blocks > 1024) blocks = 1024;
   double* part = static_cast<double*>(workspace);
-  lda_kernel<<<blocks, kThreads, 0, s>>>(num_points, rho, weights, exc, vrho, part);
+  if (vwn) {
+    lda_kernel<true><<<blocks, kThreads, 0, s>>>(num_points, rho, weights, exc, vrho, part);
+  } else {
+    lda_kernel<false><<<blocks, kThreads, 0, s>>>(num_points, rho, weights, exc, vrho, part);
+  }
   lda_sum_kernel<<<1, 32, 0, s>>>(blocks, part, sums);
   return cudaGetLastError() == cudaSuccess ? QEX_OK : QEX_CUDA_ERROR;
+}
+}  // namespace
+
+int qex_td_lda(int64_t num_points, const double* rho, const double* weights, double* exc,
+               double* vrho, double* sums, void* workspace, size_t workspace_bytes, void* stream) {
+  return lda_launch(false, num_points, rho, weights, exc, vrho, sums, workspace, workspace_bytes,
+                    stream);
+}
+
+int qex_td_lda_vwn(int64_t num_points, const double* rho, const double* weights, double* exc,
+                   double* vrho, double* sums, void* workspace, size_t workspace_bytes,
+                   void* stream) {
+  return lda_launch(true, num_points, rho, weights, exc, vrho, sums, workspace, workspace_bytes,
+                    stream);
 }
 
 size_t qex_td_vxc_workspace_size(int64_t num_points, int32_t nao) {

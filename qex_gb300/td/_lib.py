@@ -17,6 +17,7 @@ SIGNATURES = {
     "qex_td_rho": (ctypes.c_int, [_i64, _i32, _v, _v, _v, _v, _sz, _v]),
     "qex_td_lda_workspace_size": (_sz, [_i64]),
     "qex_td_lda": (ctypes.c_int, [_i64, _v, _v, _v, _v, _v, _v, _sz, _v]),
+    "qex_td_lda_vwn": (ctypes.c_int, [_i64, _v, _v, _v, _v, _v, _v, _sz, _v]),
     "qex_td_vxc_workspace_size": (_sz, [_i64, _i32]),
     "qex_td_vxc": (ctypes.c_int, [_i64, _i32, _v, _v, _v, _v, _v, _sz, _v]),
     "qex_td_gen_eigh_workspace_size": (_sz, [_i32, _i32]),

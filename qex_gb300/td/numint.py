@@ -50,8 +50,9 @@ def eval_rho(ao, dm):
     return rho
 
 
-def eval_xc_lda(rho, weights):
-    """(exc, vrho, nelec, excsum) of the Slater exchange on the grid."""
+def eval_xc_lda(rho, weights, vwn=False):
+    """(exc, vrho, nelec, excsum) of the Slater exchange on the grid; with ``vwn``
+    plus the VWN correlation (the reference's default "LDA,VWN")."""
     torch = N.require_cuda()
     L = _lib.lib()
     rho = _dev(rho, torch.float64)
@@ -61,8 +62,9 @@ def eval_xc_lda(rho, weights):
     vrho = torch.empty_like(rho)
     sums = torch.empty(2, dtype=torch.float64, device="cuda")
     ws = torch.empty(L.qex_td_lda_workspace_size(G), dtype=torch.uint8, device="cuda")
-    N.check(L.qex_td_lda(G, _lib.p(rho), _lib.p(weights), _lib.p(exc), _lib.p(vrho), _lib.p(sums),
-                         _lib.p(ws), ws.numel(), _lib.stream()), "qex_td_lda")
+    fn = L.qex_td_lda_vwn if vwn else L.qex_td_lda
+    N.check(fn(G, _lib.p(rho), _lib.p(weights), _lib.p(exc), _lib.p(vrho), _lib.p(sums),
+               _lib.p(ws), ws.numel(), _lib.stream()), "qex_td_lda")
     return exc, vrho, sums[0], sums[1]
 
 
@@ -181,8 +183,9 @@ def nr_rks(ao, weights, dm, xc_code="LDA"):
     if isinstance(xc_code, NeuralXC):
         exc, vrho, nelec, excsum = eval_xc_nn(rho, xc_code, weights)
         return nelec, excsum, vxc_matrix(ao, weights, vrho)
-    if xc_code.upper() not in ("LDA", "LDA_X", "SLATER"):
+    code = xc_code.upper().replace(" ", "")
+    if code not in ("LDA", "LDA_X", "SLATER", "LDA,VWN", "SLATER,VWN"):
         raise NotImplementedError(f"xc_code {xc_code!r}: the GPU path implements the LDA exchange "
-                                  "and the neural functional")
-    exc, vrho, nelec, excsum = eval_xc_lda(rho, weights)
+                                  "(with or without VWN correlation) and the neural functional")
+    exc, vrho, nelec, excsum = eval_xc_lda(rho, weights, vwn=code.endswith("VWN"))
     return nelec, excsum, vxc_matrix(ao, weights, vrho)

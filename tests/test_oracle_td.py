@@ -118,3 +118,20 @@ def test_nn_xc_global_oracle_is_its_own_derivative():
     fd = np.array([(o.nn_xc_global(flat, rho + h * e, H)[0] - o.nn_xc_global(flat, rho - h * e, H)[0])
                    / (2 * h) for e in np.eye(G)])
     np.testing.assert_allclose(fd, vrho, rtol=0, atol=1e-9 * np.abs(vrho).max())
+
+
+def test_vwn5_correlation_known_values_and_derivative():
+    # VWN paramagnetic fit 5 (the correlation of the reference's "LDA,VWN",
+    # qedft/train/td/rks.py:172): eps_c(rs = 1, 2, 5) of the published fit, and
+    # v_c = d(rho eps_c)/d rho
+    rs = np.array([1.0, 2.0, 5.0])
+    eps, _ = o.vwn5_c(3.0 / (4.0 * np.pi * rs ** 3))
+    np.testing.assert_allclose(eps, [-0.0600, -0.0448, -0.0281], atol=2e-4)
+    rho = np.linspace(0.01, 2.0, 30)
+    h = 1e-7
+    ep, _ = o.vwn5_c(rho + h)
+    em, _ = o.vwn5_c(rho - h)
+    _, v = o.vwn5_c(rho)
+    np.testing.assert_allclose(((rho + h) * ep - (rho - h) * em) / (2 * h), v, rtol=0, atol=1e-8)
+    e0, v0 = o.vwn5_c(np.zeros(3))
+    assert (e0 == 0).all() and (v0 == 0).all()

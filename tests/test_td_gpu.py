@@ -216,3 +216,19 @@ def test_nn_xc_global_matches_oracle(td, mols):
     res = scf.run_scf(m, max_cycle=10, xc=f)
     e_scf, _, _ = o.scf(m, max_cycle=10, nn=(f.flat, 1e-2, np.float64, 64))
     np.testing.assert_allclose(_host(res.energies), e_scf, atol=1e-5, rtol=0)
+
+
+def test_lda_vwn_matches_oracle(td, mols):
+    torch, eigh, numint, scf, W = td
+    m = mols[1]
+    rng = np.random.default_rng(21)
+    c = np.linalg.qr(rng.normal(size=(m.nao, m.nao)))[0]
+    dm = o.make_rdm1(c, np.where(np.arange(m.nao) < m.nelectron // 2, 2.0, 0.0))
+    ne, exc, vmat = numint.nr_rks(m.ao, m.weights, dm, "LDA,VWN")
+    ne_r, exc_r, vmat_r = o.nr_rks_lda(m.ao, m.weights, dm, vwn=True)
+    assert abs(float(exc) - exc_r) < 1e-10 * max(1, abs(exc_r))
+    np.testing.assert_allclose(_host(vmat), vmat_r, rtol=1e-10, atol=1e-12 * np.abs(vmat_r).max())
+    res = scf.run_scf(m, max_cycle=12, xc="LDA,VWN")
+    e_ref, _, _ = o.scf(m, max_cycle=12, vwn=True)
+    np.testing.assert_allclose(_host(res.energies), e_ref, atol=1e-5, rtol=0)
+    assert abs(_host(res.energies)[-1] - e_ref[-1]) < 1e-8
