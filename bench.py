@@ -192,6 +192,19 @@ def fp32_flops_mlp(mols, iterations_run):
 # arms
 # ---------------------------------------------------------------------------
 
+def combine_ranks(step_s, e2e_s, n_conv, n_mol, world, device):
+    """Replicas: the job's step time is the slowest rank's (max), the work is the
+    sum over ranks.  Returns (step_s, e2e_s, converged, molecules) for the job."""
+    import torch
+
+    t = torch.tensor([step_s, e2e_s], dtype=torch.float64, device=device)
+    c = torch.tensor([n_conv, n_mol], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(c, op=torch.distributed.ReduceOp.SUM)
+    return float(t[0]), float(t[1]), float(c[0]), float(c[1])
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -272,14 +285,8 @@ def run_ours(args, rank, world):
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = sum(e2e_times) / len(e2e_times)
 
-    # max over ranks
-    t_step = torch.tensor([step_s, e2e_s], dtype=torch.float64, device="cuda")
-    c = torch.tensor([n_conv, args.batch], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t_step, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(c, op=torch.distributed.ReduceOp.SUM)
-    step_s, e2e_s = float(t_step[0]), float(t_step[1])
-    total_conv, total = float(c[0]), float(c[1])
+    step_s, e2e_s, total_conv, total = combine_ranks(step_s, e2e_s, n_conv, args.batch, world,
+                                                     "cuda")
     if rank != 0:
         return None
 
