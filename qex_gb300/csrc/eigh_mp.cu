@@ -11,12 +11,15 @@
 //      e_ij = (t_ij + lambda_j r_ij) / (lambda_j - lambda_i) when the two
 //      eigenvalues are further apart than delta = 2 (|T - D|_F + |A|_F |R|_F),
 //      else r_ij / 2; X <- X + X E.  Each step squares the error (FP32 ~1e-7
-//      times the conditioning of S -> its square -> the FP64 floor); three
+//      times the conditioning of S -> its square -> the FP64 floor); four
 //      steps follow the FP32 solve, the last one checked.  The products are
 //      batched split-K FP64 GEMMs over many CTAs.
 //   3. Ascending order (stable), eigenvectors in columns.
-// Matrices whose FP32 Cholesky fails (S not numerically SPD) keep the FP64
-// path of td.cu, which applies the reference's shift
+// Overlaps whose FP32 Cholesky fails or whose pivots spread beyond 1e5 take a
+// stage 1 with the factor and the transformation in FP64 (the Jacobi stays
+// FP32).  Matrices that are not numerically SPD even in FP64, or that the
+// check of the last refinement step rejects, keep the FP64 Jacobi path of
+// td.cu, which applies the reference's shift
 // (qedft/train/td/generalized_eigensolver.py:264-330).
 #include <cuda_runtime.h>
 #include <math.h>
@@ -31,7 +34,7 @@ constexpr int kMaxSweeps32 = 24;
 constexpr int kT = 32;      // GEMM tile
 constexpr int kKC = 16;     // split-K chunk (one shared-memory stage)
 constexpr int kGThreads = 256;
-constexpr int kRefineSteps = 3;  // FP32 start -> two squarings -> checked final step
+constexpr int kRefineSteps = 4;  // FP32 start -> three squarings -> checked final step
 
 __device__ inline float block_sumf(float v, float* red) {
 #pragma unroll
@@ -57,83 +60,11 @@ __device__ inline double block_sum(double v, double* red) {
   return s;
 }
 
-// Stage 1: FP32 solve in shared memory.  X (n x n, FP64) receives L^-T U;
-// ok[b] = 1 on success, 0 when the FP32 Cholesky of S fails.
-__global__ void __launch_bounds__(kThreads) eigh32_kernel(int n, const double* __restrict__ A,
-                                                          const double* __restrict__ S,
-                                                          double* __restrict__ X,
-                                                          int* __restrict__ ok) {
-  extern __shared__ float sm[];
-  const int b = blockIdx.x;
+// Parallel cyclic Jacobi (round-robin pairs) in FP32 on the symmetric C (n x n,
+// shared memory); U (shared, set to I by the caller) accumulates the rotations.
+__device__ void jacobi32(int n, float* C, float* U, float* cs, int* pos, int* pq, float* red) {
   const long long nn = (long long)n * n;
   const int m = (n + 1) & ~1;
-  float* L = sm;
-  float* C = L + nn;
-  float* U = C + nn;
-  float* cs = U + nn;                                // 2 * (m / 2)
-  int* pos = reinterpret_cast<int*>(cs + m);         // m
-  int* pq = pos + m;                                 // m
-  float* red = reinterpret_cast<float*>(pq + m);     // 32
-  float* piv = red + 32;                             // 1
-  const double* Ab = A + b * nn;
-  const double* Sb = S + b * nn;
-  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
-    const int i = (int)(e / n), j = (int)(e % n);
-    C[e] = (float)(0.5 * (Ab[e] + Ab[(long long)j * n + i]));
-    L[e] = (float)(0.5 * (Sb[e] + Sb[(long long)j * n + i]));
-  }
-  __syncthreads();
-  // Cholesky (right-looking), lower triangle of L
-  for (int k = 0; k < n; ++k) {
-    if (threadIdx.x == 0) {
-      const float d = L[(long long)k * n + k];
-      piv[0] = d;
-      L[(long long)k * n + k] = d > 0.0f ? sqrtf(d) : 0.0f;
-    }
-    __syncthreads();
-    if (!(piv[0] > 0.0f)) {
-      if (threadIdx.x == 0) ok[b] = 0;
-      return;
-    }
-    const float inv = 1.0f / L[(long long)k * n + k];
-    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) L[(long long)i * n + k] *= inv;
-    __syncthreads();
-    const int r = n - k - 1;
-    for (long long e = threadIdx.x; e < (long long)r * r; e += blockDim.x) {
-      const int i = k + 1 + (int)(e / r), j = k + 1 + (int)(e % r);
-      if (j <= i) L[(long long)i * n + j] -= L[(long long)i * n + k] * L[(long long)j * n + k];
-    }
-    __syncthreads();
-  }
-  // C <- L^-1 C (column j per thread), then C <- C L^-T (row r per thread)
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    for (int i = 0; i < n; ++i) {
-      float s = C[(long long)i * n + j];
-      for (int k = 0; k < i; ++k) s = fmaf(-L[(long long)i * n + k], C[(long long)k * n + j], s);
-      C[(long long)i * n + j] = s / L[(long long)i * n + i];
-    }
-  }
-  __syncthreads();
-  for (int r = threadIdx.x; r < n; r += blockDim.x) {
-    for (int i = 0; i < n; ++i) {
-      float s = C[(long long)r * n + i];
-      for (int k = 0; k < i; ++k) s = fmaf(-L[(long long)i * n + k], C[(long long)r * n + k], s);
-      C[(long long)r * n + i] = s / L[(long long)i * n + i];
-    }
-  }
-  __syncthreads();
-  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
-    const int i = (int)(e / n), j = (int)(e % n);
-    if (j > i) {
-      const float v = 0.5f * (C[e] + C[(long long)j * n + i]);
-      C[e] = v;
-      C[(long long)j * n + i] = v;
-    }
-    U[e] = (i == j) ? 1.0f : 0.0f;
-  }
-  for (int i = threadIdx.x; i < m; i += blockDim.x) pos[i] = i;
-  __syncthreads();
-  // parallel cyclic Jacobi (round-robin pairs), FP32
   for (int sweep = 0; sweep < kMaxSweeps32; ++sweep) {
     float off = 0.0f, dia = 0.0f;
     for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
@@ -210,6 +141,98 @@ __global__ void __launch_bounds__(kThreads) eigh32_kernel(int n, const double* _
       __syncthreads();
     }
   }
+}
+
+// Stage 1: FP32 solve in shared memory.  X (n x n, FP64) receives L^-T U;
+// ok[b] = 1 on success, 0 when the FP32 Cholesky of S fails.
+__global__ void __launch_bounds__(kThreads) eigh32_kernel(int n, const double* __restrict__ A,
+                                                          const double* __restrict__ S,
+                                                          double* __restrict__ X,
+                                                          int* __restrict__ ok) {
+  extern __shared__ float sm[];
+  const int b = blockIdx.x;
+  const long long nn = (long long)n * n;
+  const int m = (n + 1) & ~1;
+  float* L = sm;
+  float* C = L + nn;
+  float* U = C + nn;
+  float* cs = U + nn;                                // 2 * (m / 2)
+  int* pos = reinterpret_cast<int*>(cs + m);         // m
+  int* pq = pos + m;                                 // m
+  float* red = reinterpret_cast<float*>(pq + m);     // 32
+  float* piv = red + 32;                             // 3
+  const double* Ab = A + b * nn;
+  const double* Sb = S + b * nn;
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    C[e] = (float)(0.5 * (Ab[e] + Ab[(long long)j * n + i]));
+    L[e] = (float)(0.5 * (Sb[e] + Sb[(long long)j * n + i]));
+  }
+  __syncthreads();
+  // Cholesky (right-looking), lower triangle of L; piv[1], piv[2] track the
+  // smallest and largest pivot (a lower bound of the conditioning of S)
+  if (threadIdx.x == 0) {
+    piv[1] = 3e38f;
+    piv[2] = 0.0f;
+  }
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      const float d = L[(long long)k * n + k];
+      piv[0] = d;
+      piv[1] = fminf(piv[1], d);
+      piv[2] = fmaxf(piv[2], d);
+      L[(long long)k * n + k] = d > 0.0f ? sqrtf(d) : 0.0f;
+    }
+    __syncthreads();
+    if (!(piv[0] > 0.0f)) {
+      if (threadIdx.x == 0) ok[b] = 0;
+      return;
+    }
+    const float inv = 1.0f / L[(long long)k * n + k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) L[(long long)i * n + k] *= inv;
+    __syncthreads();
+    const int r = n - k - 1;
+    for (long long e = threadIdx.x; e < (long long)r * r; e += blockDim.x) {
+      const int i = k + 1 + (int)(e / r), j = k + 1 + (int)(e % r);
+      if (j <= i) L[(long long)i * n + j] -= L[(long long)i * n + k] * L[(long long)j * n + k];
+    }
+    __syncthreads();
+  }
+  // pivots spread beyond 1e5: the FP32 factor would leave the refinement too
+  // far from the solution; the FP64-factor stage takes this matrix
+  if (piv[1] < 1e-5f * piv[2]) {
+    if (threadIdx.x == 0) ok[b] = 0;
+    return;
+  }
+  // C <- L^-1 C (column j per thread), then C <- C L^-T (row r per thread)
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    for (int i = 0; i < n; ++i) {
+      float s = C[(long long)i * n + j];
+      for (int k = 0; k < i; ++k) s = fmaf(-L[(long long)i * n + k], C[(long long)k * n + j], s);
+      C[(long long)i * n + j] = s / L[(long long)i * n + i];
+    }
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    for (int i = 0; i < n; ++i) {
+      float s = C[(long long)r * n + i];
+      for (int k = 0; k < i; ++k) s = fmaf(-L[(long long)i * n + k], C[(long long)r * n + k], s);
+      C[(long long)r * n + i] = s / L[(long long)i * n + i];
+    }
+  }
+  __syncthreads();
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    if (j > i) {
+      const float v = 0.5f * (C[e] + C[(long long)j * n + i]);
+      C[e] = v;
+      C[(long long)j * n + i] = v;
+    }
+    U[e] = (i == j) ? 1.0f : 0.0f;
+  }
+  for (int i = threadIdx.x; i < m; i += blockDim.x) pos[i] = i;
+  __syncthreads();
+  jacobi32(n, C, U, cs, pos, pq, red);
   // X = L^-T U: column j solves L^T x = u_j (back substitution)
   double* Xb = X + b * nn;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
@@ -222,6 +245,90 @@ __global__ void __launch_bounds__(kThreads) eigh32_kernel(int n, const double* _
   __syncthreads();
   for (long long e = threadIdx.x; e < nn; e += blockDim.x) Xb[e] = (double)U[e];
   if (threadIdx.x == 0) ok[b] = 1;
+}
+
+// Stage 1 for overlaps whose FP32 Cholesky fails (or whose FP32 solve the
+// refinement check rejected): S = L L^T and C = L^-1 A L^-T in FP64 (global
+// workspace), the Jacobi of C in FP32, X = L^-T U in FP64.  Runs where
+// ok[b] == 0 and sets ok[b] = 2 on success (S numerically SPD in FP64).
+__global__ void __launch_bounds__(kThreads) eigh32_fp64factor_kernel(
+    int n, const double* __restrict__ A, const double* __restrict__ S, double* __restrict__ X,
+    double* __restrict__ L64, double* __restrict__ C64, int* __restrict__ ok) {
+  const int b = blockIdx.x;
+  if (ok[b]) return;
+  extern __shared__ float sm[];
+  __shared__ double piv;
+  const long long nn = (long long)n * n;
+  const int m = (n + 1) & ~1;
+  float* C = sm;
+  float* U = C + nn;
+  float* cs = U + nn;
+  int* pos = reinterpret_cast<int*>(cs + m);
+  int* pq = pos + m;
+  float* red = reinterpret_cast<float*>(pq + m);
+  double* L = L64 + b * nn;
+  double* Cd = C64 + b * nn;
+  const double* Ab = A + b * nn;
+  const double* Sb = S + b * nn;
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    Cd[e] = 0.5 * (Ab[e] + Ab[(long long)j * n + i]);
+    L[e] = 0.5 * (Sb[e] + Sb[(long long)j * n + i]);
+  }
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      const double d = L[(long long)k * n + k];
+      piv = d;
+      L[(long long)k * n + k] = d > 0.0 ? sqrt(d) : 0.0;
+    }
+    __syncthreads();
+    if (!(piv > 0.0)) return;  // not SPD: the FP64 Jacobi path applies the shift
+    const double lkk = L[(long long)k * n + k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) L[(long long)i * n + k] /= lkk;
+    __syncthreads();
+    const int r = n - k - 1;
+    for (long long e = threadIdx.x; e < (long long)r * r; e += blockDim.x) {
+      const int i = k + 1 + (int)(e / r), j = k + 1 + (int)(e % r);
+      if (j <= i) L[(long long)i * n + j] -= L[(long long)i * n + k] * L[(long long)j * n + k];
+    }
+    __syncthreads();
+  }
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    for (int i = 0; i < n; ++i) {
+      double s = Cd[(long long)i * n + j];
+      for (int k = 0; k < i; ++k) s = fma(-L[(long long)i * n + k], Cd[(long long)k * n + j], s);
+      Cd[(long long)i * n + j] = s / L[(long long)i * n + i];
+    }
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    for (int i = 0; i < n; ++i) {
+      double s = Cd[(long long)r * n + i];
+      for (int k = 0; k < i; ++k) s = fma(-L[(long long)i * n + k], Cd[(long long)r * n + k], s);
+      Cd[(long long)r * n + i] = s / L[(long long)i * n + i];
+    }
+  }
+  __syncthreads();
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    C[e] = (float)(0.5 * (Cd[e] + Cd[(long long)j * n + i]));
+    U[e] = (i == j) ? 1.0f : 0.0f;
+  }
+  for (int i = threadIdx.x; i < m; i += blockDim.x) pos[i] = i;
+  __syncthreads();
+  jacobi32(n, C, U, cs, pos, pq, red);
+  // X = L^-T U in FP64 (column j per thread; Cd reused as the output)
+  double* Xb = X + b * nn;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    for (int i = n - 1; i >= 0; --i) {
+      double s = (double)U[(long long)i * n + j];
+      for (int k = i + 1; k < n; ++k) s = fma(-L[(long long)k * n + i], Xb[(long long)k * n + j], s);
+      Xb[(long long)i * n + j] = s / L[(long long)i * n + i];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) ok[b] = 2;
 }
 
 // Batched split-K FP64 GEMM partials: P[b][kc] = op(A_b)[:, kc chunk] B_b[kc chunk, :]
@@ -387,15 +494,21 @@ constexpr int kMaxN = 128;  // 3 n^2 FP32 matrices in shared memory
 int ksplit_of(int n) { return (n + kKC - 1) / kKC; }
 
 // Doubles of the mixed-precision area per matrix: As, Ss, X, X', T, R, E
-// (7 n^2), split-K partials (ksplit n^2), lambda (n), the ok flag (1).
+// (7 n^2), split-K partials (ksplit n^2), lambda (n), the FP64 factor and
+// transformed matrix of the fallback stage 1 (2 n^2), one spare.
 long long area_doubles(int n) {
   const long long nn = (long long)n * n;
-  return (7 + ksplit_of(n)) * nn + n + 1;
+  return (9 + ksplit_of(n)) * nn + n + 1;
+}
+
+size_t smem_factor64(int n) {
+  const int m = (n + 1) & ~1;
+  return sizeof(float) * (2 * (size_t)n * n + 3 * (size_t)m + 33);
 }
 
 size_t smem32(int n) {
   const int m = (n + 1) & ~1;
-  return sizeof(float) * (3 * (size_t)n * n + 3 * (size_t)m + 33);
+  return sizeof(float) * (3 * (size_t)n * n + 3 * (size_t)m + 35);
 }
 
 void gemm(cudaStream_t s, int batch, int n, bool ta, const double* A, const double* B, double* P,
@@ -433,12 +546,19 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
   double* E = R + per;
   double* P = E + per;
   double* lam = P + (long long)ksplit_of(n) * per;
+  double* L64 = lam + (long long)batch * n;
+  double* C64 = L64 + per;
   int* ok = ok_out;
   const int eb = (int)((per + 255) / 256 < 4096 ? (per + 255) / 256 : 4096);
   sym_kernel<<<eb, 256, 0, s>>>(batch, n, A, S, As, Ss);
   const size_t sm = smem32(n);
   cudaFuncSetAttribute(eigh32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   eigh32_kernel<<<batch, kThreads, sm, s>>>(n, As, Ss, X, ok);
+  // overlaps too ill-conditioned for the FP32 Cholesky: FP64 factor, FP32 Jacobi
+  const size_t sm64 = smem_factor64(n);
+  cudaFuncSetAttribute(eigh32_fp64factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sm64);
+  eigh32_fp64factor_kernel<<<batch, kThreads, sm64, s>>>(n, As, Ss, X, L64, C64, ok);
   for (int it = 0; it < kRefineSteps; ++it) {
     gemm(s, batch, n, false, Ss, X, P, nullptr, false, 1.0, T);   // T = S X
     gemm(s, batch, n, true, X, T, P, nullptr, true, -1.0, R);     // R = I - X^T S X
