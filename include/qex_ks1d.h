@@ -130,7 +130,8 @@ typedef struct qex_ks1d_outputs {
   int32_t* iterations_run;   /* (B) iterations that did work (not skipped as converged) */
   int32_t* stats;            /* (B, 8): eigen-solves, Rayleigh-quotient vector passes,
                                 correction updates, Sturm multisection passes,
-                                warm-route attempts, 3 reserved */
+                                warm-route attempts, warm-route fallbacks to
+                                the cold route, 2 reserved */
   int64_t* phase_cycles;     /* (B, 16): SM clock cycles per phase: Hartree, XC potential,
                                 Sturm brackets, FP32 inverse iteration, FP64 refinement,
                                 density+energy, mixing+records, whole molecule; then

@@ -755,7 +755,7 @@ struct SolveBackward {
 
 // Work counters of one eigen-solve (for the roofline tally of the benchmark).
 struct EigStats {
-  int solves, rq_vectors, updates, passes, fast;
+  int solves, rq_vectors, updates, passes, fast, fastfail;
   long long cyc[kPhases];  // clock64 cycles per phase (see write_stats)
 };
 
@@ -1277,6 +1277,7 @@ __device__ __noinline__ int eigen_solve(const Params& p, int N, double dx, int n
       }
       ok = __all_sync(kFull, ok || lane >= K);
       if (!ok) {
+        stats.fastfail += 1;
         // restore the previous eigenvalues as warm brackets and take the cold route
         if (lane < K) sm.eigprev[lane] = sm.resn[lane];
         __syncwarp();
@@ -1364,6 +1365,7 @@ __device__ inline void write_stats(const Params& p, int b, const EigStats& e) {
   p.o_stats[8 * b + 2] = e.updates;
   p.o_stats[8 * b + 3] = e.passes;
   p.o_stats[8 * b + 4] = e.fast;
+  p.o_stats[8 * b + 5] = e.fastfail;
   if (p.o_cycles)
     for (int k = 0; k < kPhases; ++k) p.o_cycles[(long long)kPhases * b + k] = e.cyc[k];
 }
