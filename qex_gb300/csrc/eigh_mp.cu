@@ -62,7 +62,7 @@ __device__ inline double block_sum(double v, double* red) {
 
 // Parallel cyclic Jacobi (round-robin pairs) in FP32 on the symmetric C (n x n,
 // shared memory); U (shared, set to I by the caller) accumulates the rotations.
-__device__ void jacobi32(int n, float* C, float* U, float* cs, int* pos, int* pq, float* red) {
+__device__ void jacobi32(int n, float* C, float* U, float* cs, int* pq, float* red) {
   const long long nn = (long long)n * n;
   const int m = (n + 1) & ~1;
   for (int sweep = 0; sweep < kMaxSweeps32; ++sweep) {
@@ -83,7 +83,10 @@ __device__ void jacobi32(int n, float* C, float* U, float* cs, int* pos, int* pq
     if (off <= 1e-12f * dia || off == 0.0f) break;
     for (int step = 0; step < m - 1; ++step) {
       for (int k = threadIdx.x; k < m / 2; k += blockDim.x) {
-        int p = pos[k], q = pos[m - 1 - k];
+        // round-robin pairing at this step: slot 0 fixed, the others rotated
+        // `step` places (closed form of rotating the slot array each step)
+        auto slot = [&](int i) { return i == 0 ? 0 : 1 + (i - 1 + (m - 1) - step % (m - 1)) % (m - 1); };
+        int p = slot(k), q = slot(m - 1 - k);
         if (p > q) {
           const int t = p;
           p = q;
@@ -133,12 +136,6 @@ __device__ void jacobi32(int n, float* C, float* U, float* cs, int* pos, int* pq
         U[(long long)i * n + q] = s * xp + c * xq;
       }
       __syncthreads();
-      if (threadIdx.x == 0) {
-        const int last = pos[m - 1];
-        for (int i = m - 1; i > 1; --i) pos[i] = pos[i - 1];
-        pos[1] = last;
-      }
-      __syncthreads();
     }
   }
 }
@@ -157,8 +154,7 @@ __global__ void __launch_bounds__(kThreads) eigh32_kernel(int n, const double* _
   float* C = L + nn;
   float* U = C + nn;
   float* cs = U + nn;                                // 2 * (m / 2)
-  int* pos = reinterpret_cast<int*>(cs + m);         // m
-  int* pq = pos + m;                                 // m
+  int* pq = reinterpret_cast<int*>(cs + m);          // m
   float* red = reinterpret_cast<float*>(pq + m);     // 32
   float* piv = red + 32;                             // 3
   const double* Ab = A + b * nn;
@@ -230,9 +226,8 @@ __global__ void __launch_bounds__(kThreads) eigh32_kernel(int n, const double* _
     }
     U[e] = (i == j) ? 1.0f : 0.0f;
   }
-  for (int i = threadIdx.x; i < m; i += blockDim.x) pos[i] = i;
   __syncthreads();
-  jacobi32(n, C, U, cs, pos, pq, red);
+  jacobi32(n, C, U, cs, pq, red);
   // X = L^-T U: column j solves L^T x = u_j (back substitution)
   double* Xb = X + b * nn;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
@@ -263,8 +258,7 @@ __global__ void __launch_bounds__(kThreads) eigh32_fp64factor_kernel(
   float* C = sm;
   float* U = C + nn;
   float* cs = U + nn;
-  int* pos = reinterpret_cast<int*>(cs + m);
-  int* pq = pos + m;
+  int* pq = reinterpret_cast<int*>(cs + m);
   float* red = reinterpret_cast<float*>(pq + m);
   double* L = L64 + b * nn;
   double* Cd = C64 + b * nn;
@@ -315,9 +309,8 @@ __global__ void __launch_bounds__(kThreads) eigh32_fp64factor_kernel(
     C[e] = (float)(0.5 * (Cd[e] + Cd[(long long)j * n + i]));
     U[e] = (i == j) ? 1.0f : 0.0f;
   }
-  for (int i = threadIdx.x; i < m; i += blockDim.x) pos[i] = i;
   __syncthreads();
-  jacobi32(n, C, U, cs, pos, pq, red);
+  jacobi32(n, C, U, cs, pq, red);
   // X = L^-T U in FP64 (column j per thread; Cd reused as the output)
   double* Xb = X + b * nn;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
@@ -503,12 +496,12 @@ long long area_doubles(int n) {
 
 size_t smem_factor64(int n) {
   const int m = (n + 1) & ~1;
-  return sizeof(float) * (2 * (size_t)n * n + 3 * (size_t)m + 33);
+  return sizeof(float) * (2 * (size_t)n * n + 2 * (size_t)m + 33);
 }
 
 size_t smem32(int n) {
   const int m = (n + 1) & ~1;
-  return sizeof(float) * (3 * (size_t)n * n + 3 * (size_t)m + 35);
+  return sizeof(float) * (3 * (size_t)n * n + 2 * (size_t)m + 35);
 }
 
 void gemm(cudaStream_t s, int batch, int n, bool ta, const double* A, const double* B, double* P,
