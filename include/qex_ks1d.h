@@ -51,6 +51,19 @@ extern "C" {
 /* W1 (17x16), b1 (16), W2 (16x16), b2 (16), W3 (16), b3 (1), as x@W+b. */
 #define QEX_MLP_NUM_PARAMS (17 * 16 + 16 + 16 * 16 + 16 + 16 + 1)
 
+/* Global-local convolutional KSR network (qedft/models/classical/global_ksr_model.py:32-80,
+ * jax_dft neural_xc) with C = 16 (the reference default) or 8 channels: the
+ * density and C - 1 exponential global convolutions, two bias-free width-3
+ * convolutions C -> C with swish, a width-1 convolution C -> 1, -swish, and
+ * the self-interaction layer.  Packed FP32 layout, QEX_KSR_NUM_PARAMS(C)
+ * floats in a DEVICE buffer, 16-byte aligned:
+ *   W1[t][c][o] (3 C C; tap t applies to the point at offset t - 1),
+ *   W2[t][c][o] (3 C C), W3[c] (C),
+ *   eta (C - 1): widths minval + (maxval - minval) * sigmoid(eta),
+ *   the self-interaction width (1). */
+#define QEX_KSR_CHANNELS 16
+#define QEX_KSR_NUM_PARAMS(c) (6 * (c) * (c) + 2 * (c))
+
 enum qex_interaction_kind {
   QEX_INTERACTION_EXPONENTIAL = 0, /* a * exp(-b |d|), jax_dft exponential_coulomb */
   QEX_INTERACTION_SOFT_COULOMB = 1 /* 1 / sqrt(d^2 + a), jax_dft soft_coulomb */
@@ -60,7 +73,8 @@ enum qex_xc_kind {
   QEX_XC_NONE = 0,
   QEX_XC_LDA_EXP_COULOMB = 1, /* exponential-Coulomb uniform-gas LDA */
   QEX_XC_POWER = 2,           /* f(n) = coefficient * (n + shift)^power */
-  QEX_XC_WINDOW_MLP = 3       /* FP32 window-17 MLP, two SiLU layers of 16 */
+  QEX_XC_WINDOW_MLP = 3,      /* FP32 window-17 MLP, two SiLU layers of 16 */
+  QEX_XC_KSR = 4              /* FP32 global-local conv network (whole-grid functional) */
 };
 
 enum qex_xc_convention {
@@ -75,6 +89,9 @@ typedef struct qex_xc_spec {
   double lda_amplitude, lda_kappa;  /* QEX_XC_LDA_EXP_COULOMB */
   double normalization;             /* QEX_XC_WINDOW_MLP input divisor */
   const float* mlp_params_host;     /* HOST pointer, QEX_MLP_NUM_PARAMS floats */
+  const float* ksr_params;          /* DEVICE pointer, QEX_KSR_NUM_PARAMS(ksr_channels) floats */
+  double ksr_minval, ksr_maxval;    /* range of the global-convolution widths */
+  int32_t ksr_channels;             /* 16 or 8 (QEX_XC_KSR) */
 } qex_xc_spec;
 
 typedef struct qex_ks1d_options {

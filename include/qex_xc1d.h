@@ -14,6 +14,13 @@
  * E_xc per molecule.  The window MLP needs a workspace of
  * qex_xc1d_workspace_size(total_points) bytes, total_points >= every
  * grid_offsets[b] + num_grids[b].
+ *
+ *   qex_ksr1d_eval <- the KSR functional's xc_energy_density_fn(density, params)
+ *                    and its gradient (qedft/models/classical/global_ksr_model.py:32-80,
+ *                    jax_dft neural_xc.global_functional), evaluated per
+ *                    molecule on its own grid.  Same outputs; one warp per
+ *                    molecule, no workspace (shared memory sized by
+ *                    max_num_grids >= every num_grids[b]).
  */
 #ifndef QEX_XC1D_H_
 #define QEX_XC1D_H_
@@ -34,6 +41,11 @@ int qex_xc1d_eval(int32_t num_molecules, int64_t total_points, const int32_t* nu
                   const qex_xc_spec* xc, const double* density, double* values,
                   double* potential, double* energy, void* workspace, size_t workspace_bytes,
                   void* stream);
+
+int qex_ksr1d_eval(int32_t num_molecules, int32_t max_num_grids, const int32_t* num_grids,
+                   const int64_t* grid_offsets, const double* grid_spacing,
+                   const qex_xc_spec* xc, const double* density, double* values,
+                   double* potential, double* energy, void* stream);
 
 #ifdef __cplusplus
 }

@@ -5,6 +5,6 @@ in ``include/``); Python mirrors the reference's interfaces on top of it.
 """
 
 from . import networks, xc  # noqa: F401
-from .xc import LDAExpCoulomb, Partial, PowerXC, WindowMLPFunctional  # noqa: F401
+from .xc import KSRFunctional, LDAExpCoulomb, Partial, PowerXC, WindowMLPFunctional  # noqa: F401
 
 __version__ = "0.1.0"

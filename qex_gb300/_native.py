@@ -27,6 +27,7 @@ QEX_XC_NONE = 0
 QEX_XC_LDA_EXP_COULOMB = 1
 QEX_XC_POWER = 2
 QEX_XC_WINDOW_MLP = 3
+QEX_XC_KSR = 4
 QEX_XC_AMPLITUDE = 0
 QEX_XC_LOCAL = 1
 
@@ -34,6 +35,12 @@ MAX_EIGENPAIRS = 16
 MLP_WINDOW = 17
 MLP_HIDDEN = 16
 MLP_NUM_PARAMS = 17 * 16 + 16 + 16 * 16 + 16 + 16 + 1
+KSR_CHANNELS = 16
+
+
+def ksr_num_params(channels: int) -> int:
+    return 6 * channels * channels + 2 * channels
+
 
 _c_p = ctypes.c_void_p
 
@@ -49,6 +56,10 @@ class XcSpec(ctypes.Structure):
         ("lda_kappa", ctypes.c_double),
         ("normalization", ctypes.c_double),
         ("mlp_params_host", ctypes.POINTER(ctypes.c_float)),
+        ("ksr_params", _c_p),
+        ("ksr_minval", ctypes.c_double),
+        ("ksr_maxval", ctypes.c_double),
+        ("ksr_channels", ctypes.c_int32),
     ]
 
 

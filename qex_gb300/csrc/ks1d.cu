@@ -30,6 +30,7 @@
 #include <mutex>
 
 #include "ks1d_common.cuh"
+#include "ksr_device.cuh"
 #include "xc_device.cuh"
 #include "qex_ks1d.h"
 
@@ -71,6 +72,9 @@ struct Params {
   int mix_slots;
   int xc_kind, xc_conv;
   double xc_a, xc_p, xc_shift, lda_A, lda_kappa;
+  const float* ksr_w;  // packed KSR network (device)
+  double ksr_lo, ksr_hi;
+  int ksr_c;
   // outputs
   double* o_energy;
   double* o_gap;
@@ -137,6 +141,7 @@ __host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax, bool adjoi
   off = (off + 15) & ~(size_t)15;  // float4 ring and RR matrices below
   L.f32 = off;
   size_t xc_floats = 2 * (size_t)(nmax + 2 * kPadMlp) + (size_t)kMlpScratch * kWarp;
+  if (ksr_scratch_floats(nmax) > xc_floats) xc_floats = ksr_scratch_floats(nmax);
   size_t hart_floats = 2 * (size_t)nmax + 2;  // one FP64 scan vector
   // FP32 diagonal, then the ring of the streamed solves (16-byte aligned)
   const size_t ring_off = ((size_t)L.nstr + 3) / 4 * 4;
@@ -406,6 +411,18 @@ __device__ __noinline__ double xc_eval(const Params& p, int N, double dx, const 
         if (want_v) vout[i] = dx * df;
       }
       if (frec) frec[i] = f;
+    }
+  } else if (p.xc_kind == QEX_XC_KSR) {
+    if (p.ksr_c == 16) {
+      e = want_v ? ksr_eval<16, true>(p.ksr_w, p.ksr_lo, p.ksr_hi, N, dx, n, local, vout, frec,
+                                      sm.f32, lane)
+                 : ksr_eval<16, false>(p.ksr_w, p.ksr_lo, p.ksr_hi, N, dx, n, local, nullptr,
+                                       frec, sm.f32, lane);
+    } else {
+      e = want_v ? ksr_eval<8, true>(p.ksr_w, p.ksr_lo, p.ksr_hi, N, dx, n, local, vout, frec,
+                                     sm.f32, lane)
+                 : ksr_eval<8, false>(p.ksr_w, p.ksr_lo, p.ksr_hi, N, dx, n, local, nullptr,
+                                      frec, sm.f32, lane);
     }
   } else {
     // Window MLP: stage n / norm as FP32 with 8 zeros either side; v_xc
@@ -2074,10 +2091,19 @@ int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_opt
   P.xc_shift = xc->shift;
   P.lda_A = xc->lda_amplitude;
   P.lda_kappa = xc->lda_kappa;
-  if (xc->kind < QEX_XC_NONE || xc->kind > QEX_XC_WINDOW_MLP) return QEX_BAD_ARG;
+  if (xc->kind < QEX_XC_NONE || xc->kind > QEX_XC_KSR) return QEX_BAD_ARG;
   if (xc->convention != QEX_XC_AMPLITUDE && xc->convention != QEX_XC_LOCAL) return QEX_BAD_ARG;
   if (xc->kind == QEX_XC_WINDOW_MLP) {
     if (!fill_mlp_params(P.mlp, xc)) return QEX_BAD_ARG;
+  }
+  if (xc->kind == QEX_XC_KSR) {
+    if (!xc->ksr_params || reinterpret_cast<uintptr_t>(xc->ksr_params) % 16 != 0) return QEX_BAD_ARG;
+    if (!(xc->ksr_maxval >= xc->ksr_minval) || !(xc->ksr_minval > 0.0)) return QEX_BAD_ARG;
+    if (xc->ksr_channels != 8 && xc->ksr_channels != 16) return QEX_BAD_ARG;
+    P.ksr_c = xc->ksr_channels;
+    P.ksr_w = xc->ksr_params;
+    P.ksr_lo = xc->ksr_minval;
+    P.ksr_hi = xc->ksr_maxval;
   }
   if (out) {
     P.o_energy = out->total_energy;

@@ -10,6 +10,7 @@
 #include <string.h>
 
 #include "ks1d_common.cuh"
+#include "ksr_device.cuh"
 #include "qex_xc1d.h"
 #include "xc_device.cuh"
 
@@ -117,10 +118,97 @@ __global__ void __launch_bounds__(kThreads) xc1d_kernel(const __grid_constant__ 
   if (threadIdx.x == 0 && p.energy) p.energy[b] = e * dx;
 }
 
+struct KsrEvalParams {
+  int num_molecules;
+  const int32_t* num_grids;
+  const int64_t* offsets;
+  const double* spacing;
+  const double* density;
+  double* values;
+  double* potential;
+  double* energy;
+  int conv;
+  int nmax;
+  int channels;
+  const float* w;
+  double lo, hi;
+};
+
+template <int C>
+__device__ double ksr_one(const KsrEvalParams& p, int N, double dx, long long off, bool local,
+                          double* vals, float* scratch, int lane) {
+  return p.potential ? ksr_eval<C, true>(p.w, p.lo, p.hi, N, dx, p.density + off, local,
+                                         p.potential + off, vals, scratch, lane)
+                     : ksr_eval<C, false>(p.w, p.lo, p.hi, N, dx, p.density + off, local,
+                                          nullptr, vals, scratch, lane);
+}
+
+// One warp per molecule; the warp-level evaluation shared with the SCF kernel.
+__global__ void __launch_bounds__(kWarp) ksr1d_kernel(const __grid_constant__ KsrEvalParams p) {
+  extern __shared__ __align__(16) float ksm[];
+  const int b = blockIdx.x;
+  const int lane = threadIdx.x;
+  if (b >= p.num_molecules) return;
+  const int N = p.num_grids[b];
+  if (N < 1 || N > p.nmax) {
+    if (lane == 0 && p.energy) p.energy[b] = nan("");
+    return;
+  }
+  const long long off = p.offsets[b];
+  const double dx = p.spacing[b];
+  const bool local = p.conv == QEX_XC_LOCAL;
+  double* vals = p.values ? p.values + off : nullptr;
+  double e = p.channels == 16 ? ksr_one<16>(p, N, dx, off, local, vals, ksm, lane)
+                              : ksr_one<8>(p, N, dx, off, local, vals, ksm, lane);
+  e = warp_sum(e);
+  if (lane == 0 && p.energy) p.energy[b] = e * dx;
+}
+
 }  // namespace
 }  // namespace qex
 
 extern "C" {
+
+int qex_ksr1d_eval(int32_t num_molecules, int32_t max_num_grids, const int32_t* num_grids,
+                   const int64_t* grid_offsets, const double* grid_spacing,
+                   const qex_xc_spec* xc, const double* density, double* values,
+                   double* potential, double* energy, void* stream) {
+  using namespace qex;
+  if (num_molecules < 0 || !xc || xc->kind != QEX_XC_KSR) return QEX_BAD_ARG;
+  if (xc->convention != QEX_XC_AMPLITUDE && xc->convention != QEX_XC_LOCAL) return QEX_BAD_ARG;
+  if (num_molecules == 0) return QEX_OK;
+  if (!num_grids || !grid_offsets || !grid_spacing || !density || max_num_grids < 1)
+    return QEX_BAD_ARG;
+  if (!xc->ksr_params || reinterpret_cast<uintptr_t>(xc->ksr_params) % 16 != 0) return QEX_BAD_ARG;
+  if (!(xc->ksr_maxval >= xc->ksr_minval) || !(xc->ksr_minval > 0.0)) return QEX_BAD_ARG;
+  if (xc->ksr_channels != 8 && xc->ksr_channels != 16) return QEX_BAD_ARG;
+  const size_t smem = sizeof(float) * ksr_scratch_floats(max_num_grids);
+  int dev = 0, max_optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return QEX_CUDA_ERROR;
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (smem > (size_t)max_optin) return QEX_BAD_ARG;
+  if (cudaFuncSetAttribute(ksr1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return QEX_CUDA_ERROR;
+  KsrEvalParams P;
+  memset(&P, 0, sizeof(P));
+  P.num_molecules = num_molecules;
+  P.num_grids = num_grids;
+  P.offsets = grid_offsets;
+  P.spacing = grid_spacing;
+  P.density = density;
+  P.values = values;
+  P.potential = potential;
+  P.energy = energy;
+  P.conv = xc->convention;
+  P.nmax = max_num_grids;
+  P.channels = xc->ksr_channels;
+  P.w = xc->ksr_params;
+  P.lo = xc->ksr_minval;
+  P.hi = xc->ksr_maxval;
+  ksr1d_kernel<<<num_molecules, kWarp, smem, static_cast<cudaStream_t>(stream)>>>(P);
+  return cudaGetLastError() == cudaSuccess ? QEX_OK : QEX_CUDA_ERROR;
+}
 
 int qex_xc1d_workspace_size(int64_t total_points, const qex_xc_spec* xc, size_t* bytes) {
   if (!bytes || !xc || total_points < 0) return QEX_BAD_ARG;

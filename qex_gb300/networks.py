@@ -18,7 +18,7 @@ from typing import Protocol
 import numpy as np
 
 from . import _native as N
-from .xc import LDAExpCoulomb, WindowMLPFunctional, XCFunctional
+from .xc import LDAExpCoulomb, Partial, WindowMLPFunctional, XCFunctional
 
 
 class KohnShamNetwork(Protocol):
@@ -128,3 +128,146 @@ def build_xc_functional(network, grids, config: dict | None = None):
         return params
 
     return init_fn, _XCEnergyDensityFn(functional)
+
+
+# ---------------------------------------------------------------------------
+# Global-local convolutional KSR functional
+# ---------------------------------------------------------------------------
+
+KSR_DEFAULT_CONFIG = {
+    "num_global_filters": 16,
+    "num_local_filters": 16,
+    "num_local_conv_layers": 2,
+    "activation": "swish",
+    "minval": 0.1,
+    "maxval": 2.385345,
+    "downsample_factor": 0,
+}
+
+
+def _is_power_of_two(n: int) -> bool:
+    return n > 0 and (n & (n - 1)) == 0
+
+
+class KSRNetwork:
+    """(init_fn, apply_fn) pair of the global-local conv network, as built by
+    jax_dft ``neural_xc.build_global_local_conv_net`` (called at
+    ``qedft/models/classical/global_ksr_model.py:62-71``).  Carries the GPU
+    description; ``self_interaction`` is set by
+    ``wrap_network_with_self_interaction_layer``."""
+
+    def __init__(self, channels, grids, minval, maxval, self_interaction=False):
+        self.channels = int(channels)
+        self.grids = np.asarray(grids, dtype=np.float64)
+        self.minval, self.maxval = float(minval), float(maxval)
+        self.self_interaction = bool(self_interaction)
+
+    def _init_net(self, g):
+        c = self.channels
+        # eta ~ normal(0, 0.01) (the exponential convolution's initialiser);
+        # bias-free conv kernels Glorot-normal over (width * channels) fans
+        eta = g.normal(0.0, 0.01, size=c - 1)
+        std3 = np.sqrt(2.0 / (3 * c + 3 * c))
+        std1 = np.sqrt(2.0 / (c + 1))
+        w1 = np.clip(g.normal(0.0, std3, size=(3, c, c)), -2 * std3, 2 * std3)
+        w2 = np.clip(g.normal(0.0, std3, size=(3, c, c)), -2 * std3, 2 * std3)
+        w3 = np.clip(g.normal(0.0, std1, size=(1, c, 1)), -2 * std1, 2 * std1)
+        block = [(), ((), [(eta,)]), ()]
+        return [block, (w1,), (), (w2,), (), (w3,), ()]
+
+    def init_fn(self, rng, input_shape=None):
+        g = _rng(rng)
+        net = self._init_net(g)
+        if self.self_interaction:
+            return input_shape, [(), ((), net), (np.array(1.0),)]
+        return input_shape, net
+
+    def __iter__(self):
+        return iter((self.init_fn, self.apply_fn))
+
+    def apply_fn(self, params, inputs, **kwargs):
+        raise NotImplementedError(
+            "the KSR network is evaluated by its global functional on the GPU; use "
+            "global_functional(network, grids)")
+
+
+def build_global_local_conv_net(num_global_filters, num_local_filters, num_local_conv_layers,
+                                activation, grids, minval, maxval, downsample_factor):
+    """jax_dft ``neural_xc.build_global_local_conv_net`` with the arguments of
+    ``qedft/models/classical/global_ksr_model.py:62-71``.  The GPU kernels take
+    equal global and local filter counts of 8 or 16, two local layers, swish
+    and no downsampling; the grid must have 2^k + 1 points (ValueError
+    otherwise, as ``tests/test_global_ksr_model.py:103-111`` expects)."""
+    n = int(np.asarray(grids).shape[0])
+    if not _is_power_of_two(n - 1):
+        raise ValueError(f"the number of grid points must be 2^k + 1, got {n}")
+    if num_global_filters != num_local_filters or num_global_filters not in (8, 16):
+        raise ValueError("the GPU KSR network takes 8 or 16 global and local filters")
+    if num_local_conv_layers != 2 or activation != "swish" or downsample_factor != 0:
+        raise ValueError("the GPU KSR network has two swish local layers and no downsampling")
+    return KSRNetwork(num_global_filters, grids, minval, maxval)
+
+
+def wrap_network_with_self_interaction_layer(network, grids, interaction_fn=None):
+    """jax_dft ``neural_xc.wrap_network_with_self_interaction_layer``
+    (``global_ksr_model.py:73-77``); the self-interaction Hartree term uses the
+    exponential Coulomb interaction with its default constants."""
+    if not isinstance(network, KSRNetwork):
+        raise TypeError("expected a network from build_global_local_conv_net")
+    return KSRNetwork(network.channels, grids, network.minval, network.maxval,
+                      self_interaction=True)
+
+
+def global_functional(network, grids):
+    """jax_dft ``neural_xc.global_functional`` (``global_ksr_model.py:79``):
+    (init_fn(rng) -> params, xc_energy_density_fn(density, params) -> eps).
+
+    ``xc_energy_density_fn`` evaluates the network on the GPU
+    (``qex_ksr1d_eval``) and carries its ``KSRFunctional``, so it can be
+    passed (bound with ``Partial``) to the SCF drivers of ``qex_gb300.od``."""
+    from .xc import KSRFunctional
+
+    if not isinstance(network, KSRNetwork) or not network.self_interaction:
+        raise NotImplementedError(
+            "the GPU KSR functional includes the self-interaction layer; wrap the network "
+            "with wrap_network_with_self_interaction_layer first")
+    grids = np.asarray(grids, dtype=np.float64)
+    functional = KSRFunctional(network.channels, network.minval, network.maxval)
+
+    def init_fn(rng):
+        return network.init_fn(rng, (-1, grids.shape[0], 1))[1]
+
+    def xc_energy_density_fn(density, params):
+        from .od import utils as _u
+        from .od.xc_eval import ksr_eval
+
+        n = np.asarray(density, dtype=np.float64)
+        if n.shape != grids.shape:
+            raise ValueError(f"density must have shape {grids.shape}, got {n.shape}")
+        return ksr_eval([n], _u.get_dx(grids), Partial(functional, params=params),
+                        potential=False)[0][2]
+
+    xc_energy_density_fn.functional = functional
+    return init_fn, xc_energy_density_fn
+
+
+def create_ksr_model_from_config(grids, config: dict | None = None):
+    """(network, init_fn, apply_fn) as ``qedft/models/classical/global_ksr_model.py:32-80``."""
+    cfg = dict(KSR_DEFAULT_CONFIG)
+    if config is not None:
+        cfg = {k: config.get(k, v) for k, v in KSR_DEFAULT_CONFIG.items()}
+    network = build_global_local_conv_net(
+        num_global_filters=cfg["num_global_filters"], num_local_filters=cfg["num_local_filters"],
+        num_local_conv_layers=cfg["num_local_conv_layers"], activation=cfg["activation"],
+        grids=grids, minval=cfg["minval"], maxval=cfg["maxval"],
+        downsample_factor=cfg["downsample_factor"])
+    network = wrap_network_with_self_interaction_layer(network, grids=grids)
+    init_fn, apply_fn = global_functional(network, grids=grids)
+    return network, init_fn, apply_fn
+
+
+def ksr_params_dict(params) -> dict:
+    """Plain-array form of a KSR parameter tree: eta, conv (two kernels), out, width."""
+    from .xc import KSRFunctional
+
+    return KSRFunctional.as_dict(params)

@@ -128,6 +128,71 @@ class WindowMLPFunctional(XCFunctional):
         return s, flat  # keep the host buffer alive for the call
 
 
+class KSRFunctional(XCFunctional):
+    """Global-local convolutional KSR network with the self-interaction layer
+    (``qedft/models/classical/global_ksr_model.py:32-80``), FP32 on the GPU.
+
+    A whole-grid functional: eps_i depends on the density at every point
+    (through the exponential global convolutions and the self-interaction
+    Hartree term), so the kernels evaluate it per molecule and back-propagate
+    the cotangent through it for v_xc.  ``params`` is the stax parameter tree
+    of ``create_ksr_model_from_config`` (the nesting of the trained
+    ``data/od/h2/h2_optimal.pkl``) or the dict form of
+    ``qex_gb300.networks.ksr_params_dict``.
+    """
+
+    kind = N.QEX_XC_KSR
+
+    def __init__(self, channels=N.KSR_CHANNELS, minval=0.1, maxval=2.385345):
+        if channels not in (8, 16):
+            raise ValueError("the GPU KSR network has 8 or 16 channels")
+        self.channels = int(channels)
+        self.minval, self.maxval = float(minval), float(maxval)
+        self._dev = None  # (packed bytes, device buffer)
+
+    @staticmethod
+    def as_dict(params) -> dict:
+        if isinstance(params, dict):
+            return params
+        net = params[1][1]
+        return {"eta": np.asarray(net[0][1][1][0][0]),
+                "conv": [np.asarray(layer[0]) for layer in net[1:-2] if len(layer) == 1],
+                "out": np.asarray(net[-2][0]), "width": float(np.asarray(params[2][0]))}
+
+    def pack(self, params) -> np.ndarray:
+        p = self.as_dict(params)
+        c = self.channels
+        w1, w2 = (np.asarray(w, np.float32) for w in p["conv"])
+        w3 = np.asarray(p["out"], np.float32)
+        eta = np.asarray(p["eta"], np.float32).reshape(-1)
+        if w1.shape != (3, c, c) or w2.shape != (3, c, c) or w3.shape != (1, c, 1) or eta.size != c - 1:
+            raise ValueError(f"KSR params do not match {c} channels")
+        flat = np.concatenate([w1.reshape(-1), w2.reshape(-1), w3.reshape(-1), eta,
+                               np.asarray([p["width"]], np.float32)])
+        assert flat.size == N.ksr_num_params(c)
+        return np.ascontiguousarray(flat, dtype=np.float32)
+
+    def device_params(self, params):
+        """The packed network on the current CUDA device (re-uploaded only when it changes)."""
+        torch = N.require_cuda()
+        flat = self.pack(params)
+        key = flat.tobytes()
+        if self._dev is None or self._dev[0] != key or self._dev[1].device != torch.device(
+                "cuda", torch.cuda.current_device()):
+            self._dev = (key, torch.as_tensor(flat, device="cuda"))
+        return self._dev[1]
+
+    def spec(self, params, convention):
+        if params is None:
+            raise ValueError("KSRFunctional needs params")
+        s, _ = super().spec(params, convention)
+        buf = self.device_params(params)
+        s.ksr_params = buf.data_ptr()
+        s.ksr_minval, s.ksr_maxval = self.minval, self.maxval
+        s.ksr_channels = self.channels
+        return s, buf
+
+
 class Partial:
     """Minimal stand-in for ``jax.tree_util.Partial``: a functional with bound
     keyword arguments (``params``), as built at ``qedft/train/od/train.py:102-105``."""

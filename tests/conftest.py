@@ -20,4 +20,5 @@ def golden():
     return {
         "ref": dict(np.load(os.path.join(here, "ks1d_reference_data.npz"))),
         "oracle": dict(np.load(os.path.join(here, "ks1d_oracle.npz"))),
+        "ksr": dict(np.load(os.path.join(here, "ksr_h2.npz"))),
     }
