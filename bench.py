@@ -188,6 +188,81 @@ def fp32_flops_mlp(mols, iterations_run):
     return float(sum(float(it) * m.num_grids * (3 * fwd) for m, it in zip(mols, iterations_run)))
 
 
+# global-local conv KSR network (16 channels), FP32 flops per grid point of one
+# KS iteration: the forward pass (16 two-sided exponential scans 112, two
+# width-3 16->16 convolutions 2 x 1536, swish 2 x 64, output layer and
+# self-interaction 39) is 3351; the backward pass 3414; an iteration runs the
+# forward and backward passes at the input density (v_xc) and the forward pass
+# at the output density (E_xc)
+KSR_FLOPS_PER_POINT = 3351 + 3414 + 3351
+
+
+def ksr_trained_params():
+    """The trained H2 network shipped with the reference (data/od/h2/h2_optimal.pkl),
+    stored as plain arrays in the test fixtures."""
+    k = np.load(os.path.join(ROOT, "tests", "golden", "ksr_h2.npz"))
+    return {"eta": k["eta"], "conv": [k["w1"], k["w2"]], "out": k["w3"],
+            "width": float(k["width"])}
+
+
+def run_ksr(args, peak64, peak32, flush):
+    """KSR workload: 4096 H2 molecules (unit charges at +-R/2, R ~ U[0.5, 3.0]
+    from the seed), 513 points at 0.08, the trained global-local conv network,
+    jax_dft local convention with reflection symmetry, 15 iterations, one
+    mixing step, five-point kinetic operator (the reference's KSR training SCF,
+    qedft/train/od/train.py:84-125)."""
+    import torch
+
+    import qex_gb300
+    from qex_gb300.od import engine as eng
+
+    rng = np.random.default_rng(args.seed + 1)
+    B, iters = args.batch, 15
+    mols = [eng.Molecule1D(num_grids=513, grid_spacing=0.08, locations=np.array([-r / 2, r / 2]),
+                           nuclear_charges=np.array([1.0, 1.0]), num_electrons=2)
+            for r in rng.uniform(0.5, 3.0, B)]
+    batch = eng.PackedBatch(mols)
+    xc = qex_gb300.Partial(qex_gb300.KSRFunctional(16), params=ksr_trained_params())
+    cfg = eng.SolveConfig(num_iterations=iters, alpha=0.5, alpha_decay=0.9,
+                          num_mixing_iterations=1, convention="local", stencil=5,
+                          enforce_reflection_symmetry=True)
+    engine = eng.Ks1dEngine(autotune=True)
+    out = engine.allocate_outputs(batch, cfg, ("energy", "final_density"))
+    for _ in range(args.warmup):
+        engine.solve(batch, xc, cfg, out=out)
+    stream = torch.cuda.current_stream()
+    times = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        engine.solve(batch, xc, cfg, out=out)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    step_s = sum(times) / len(times)
+    energy = out["energy"].cpu().numpy()
+    status = out["status"].cpu().numpy()
+    iters_run = out["iterations_run"].cpu().numpy()
+    stats = out["stats"].cpu().numpy()
+    conv = (np.abs(energy[:, -1] - energy[:, -2]) < E_CONV) & ((status & 0xFFFF) == 0)
+    w64 = fp64_flops(mols, iters_run, stats)
+    w32 = float(KSR_FLOPS_PER_POINT * 513 * iters_run.sum())
+    bound_s = w64 / (peak64 * 1e12) + (w32 / (peak32 * 1e12) if peak32 else 0.0)
+    return {
+        "workload": f"{B} H2 molecules, R ~ U[0.5,3.0] bohr, 513 points, trained global-local "
+                    f"conv KSR network (FP32, 16 channels), local convention, reflection "
+                    f"symmetry, {iters} iterations, 5-point kinetic",
+        "ms_per_step": step_s * 1e3, "solves_per_s": B / step_s,
+        "converged_solves_per_s": float(conv.sum()) / step_s,
+        "converged_fraction": float(conv.mean()),
+        "roofline": {"bound": "fp64+fp32", "achieved_fp32_tflops": w32 / step_s / 1e12,
+                     "peak_fp32_tflops": peak32, "achieved_fp64_tflops": w64 / step_s / 1e12,
+                     "peak_fp64_tflops": peak64, "frac": bound_s / step_s,
+                     "fp32_flops_per_step": w32, "fp64_flops_per_step": w64},
+    }
+
+
 # ---------------------------------------------------------------------------
 # arms
 # ---------------------------------------------------------------------------
@@ -308,6 +383,9 @@ def run_ours(args, rank, world):
                "sample": f"{cn} molecules of the same workload, reference algorithm (dense "
                          f"eigh, materialised Hartree kernel), {cconv} converged, {dt:.1f} s wall",
                "total_solves_per_s": cn / dt}
+    ksr = None
+    if world == 1 and not args.no_ksr:
+        ksr = run_ksr(args, peak64, peak32, flush)
     serving = None
     if world == 1 and not args.no_serving:
         serving = run_serving(args)
@@ -339,6 +417,8 @@ def run_ours(args, rank, world):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if ksr is not None:
+        line["ksr"] = ksr
     if serving is not None:
         line["serving"] = serving
     return line
@@ -451,6 +531,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-ksr", action="store_true")
     ap.add_argument("--serving-rates", type=float, nargs="*", default=[1000.0, 5000.0])
     ap.add_argument("--serving-seconds", type=float, default=1.0)
     ap.add_argument("--mix-rates", type=float, nargs="*", default=[100.0, 200.0])

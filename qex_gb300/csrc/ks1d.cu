@@ -75,6 +75,7 @@ struct Params {
   const float* ksr_w;  // packed KSR network (device)
   double ksr_lo, ksr_hi;
   int ksr_c;
+  int ksr_slot;  // constant-memory slot holding the network for this launch
   // outputs
   double* o_energy;
   double* o_gap;
@@ -412,18 +413,6 @@ __device__ __noinline__ double xc_eval(const Params& p, int N, double dx, const 
       }
       if (frec) frec[i] = f;
     }
-  } else if (p.xc_kind == QEX_XC_KSR) {
-    if (p.ksr_c == 16) {
-      e = want_v ? ksr_eval<16, true>(p.ksr_w, p.ksr_lo, p.ksr_hi, N, dx, n, local, vout, frec,
-                                      sm.f32, lane)
-                 : ksr_eval<16, false>(p.ksr_w, p.ksr_lo, p.ksr_hi, N, dx, n, local, nullptr,
-                                       frec, sm.f32, lane);
-    } else {
-      e = want_v ? ksr_eval<8, true>(p.ksr_w, p.ksr_lo, p.ksr_hi, N, dx, n, local, vout, frec,
-                                     sm.f32, lane)
-                 : ksr_eval<8, false>(p.ksr_w, p.ksr_lo, p.ksr_hi, N, dx, n, local, nullptr,
-                                      frec, sm.f32, lane);
-    }
   } else {
     // Window MLP: stage n / norm as FP32 with 8 zeros either side; v_xc
     // contributions are accumulated in FP32 shared memory, one window offset
@@ -478,6 +467,34 @@ __device__ __noinline__ double xc_eval(const Params& p, int N, double dx, const 
         vout[i] = local ? v : dx * v;
       }
     }
+  }
+  __syncwarp();
+  if (reflect_xc) {
+    if (want_v) flip_avg_global(vout, N, lane);
+    if (frec) flip_avg_global(frec, N, lane);
+  }
+  return warp_sum(e) * dx;
+}
+
+// The KSR functional's counterpart of xc_eval, called from the kernel body
+// directly: its register footprint then does not add to xc_eval's at the
+// other functionals' call sites.
+__device__ __noinline__ double ksr_xc(const Params& p, int N, double dx, const Smem& sm,
+                                      bool want_v, double* vout, double* frec, bool reflect_xc,
+                                      int lane) {
+  const double* n = sm.s64a + kPad64;
+  const bool local = (p.xc_conv == QEX_XC_LOCAL);
+  double e;
+  if (p.ksr_c == 16) {
+    e = want_v ? ksr_eval<16, true, 1>(p.ksr_w, p.ksr_slot, p.ksr_lo, p.ksr_hi, N, dx, n, local,
+                                    vout, frec, sm.f32, lane)
+               : ksr_eval<16, false, 1>(p.ksr_w, p.ksr_slot, p.ksr_lo, p.ksr_hi, N, dx, n, local,
+                                     nullptr, frec, sm.f32, lane);
+  } else {
+    e = want_v ? ksr_eval<8, true, 1>(p.ksr_w, p.ksr_slot, p.ksr_lo, p.ksr_hi, N, dx, n, local,
+                                   vout, frec, sm.f32, lane)
+               : ksr_eval<8, false, 1>(p.ksr_w, p.ksr_slot, p.ksr_lo, p.ksr_hi, N, dx, n, local,
+                                    nullptr, frec, sm.f32, lane);
   }
   __syncwarp();
   if (reflect_xc) {
@@ -1390,7 +1407,11 @@ __device__ inline void write_stats(const Params& p, int b, const EigStats& e) {
 // ---------------------------------------------------------------------------
 // The kernel
 // ---------------------------------------------------------------------------
-template <int kBand, bool kRes>
+// kKsr: the KSR functional's instantiation.  Its evaluation needs far more
+// registers than the other functionals', and a callee that large anywhere in
+// the call graph makes the whole persistent kernel spill, so only this
+// instantiation calls it.
+template <int kBand, bool kRes, bool kKsr>
 __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__ Params p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x;
@@ -1544,7 +1565,11 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
         }
         __syncwarp();
       }
-      xc_eval(p, N, dx, sm, true, vxc, vf, reflect_xc, lane);
+      if constexpr (kKsr) {
+        ksr_xc(p, N, dx, sm, true, vxc, vf, reflect_xc, lane);
+      } else {
+        xc_eval(p, N, dx, sm, true, vxc, vf, reflect_xc, lane);
+      }
       // |dv_KS|_inf in FP32, rounded up: it only sizes brackets and picks the
       // warm route, both of which are verified
       float dvl = 0.0f;
@@ -1589,7 +1614,12 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
         __syncwarp();
       }
       long long tsub = clock64();
-      const double exc = xc_eval(p, N, dx, sm, false, nullptr, nullptr, false, lane);
+      double exc;
+      if constexpr (kKsr) {
+        exc = ksr_xc(p, N, dx, sm, false, nullptr, nullptr, false, lane);
+      } else {
+        exc = xc_eval(p, N, dx, sm, false, nullptr, nullptr, false, lane);
+      }
       lap(est, tsub, 14);
       const double energy = tee - eks + eh + exc + eext;
       if (p.reflect) flip_avg_global(nout, N, lane);
@@ -2181,28 +2211,38 @@ int launch_adjoint(const Params& P, cudaStream_t stream) {
   return QEX_OK;
 }
 
-template <int kBand, bool kRes>
+template <int kBand, bool kRes, bool kKsr>
 int launch_variant(const Params& P, cudaStream_t stream, size_t smem, int per_sm, int sms) {
-  cudaError_t e =
-      cudaFuncSetAttribute(ks1d_kernel<kBand, kRes>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(ks1d_kernel<kBand, kRes, kKsr>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return QEX_CUDA_ERROR;
   long long grid = (long long)sms * per_sm;
   if (grid > P.num_molecules) grid = P.num_molecules;
   e = cudaMemsetAsync(P.counter, 0, sizeof(int), stream);
   if (e != cudaSuccess) return QEX_CUDA_ERROR;
-  ks1d_kernel<kBand, kRes><<<(unsigned)grid, kWarp, smem, stream>>>(P);
-  if (cudaGetLastError() != cudaSuccess) return QEX_CUDA_ERROR;
+  if constexpr (kKsr) {
+    KsrStage stage(P.ksr_w, 6 * P.ksr_c * P.ksr_c + 2 * P.ksr_c, stream);
+    if (stage.slot() < 0) return QEX_CUDA_ERROR;
+    Params Q = P;
+    Q.ksr_slot = stage.slot();
+    ks1d_kernel<kBand, kRes, kKsr><<<(unsigned)grid, kWarp, smem, stream>>>(Q);
+    if (cudaGetLastError() != cudaSuccess || !stage.finish()) return QEX_CUDA_ERROR;
+  } else {
+    ks1d_kernel<kBand, kRes, kKsr><<<(unsigned)grid, kWarp, smem, stream>>>(P);
+    if (cudaGetLastError() != cudaSuccess) return QEX_CUDA_ERROR;
+  }
   g_last_launches = 1;
   return QEX_OK;
 }
 
-template <int kBand, bool kRes>
+template <int kBand, bool kRes, bool kKsr>
 int blocks_per_sm(size_t smem) {
   int per_sm = 0;
-  if (cudaFuncSetAttribute(ks1d_kernel<kBand, kRes>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess)
+  if (cudaFuncSetAttribute(ks1d_kernel<kBand, kRes, kKsr>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks1d_kernel<kBand, kRes>, kWarp, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks1d_kernel<kBand, kRes, kKsr>, kWarp,
+                                                smem);
   return per_sm;
 }
 
@@ -2220,18 +2260,28 @@ int launch(const Params& P, cudaStream_t stream) {
   const size_t smem_s = smem_layout(P.nmax, P.kmax, false, false).total;
   const size_t smem_r = smem_layout(P.nmax, P.kmax, false, true).total;
   const bool band2 = (P.stencil == 5);
+  if (P.xc_kind == QEX_XC_KSR) {
+    // the KSR instantiation streams its solve planes (one variant per stencil)
+    if ((int)smem_s > max_optin) return QEX_BAD_ARG;
+    int per = band2 ? blocks_per_sm<2, false, true>(smem_s) : blocks_per_sm<1, false, true>(smem_s);
+    if (per < 1) per = 1;
+    return band2 ? launch_variant<2, false, true>(P, stream, smem_s, per, sms)
+                 : launch_variant<1, false, true>(P, stream, smem_s, per, sms);
+  }
   if (P.planes != 2 && (int)smem_r <= max_optin) {
-    const int per_r = band2 ? blocks_per_sm<2, true>(smem_r) : blocks_per_sm<1, true>(smem_r);
+    const int per_r =
+        band2 ? blocks_per_sm<2, true, false>(smem_r) : blocks_per_sm<1, true, false>(smem_r);
     if (per_r >= 1 && (P.planes == 1 || (long long)P.num_molecules <= (long long)sms * per_r)) {
-      return band2 ? launch_variant<2, true>(P, stream, smem_r, per_r, sms)
-                   : launch_variant<1, true>(P, stream, smem_r, per_r, sms);
+      return band2 ? launch_variant<2, true, false>(P, stream, smem_r, per_r, sms)
+                   : launch_variant<1, true, false>(P, stream, smem_r, per_r, sms);
     }
   }
   if (P.planes == 1 || (int)smem_s > max_optin) return QEX_BAD_ARG;
-  int per_s = band2 ? blocks_per_sm<2, false>(smem_s) : blocks_per_sm<1, false>(smem_s);
+  int per_s =
+      band2 ? blocks_per_sm<2, false, false>(smem_s) : blocks_per_sm<1, false, false>(smem_s);
   if (per_s < 1) per_s = 1;
-  return band2 ? launch_variant<2, false>(P, stream, smem_s, per_s, sms)
-               : launch_variant<1, false>(P, stream, smem_s, per_s, sms);
+  return band2 ? launch_variant<2, false, false>(P, stream, smem_s, per_s, sms)
+               : launch_variant<1, false, false>(P, stream, smem_s, per_s, sms);
 }
 
 }  // namespace

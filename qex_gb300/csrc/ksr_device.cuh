@@ -24,6 +24,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <mutex>
+
 #include "ks1d_common.cuh"
 #include "qex_ks1d.h"
 
@@ -45,6 +47,15 @@ struct KsrLayout {
   static constexpr int kWidth = 6 * C * C + 2 * C - 1;
   static constexpr int kParams = 6 * C * C + 2 * C;
 };
+
+// The network of a launch is staged in constant memory (one slot per launch,
+// see KsrStage below) so that every weight is a warp-uniform operand of the
+// FMA that uses it.  Loading the weights per lane (global or shared memory)
+// writes each one into 32 registers, and that register write-back, not the
+// arithmetic, bounded the evaluation.
+constexpr int kKsrSlots = 4;
+constexpr int kKsrSlotFloat4 = (6 * kKsrMaxC * kKsrMaxC + 2 * kKsrMaxC) / 4;
+static __constant__ float4 c_ksr_w[kKsrSlots][kKsrSlotFloat4];
 
 __host__ __device__ inline int ksr_chunks(int n) { return (n + kKsrOwn - 1) / kKsrOwn; }
 
@@ -109,14 +120,14 @@ __device__ __forceinline__ float ksr_sigmoid(float x) { return __fdividef(1.0f, 
 
 // z[o] += sum_t v(p + t - 1) W[t][c][o] for one input channel c (Wc = &W[0][c][0])
 template <int C>
-__device__ __forceinline__ void ksr_conv_in(float (&z)[C], float v, const float4* __restrict__ Wc) {
+__device__ __forceinline__ void ksr_conv_in(float (&z)[C], float v, const float4* Wc) {
   const float vm = __shfl_up_sync(kFull, v, 1);
   const float vp = __shfl_down_sync(kFull, v, 1);
   #pragma unroll
   for (int q = 0; q < C / 4; ++q) {
-    const float4 a = __ldg(Wc + q);
-    const float4 b = __ldg(Wc + C * C / 4 + q);
-    const float4 c = __ldg(Wc + C * C / 2 + q);
+    const float4 a = *(Wc + q);
+    const float4 b = *(Wc + C * C / 4 + q);
+    const float4 c = *(Wc + C * C / 2 + q);
     z[4 * q + 0] = fmaf(vm, a.x, fmaf(v, b.x, fmaf(vp, c.x, z[4 * q + 0])));
     z[4 * q + 1] = fmaf(vm, a.y, fmaf(v, b.y, fmaf(vp, c.y, z[4 * q + 1])));
     z[4 * q + 2] = fmaf(vm, a.z, fmaf(v, b.z, fmaf(vp, c.z, z[4 * q + 2])));
@@ -126,11 +137,11 @@ __device__ __forceinline__ void ksr_conv_in(float (&z)[C], float v, const float4
 
 // sum_o d[o] W[t][c][o] (Wtc = &W[t][c][0])
 template <int C>
-__device__ __forceinline__ float ksr_dot_row(const float (&d)[C], const float4* __restrict__ Wtc) {
+__device__ __forceinline__ float ksr_dot_row(const float (&d)[C], const float4* Wtc) {
   float s = 0.0f;
   #pragma unroll
   for (int q = 0; q < C / 4; ++q) {
-    const float4 a = __ldg(Wtc + q);
+    const float4 a = *(Wtc + q);
     s = fmaf(d[4 * q + 0], a.x, s);
     s = fmaf(d[4 * q + 1], a.y, s);
     s = fmaf(d[4 * q + 2], a.z, s);
@@ -184,19 +195,22 @@ __device__ inline double ksr_setup(const float* __restrict__ w, double lo, doubl
   return beta;
 }
 
-template <int C, bool kWantV>
-__device__ __noinline__ double ksr_eval(const float* __restrict__ w, double lo, double hi, int N,
-                                        double dx, const double* n, bool local, double* vout,
-                                        double* frec, float* scratch, int lane) {
+// kGroup scans are staged and run together (independent shuffle chains that
+// overlap); more groups need more registers, so the SCF kernel, which calls
+// this under its register cap, uses 1 and the standalone evaluator 4.
+template <int C, bool kWantV, int kGroup>
+__device__ __noinline__ double ksr_eval(const float* __restrict__ w, int slot, double lo, double hi,
+                                        int N, double dx, const double* n, bool local,
+                                        double* vout, double* frec, float* scratch, int lane) {
   using Ly = KsrLayout<C>;
   const int K = ksr_chunks(N);
   const KsrScratch S = ksr_carve<C>(scratch, K);
   double dbeta;
   const double beta = ksr_setup<C>(w, lo, hi, N, dx, n, S, K, dbeta, lane);
   const float fb = (float)beta, f1b = (float)(1.0 - beta);
-  const float4* __restrict__ W1 = reinterpret_cast<const float4*>(w + Ly::kW1);
-  const float4* __restrict__ W2 = reinterpret_cast<const float4*>(w + Ly::kW2);
-  const float4* __restrict__ W3 = reinterpret_cast<const float4*>(w + Ly::kW3);
+  const float4* W1 = c_ksr_w[slot] + Ly::kW1 / 4;
+  const float4* W2 = c_ksr_w[slot] + Ly::kW2 / 4;
+  const float4* W3 = c_ksr_w[slot] + Ly::kW3 / 4;
 
   // right carries of the forward scans: chunk k needs R(p0_k + 32), which is
   // lane 32 - kKsrOwn of chunk k + 1
@@ -204,12 +218,27 @@ __device__ __noinline__ double ksr_eval(const float* __restrict__ w, double lo, 
   for (int k = K - 1; k >= 1; --k) {
     const int p = k * kKsrOwn - kKsrHalo + lane;
     const float x = (p >= 0 && p < N) ? (float)n[p] : 0.0f;
+    // kGroup channels per pass, staged in registers: their scan chains overlap
     #pragma unroll 1
-    for (int j = 0; j < Ly::kScans; ++j) {
-      float R = ksr_scan_down(x, S.r[j], lane);
-      R = fmaf(S.pr[j * kWarp + lane], S.rc[k * Ly::kScans + j], R);
-      const float nxt = __shfl_sync(kFull, R, kWarp - kKsrOwn);
-      if (lane == 0) S.rc[(k - 1) * Ly::kScans + j] = nxt;
+    for (int j0 = 0; j0 < Ly::kScans; j0 += kGroup) {
+      float R[kGroup];
+      #pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        const int j = j0 + i;
+        R[i] = S.pr[j * kWarp + lane] * S.rc[k * Ly::kScans + j];
+      }
+      float r[kGroup];
+      #pragma unroll
+      for (int i = 0; i < kGroup; ++i) r[i] = S.r[j0 + i];
+      #pragma unroll
+      for (int i = 0; i < kGroup; ++i) R[i] += ksr_scan_down(x, r[i], lane);
+      float nxt[kGroup];
+      #pragma unroll
+      for (int i = 0; i < kGroup; ++i) nxt[i] = __shfl_sync(kFull, R[i], kWarp - kKsrOwn);
+      if (lane == 0) {
+        #pragma unroll
+        for (int i = 0; i < kGroup; ++i) S.rc[(k - 1) * Ly::kScans + j0 + i] = nxt[i];
+      }
     }
     __syncwarp();
   }
@@ -228,20 +257,39 @@ __device__ __noinline__ double ksr_eval(const float* __restrict__ w, double lo, 
     for (int o = 0; o < C; ++o) z1[o] = 0.0f;
     ksr_conv_in(z1, x, W1);  // channel 0: the density
     float h = 0.0f;
+    // kGroup scans per pass, their tables and carries staged in registers so
+    // their shuffle chains overlap
     #pragma unroll 1
-    for (int j = 0; j < Ly::kScans; ++j) {
-      const float r = S.r[j];
-      float L = ksr_scan_up(x, r, lane);
-      L = fmaf(S.pf[j * kWarp + lane], S.lc[j], L);
-      float R = ksr_scan_down(x, r, lane);
-      R = fmaf(S.pr[j * kWarp + lane], S.rc[k * Ly::kScans + j], R);
-      const float carry = __shfl_sync(kFull, L, kKsrOwn - 1);
-      const float G = S.cf[j] * (L + R - x);
-      if (lane == 0) S.lc[j] = carry;
-      if (j < Ly::kScans - 1) {
-        ksr_conv_in(z1, in ? G : 0.0f, W1 + (j + 1) * (C / 4));
-      } else {
-        h = G;
+    for (int j0 = 0; j0 < Ly::kScans; j0 += kGroup) {
+      float L[kGroup], R[kGroup], r[kGroup];
+      #pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        const int j = j0 + i;
+        r[i] = S.r[j];
+        L[i] = S.pf[j * kWarp + lane] * S.lc[j];
+        R[i] = S.pr[j * kWarp + lane] * S.rc[k * Ly::kScans + j];
+      }
+      #pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        L[i] += ksr_scan_up(x, r[i], lane);
+        R[i] += ksr_scan_down(x, r[i], lane);
+      }
+      float carry[kGroup];
+      #pragma unroll
+      for (int i = 0; i < kGroup; ++i) carry[i] = __shfl_sync(kFull, L[i], kKsrOwn - 1);
+      if (lane == 0) {
+        #pragma unroll
+        for (int i = 0; i < kGroup; ++i) S.lc[j0 + i] = carry[i];
+      }
+      #pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        const int j = j0 + i;
+        const float G = S.cf[j] * (L[i] + R[i] - x);
+        if (j < Ly::kScans - 1) {
+          ksr_conv_in(z1, in ? G : 0.0f, W1 + (j + 1) * (C / 4));
+        } else {
+          h = G;
+        }
       }
     }
     __syncwarp();
@@ -263,7 +311,7 @@ __device__ __noinline__ double ksr_eval(const float* __restrict__ w, double lo, 
         const float4* Wr = W2 + (t * C + c) * (C / 4);
         #pragma unroll
         for (int q = 0; q < C / 4; ++q) {
-          const float4 wv = __ldg(Wr + q);
+          const float4 wv = *(Wr + q);
           qv[4 * q + 0] = fmaf(a[c], wv.x, qv[4 * q + 0]);
           qv[4 * q + 1] = fmaf(a[c], wv.y, qv[4 * q + 1]);
           qv[4 * q + 2] = fmaf(a[c], wv.z, qv[4 * q + 2]);
@@ -277,7 +325,7 @@ __device__ __noinline__ double ksr_eval(const float* __restrict__ w, double lo, 
     float y = 0.0f;
     #pragma unroll
     for (int q = 0; q < C / 4; ++q) {
-      const float4 wv = __ldg(W3 + q);
+      const float4 wv = *(W3 + q);
       a[4 * q + 0] = z2[4 * q + 0] * ksr_sigmoid(z2[4 * q + 0]);
       a[4 * q + 1] = z2[4 * q + 1] * ksr_sigmoid(z2[4 * q + 1]);
       a[4 * q + 2] = z2[4 * q + 2] * ksr_sigmoid(z2[4 * q + 2]);
@@ -305,7 +353,7 @@ __device__ __noinline__ double ksr_eval(const float* __restrict__ w, double lo, 
     float dz[C];
     #pragma unroll
     for (int q = 0; q < C / 4; ++q) {
-      const float4 wv = __ldg(W3 + q);
+      const float4 wv = *(W3 + q);
       const float w4[4] = {wv.x, wv.y, wv.z, wv.w};
       #pragma unroll
       for (int i = 0; i < 4; ++i) {
@@ -344,29 +392,43 @@ __device__ __noinline__ double ksr_eval(const float* __restrict__ w, double lo, 
     }
     const int lo_idx = lane >= kKsrHalo ? lane - kKsrHalo : 0;
     #pragma unroll 1
-    for (int j = 0; j < Ly::kScans; ++j) {
-      float u;
-      if (j < Ly::kScans - 1) {
-        const float4* Wc = W1 + (j + 1) * (C / 4);
-        const float P0 = ksr_dot_row(dz, Wc);
-        const float P1 = ksr_dot_row(dz, Wc + C * C / 4);
-        const float P2 = ksr_dot_row(dz, Wc + C * C / 2);
-        u = __shfl_down_sync(kFull, P0, 1) + P1 + __shfl_up_sync(kFull, P2, 1);
-      } else {
-        u = g;
+    for (int j0 = 0; j0 < Ly::kScans; j0 += kGroup) {
+      float u[kGroup], L[kGroup], T[kGroup], r[kGroup];
+      #pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        const int j = j0 + i;
+        r[i] = S.r[j];
+        L[i] = S.pf[j * kWarp + lo_idx] * S.lb[j];
+        if (j < Ly::kScans - 1) {
+          const float4* Wc = W1 + (j + 1) * (C / 4);
+          const float P0 = ksr_dot_row(dz, Wc);
+          const float P1 = ksr_dot_row(dz, Wc + C * C / 4);
+          const float P2 = ksr_dot_row(dz, Wc + C * C / 2);
+          u[i] = __shfl_down_sync(kFull, P0, 1) + P1 + __shfl_up_sync(kFull, P2, 1);
+        } else {
+          u[i] = g;
+        }
+        u[i] = owned ? u[i] : 0.0f;
       }
-      u = owned ? u : 0.0f;
-      const float r = S.r[j];
-      float L = ksr_scan_up(u, r, lane);
-      L = fmaf(S.pf[j * kWarp + lo_idx], S.lb[j], L);
-      const float T = ksr_scan_down(u, r, lane);
-      const float carry = __shfl_sync(kFull, L, kKsrHalo + kKsrOwn - 1);
-      const float loc = __shfl_sync(kFull, T, kKsrHalo);
+      #pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        L[i] += ksr_scan_up(u[i], r[i], lane);
+        T[i] = ksr_scan_down(u[i], r[i], lane);
+      }
+      float carry[kGroup], loc[kGroup];
+      #pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        carry[i] = __shfl_sync(kFull, L[i], kKsrHalo + kKsrOwn - 1);
+        loc[i] = __shfl_sync(kFull, T[i], kKsrHalo);
+        dn = fmaf(S.cb[j0 + i], L[i] + T[i] - u[i], dn);
+      }
       if (lane == 0) {
-        S.lb[j] = carry;
-        S.rl[k * Ly::kScans + j] = loc;
+        #pragma unroll
+        for (int i = 0; i < kGroup; ++i) {
+          S.lb[j0 + i] = carry[i];
+          S.rl[k * Ly::kScans + j0 + i] = loc[i];
+        }
       }
-      dn = fmaf(S.cb[j], L + T - u, dn);
     }
     __syncwarp();
     if (owned) {
@@ -405,4 +467,77 @@ __device__ __noinline__ double ksr_eval(const float* __restrict__ w, double lo, 
   return e;
 }
 
+// ---------------------------------------------------------------------------
+// Host: constant-slot staging.  A slot belongs to the stream that last used it;
+// launches on that stream re-stage it in stream order.  A slot that changes
+// hands is first waited on (the previous owner's last launch), so concurrent
+// launches on different streams with different networks never share a slot
+// while one of them runs.  Under stream capture the copy is captured with the
+// launch and no cross-stream wait is added (run captured graphs on the stream
+// that captured them).  Each translation unit that includes this header has
+// its own constant array and its own slot table.
+// ---------------------------------------------------------------------------
+// Internal linkage throughout: the staging code must write the constant
+// array of the translation unit whose kernels read it.
+namespace {
+
+struct KsrSlotTable {
+  cudaStream_t owner[kKsrSlots];
+  cudaEvent_t done[kKsrSlots];
+  bool used[kKsrSlots];
+  int next;
+};
+constexpr int kKsrMaxDevices = 64;
+std::mutex g_ksr_mutex;
+KsrSlotTable g_ksr_slots[kKsrMaxDevices];
+
+class KsrStage {
+ public:
+  // Stages nfloats floats of the device buffer `params` for a launch on `stream`.
+  KsrStage(const float* params, int nfloats, cudaStream_t stream)
+      : lock_(g_ksr_mutex), stream_(stream) {
+    if (nfloats > 4 * kKsrSlotFloat4 || cudaGetDevice(&dev_) != cudaSuccess || dev_ < 0 ||
+        dev_ >= kKsrMaxDevices)
+      return;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) return;
+    capturing_ = cap != cudaStreamCaptureStatusNone;
+    KsrSlotTable& t = g_ksr_slots[dev_];
+    int s = -1;
+    for (int i = 0; i < kKsrSlots; ++i)
+      if (t.used[i] && t.owner[i] == stream) s = i;
+    if (s < 0) {
+      s = t.next;
+      t.next = (t.next + 1) % kKsrSlots;
+      if (!t.used[s]) {
+        if (cudaEventCreateWithFlags(&t.done[s], cudaEventDisableTiming) != cudaSuccess) return;
+        t.used[s] = true;
+      } else if (!capturing_ && cudaStreamWaitEvent(stream, t.done[s], 0) != cudaSuccess) {
+        return;
+      }
+      t.owner[s] = stream;
+    }
+    if (cudaMemcpyToSymbolAsync(c_ksr_w, params, sizeof(float) * (size_t)nfloats,
+                                sizeof(float4) * (size_t)kKsrSlotFloat4 * (size_t)s,
+                                cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+      return;
+    slot_ = s;
+  }
+  int slot() const { return slot_; }
+  // Call after the launch that reads the slot.
+  bool finish() {
+    if (slot_ < 0) return false;
+    if (capturing_) return true;
+    return cudaEventRecord(g_ksr_slots[dev_].done[slot_], stream_) == cudaSuccess;
+  }
+
+ private:
+  std::lock_guard<std::mutex> lock_;
+  cudaStream_t stream_;
+  int dev_ = -1;
+  int slot_ = -1;
+  bool capturing_ = false;
+};
+
+}  // namespace
 }  // namespace qex

@@ -130,6 +130,7 @@ struct KsrEvalParams {
   int conv;
   int nmax;
   int channels;
+  int slot;
   const float* w;
   double lo, hi;
 };
@@ -137,9 +138,9 @@ struct KsrEvalParams {
 template <int C>
 __device__ double ksr_one(const KsrEvalParams& p, int N, double dx, long long off, bool local,
                           double* vals, float* scratch, int lane) {
-  return p.potential ? ksr_eval<C, true>(p.w, p.lo, p.hi, N, dx, p.density + off, local,
+  return p.potential ? ksr_eval<C, true, 4>(p.w, p.slot, p.lo, p.hi, N, dx, p.density + off, local,
                                          p.potential + off, vals, scratch, lane)
-                     : ksr_eval<C, false>(p.w, p.lo, p.hi, N, dx, p.density + off, local,
+                     : ksr_eval<C, false, 4>(p.w, p.slot, p.lo, p.hi, N, dx, p.density + off, local,
                                           nullptr, vals, scratch, lane);
 }
 
@@ -206,8 +207,14 @@ int qex_ksr1d_eval(int32_t num_molecules, int32_t max_num_grids, const int32_t* 
   P.w = xc->ksr_params;
   P.lo = xc->ksr_minval;
   P.hi = xc->ksr_maxval;
-  ksr1d_kernel<<<num_molecules, kWarp, smem, static_cast<cudaStream_t>(stream)>>>(P);
-  return cudaGetLastError() == cudaSuccess ? QEX_OK : QEX_CUDA_ERROR;
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  KsrStage stage(xc->ksr_params, 6 * xc->ksr_channels * xc->ksr_channels + 2 * xc->ksr_channels,
+                 s);
+  if (stage.slot() < 0) return QEX_CUDA_ERROR;
+  P.slot = stage.slot();
+  ksr1d_kernel<<<num_molecules, kWarp, smem, s>>>(P);
+  if (cudaGetLastError() != cudaSuccess || !stage.finish()) return QEX_CUDA_ERROR;
+  return QEX_OK;
 }
 
 int qex_xc1d_workspace_size(int64_t total_points, const qex_xc_spec* xc, size_t* bytes) {
