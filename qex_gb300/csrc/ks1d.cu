@@ -2221,7 +2221,7 @@ int launch_variant(const Params& P, cudaStream_t stream, size_t smem, int per_sm
   e = cudaMemsetAsync(P.counter, 0, sizeof(int), stream);
   if (e != cudaSuccess) return QEX_CUDA_ERROR;
   if constexpr (kKsr) {
-    KsrStage stage(P.ksr_w, 6 * P.ksr_c * P.ksr_c + 2 * P.ksr_c, stream);
+    auto stage = ksr_stage(P.ksr_w, 6 * P.ksr_c * P.ksr_c + 2 * P.ksr_c, stream);
     if (stage.slot() < 0) return QEX_CUDA_ERROR;
     Params Q = P;
     Q.ksr_slot = stage.slot();

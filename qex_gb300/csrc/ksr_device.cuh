@@ -26,6 +26,7 @@
 
 #include <mutex>
 
+#include "const_slots.cuh"
 #include "ks1d_common.cuh"
 #include "qex_ks1d.h"
 
@@ -48,11 +49,8 @@ struct KsrLayout {
   static constexpr int kParams = 6 * C * C + 2 * C;
 };
 
-// The network of a launch is staged in constant memory (one slot per launch,
-// see KsrStage below) so that every weight is a warp-uniform operand of the
-// FMA that uses it.  Loading the weights per lane (global or shared memory)
-// writes each one into 32 registers, and that register write-back, not the
-// arithmetic, bounded the evaluation.
+// The network of a launch is staged in constant memory (const_slots.cuh) so
+// that every weight is a warp-uniform operand of the FMA that uses it.
 constexpr int kKsrSlots = 4;
 constexpr int kKsrSlotFloat4 = (6 * kKsrMaxC * kKsrMaxC + 2 * kKsrMaxC) / 4;
 static __constant__ float4 c_ksr_w[kKsrSlots][kKsrSlotFloat4];
@@ -467,77 +465,14 @@ __device__ __noinline__ double ksr_eval(const float* __restrict__ w, int slot, d
   return e;
 }
 
-// ---------------------------------------------------------------------------
-// Host: constant-slot staging.  A slot belongs to the stream that last used it;
-// launches on that stream re-stage it in stream order.  A slot that changes
-// hands is first waited on (the previous owner's last launch), so concurrent
-// launches on different streams with different networks never share a slot
-// while one of them runs.  Under stream capture the copy is captured with the
-// launch and no cross-stream wait is added (run captured graphs on the stream
-// that captured them).  Each translation unit that includes this header has
-// its own constant array and its own slot table.
-// ---------------------------------------------------------------------------
-// Internal linkage throughout: the staging code must write the constant
-// array of the translation unit whose kernels read it.
+// Host: the slot table of this translation unit's KSR constant array.
 namespace {
+ConstSlots<kKsrSlots> g_ksr_const;
 
-struct KsrSlotTable {
-  cudaStream_t owner[kKsrSlots];
-  cudaEvent_t done[kKsrSlots];
-  bool used[kKsrSlots];
-  int next;
-};
-constexpr int kKsrMaxDevices = 64;
-std::mutex g_ksr_mutex;
-KsrSlotTable g_ksr_slots[kKsrMaxDevices];
-
-class KsrStage {
- public:
-  // Stages nfloats floats of the device buffer `params` for a launch on `stream`.
-  KsrStage(const float* params, int nfloats, cudaStream_t stream)
-      : lock_(g_ksr_mutex), stream_(stream) {
-    if (nfloats > 4 * kKsrSlotFloat4 || cudaGetDevice(&dev_) != cudaSuccess || dev_ < 0 ||
-        dev_ >= kKsrMaxDevices)
-      return;
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) return;
-    capturing_ = cap != cudaStreamCaptureStatusNone;
-    KsrSlotTable& t = g_ksr_slots[dev_];
-    int s = -1;
-    for (int i = 0; i < kKsrSlots; ++i)
-      if (t.used[i] && t.owner[i] == stream) s = i;
-    if (s < 0) {
-      s = t.next;
-      t.next = (t.next + 1) % kKsrSlots;
-      if (!t.used[s]) {
-        if (cudaEventCreateWithFlags(&t.done[s], cudaEventDisableTiming) != cudaSuccess) return;
-        t.used[s] = true;
-      } else if (!capturing_ && cudaStreamWaitEvent(stream, t.done[s], 0) != cudaSuccess) {
-        return;
-      }
-      t.owner[s] = stream;
-    }
-    if (cudaMemcpyToSymbolAsync(c_ksr_w, params, sizeof(float) * (size_t)nfloats,
-                                sizeof(float4) * (size_t)kKsrSlotFloat4 * (size_t)s,
-                                cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
-      return;
-    slot_ = s;
-  }
-  int slot() const { return slot_; }
-  // Call after the launch that reads the slot.
-  bool finish() {
-    if (slot_ < 0) return false;
-    if (capturing_) return true;
-    return cudaEventRecord(g_ksr_slots[dev_].done[slot_], stream_) == cudaSuccess;
-  }
-
- private:
-  std::lock_guard<std::mutex> lock_;
-  cudaStream_t stream_;
-  int dev_ = -1;
-  int slot_ = -1;
-  bool capturing_ = false;
-};
-
+// Stages nfloats floats of the device buffer `params` for a launch on `stream`.
+inline ConstStage<kKsrSlots> ksr_stage(const float* params, int nfloats, cudaStream_t stream) {
+  return ConstStage<kKsrSlots>(g_ksr_const, (const void*)&c_ksr_w, sizeof(c_ksr_w[0]), params,
+                               sizeof(float) * (size_t)nfloats, cudaMemcpyDeviceToDevice, stream);
+}
 }  // namespace
 }  // namespace qex

@@ -10,8 +10,9 @@
 
 namespace qex {
 
-// Window-MLP weights, passed by value in kernel parameters so that every
-// weight is a constant-bank operand of the FMA that uses it.
+// Window-MLP weights, carried by value in the kernel parameters and copied
+// into shared memory by each warp.  (Constant-memory slots, which pay off for
+// the larger KSR network, measured 2% slower here.)
 struct MlpParams {
   float w1[QEX_MLP_WINDOW * QEX_MLP_HIDDEN];
   float b1[QEX_MLP_HIDDEN];
@@ -104,6 +105,7 @@ __device__ inline float silu_d(float z, float& d) {
 // scr[k * ss] (k < 17) receives d eps / d input_k on return.
 constexpr int kMlpFloats = 580;  // 577 weights padded to 16 bytes
 constexpr int kMlpScratch = 32;  // h1, then d1 (overwritten in place by g1)
+
 
 __device__ inline void mlp_load4(const float* W, int off, float& a, float& b, float& c, float& d) {
   float4 r = *reinterpret_cast<const float4*>(W + off);
