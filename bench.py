@@ -263,6 +263,57 @@ def run_ksr(args, peak64, peak32, flush):
     }
 
 
+def run_ksr_eval(args):
+    """The KSR network alone (qex_ksr1d_eval, forward and backward, local
+    convention) on args.batch copies of the eight reference H2 densities."""
+    import ctypes
+
+    import torch
+
+    import qex_gb300
+    from qex_gb300 import _native
+    from qex_gb300.od import xc_eval
+
+    lib = xc_eval._lib()
+    k = np.load(os.path.join(ROOT, "tests", "golden", "ksr_h2.npz"))
+    fn = qex_gb300.KSRFunctional(16)
+    spec, keep = fn.spec(ksr_trained_params(), _native.QEX_XC_LOCAL)
+    B = args.batch
+    dens = np.tile(k["densities"], (B // len(k["densities"]) + 1, 1))[:B]
+    dev = torch.device("cuda")
+    d = torch.as_tensor(dens.reshape(-1), device=dev)
+    ng = torch.full((B,), 513, dtype=torch.int32, device=dev)
+    off = torch.arange(B, dtype=torch.int64, device=dev) * 513
+    dx = torch.full((B,), 0.08, dtype=torch.float64, device=dev)
+    vals, pot = torch.empty_like(d), torch.empty_like(d)
+    en = torch.empty(B, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+    st = ctypes.c_void_p(stream.cuda_stream)
+
+    def run():
+        _native.check(lib.qex_ksr1d_eval(B, 513, ng.data_ptr(), off.data_ptr(), dx.data_ptr(),
+                                         ctypes.byref(spec), d.data_ptr(), vals.data_ptr(),
+                                         pot.data_ptr(), en.data_ptr(), st), "qex_ksr1d_eval")
+
+    for _ in range(args.warmup):
+        run()
+    times = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = sorted(times)[len(times) // 2]
+    flops = (3351 + 3414) * 513 * B
+    _, peak32 = _native.measure_fma_peak()
+    del keep
+    return {"workload": f"KSR network forward+backward, {B} densities x 513 points",
+            "ms": t * 1e3, "achieved_fp32_tflops": flops / t / 1e12, "peak_fp32_tflops": peak32,
+            "frac": flops / t / 1e12 / peak32}
+
+
 # ---------------------------------------------------------------------------
 # arms
 # ---------------------------------------------------------------------------
@@ -532,6 +583,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-ksr", action="store_true")
+    ap.add_argument("--ksr-only", action="store_true",
+                    help="time only the KSR SCF workload (profiling)")
+    ap.add_argument("--ksr-eval", action="store_true",
+                    help="time only the standalone KSR network evaluation (profiling)")
     ap.add_argument("--serving-rates", type=float, nargs="*", default=[1000.0, 5000.0])
     ap.add_argument("--serving-seconds", type=float, default=1.0)
     ap.add_argument("--mix-rates", type=float, nargs="*", default=[100.0, 200.0])
@@ -545,6 +600,19 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         torch.distributed.init_process_group("nccl")
+    if args.ksr_only or args.ksr_eval:
+        import torch
+
+        from qex_gb300 import _native
+
+        _native.load()
+        if args.ksr_eval:
+            print(json.dumps({"ksr_eval": run_ksr_eval(args)}), flush=True)
+        else:
+            peak64, peak32 = _native.measure_fma_peak()
+            flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+            print(json.dumps({"ksr": run_ksr(args, peak64, peak32, flush)}), flush=True)
+        return
     line = run_ours(args, rank, world) if args.impl == "ours" else run_reference(args, rank, world)
     if line is not None:
         print(json.dumps(line), flush=True)

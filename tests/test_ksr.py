@@ -246,3 +246,28 @@ def test_ragged_ksr_batch_matches_oracle(qx):
             assert _l2(dens[i], ref["density"][-1], 0.08) < D32
             checked += 1
         assert checked >= 4
+
+
+@pytest.mark.gpu
+def test_reference_binding_through_jit_scf(qx, golden):
+    """The reference's binding: the model's apply_fn bound to its params with
+    Partial and passed to jax_dft's kohn_sham (qedft/train/od/train.py:96-122)."""
+    qex, od = qx
+    from qex_gb300 import networks
+
+    k = golden["ksr"]
+    grids = k["grids"]
+    _, _, apply_fn = networks.create_ksr_model_from_config(grids)
+    row = 1
+    i = int(k["scf_index"][row])
+    ve = o.get_atomic_chain_potential(grids, k["locations"][i], k["nuclear_charges"][i],
+                                      o.exponential_coulomb)
+    n0 = o.solve_noninteracting_system(ve, 2, grids, 5)[0]
+    st = od.jit_scf.kohn_sham(k["locations"][i], k["nuclear_charges"][i], 2, 15, grids,
+                              qex.Partial(apply_fn, params=_trained(golden)),
+                              od.utils.exponential_coulomb, n0,
+                              enforce_reflection_symmetry=True, num_mixing_iterations=1)
+    np.testing.assert_allclose(st.total_energy, k["scf_total_energy"][row], atol=E32, rtol=0)
+    assert _l2(st.density[-1], k["scf_final_density"][row], 0.08) < D32
+    eps = apply_fn(k["densities"][1], _trained(golden))
+    np.testing.assert_allclose(eps, k["eps_1"], atol=2e-6, rtol=0)
