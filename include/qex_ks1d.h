@@ -209,7 +209,8 @@ int qex_ks1d_noninteracting(const qex_ks1d_batch* batch, const qex_ks1d_options*
  * mixing factor alpha_t.  Outputs: the gradient with respect to n_t (packed)
  * and, ACCUMULATED into grad_params (B, QEX_MLP_NUM_PARAMS), the gradient
  * with respect to the window-MLP parameters.  Window-MLP XC in the local
- * convention, exponential interaction, one mixing difference. */
+ * convention, exponential interaction, one mixing difference; reflection
+ * symmetry (enforce_reflection_symmetry) on or off. */
 int qex_ks1d_adjoint_workspace_size(const qex_ks1d_options* options, int32_t num_molecules,
                                     size_t* bytes);
 int qex_ks1d_adjoint_step(const qex_ks1d_batch* batch, const qex_ks1d_options* options,

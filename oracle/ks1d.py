@@ -658,6 +658,20 @@ def config3_loss(energies, densities, target_energies, target_densities, grids,
     return float(np.sum(e * e) + density_weight * np.sum(d * d) * dx)
 
 
+def reference_training_loss(energies, final_densities, target_energy, target_density, grids,
+                            num_electrons, discount=0.9, ks_iter_to_ignore=10):
+    """The reference's training loss, ``qedft/train/od/train.py:296-318``: the
+    discounted trajectory MSE of the energies from ``ks_iter_to_ignore`` on,
+    over Ne, plus the MSE of the final densities times dx N, over Ne (jax_dft
+    ``losses``, restated in ``qedft/train/od/losses_no_jit.py:8-102``)."""
+    grids = np.asarray(grids, dtype=np.float64)
+    e = np.asarray(energies, dtype=np.float64)[:, ks_iter_to_ignore:]
+    loss = trajectory_mse(target_energy, e, discount) / num_electrons
+    d = np.asarray(target_density, dtype=np.float64) - np.asarray(final_densities, dtype=np.float64)
+    loss += float(np.mean(d * d)) * get_dx(grids) * grids.size / num_electrons
+    return float(loss)
+
+
 def trajectory_mse(target, predict, discount):
     """Discounted trajectory MSE (jax_dft ``losses.trajectory_mse``; ``qedft/train/od/train.py:296-302``).
 

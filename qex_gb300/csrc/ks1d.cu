@@ -1966,10 +1966,19 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
       }
       __syncwarp();
     }
-    // forward quantities at n_t
+    // forward quantities at n_t.  With reflection symmetry (jax_dft
+    // kohn_sham_iteration) the XC functional sees s = P n with
+    // P = (I + flip) / 2 and its outputs are flip-averaged; P is linear and
+    // self-adjoint, so the reverse pass below applies P to the same places.
+    const bool refl = p.reflect != 0;
     stage64(sm.s64a, vn, N, lane);
     hartree(p, N, dx, sm, vh, kt, lane);
-    xc_eval(p, N, dx, sm, true, vxc, nullptr, false, lane);
+    if (refl) {
+      #pragma unroll 1
+      for (int i = lane; i < N; i += kWarp) sm.s64a[kPad64 + i] = 0.5 * (vn[i] + vn[N - 1 - i]);
+      __syncwarp();
+    }
+    xc_eval(p, N, dx, sm, true, vxc, nullptr, refl, lane);
     #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) vks[i] = vh[i] + vxc[i] + vext[i];
     __syncwarp();
@@ -1990,26 +1999,44 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
     if (gE != 0.0) {
       stage64(sm.s64a, nout, N, lane);
       hartree(p, N, dx, sm, t1, kt, lane);
-      xc_eval(p, N, dx, sm, true, t2, nullptr, false, lane);
+      if (refl) {
+        #pragma unroll 1
+        for (int i = lane; i < N; i += kWarp)
+          sm.s64a[kPad64 + i] = 0.5 * (nout[i] + nout[N - 1 - i]);
+        __syncwarp();
+      }
+      xc_eval(p, N, dx, sm, true, t2, nullptr, refl, lane);
     }
+    // the mixing reads the reflected output density: its cotangent is P gnext
     #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) {
-      double g = at * p.a_gnext[off + i];
+      const double gx = refl ? 0.5 * (p.a_gnext[off + i] + p.a_gnext[off + N - 1 - i])
+                             : p.a_gnext[off + i];
+      double g = at * gx;
       if (gE != 0.0) g += gE * dx * (t1[i] + t2[i] + vext[i] - vks[i]);
       gm[i] = g;
     }
     __syncwarp();
     if (gE != 0.0) {
+      // E_xc = dx sum eps_i(s) s_i at s = P m (s = m without reflection)
+      const double* sm_out = nout;
+      if (refl) {
+        #pragma unroll 1
+        for (int i = lane; i < N; i += kWarp) t1[i] = 0.5 * (nout[i] + nout[N - 1 - i]);
+        __syncwarp();
+        sm_out = t1;
+      }
       const float ninv = p.mlp.norm_inv;
       #pragma unroll 1
       for (int i = lane; i < N + 2 * kPadMlp; i += kWarp) {
         const int k = i - kPadMlp;
-        n32[i] = (k >= 0 && k < N) ? (float)nout[k] * ninv : 0.0f;
+        n32[i] = (k >= 0 && k < N) ? (float)sm_out[k] * ninv : 0.0f;
         gacc[i] = 0.0f;
       }
       __syncwarp();
-      // ybar_i = gE dx m_i (local convention E_xc = dx sum eps_i m_i); no tangent
-      mlp_adjoint_pass(p, N, n32, n32, false, nout, gE * dx, nout, gacc, gn, rec, sm, acc, lane);
+      // ybar_i = gE dx s_i (local convention E_xc = dx sum eps_i s_i); no tangent
+      mlp_adjoint_pass(p, N, n32, n32, false, sm_out, gE * dx, sm_out, gacc, gn, rec, sm, acc,
+                       lane);
     }
     // ---- gv = chi gm
     sternheimer<kBand>(p, N, dx, ne, vks, X, gm, Y, Bv, gv, sm, lane);
@@ -2019,20 +2046,42 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
     #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) gn[i] = (1.0 - at) * p.a_gnext[off + i] + t1[i];
     {
+      // with reflection: v_xc(n) . u = v(s) . (P u), s = P n, and the gradient
+      // with respect to s goes back through P; vh and vxc are free here
+      const double* sv = vn;
+      const double* uv = gv;
+      double* xg = gn;
+      if (refl) {
+        #pragma unroll 1
+        for (int i = lane; i < N; i += kWarp) {
+          vh[i] = 0.5 * (vn[i] + vn[N - 1 - i]);
+          vxc[i] = 0.5 * (gv[i] + gv[N - 1 - i]);
+          t2[i] = 0.0;
+        }
+        __syncwarp();
+        sv = vh;
+        uv = vxc;
+        xg = t2;
+      }
       const float ninv = p.mlp.norm_inv;
       #pragma unroll 1
       for (int i = lane; i < N + 2 * kPadMlp; i += kWarp) {
         const int k = i - kPadMlp;
-        n32[i] = (k >= 0 && k < N) ? (float)vn[k] * ninv : 0.0f;
-        u32[i] = (k >= 0 && k < N) ? (float)gv[k] * ninv : 0.0f;
+        n32[i] = (k >= 0 && k < N) ? (float)sv[k] * ninv : 0.0f;
+        u32[i] = (k >= 0 && k < N) ? (float)uv[k] * ninv : 0.0f;
         gacc[i] = 0.0f;
       }
       __syncwarp();
       // local convention: v_xc(n) . u = sum_i [eps_i u_i + n_i D eps_i[u window]]
-      mlp_adjoint_pass(p, N, n32, u32, true, gv, 1.0, vn, gacc, gn, rec, sm, acc, lane);
+      mlp_adjoint_pass(p, N, n32, u32, true, uv, 1.0, sv, gacc, xg, rec, sm, acc, lane);
       #pragma unroll 1
-      for (int i = lane; i < N; i += kWarp) gn[i] += (double)gacc[i + kPadMlp];
+      for (int i = lane; i < N; i += kWarp) xg[i] += (double)gacc[i + kPadMlp];
       __syncwarp();
+      if (refl) {
+        #pragma unroll 1
+        for (int i = lane; i < N; i += kWarp) gn[i] += 0.5 * (t2[i] + t2[N - 1 - i]);
+        __syncwarp();
+      }
     }
     #pragma unroll 1
     for (int i = lane; i < N; i += kWarp) p.a_gn[off + i] = gn[i];
@@ -2396,8 +2445,8 @@ int qex_ks1d_adjoint_step(const qex_ks1d_batch* batch, const qex_ks1d_options* o
       !grad_params)
     return QEX_BAD_ARG;
   if (xc->kind != QEX_XC_WINDOW_MLP || xc->convention != QEX_XC_LOCAL) return QEX_BAD_ARG;
-  if (options->interaction != QEX_INTERACTION_EXPONENTIAL || options->enforce_reflection_symmetry ||
-      options->external_potential_given || options->num_mixing_iterations != 1)
+  if (options->interaction != QEX_INTERACTION_EXPONENTIAL || options->external_potential_given ||
+      options->num_mixing_iterations != 1)
     return QEX_BAD_ARG;
   size_t need = 0;
   int rc = qex_ks1d_adjoint_workspace_size(options, batch->num_molecules, &need);

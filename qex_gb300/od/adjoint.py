@@ -1,10 +1,16 @@
 """Hand-written adjoint of the unrolled 1D SCF (the differentiation configuration).
 
-Loss (per batch): L = sum_b (E_b - E*_b)^2 + w sum_b ||n_b - n*_b||^2 dx, with
-E the last iteration's total energy and n the final mixed density; gradient
-with respect to the window-MLP parameters (what ``jax.value_and_grad`` over
-the scanned SCF gives at ``qedft/train/od/trainer.py:139-143``, with the loss
-of ``qedft/train/od/train.py:250-323`` replaced by this one).
+Losses (``Config3Loss``, ``TrajectoryLoss``), both functions of the
+per-iteration total energies and the final mixed density:
+  * the differentiation configuration's L = sum_b (E_b - E*_b)^2
+    + w sum_b ||n_b - n*_b||^2 dx on the last iteration;
+  * the reference's training loss (``qedft/train/od/train.py:250-323``):
+    the discounted trajectory MSE of the energies from iteration
+    ``ks_iter_to_ignore`` on, over Ne, plus the final-density MSE times dx N,
+    over Ne.
+The gradient is with respect to the window-MLP parameters: what
+``jax.value_and_grad`` over the scanned SCF gives at
+``qedft/train/od/trainer.py:139-143``.
 
 Forward: segments of ``checkpoint_every`` iterations, keeping only the input
 density of each segment.  Backward: each segment is recomputed from its
@@ -29,6 +35,70 @@ _ADJ_SIG = (ctypes.c_int, [ctypes.POINTER(N.Ks1dBatch), ctypes.POINTER(N.Ks1dOpt
                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p])
 
 
+class Config3Loss:
+    """L = sum_b (E_b,T-1 - E*_b)^2 + w sum_b ||n_b - n*_b||^2 dx."""
+
+    def __init__(self, density_weight=0.1):
+        self.w = float(density_weight)
+
+    def value(self, energies, final, t_e, t_n, dx_pts, ne, ne_pts):
+        de = energies[:, -1] - t_e
+        dn = final - t_n
+        return float((de * de).sum() + self.w * (dn * dn * dx_pts).sum())
+
+    def grad_density(self, final, t_n, dx_pts, ne_pts, batch_size):
+        return 2.0 * self.w * (final - t_n) * dx_pts
+
+    def grad_energy(self, t, energies, t_e, ne):
+        T = energies.shape[1]
+        return 2.0 * (energies[:, T - 1] - t_e) if t == T - 1 else None
+
+
+class TrajectoryLoss:
+    """The reference's training loss (``qedft/train/od/train.py:296-318`` with
+    jax_dft ``losses.trajectory_mse`` / ``mean_square_error``, restated in
+    ``qedft/train/od/losses_no_jit.py:8-102``):
+
+      L = mean_b sum_k d^(K-1-k) (E_b,ig+k - E*_b)^2 / Ne
+        + mean_b,i (n_b,i - n*_b,i)^2 dx N / Ne,        K = T - ig,
+
+    ig = ``ks_iter_to_ignore``, d = ``discount``; Ne per molecule (the
+    reference's datasets hold one Ne), and the density mean taken per molecule
+    (sum_i (dn)^2 dx / Ne, averaged over the batch), which is the reference's
+    mean over (B, N) times dx N when all molecules share N."""
+
+    def __init__(self, discount=0.9, ks_iter_to_ignore=10):
+        self.discount = float(discount)
+        self.ignore = int(ks_iter_to_ignore)
+
+    def weights(self, T):
+        K = T - self.ignore
+        if K < 1:
+            raise ValueError("ks_iter_to_ignore leaves no iterations in the loss")
+        return self.discount ** np.arange(K - 1, -1, -1, dtype=np.float64)
+
+    def value(self, energies, final, t_e, t_n, dx_pts, ne, ne_pts):
+        import torch
+
+        B, T = energies.shape
+        w = torch.as_tensor(self.weights(T), device=energies.device)
+        de = energies[:, self.ignore:] - t_e[:, None]
+        traj = (((de * de) * w[None, :]).sum(dim=1) / ne).sum() / B
+        dn = final - t_n
+        dens = (dn * dn * dx_pts / ne_pts).sum() / B
+        return float(traj + dens)
+
+    def grad_density(self, final, t_n, dx_pts, ne_pts, batch_size):
+        return 2.0 * (final - t_n) * dx_pts / ne_pts / batch_size
+
+    def grad_energy(self, t, energies, t_e, ne):
+        B, T = energies.shape
+        if t < self.ignore:
+            return None
+        w = self.weights(T)[t - self.ignore]
+        return 2.0 * w * (energies[:, t] - t_e) / ne / B
+
+
 @dataclasses.dataclass
 class AdjointResult:
     loss: float
@@ -51,10 +121,21 @@ class Ks1dAdjoint:
 
     def value_and_grad(self, batch: PackedBatch, xc, cfg: SolveConfig, target_energy,
                        target_density, density_weight: float = 0.1,
-                       checkpoint_every: int = 5) -> AdjointResult:
+                       checkpoint_every: int = 5, loss=None,
+                       initial_density=None) -> AdjointResult:
+        """Loss and gradient; ``loss`` is a ``Config3Loss`` (the default, with
+        ``density_weight``) or a ``TrajectoryLoss``.  Reflection symmetry
+        (``cfg.enforce_reflection_symmetry``) is differentiated as well.
+        ``initial_density`` (packed) defaults to the non-interacting density
+        of v_ext (jax_dft ``get_initial_density(..., 'noninteracting')``)."""
         torch = N.require_cuda()
         if cfg.convention != "local" or cfg.num_mixing_iterations != 1:
             raise ValueError("the adjoint covers the local convention with one mixing difference")
+        if cfg.density_mse_converge_tolerance > 0:
+            raise ValueError("the adjoint differentiates the fixed-iteration SCF "
+                             "(density_mse_converge_tolerance <= 0)")
+        if loss is None:
+            loss = Config3Loss(density_weight)
         functional, params = resolve(xc)
         spec, keep = functional.spec(params, _convention(cfg))
         dev = batch.device
@@ -64,11 +145,19 @@ class Ks1dAdjoint:
                                        batch.num_grids_host), device=dev)
         t_e = torch.as_tensor(np.asarray(target_energy, np.float64), device=dev)
         t_n = torch.as_tensor(np.asarray(target_density, np.float64), device=dev)
+        ne_host = np.array([m.num_electrons for m in batch.molecules], dtype=np.float64)
+        ne = torch.as_tensor(ne_host, device=dev)
+        ne_pts = torch.as_tensor(np.repeat(ne_host, batch.num_grids_host), device=dev)
 
-        # initial density: non-interacting ground state of v_ext
-        one = SolveConfig(**{**dataclasses.asdict(cfg), "num_iterations": 1})
-        out1 = self.engine.solve(batch, xc, one, records=("external_potential",), bucketed=False)
-        n0, _, _, _ = self.engine.noninteracting(batch, out1["external_potential"], cfg.stencil)
+        if initial_density is not None:
+            n0 = torch.as_tensor(np.asarray(initial_density, np.float64), device=dev).contiguous()
+        else:
+            # non-interacting ground state of v_ext
+            one = SolveConfig(**{**dataclasses.asdict(cfg), "num_iterations": 1})
+            out1 = self.engine.solve(batch, xc, one, records=("external_potential",),
+                                     bucketed=False)
+            n0, _, _, _ = self.engine.noninteracting(batch, out1["external_potential"],
+                                                     cfg.stencil)
 
         def segment(n_start, t0, steps, records):
             c = SolveConfig(**{**dataclasses.asdict(cfg), "num_iterations": steps,
@@ -87,13 +176,10 @@ class Ks1dAdjoint:
             energies[:, t0:t0 + steps] = out["energy"]
             n = out["final_density"].clone()
         status = out["status"].clone()
-        e_last = energies[:, T - 1]
-        de = e_last - t_e
-        dn = n - t_n
-        loss = float((de * de).sum() + density_weight * (dn * dn * dx).sum())
+        loss_value = loss.value(energies, n, t_e, t_n, dx, ne, ne_pts)
 
         # ---- backward
-        gnext = (2.0 * density_weight * dn * dx).contiguous()
+        gnext = loss.grad_density(n, t_n, dx, ne_pts, B).contiguous()
         genergy = torch.zeros(B, dtype=torch.float64, device=dev)
         gtheta = torch.zeros((B, N.MLP_NUM_PARAMS), dtype=torch.float64, device=dev)
         gn = torch.empty_like(gnext)
@@ -123,8 +209,9 @@ class Ks1dAdjoint:
             for k in range(steps - 1, -1, -1):
                 t = t0 + k
                 genergy.zero_()
-                if t == T - 1:
-                    genergy.copy_(2.0 * de)
+                ge = loss.grad_energy(t, energies, t_e, ne)
+                if ge is not None:
+                    genergy.copy_(ge)
                 alpha_t = cfg.alpha * cfg.alpha_decay ** t
                 rc = self.lib.qex_ks1d_adjoint_step(
                     ctypes.byref(cb), ctypes.byref(opts), ctypes.byref(spec),
@@ -138,5 +225,6 @@ class Ks1dAdjoint:
         grad = gtheta.sum(dim=0)
         torch.cuda.current_stream().synchronize()
         del keep
-        return AdjointResult(loss=loss, grad=grad.cpu().numpy(), energies=energies.cpu().numpy(),
+        return AdjointResult(loss=loss_value, grad=grad.cpu().numpy(),
+                             energies=energies.cpu().numpy(),
                              final_density=n.cpu().numpy(), status=status.cpu().numpy())
