@@ -314,6 +314,45 @@ def run_ksr_eval(args):
             "frac": flops / t / 1e12 / peak32}
 
 
+def run_fermi_eval(args):
+    """Fermi-Dirac occupation search (``qex_td_fermi_occupations``, stable mode,
+    100 damped Newton steps at most) on args.batch spectra of 220 orbitals,
+    against the oracle's per-spectrum loop on the host."""
+    import torch
+
+    from qex_gb300.td import fermi
+
+    rng = np.random.default_rng(args.seed)
+    B, n = args.batch, 220
+    e = np.sort(rng.uniform(-3.0, 3.0, (B, n)), axis=1)
+    ne = 2.0 * rng.integers(1, n // 2, B)
+    ed = torch.as_tensor(e, device="cuda")
+    nd = torch.as_tensor(ne, device="cuda")
+    for _ in range(args.warmup):
+        fermi.get_fractional_occupations_jax_stable(ed, nd, 0.04, None, 0.0, 0.6, 100)
+    stream = torch.cuda.current_stream()
+    times = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fermi.get_fractional_occupations_jax_stable(ed, nd, 0.04, None, 0.0, 0.6, 100)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = sorted(times)[len(times) // 2]
+    from oracle import td as otd
+
+    k = min(B, 64)
+    t0 = time.perf_counter()
+    for i in range(k):
+        otd.get_fractional_occupations_jax_stable(e[i], float(ne[i]), 0.04, None, 0.0, 0.6, 100)
+    cpu = (time.perf_counter() - t0) / k
+    return {"workload": f"Fermi occupations, {B} spectra x {n} orbitals, theta 0.04",
+            "ms": t * 1e3, "spectra_per_s": B / t,
+            "cpu_baseline": {"spectra_per_s": 1.0 / cpu, "cores": 1, "kind": "port",
+                             "sample": f"{k} spectra, oracle loop"}}
+
+
 # ---------------------------------------------------------------------------
 # arms
 # ---------------------------------------------------------------------------
@@ -587,6 +626,8 @@ def main():
                     help="time only the KSR SCF workload (profiling)")
     ap.add_argument("--ksr-eval", action="store_true",
                     help="time only the standalone KSR network evaluation (profiling)")
+    ap.add_argument("--fermi-eval", action="store_true",
+                    help="time only the Fermi-Dirac occupation search")
     ap.add_argument("--serving-rates", type=float, nargs="*", default=[1000.0, 5000.0])
     ap.add_argument("--serving-seconds", type=float, default=1.0)
     ap.add_argument("--mix-rates", type=float, nargs="*", default=[100.0, 200.0])
@@ -600,6 +641,12 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         torch.distributed.init_process_group("nccl")
+    if args.fermi_eval:
+        from qex_gb300 import _native
+
+        _native.load()
+        print(json.dumps({"fermi_eval": run_fermi_eval(args)}), flush=True)
+        return
     if args.ksr_only or args.ksr_eval:
         import torch
 

@@ -17,6 +17,10 @@
  *                            qedft/train/td/generalized_eigensolver.py:264-330
  *   qex_td_make_rdm1      <- make_rdm1, qedft/train/td/hf.py:303-308 and
  *                            qedft/train/td/scf_functions_masked.py:290-303
+ *   qex_td_fermi_occupations <- optimize_fermi_occupations /
+ *                            get_fractional_occupations_jax /
+ *                            get_fractional_occupations_jax_stable,
+ *                            qedft/train/td/fermi.py:145-219, 301-390, 393-497
  *   qex_td_diis_error     <- get_diis_error, qedft/train/td/jax_diis.py:107-114
  *   qex_td_diis_extrapolate <- update_diis_state + extrapolate_fock,
  *                            qedft/train/td/jax_diis.py:26-104
@@ -80,6 +84,20 @@ size_t qex_td_gen_eigh_workspace_size(int32_t batch, int32_t n);
 int qex_td_gen_eigh(int32_t batch, int32_t n, const double* A, const double* S, double* w,
                     double* V, int32_t* status, void* workspace, size_t workspace_bytes,
                     void* stream);
+
+/* Fermi-Dirac occupations of `batch` orbital spectra (mo_energy: (batch, n),
+ * n_electrons: (batch)), by damped Newton steps on the chemical potential.
+ * mode 0: stop once (N - sum occ)^2 < 1e-9, status QEX_NOT_CONVERGED when it
+ * ends above 1e-2 (start mo_energy[0] + mu_shift); mode 1: min(max_steps, 100)
+ * steps (same start); mode 2: start at the HOMO/LUMO midpoint, fall back to
+ * theta = 0.01 when the count misses by 1e-2.  mu_initial (batch) or NULL.
+ * Outputs: occ (batch, n); mu, entropic_energy (theta sum 2[f ln f +
+ * (1-f) ln(1-f)]), loss and status (batch), any of these four may be NULL. */
+int qex_td_fermi_occupations(int32_t batch, int32_t n, const double* mo_energy,
+                             const double* n_electrons, double theta, const double* mu_initial,
+                             double mu_shift, double step_grad, int32_t max_steps, int32_t mode,
+                             double* occ, double* mu, double* entropic_energy, double* loss,
+                             int32_t* status, void* stream);
 
 /* D = C diag(occ) C^T for `batch` matrices (C: (batch, n, n), occ: (batch, n)). */
 int qex_td_make_rdm1(int32_t batch, int32_t n, const double* C, const double* occ, double* D,

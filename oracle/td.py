@@ -262,6 +262,149 @@ def masked_generalized_eigh(fock, s1e, mask):
 # Occupations, density matrix, DIIS, energies
 # ----------------------------------------------------------------------------
 
+# ----------------------------------------------------------------------------
+# Fractional (Fermi-Dirac) occupations, qedft/train/td/fermi.py
+# ----------------------------------------------------------------------------
+
+def fermi_function4entropy(energy, mu, theta):
+    """1 / (1 + exp((e - mu) / theta)) (``qedft/train/td/fermi.py:13-29``)."""
+    with np.errstate(over="ignore"):  # exp -> inf gives the limit 0
+        return 1.0 / (1.0 + np.exp((np.asarray(energy, np.float64) - mu) / theta))
+
+
+def fermi_function(energy, mu, theta):
+    """2 / (1 + exp((e - mu) / theta)), restricted occupation (``fermi.py:32-50``)."""
+    return 2.0 * fermi_function4entropy(energy, mu, theta)
+
+
+def _fermi_count(mu, mo_energy, theta):
+    """F = sum occ and its first two mu-derivatives."""
+    s = fermi_function4entropy(mo_energy, mu, theta)
+    q = s * (1.0 - s)
+    return (float(np.sum(2.0 * s)), float(np.sum(2.0 * q)) / theta,
+            float(np.sum(2.0 * q * (1.0 - 2.0 * s))) / (theta * theta))
+
+
+def loss_fermi_function(mu, mo_energy, n, theta):
+    """(N - sum occ)^2 (``fermi.py:53-78``)."""
+    return (n - _fermi_count(mu, mo_energy, theta)[0]) ** 2
+
+
+def _loss_derivatives(mu, mo_energy, n, theta):
+    """d/dmu and d2/dmu2 of the loss (what jax.grad gives at ``fermi.py:142-143``)."""
+    f, f1, f2 = _fermi_count(mu, mo_energy, theta)
+    r = n - f
+    return -2.0 * r * f1, 2.0 * f1 * f1 - 2.0 * r * f2
+
+
+def make_occ_fermi(mu, mo_energy, theta):
+    """``fermi.py:81-100``."""
+    return fermi_function(mo_energy, mu, theta)
+
+
+def entropy(f):
+    """f ln f + (1 - f) ln(1 - f) (``fermi.py:103-115``), with 0 ln 0 = 0 (the
+    reference's expression evaluates to NaN where an occupation is exactly 0 or 1)."""
+    f = np.asarray(f, np.float64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        a = np.where(f > 0.0, f * np.log(np.where(f > 0.0, f, 1.0)), 0.0)
+        b = np.where(f < 1.0, (1.0 - f) * np.log(np.where(f < 1.0, 1.0 - f, 1.0)), 0.0)
+    return a + b
+
+
+def etropic_energy_contribution(mu, mo_energy, theta):
+    """theta sum 2 entropy(f) (``fermi.py:118-139``)."""
+    return float(theta * np.sum(2.0 * entropy(fermi_function4entropy(mo_energy, mu, theta))))
+
+
+def optimize_fermi_occupations(mo_energy, n_electrons, theta=0.04, mu_initial=None,
+                               mu_shift=0.001, step_grad=0.6, max_steps=100, tol=1e-9):
+    """Damped Newton on the chemical potential, stopping once the loss is below
+    ``tol``; ValueError if it ends above 1e-2 (``fermi.py:145-219``)."""
+    e = np.asarray(mo_energy, np.float64)
+    mu = float(e[0] + mu_shift) if mu_initial is None else float(mu_initial)
+    loss = 100.0
+    for _ in range(int(max_steps)):
+        g, gg = _loss_derivatives(mu, e, n_electrons, theta)
+        safe = 1e-10 * np.sign(gg) if abs(gg) < 1e-10 else gg
+        mu = mu - step_grad * g / safe
+        loss = loss_fermi_function(mu, e, n_electrons, theta)
+        if loss < tol:
+            break
+    if loss > 1e-2:
+        raise ValueError(f"Fermi occupation optimization failed: loss={loss}.")
+    return make_occ_fermi(mu, e, theta), etropic_energy_contribution(mu, e, theta), mu, loss
+
+
+def get_fractional_occupations(mo_energy, n_electrons, frac_mo_occ=1, frac_theta=0.04,
+                               frac_mu=None, frac_mu_shift=0.001, frac_step_grad=0.6,
+                               frac_max_steps=100):
+    """``fermi.py:222-298``: 1 -> Fermi-Dirac, an array -> given, None -> aufbau
+    with a fractional remainder."""
+    e = np.asarray(mo_energy, np.float64)
+    if isinstance(frac_mo_occ, (int, float)) and not isinstance(frac_mo_occ, bool) \
+            and frac_mo_occ == 1:
+        return optimize_fermi_occupations(e, n_electrons, frac_theta, frac_mu, frac_mu_shift,
+                                          frac_step_grad, frac_max_steps)
+    if isinstance(frac_mo_occ, np.ndarray):
+        return frac_mo_occ, 0.0, None, None
+    if frac_mo_occ is None:
+        occ = np.zeros_like(e)
+        rem = float(n_electrons)
+        for i in range(e.size):
+            if rem >= 2.0:
+                occ[i], rem = 2.0, rem - 2.0
+            elif rem > 0.0:
+                occ[i], rem = rem, 0.0
+            else:
+                break
+        return occ, 0.0, None, None
+    raise ValueError(f"frac_mo_occ={frac_mo_occ} not implemented")
+
+
+def get_fractional_occupations_jax(mo_energy, n_electrons, theta, frac_mu, frac_mu_shift,
+                                   frac_step_grad, frac_max_steps):
+    """Fixed number of damped Newton steps, min(frac_max_steps, 100), no early
+    stop (``fermi.py:301-390``)."""
+    e = np.asarray(mo_energy, np.float64)
+    mu = float(e[0] + frac_mu_shift) if frac_mu is None else float(frac_mu)
+    loss = 1.0
+    for _ in range(min(int(frac_max_steps), 100)):
+        g, gg = _loss_derivatives(mu, e, n_electrons, theta)
+        safe = np.sign(gg) * max(abs(gg), 1e-10)
+        mu = mu - frac_step_grad * g / safe
+        loss = loss_fermi_function(mu, e, n_electrons, theta)
+    return (make_occ_fermi(mu, e, theta), etropic_energy_contribution(mu, e, theta), mu, loss)
+
+
+def get_fractional_occupations_jax_stable(mo_energy, n_electrons, theta, frac_mu, frac_mu_shift,
+                                          frac_step_grad, frac_max_steps):
+    """Newton from the HOMO/LUMO midpoint; if the electron count misses by 1e-2
+    or more, 10 fixed-point steps at theta = 0.01 from the midpoint instead
+    (``fermi.py:393-497``).  Loss reported as 0."""
+    e = np.asarray(mo_energy, np.float64)
+    n = e.size
+    n_double = int(np.floor(n_electrons / 2.0))
+    rem = n_electrons - 2.0 * n_double
+    homo = max(n_double - 1, 0)
+    lumo = min(n_double + (1 if rem > 0 else 0), n - 1)
+    default_mu = 0.5 * (e[homo] + e[lumo])
+    mu = default_mu if frac_mu is None else float(frac_mu)
+    for _ in range(min(int(frac_max_steps), 100)):
+        g, gg = _loss_derivatives(mu, e, n_electrons, theta)
+        safe = 1e-10 if abs(gg) < 1e-10 else gg
+        mu = mu - frac_step_grad * g / safe
+    occ = make_occ_fermi(mu, e, theta)
+    if abs(np.sum(occ) - n_electrons) < 1e-2:
+        return occ, etropic_energy_contribution(mu, e, theta), mu, 0.0
+    small = 0.01
+    mu_fb = default_mu
+    for _ in range(10):
+        mu_fb = mu_fb - 0.1 * (np.sum(make_occ_fermi(mu_fb, e, small)) - n_electrons)
+    return (make_occ_fermi(mu_fb, e, small), etropic_energy_contribution(mu_fb, e, small),
+            mu_fb, 0.0)
+
+
 def get_occ(nelectron, mo_energy):
     """Aufbau, 2 electrons in each of the lowest Ne/2 orbitals
     (``qedft/train/td/scf_functions_masked.py:176-186``)."""
@@ -320,10 +463,13 @@ def energy_tot(dm, h1e, J, exc, e_nuc):
     return float(np.einsum("ij,ji->", dm, h1e) + 0.5 * np.einsum("ij,ij->", dm, J) + exc + e_nuc)
 
 
-def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, nn=None, vwn=False):
+def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, nn=None, vwn=False, fermi=None):
     """Fixed-cycle SCF of ``qedft/train/td/scf_functions_masked.py:907-967`` with
     the low-rank Coulomb model and the LDA exchange, or with ``nn = (flat,
-    scale, dtype)`` the neural functional."""
+    scale, dtype)`` the neural functional.  ``fermi`` (a dict: theta, mode
+    "stable" (default) / "jax" / "optimize", max_steps, step_grad, mu_shift, mu) replaces
+    the aufbau occupations by Fermi-Dirac ones (``qedft/train/td/fermi.py``);
+    the per-cycle entropic energies are then returned as a fourth value."""
     ao, w = mol.ao, mol.weights
     if nn is None:
         def rks(ao, w, dm):
@@ -332,21 +478,42 @@ def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, nn=None, vwn=Fals
         def rks(ao, w, dm):
             return nr_rks_nn(ao, w, dm, *nn)
     s1e, h1e = mol.s1e, mol.h1e
+
+    def occupations(mo_e):
+        if fermi is None:
+            return get_occ(mol.nelectron, mo_e), 0.0
+        args = (mo_e, float(mol.nelectron), fermi.get("theta", 0.04), fermi.get("mu"),
+                fermi.get("mu_shift", 0.001), fermi.get("step_grad", 0.6),
+                fermi.get("max_steps", 100))
+        mode = fermi.get("mode", "stable")
+        if mode == "jax":
+            occ, entr, _, _ = get_fractional_occupations_jax(*args)
+        elif mode == "stable":
+            occ, entr, _, _ = get_fractional_occupations_jax_stable(*args)
+        else:
+            occ, entr, _, _ = optimize_fermi_occupations(mo_e, float(mol.nelectron), args[2],
+                                                         args[3], args[4], args[5], args[6])
+        return occ, entr
+
     e0, c0 = generalized_eigh(h1e, s1e)
-    dm = make_rdm1(c0, get_occ(mol.nelectron, e0))
+    dm = make_rdm1(c0, occupations(e0)[0])
     J = coulomb_lowrank(mol.eri_factors, dm)
     _, exc, vxc = rks(ao, w, dm)
     vhf = J + vxc
     diis = DIIS(diis_max_vec)
-    energies = []
+    energies, entropic = [], []
     for cycle in range(max_cycle):
         fock = h1e + vhf
         if cycle >= diis_start_cycle:
             fock = diis.update(fock, dm, s1e)
         mo_e, mo_c = generalized_eigh(fock, s1e)
-        dm = make_rdm1(mo_c, get_occ(mol.nelectron, mo_e))
+        occ, entr = occupations(mo_e)
+        entropic.append(entr)
+        dm = make_rdm1(mo_c, occ)
         J = coulomb_lowrank(mol.eri_factors, dm)
         _, exc, vxc = rks(ao, w, dm)
         vhf = J + vxc
         energies.append(energy_tot(dm, h1e, J, exc, mol.energy_nuc))
+    if fermi is not None:
+        return np.array(energies), dm, mo_e, np.array(entropic)
     return np.array(energies), dm, mo_e

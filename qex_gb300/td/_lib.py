@@ -23,6 +23,9 @@ SIGNATURES = {
     "qex_td_gen_eigh_workspace_size": (_sz, [_i32, _i32]),
     "qex_td_gen_eigh": (ctypes.c_int, [_i32, _i32, _v, _v, _v, _v, _v, _v, _sz, _v]),
     "qex_td_make_rdm1": (ctypes.c_int, [_i32, _i32, _v, _v, _v, _v]),
+    "qex_td_fermi_occupations": (ctypes.c_int, [_i32, _i32, _v, _v, ctypes.c_double, _v,
+                                                ctypes.c_double, ctypes.c_double, _i32, _i32,
+                                                _v, _v, _v, _v, _v, _v]),
     "qex_td_diis_error": (ctypes.c_int, [_i32, _v, _v, _v, _v, _v, _sz, _v]),
     "qex_td_diis_extrapolate": (ctypes.c_int, [_i32, _i32, _i32, _v, _v, _v, _v, _v]),
     "qex_td_coulomb": (ctypes.c_int, [_i32, _i32, _v, _v, _v, _v, _sz, _v]),

@@ -107,15 +107,37 @@ class ScfResult:
     mo_energy: object
     mo_coeff: object
     status: object
+    entropic_energy: object = None  # (max_cycle,) with Fermi occupations
+    mo_occ: object = None
 
 
 def energy_tot(dm, h1e, J, excsum, energy_nuc):
     return (dm * h1e.T).sum() + 0.5 * (dm * J).sum() + excsum + energy_nuc
 
 
-def run_scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, diis_min_vecs=2, xc="LDA"):
+def _fermi_occ(nelectron, mo_energy, fermi):
+    from .fermi import _run
+
+    occ, entr, _, _, _ = _run(mo_energy, float(nelectron), fermi.get("theta", 0.04),
+                              fermi.get("mu"), fermi.get("mu_shift", 0.001),
+                              fermi.get("step_grad", 0.6), fermi.get("max_steps", 100),
+                              {"optimize": 0, "jax": 1, "stable": 2}[fermi.get("mode", "stable")])
+    return occ, entr
+
+
+def run_scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, diis_min_vecs=2, xc="LDA",
+            fermi=None):
     """Fixed-cycle SCF for one synthetic molecule (factored Coulomb; the LDA
-    exchange, or a ``numint.NeuralXC`` functional as ``xc``)."""
+    exchange, or a ``numint.NeuralXC`` functional as ``xc``).
+
+    ``fermi``: None for aufbau occupations, or a dict (``theta``, ``mode`` in
+    "stable" (the default: Newton from the HOMO/LUMO midpoint) / "jax" /
+    "optimize" (both start just above the lowest orbital and stall when the
+    gaps are many theta wide), ``max_steps``, ``step_grad``, ``mu_shift``,
+    ``mu``) for Fermi-Dirac occupations in every cycle (``qedft/train/td/fermi.py``,
+    the ``frac_*`` options of ``qedft/config/default_config_td.yaml``); the
+    density matrix then spans all orbitals and the cycle's entropic energy
+    theta sum 2[f ln f + (1-f) ln(1-f)] is returned beside the energy."""
     torch = N.require_cuda()
     ao = _dev(mol.ao, torch.float64)
     w = _dev(mol.weights, torch.float64)
@@ -124,7 +146,14 @@ def run_scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, diis_min_vecs
     fac = _dev(mol.eri_factors, torch.float64)
     n = s1e.shape[0]
     e0, c0 = generalized_eigh(h1e, s1e)
-    dm = make_rdm1(c0, get_occ(mol.nelectron, e0))
+
+    def occupations(mo_e):
+        if fermi is None:
+            return get_occ(mol.nelectron, mo_e), None
+        return _fermi_occ(mol.nelectron, mo_e, fermi)
+
+    occ, _ = occupations(e0)
+    dm = make_rdm1(c0, occ)
 
     def veff(dm):
         J = coulomb(fac, dm)
@@ -135,6 +164,7 @@ def run_scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, diis_min_vecs
     diis = DIIS(n, diis_max_vec, diis_min_vecs)
     energies = torch.empty(max_cycle, dtype=torch.float64, device="cuda")
     status = torch.zeros(max_cycle, dtype=torch.int32, device="cuda")
+    entropic = torch.zeros(max_cycle, dtype=torch.float64, device="cuda") if fermi else None
     mo_e = mo_c = None
     for cycle in range(max_cycle):
         fock = h1e + vhf
@@ -142,7 +172,10 @@ def run_scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, diis_min_vecs
             fock = diis.update(fock, dm, s1e)
         mo_e, mo_c, st = generalized_eigh(fock, s1e, return_status=True)
         status[cycle] = st
-        dm = make_rdm1(mo_c, get_occ(mol.nelectron, mo_e))
+        occ, entr = occupations(mo_e)
+        if entr is not None:
+            entropic[cycle] = entr
+        dm = make_rdm1(mo_c, occ)
         vhf, J, exc = veff(dm)
         energies[cycle] = energy_tot(dm, h1e, J, exc, mol.energy_nuc)
-    return ScfResult(energies, dm, mo_e, mo_c, status)
+    return ScfResult(energies, dm, mo_e, mo_c, status, entropic, occ)
