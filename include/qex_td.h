@@ -17,6 +17,13 @@
  *                            qedft/train/td/generalized_eigensolver.py:264-330
  *   qex_td_make_rdm1      <- make_rdm1, qedft/train/td/hf.py:303-308 and
  *                            qedft/train/td/scf_functions_masked.py:290-303
+ *   qex_td_eval_ao_deriv1 <- eval_gto 'GTOval_cart_deriv1' (ao_deriv = 1 in the GGA
+ *                            branch of nr_rks, qedft/train/td/numint_legacy.py:175-177)
+ *   qex_td_rho_gga        <- make_rho(..., "GGA"), numint_legacy.py:180, 351-397
+ *   qex_td_gga_pbe_x      <- eval_xc for a GGA functional + _rks_gga_wv0,
+ *                            numint_legacy.py:181-193 (PBE exchange, restated)
+ *   qex_td_vxc_gga        <- _scale_ao(ao, wv) + _dot_ao_ao + (V + V^T),
+ *                            numint_legacy.py:194-196, 337
  *   qex_td_fermi_occupations <- optimize_fermi_occupations /
  *                            get_fractional_occupations_jax /
  *                            get_fractional_occupations_jax_stable,
@@ -98,6 +105,27 @@ int qex_td_fermi_occupations(int32_t batch, int32_t n, const double* mo_energy,
                              double mu_shift, double step_grad, int32_t max_steps, int32_t mode,
                              double* occ, double* mu, double* entropic_energy, double* loss,
                              int32_t* status, void* stream);
+
+/* GGA numint.  ao4: (4, G, nao) AO values then d/dx, d/dy, d/dz;
+ * rho4: (4, G) rho then its gradient; wv: (4, G) the GGA potential weights
+ * 0.5 w de/drho and 2 w de/dsigma grad rho. */
+int qex_td_eval_ao_deriv1(int64_t num_points, const double* coords, int32_t num_shells,
+                          const double* centers, const int32_t* l, const int32_t* prim_offset,
+                          const int32_t* ao_offset, const double* exponents,
+                          const double* coefficients, int32_t nao, double* ao4, void* stream);
+size_t qex_td_rho_gga_workspace_size(int64_t num_points, int32_t nao);
+int qex_td_rho_gga(int64_t num_points, int32_t nao, const double* ao4, const double* dm,
+                   double* rho4, void* workspace, size_t workspace_bytes, void* stream);
+/* PBE exchange (spin-unpolarised): exc (G, per particle; may be NULL), wv,
+ * sums[0] = sum w rho, sums[1] = sum w rho exc (deterministic). */
+size_t qex_td_gga_pbe_x_workspace_size(int64_t num_points);
+int qex_td_gga_pbe_x(int64_t num_points, const double* rho4, const double* weights, double* exc,
+                     double* wv, double* sums, void* workspace, size_t workspace_bytes,
+                     void* stream);
+/* vmat = M + M^T, M = ao0^T (sum_n wv_n o ao_n). */
+size_t qex_td_vxc_gga_workspace_size(int64_t num_points, int32_t nao);
+int qex_td_vxc_gga(int64_t num_points, int32_t nao, const double* ao4, const double* wv,
+                   double* vmat, void* workspace, size_t workspace_bytes, void* stream);
 
 /* D = C diag(occ) C^T for `batch` matrices (C: (batch, n, n), occ: (batch, n)). */
 int qex_td_make_rdm1(int32_t batch, int32_t n, const double* C, const double* occ, double* D,

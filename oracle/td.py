@@ -116,6 +116,57 @@ def vwn5_c(rho):
     return np.where(ok, eps, 0.0), np.where(ok, v, 0.0)
 
 
+def pbe_x(rho, sigma):
+    """PBE exchange, spin-unpolarised (Perdew, Burke, Ernzerhof, PRL 77, 3865
+    (1996); libxc's GGA_X_PBE): e = A rho^(4/3) F(s^2), F(u) = 1 + kappa -
+    kappa / (1 + mu u / kappa), s = |grad rho| / (2 (3 pi^2)^(1/3) rho^(4/3)).
+    Returns (exc per particle, vrho = de/drho, vsigma = de/dsigma)."""
+    rho = np.asarray(rho, dtype=np.float64)
+    sigma = np.asarray(sigma, dtype=np.float64)
+    A = -0.75 * (3.0 / math.pi) ** (1.0 / 3.0)
+    kappa, mu = 0.804, 0.2195149727645171
+    cs = 1.0 / (4.0 * (3.0 * math.pi ** 2) ** (2.0 / 3.0))
+    ok = rho > 1e-14
+    r = np.where(ok, rho, 1.0)
+    r13 = np.cbrt(r)
+    r43 = r * r13
+    u = cs * sigma / (r43 * r43)
+    den = kappa + mu * u
+    F = 1.0 + kappa - kappa * kappa / den
+    dF = kappa * kappa * mu / (den * den)
+    exc = A * r13 * F
+    vr = A * r13 * (4.0 / 3.0 * F - 8.0 / 3.0 * u * dF)
+    vs = A * cs * dF / r43
+    return np.where(ok, exc, 0.0), np.where(ok, vr, 0.0), np.where(ok, vs, 0.0)
+
+
+def eval_rho_gga(ao4, dm):
+    """(4, G): rho and grad rho (make_rho "GGA", ``numint_legacy.py:180``;
+    pyscf eval_rho with c0 = ao0 D, rho_q = 2 sum c0 ao_q)."""
+    c0 = ao4[0] @ dm
+    out = np.empty((4, ao4.shape[1]))
+    out[0] = np.einsum("gi,gi->g", c0, ao4[0])
+    for q in range(1, 4):
+        out[q] = 2.0 * np.einsum("gi,gi->g", c0, ao4[q])
+    return out
+
+
+def nr_rks_gga(ao4, weights, dm):
+    """The GGA branch of ``qedft/train/td/numint_legacy.py:175-198`` with PBE
+    exchange: wv0 = 0.5 w vrho, wv_q = 2 w vsigma drho/dq (``_rks_gga_wv0``),
+    aow = sum_n wv_n ao_n (``_scale_ao``), vmat = ao0^T aow + transpose (:337)."""
+    rho = eval_rho_gga(ao4, dm)
+    sigma = np.sum(rho[1:] ** 2, axis=0)
+    exc, vrho, vsigma = pbe_x(rho[0], sigma)
+    den = rho[0] * weights
+    wv = np.empty((4, rho.shape[1]))
+    wv[0] = 0.5 * weights * vrho
+    wv[1:] = 2.0 * weights * vsigma * rho[1:]
+    aow = np.einsum("npi,np->pi", ao4, wv)
+    vmat = ao4[0].T @ aow
+    return den.sum(), float(np.dot(den, exc)), vmat + vmat.T
+
+
 def nr_rks_lda(ao, weights, dm, vwn=False):
     """(nelec, excsum, vmat) of ``qedft/train/td/numint_legacy.py:122-164,337``:
     aow = 0.5 * w * vrho * ao; vmat = ao^T aow; vmat += vmat^T."""
@@ -463,15 +514,23 @@ def energy_tot(dm, h1e, J, exc, e_nuc):
     return float(np.einsum("ij,ji->", dm, h1e) + 0.5 * np.einsum("ij,ij->", dm, J) + exc + e_nuc)
 
 
-def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, nn=None, vwn=False, fermi=None):
+def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, nn=None, vwn=False, fermi=None,
+        gga=False):
     """Fixed-cycle SCF of ``qedft/train/td/scf_functions_masked.py:907-967`` with
     the low-rank Coulomb model and the LDA exchange, or with ``nn = (flat,
     scale, dtype)`` the neural functional.  ``fermi`` (a dict: theta, mode
     "stable" (default) / "jax" / "optimize", max_steps, step_grad, mu_shift, mu) replaces
     the aufbau occupations by Fermi-Dirac ones (``qedft/train/td/fermi.py``);
-    the per-cycle entropic energies are then returned as a fourth value."""
+    the per-cycle entropic energies are then returned as a fourth value.
+    ``gga=True`` uses the GGA branch with PBE exchange (``nr_rks_gga``)."""
     ao, w = mol.ao, mol.weights
-    if nn is None:
+    if gga:
+        ao = eval_ao(mol.shells, mol.coords, deriv=1)
+        ao = np.concatenate([ao[0][None], ao[1]], axis=0)
+
+        def rks(ao, w, dm):
+            return nr_rks_gga(ao, w, dm)
+    elif nn is None:
         def rks(ao, w, dm):
             return nr_rks_lda(ao, w, dm, vwn=vwn)
     else:

@@ -23,6 +23,14 @@ SIGNATURES = {
     "qex_td_gen_eigh_workspace_size": (_sz, [_i32, _i32]),
     "qex_td_gen_eigh": (ctypes.c_int, [_i32, _i32, _v, _v, _v, _v, _v, _v, _sz, _v]),
     "qex_td_make_rdm1": (ctypes.c_int, [_i32, _i32, _v, _v, _v, _v]),
+    "qex_td_eval_ao_deriv1": (ctypes.c_int, [_i64, _v, _i32, _v, _v, _v, _v, _v, _v, _i32, _v,
+                                             _v]),
+    "qex_td_rho_gga_workspace_size": (_sz, [_i64, _i32]),
+    "qex_td_rho_gga": (ctypes.c_int, [_i64, _i32, _v, _v, _v, _v, _sz, _v]),
+    "qex_td_gga_pbe_x_workspace_size": (_sz, [_i64]),
+    "qex_td_gga_pbe_x": (ctypes.c_int, [_i64, _v, _v, _v, _v, _v, _v, _sz, _v]),
+    "qex_td_vxc_gga_workspace_size": (_sz, [_i64, _i32]),
+    "qex_td_vxc_gga": (ctypes.c_int, [_i64, _i32, _v, _v, _v, _v, _sz, _v]),
     "qex_td_fermi_occupations": (ctypes.c_int, [_i32, _i32, _v, _v, ctypes.c_double, _v,
                                                 ctypes.c_double, ctypes.c_double, _i32, _i32,
                                                 _v, _v, _v, _v, _v, _v]),

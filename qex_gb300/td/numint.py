@@ -176,9 +176,86 @@ def vxc_matrix(ao, weights, vrho):
     return vmat
 
 
+GGA_CODES = ("PBE_X", "GGA_X_PBE")
+
+
+def eval_ao_deriv1(mol, coords=None):
+    """(4, G, nao): AO values and their x, y, z derivatives (pyscf's ao_deriv = 1
+    layout, as the GGA branch of ``numint_legacy.py:175-177`` requests)."""
+    torch = N.require_cuda()
+    L = _lib.lib()
+    coords = _dev(mol.coords if coords is None else coords, torch.float64)
+    centers, l, poff, aoff, ex, co = mol.shell_arrays()
+    G = coords.shape[0]
+    ao4 = torch.empty((4, G, mol.nao), dtype=torch.float64, device="cuda")
+    args = [_dev(x) for x in (centers, l, poff, aoff, ex, co)]
+    N.check(L.qex_td_eval_ao_deriv1(G, _lib.p(coords), len(mol.shells),
+                                    *[_lib.p(a) for a in args], mol.nao, _lib.p(ao4),
+                                    _lib.stream()), "qex_td_eval_ao_deriv1")
+    return ao4
+
+
+def eval_rho_gga(ao4, dm):
+    """(4, G): rho and its gradient (make_rho "GGA", ``numint_legacy.py:180,351-397``)."""
+    torch = N.require_cuda()
+    L = _lib.lib()
+    ao4 = _dev(ao4, torch.float64)
+    dm = _dev(dm, torch.float64)
+    _, G, n = ao4.shape
+    ws = torch.empty(max(L.qex_td_rho_gga_workspace_size(G, n), 8), dtype=torch.uint8,
+                     device="cuda")
+    rho4 = torch.empty((4, G), dtype=torch.float64, device="cuda")
+    N.check(L.qex_td_rho_gga(G, n, _lib.p(ao4), _lib.p(dm), _lib.p(rho4), _lib.p(ws), ws.numel(),
+                             _lib.stream()), "qex_td_rho_gga")
+    return rho4
+
+
+def eval_xc_pbe_x(rho4, weights):
+    """PBE exchange on the grid: (exc, wv, nelec, excsum), wv the GGA potential
+    weights of ``_rks_gga_wv0`` (0.5 w vrho, 2 w vsigma grad rho)."""
+    torch = N.require_cuda()
+    L = _lib.lib()
+    G = rho4.shape[1]
+    w = _dev(weights, torch.float64)
+    exc = torch.empty(G, dtype=torch.float64, device="cuda")
+    wv = torch.empty((4, G), dtype=torch.float64, device="cuda")
+    sums = torch.empty(2, dtype=torch.float64, device="cuda")
+    ws = torch.empty(max(L.qex_td_gga_pbe_x_workspace_size(G), 8), dtype=torch.uint8,
+                     device="cuda")
+    N.check(L.qex_td_gga_pbe_x(G, _lib.p(rho4), _lib.p(w), _lib.p(exc), _lib.p(wv), _lib.p(sums),
+                               _lib.p(ws), ws.numel(), _lib.stream()), "qex_td_gga_pbe_x")
+    return exc, wv, sums[0], sums[1]
+
+
+def vxc_matrix_gga(ao4, wv):
+    """ao0^T (sum_n wv_n o ao_n) + transpose (``numint_legacy.py:194-196,337``)."""
+    torch = N.require_cuda()
+    L = _lib.lib()
+    _, G, n = ao4.shape
+    ws = torch.empty(max(L.qex_td_vxc_gga_workspace_size(G, n), 8), dtype=torch.uint8,
+                     device="cuda")
+    vmat = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    N.check(L.qex_td_vxc_gga(G, n, _lib.p(ao4), _lib.p(wv), _lib.p(vmat), _lib.p(ws), ws.numel(),
+                             _lib.stream()), "qex_td_vxc_gga")
+    return vmat
+
+
+def nr_rks_gga(ao4, weights, dm, xc_code="PBE_X"):
+    """(nelec, excsum, vmat) of the GGA branch of ``numint_legacy.py:175-198``."""
+    code = xc_code.upper().replace(" ", "")
+    if code not in GGA_CODES:
+        raise NotImplementedError(f"GGA xc_code {xc_code!r}: the GPU path implements PBE exchange")
+    rho4 = eval_rho_gga(ao4, dm)
+    _, wv, nelec, excsum = eval_xc_pbe_x(rho4, weights)
+    return nelec, excsum, vxc_matrix_gga(ao4, wv)
+
+
 def nr_rks(ao, weights, dm, xc_code="LDA"):
-    """(nelec, excsum, vmat) (``numint_legacy.py:122-164,337``) for the LDA exchange
-    or, with a ``NeuralXC`` as ``xc_code``, the neural functional (``xc.py:57-87``)."""
+    """(nelec, excsum, vmat) (``numint_legacy.py:122-164,337``) for the LDA exchange,
+    with a ``NeuralXC`` as ``xc_code`` the neural functional (``xc.py:57-87``),
+    or a GGA code ("PBE_X") with ``ao`` the (4, G, nao) values and gradients."""
+    if isinstance(xc_code, str) and xc_code.upper().replace(" ", "") in GGA_CODES:
+        return nr_rks_gga(ao, weights, dm, xc_code)
     rho = eval_rho(ao, dm)
     if isinstance(xc_code, NeuralXC):
         exc, vrho, nelec, excsum = eval_xc_nn(rho, xc_code, weights)

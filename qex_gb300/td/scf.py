@@ -138,8 +138,11 @@ def run_scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, diis_min_vecs
     the ``frac_*`` options of ``qedft/config/default_config_td.yaml``); the
     density matrix then spans all orbitals and the cycle's entropic energy
     theta sum 2[f ln f + (1-f) ln(1-f)] is returned beside the energy."""
+    from .numint import GGA_CODES, eval_ao_deriv1
+
     torch = N.require_cuda()
-    ao = _dev(mol.ao, torch.float64)
+    gga = isinstance(xc, str) and xc.upper().replace(" ", "") in GGA_CODES
+    ao = eval_ao_deriv1(mol) if gga else _dev(mol.ao, torch.float64)
     w = _dev(mol.weights, torch.float64)
     s1e = _dev(mol.s1e, torch.float64)
     h1e = _dev(mol.h1e, torch.float64)
