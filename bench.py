@@ -353,6 +353,37 @@ def run_fermi_eval(args):
                              "sample": f"{k} spectra, oracle loop"}}
 
 
+def run_grid_eval(args):
+    """Becke/Stratmann molecular grid (level 3) for seeded synthetic molecules of
+    8 and 20 atoms: GPU build time, against the oracle's NumPy partition."""
+    import torch
+
+    from oracle import td as otd
+    from qex_gb300.td import grids, workloads
+
+    out = {}
+    for na in (8, 20):
+        m = workloads.synthetic_molecule(na, seed=na, with_integrals=False)
+        g = grids.Grids(m)
+        for _ in range(args.warmup):
+            g.build()
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            g.build()
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        t = sorted(times)[len(times) // 2]
+        t0 = time.perf_counter()
+        otd.becke_grid(m.charges, m.positions, 3)
+        cpu = time.perf_counter() - t0
+        out[f"atoms_{na}"] = {"points": int(g.weights.numel()), "ms": t * 1e3,
+                              "cpu_baseline_ms": cpu * 1e3, "cpu_cores": 1}
+    return {"workload": "Becke/Stratmann grid, level 3 (host tables + GPU partition), "
+                        "wall time per build", **out}
+
+
 # ---------------------------------------------------------------------------
 # arms
 # ---------------------------------------------------------------------------
@@ -628,6 +659,8 @@ def main():
                     help="time only the standalone KSR network evaluation (profiling)")
     ap.add_argument("--fermi-eval", action="store_true",
                     help="time only the Fermi-Dirac occupation search")
+    ap.add_argument("--grid-eval", action="store_true",
+                    help="time only the molecular grid build")
     ap.add_argument("--serving-rates", type=float, nargs="*", default=[1000.0, 5000.0])
     ap.add_argument("--serving-seconds", type=float, default=1.0)
     ap.add_argument("--mix-rates", type=float, nargs="*", default=[100.0, 200.0])
@@ -641,6 +674,12 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         torch.distributed.init_process_group("nccl")
+    if args.grid_eval:
+        from qex_gb300 import _native
+
+        _native.load()
+        print(json.dumps({"grid_eval": run_grid_eval(args)}), flush=True)
+        return
     if args.fermi_eval:
         from qex_gb300 import _native
 

@@ -24,6 +24,9 @@
  *                            numint_legacy.py:181-193 (PBE exchange, restated)
  *   qex_td_vxc_gga        <- _scale_ao(ao, wv) + _dot_ao_ao + (V + V^T),
  *                            numint_legacy.py:194-196, 337
+ *   qex_td_becke_grid     <- pyscf.dft.gen_grid.Grids(mol).build() with
+ *                            becke_scheme = stratmann, as used at
+ *                            qedft/data_io/td/dataset_generation.py:139-142
  *   qex_td_fermi_occupations <- optimize_fermi_occupations /
  *                            get_fractional_occupations_jax /
  *                            get_fractional_occupations_jax_stable,
@@ -126,6 +129,18 @@ int qex_td_gga_pbe_x(int64_t num_points, const double* rho4, const double* weigh
 size_t qex_td_vxc_gga_workspace_size(int64_t num_points, int32_t nao);
 int qex_td_vxc_gga(int64_t num_points, int32_t nao, const double* ao4, const double* wv,
                    double* vmat, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Molecular grid: atom a contributes num_radial[a] x num_angular points
+ * (atom_point_offset[a], packed atom by atom), x = R_a + r_i u_j with weight
+ * w_i w_j times Becke's partition P_a / sum_b P_b.  radial_weights include
+ * r^2 dr, angular_weights sum to 4 pi.  size_adjust (natom x natom) is Becke's
+ * a_bc or NULL; scheme 0 Becke's switching function, 1 Stratmann's. */
+int qex_td_becke_grid(int32_t natom, const double* atom_xyz, const double* size_adjust,
+                      const int64_t* atom_point_offset, const int32_t* num_radial,
+                      const int64_t* radial_offset, const double* radial_nodes,
+                      const double* radial_weights, int32_t num_angular,
+                      const double* angular_nodes, const double* angular_weights, int32_t scheme,
+                      int64_t num_points, double* coords, double* weights, void* stream);
 
 /* D = C diag(occ) C^T for `batch` matrices (C: (batch, n, n), occ: (batch, n)). */
 int qex_td_make_rdm1(int32_t batch, int32_t n, const double* C, const double* occ, double* D,

@@ -576,3 +576,95 @@ def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, nn=None, vwn=Fals
     if fermi is not None:
         return np.array(energies), dm, mo_e, np.array(entropic)
     return np.array(energies), dm, mo_e
+
+
+# ----------------------------------------------------------------------------
+# Molecular grids (pyscf gen_grid.Grids with becke_scheme = stratmann, as the
+# reference builds them at qedft/data_io/td/dataset_generation.py:139-142)
+# ----------------------------------------------------------------------------
+
+_BRAGG = {1: 0.35, 2: 1.40, 3: 1.45, 4: 1.05, 5: 0.85, 6: 0.70, 7: 0.65, 8: 0.60, 9: 0.50,
+          10: 1.50}
+_XI = {1: 0.8, 2: 0.9, 3: 1.8, 4: 1.4, 5: 1.3, 6: 1.1, 7: 0.9, 8: 0.9, 9: 0.9, 10: 0.9}
+_RAD = ((10, 30, 40, 50, 60, 70, 80, 90, 100, 200), (15, 40, 60, 75, 90, 105, 120, 135, 150, 200))
+_ANG = (6, 8, 10, 12, 14, 16, 18, 20, 22, 24)
+
+
+def radial_m4(n, xi):
+    """Treutler-Ahlrichs M4 mapping r = xi/ln2 (1+x)^0.6 ln(2/(1-x)) on the
+    Chebyshev nodes of the second kind x_i = cos(i pi/(n+1)) (J. Chem. Phys.
+    102, 346 (1995)); weights r^2 dr with dr = pi/(n+1) sin(theta_i) r'(x_i)."""
+    th = np.arange(1, n + 1) * math.pi / (n + 1)
+    x = np.cos(th)
+    r = xi / math.log(2.0) * (1.0 + x) ** 0.6 * np.log(2.0 / (1.0 - x))
+    drdx = xi / math.log(2.0) * ((0.6 * (1.0 + x) ** -0.4) * np.log(2.0 / (1.0 - x))
+                                 + (1.0 + x) ** 0.6 / (1.0 - x))
+    dr = math.pi / (n + 1) * np.sin(th) * drdx
+    return r[::-1], (r * r * dr)[::-1]
+
+
+def angular_rule(n_theta):
+    """Gauss-Legendre in cos(theta) x 2 n_theta uniform phi (offset half a step)."""
+    t, wt = np.polynomial.legendre.leggauss(n_theta)
+    n_phi = 2 * n_theta
+    phi = (np.arange(n_phi) + 0.5) * 2.0 * math.pi / n_phi
+    st = np.sqrt(1.0 - t * t)
+    u = np.stack([np.outer(st, np.cos(phi)).ravel(), np.outer(st, np.sin(phi)).ravel(),
+                  np.repeat(t, n_phi)], axis=1)
+    return u, np.repeat(wt, n_phi) * 2.0 * math.pi / n_phi
+
+
+def switch_g(mu, scheme="stratmann"):
+    """Stratmann's polynomial (a = 0.64; CPL 257, 213 (1996)) or Becke's three
+    iterations of 1.5 m - 0.5 m^3 (J. Chem. Phys. 88, 2547 (1988))."""
+    mu = np.asarray(mu, dtype=np.float64)
+    if scheme == "stratmann":
+        a = 0.64
+        m = mu / a
+        m2 = m * m
+        g = m * (35.0 + m2 * (-35.0 + m2 * (21.0 - 5.0 * m2))) / 16.0
+        return np.where(mu <= -a, -1.0, np.where(mu >= a, 1.0, g))
+    g = mu
+    for _ in range(3):
+        g = 1.5 * g - 0.5 * g ** 3
+    return g
+
+
+def becke_grid(charges, positions, level=3, scheme="stratmann", size_adjust=True):
+    """(coords (G, 3), weights (G)): atom-centred M4 x product grids, Becke's
+    partition with his size adjustment (a_bc from the Bragg-Slater radius ratio,
+    clipped to 1/2) and the chosen switching function; points packed atom by
+    atom, radial-major."""
+    z = [int(q) for q in charges]
+    xyz = np.asarray(positions, dtype=np.float64).reshape(-1, 3)
+    u, wa = angular_rule(_ANG[level])
+    pts, wts = [], []
+    for a, za in enumerate(z):
+        r, wr = radial_m4(_RAD[0 if za <= 2 else 1][level], _XI.get(za, 1.0))
+        pts.append((xyz[a][None, None, :] + r[:, None, None] * u[None, :, :]).reshape(-1, 3))
+        wts.append(np.outer(wr, wa).ravel())
+    R = np.array([_BRAGG.get(q, 1.0) for q in z])
+    chi = R[:, None] / R[None, :]
+    uu = (chi - 1.0) / (chi + 1.0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        adj = np.clip(np.where(np.abs(uu) > 0, uu / (uu * uu - 1.0), 0.0), -0.5, 0.5)
+    coords, weights = [], []
+    nat = len(z)
+    for a in range(nat):
+        x = pts[a]
+        if nat == 1:
+            coords.append(x)
+            weights.append(wts[a])
+            continue
+        d = np.linalg.norm(x[:, None, :] - xyz[None, :, :], axis=2)  # (G_a, natom)
+        P = np.ones((x.shape[0], nat))
+        for b in range(nat):
+            for c in range(nat):
+                if b == c:
+                    continue
+                mu = (d[:, b] - d[:, c]) / np.linalg.norm(xyz[b] - xyz[c])
+                nu = mu + adj[b, c] * (1.0 - mu * mu) if size_adjust else mu
+                P[:, b] *= 0.5 * (1.0 - switch_g(nu, scheme))
+        coords.append(x)
+        weights.append(wts[a] * P[:, a] / P.sum(axis=1))
+    return np.concatenate(coords), np.concatenate(weights)

@@ -8,7 +8,9 @@ documented synthetic model built on the molecule's own grid:
   shells (1-3 primitives, exponents log-uniform in [0.1, 50]);
 * grid: points drawn from Gaussian clouds around the atoms, with Monte-Carlo
   importance weights 1 / (G p(r)) times a random factor in [0.9, 1.1]
-  (positive random weights);
+  (positive random weights); or, with ``grid="becke"``, the Becke/Stratmann
+  molecular grid of ``qex_gb300.td.grids`` at ``level`` (built on the GPU),
+  on which the quadratures below are accurate;
 * S = ao^T W ao, T = 1/2 sum_c (d_c ao)^T W (d_c ao),
   V = -ao^T diag(w sum_A Z_A / sqrt(|r - R_A|^2 + 0.2)) ao, h1e = T + V;
 * two-electron integrals in factored form (ij|kl) = sum_P B_Pij B_Pkl with
@@ -104,7 +106,8 @@ def ao_values(shells, coords, deriv=False):
 
 
 def synthetic_molecule(num_atoms: int, seed: int = 0, points_per_atom: int = 620,
-                       with_integrals: bool = True) -> Molecule3D:
+                       with_integrals: bool = True, grid: str = "cloud",
+                       level: int = 3) -> Molecule3D:
     rng = np.random.default_rng(seed)
     names = rng.choice(["H", "C", "N", "O"], size=num_atoms, p=[0.4, 0.2, 0.2, 0.2])
     Z = np.array([ELEMENTS[x] for x in names], dtype=np.float64)
@@ -132,6 +135,18 @@ def synthetic_molecule(num_atoms: int, seed: int = 0, points_per_atom: int = 620
     d2 = ((coords[:, None, :] - pos[None, :, :]) ** 2).sum(-1)
     dens = np.exp(-0.5 * d2 / sig ** 2).mean(axis=1) / (2 * math.pi * sig ** 2) ** 1.5
     weights = rng.uniform(0.9, 1.1, G) / (G * dens)
+    if grid == "becke":
+        from .grids import Grids
+
+        g = Grids(Molecule3D(charges=Z, positions=pos, shells=[], coords=coords,
+                             weights=weights, nelectron=0))
+        g.level = level
+        g.build()
+        coords = g.coords.cpu().numpy()
+        weights = g.weights.cpu().numpy()
+        G = weights.size
+    elif grid != "cloud":
+        raise ValueError(f"grid must be 'cloud' or 'becke', got {grid!r}")
     ne = int(Z.sum())
     ne -= ne % 2
     mol = Molecule3D(charges=Z, positions=pos, shells=shells, coords=coords, weights=weights,
