@@ -384,6 +384,53 @@ def run_grid_eval(args):
                         "wall time per build", **out}
 
 
+def run_train_eval(args):
+    """One value-and-gradient of the reference's training loss (what L-BFGS-B
+    calls per step, qedft/train/od/train.py:402-466) on the GPU adjoint:
+    args.batch H2 molecules (R ~ U[0.5, 3.0]), 513 points, window MLP, jax_dft
+    SCF with reflection symmetry, 15 iterations, checkpoints every 5; targets
+    from the exp-Coulomb LDA solve of the same molecules."""
+    import torch
+
+    from qex_gb300 import networks
+    from qex_gb300.od import engine as eng
+    from qex_gb300.od import train as tr
+
+    rng = np.random.default_rng(args.seed + 2)
+    B = args.batch
+    R = rng.uniform(0.5, 3.0, B)
+    loc = np.stack([-R / 2, R / 2], axis=1)
+    z = np.ones((B, 2))
+    grids = (np.arange(513) - 256) * 0.08
+    mols = [eng.Molecule1D.from_grids(grids, l_, z_, 2) for l_, z_ in zip(loc, z)]
+    batch = eng.PackedBatch(mols, sort=False)
+    import qex_gb300
+
+    cfg = tr.solve_config({})
+    out = eng.default_engine().solve(batch, qex_gb300.LDAExpCoulomb(), cfg,
+                                     records=("energy", "final_density"))
+    te = out["energy"][:, -1].cpu().numpy()
+    tn = out["final_density"].cpu().numpy().reshape(B, 513)
+    init_fn, xc_fn = networks.build_xc_functional(networks.WindowMLP().build_network(None), grids)
+    spec, flat = tr.flatten(init_fn(0))
+    vg = tr.create_value_and_grad_fn(xc_fn, spec, grids, 2, {})
+    for _ in range(max(1, args.warmup)):
+        vg(flat, loc, z, None, te, tn)
+    times = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loss, grad = vg(flat, loc, z, None, te, tn)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    t = sorted(times)[len(times) // 2]
+    return {"workload": f"value and gradient of the reference training loss, {B} H2 molecules, "
+                        "513 points, window MLP, 15 iterations with reflection symmetry, "
+                        "checkpoints every 5", "s_per_step": t,
+            "molecule_gradients_per_s": B / t, "loss": float(loss),
+            "grad_norm": float(np.linalg.norm(grad))}
+
+
 # ---------------------------------------------------------------------------
 # arms
 # ---------------------------------------------------------------------------
@@ -661,6 +708,8 @@ def main():
                     help="time only the Fermi-Dirac occupation search")
     ap.add_argument("--grid-eval", action="store_true",
                     help="time only the molecular grid build")
+    ap.add_argument("--train-eval", action="store_true",
+                    help="time only one training-loss value and gradient")
     ap.add_argument("--serving-rates", type=float, nargs="*", default=[1000.0, 5000.0])
     ap.add_argument("--serving-seconds", type=float, default=1.0)
     ap.add_argument("--mix-rates", type=float, nargs="*", default=[100.0, 200.0])
@@ -674,6 +723,12 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         torch.distributed.init_process_group("nccl")
+    if args.train_eval:
+        from qex_gb300 import _native
+
+        _native.load()
+        print(json.dumps({"train_eval": run_train_eval(args)}), flush=True)
+        return
     if args.grid_eval:
         from qex_gb300 import _native
 
