@@ -431,6 +431,35 @@ def run_train_eval(args):
             "grad_norm": float(np.linalg.norm(grad))}
 
 
+def run_ints_eval(args):
+    """Analytic one-electron integrals and density-fitting factors (int3c2e,
+    int2c2e, Cholesky, substitution) for seeded synthetic molecules of 8 and
+    20 atoms; wall time per build (the oracle's loops are too slow to time
+    beside them at these sizes)."""
+    import torch
+
+    from qex_gb300.td import integrals, workloads
+
+    out = {}
+    for na in (8, 20):
+        m = workloads.synthetic_molecule(na, seed=na, with_integrals=False)
+        aux = integrals.even_tempered_aux(m)
+        for _ in range(args.warmup):
+            integrals.int1e(m)
+            integrals.df_factors(m, aux)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        integrals.int1e(m)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        integrals.df_factors(m, aux)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        out[f"atoms_{na}"] = {"nao": int(m.nao), "naux": int(sum(1 if s.l == 0 else 3 for s in aux)),
+                              "int1e_ms": (t1 - t0) * 1e3, "df_ms": (t2 - t1) * 1e3}
+    return {"workload": "analytic S, T, V and density-fitted Coulomb factors", **out}
+
+
 # ---------------------------------------------------------------------------
 # arms
 # ---------------------------------------------------------------------------
@@ -710,6 +739,8 @@ def main():
                     help="time only the molecular grid build")
     ap.add_argument("--train-eval", action="store_true",
                     help="time only one training-loss value and gradient")
+    ap.add_argument("--ints-eval", action="store_true",
+                    help="time only the analytic integrals and density fitting")
     ap.add_argument("--serving-rates", type=float, nargs="*", default=[1000.0, 5000.0])
     ap.add_argument("--serving-seconds", type=float, default=1.0)
     ap.add_argument("--mix-rates", type=float, nargs="*", default=[100.0, 200.0])
@@ -723,6 +754,12 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         torch.distributed.init_process_group("nccl")
+    if args.ints_eval:
+        from qex_gb300 import _native
+
+        _native.load()
+        print(json.dumps({"ints_eval": run_ints_eval(args)}), flush=True)
+        return
     if args.train_eval:
         from qex_gb300 import _native
 

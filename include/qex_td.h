@@ -27,6 +27,10 @@
  *   qex_td_becke_grid     <- pyscf.dft.gen_grid.Grids(mol).build() with
  *                            becke_scheme = stratmann, as used at
  *                            qedft/data_io/td/dataset_generation.py:139-142
+ *   qex_td_int1e          <- int1e_ovlp, int1e_kin, int1e_nuc (libcint through pyscf)
+ *   qex_td_int3c2e, qex_td_int2c2e, qex_td_df_factors
+ *                         <- density-fitted J, qedft/train/td/hf.py:425-449 (pyscfad
+ *                            df_jk: int3c2e, int2c2e and the Cholesky-fitted factors)
  *   qex_td_fermi_occupations <- optimize_fermi_occupations /
  *                            get_fractional_occupations_jax /
  *                            get_fractional_occupations_jax_stable,
@@ -141,6 +145,30 @@ int qex_td_becke_grid(int32_t natom, const double* atom_xyz, const double* size_
                       const double* radial_weights, int32_t num_angular,
                       const double* angular_nodes, const double* angular_weights, int32_t scheme,
                       int64_t num_points, double* coords, double* weights, void* stream);
+
+/* Gaussian integrals over Cartesian s/p shells (shell arrays as qex_td_eval_ao).
+ * S, T, V: (nao, nao); V = -sum_C Z_C <i|1/|r - C||j>. */
+int qex_td_int1e(int32_t num_shells, const double* centers, const int32_t* l,
+                 const int32_t* prim_offset, const int32_t* ao_offset, const double* exponents,
+                 const double* coefficients, int32_t nao, int32_t natom, const double* charges,
+                 const double* positions, double* S, double* T, double* V, void* stream);
+/* (ij|P): (naux, nao, nao). */
+int qex_td_int3c2e(int32_t num_shells, const double* centers, const int32_t* l,
+                   const int32_t* prim_offset, const int32_t* ao_offset, const double* exponents,
+                   const double* coefficients, int32_t nao, int32_t num_aux_shells,
+                   const double* aux_centers, const int32_t* aux_l, const int32_t* aux_prim_offset,
+                   const int32_t* aux_offset, const double* aux_exponents,
+                   const double* aux_coefficients, int32_t naux, double* out, void* stream);
+/* (P|Q): (naux, naux). */
+int qex_td_int2c2e(int32_t num_aux_shells, const double* aux_centers, const int32_t* aux_l,
+                   const int32_t* aux_prim_offset, const int32_t* aux_offset,
+                   const double* aux_exponents, const double* aux_coefficients, int32_t naux,
+                   double* out, void* stream);
+/* In place: metric (naux, naux) -> its lower Cholesky factor L; int3c
+ * (naux, cols) -> L^-1 int3c.  status (device int) QEX_NUMERICAL if the
+ * metric is not positive definite. */
+int qex_td_df_factors(int32_t naux, int64_t cols, double* metric, double* int3c,
+                      int32_t* status, void* stream);
 
 /* D = C diag(occ) C^T for `batch` matrices (C: (batch, n, n), occ: (batch, n)). */
 int qex_td_make_rdm1(int32_t batch, int32_t n, const double* C, const double* occ, double* D,

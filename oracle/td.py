@@ -668,3 +668,215 @@ def becke_grid(charges, positions, level=3, scheme="stratmann", size_adjust=True
         coords.append(x)
         weights.append(wts[a] * P[:, a] / P.sum(axis=1))
     return np.concatenate(coords), np.concatenate(weights)
+
+
+# ----------------------------------------------------------------------------
+# Gaussian integrals (McMurchie-Davidson; Helgaker, Joergensen, Olsen,
+# "Molecular Electronic-Structure Theory", ch. 9) for Cartesian s and p
+# primitives: what pyscf's libcint provides to the reference (int1e_ovlp,
+# int1e_kin, int1e_nuc, int3c2e, int2c2e for density fitting,
+# qedft/train/td/hf.py:425-449 via pyscfad df_jk).
+# ----------------------------------------------------------------------------
+
+def boys(n, T):
+    """F_n(T) = int_0^1 t^(2n) exp(-T t^2) dt, through the regularised lower
+    incomplete gamma function: Gamma(n+1/2) P(n+1/2, T) / (2 T^(n+1/2))."""
+    from scipy.special import gamma, gammainc
+
+    T = float(T)
+    if T < 1e-12:
+        return 1.0 / (2 * n + 1) - T / (2 * n + 3)
+    return gamma(n + 0.5) * gammainc(n + 0.5, T) / (2.0 * T ** (n + 0.5))
+
+
+def _hermite_e(i, j, a, b, XAB):
+    """E^{ij}_t, t = 0..i+j, for one Cartesian direction (the Gaussian product
+    of exponents a, b separated by XAB = A - B)."""
+    p = a + b
+    mu = a * b / p
+    XPA = -b / p * XAB
+    XPB = a / p * XAB
+    E = {(0, 0): np.array([math.exp(-mu * XAB * XAB)])}
+
+    def get(ii, jj):
+        if (ii, jj) in E:
+            return E[(ii, jj)]
+        if ii > 0:
+            prev = get(ii - 1, jj)
+            X = XPA
+        else:
+            prev = get(ii, jj - 1)
+            X = XPB
+        n = ii + jj
+        out = np.zeros(n + 1)
+        for t in range(n + 1):
+            v = X * (prev[t] if t < prev.size else 0.0)
+            if t >= 1:
+                v += prev[t - 1] / (2.0 * p)
+            if t + 1 < prev.size:
+                v += (t + 1) * prev[t + 1]
+            out[t] = v
+        E[(ii, jj)] = out
+        return out
+
+    return get(i, j)
+
+
+def _hermite_r(L, p, X, Y, Z):
+    """R_{tuv} (t+u+v <= L) of the Hermite Coulomb integrals for exponent p and
+    the vector (X, Y, Z) between the Hermite centres."""
+    T = p * (X * X + Y * Y + Z * Z)
+    R = {}
+
+    def r(n, t, u, v):
+        key = (n, t, u, v)
+        if key in R:
+            return R[key]
+        if t < 0 or u < 0 or v < 0:
+            return 0.0
+        if t == u == v == 0:
+            val = (-2.0 * p) ** n * boys(n, T)
+        elif t > 0:
+            val = (t - 1) * r(n + 1, t - 2, u, v) + X * r(n + 1, t - 1, u, v)
+        elif u > 0:
+            val = (u - 1) * r(n + 1, t, u - 2, v) + Y * r(n + 1, t, u - 1, v)
+        else:
+            val = (v - 1) * r(n + 1, t, u, v - 2) + Z * r(n + 1, t, u, v - 1)
+        R[key] = val
+        return val
+
+    return lambda t, u, v: r(0, t, u, v)
+
+
+_CART = {0: [(0, 0, 0)], 1: [(1, 0, 0), (0, 1, 0), (0, 0, 1)]}
+
+
+def _prims(shell):
+    return list(zip(shell.exponents, shell.coefficients))
+
+
+def int1e(shells, charges, positions):
+    """(S, T, V): overlap, kinetic and nuclear attraction -sum_C Z_C / |r - C|
+    over the contracted Cartesian shells."""
+    n = nao_of(shells)
+    S, T, V = np.zeros((n, n)), np.zeros((n, n)), np.zeros((n, n))
+    offs = np.cumsum([0] + [1 if s.l == 0 else 3 for s in shells])
+    pos = np.asarray(positions, dtype=np.float64).reshape(-1, 3)
+    for ia, A in enumerate(shells):
+        for ib, B in enumerate(shells):
+            AB = A.center - B.center
+            for a, ca in _prims(A):
+                for b, cb in _prims(B):
+                    p = a + b
+                    P = (a * A.center + b * B.center) / p
+                    for ka, la in enumerate(_CART[A.l]):
+                        for kb, lb in enumerate(_CART[B.l]):
+                            Ed = [[_hermite_e(la[d], j, a, b, AB[d]) for j in range(lb[d] + 3)]
+                                  for d in range(3)]
+                            s1 = [Ed[d][lb[d]][0] * math.sqrt(math.pi / p) for d in range(3)]
+
+                            def sij(d, j):
+                                return (Ed[d][j][0] * math.sqrt(math.pi / p)) if j >= 0 else 0.0
+
+                            t1 = []
+                            for d in range(3):
+                                j = lb[d]
+                                t1.append(-0.5 * (j * (j - 1) * sij(d, j - 2)
+                                                  - 2.0 * b * (2 * j + 1) * sij(d, j)
+                                                  + 4.0 * b * b * sij(d, j + 2)))
+                            i, j = offs[ia] + ka, offs[ib] + kb
+                            cc = ca * cb
+                            S[i, j] += cc * s1[0] * s1[1] * s1[2]
+                            T[i, j] += cc * (t1[0] * s1[1] * s1[2] + s1[0] * t1[1] * s1[2]
+                                             + s1[0] * s1[1] * t1[2])
+                            Eab = [Ed[d][lb[d]] for d in range(3)]
+                            for zc, C in zip(charges, pos):
+                                PC = P - C
+                                Rf = _hermite_r(la[0] + lb[0] + la[1] + lb[1] + la[2] + lb[2], p,
+                                                *PC)
+                                acc = 0.0
+                                for t in range(Eab[0].size):
+                                    for u in range(Eab[1].size):
+                                        for v in range(Eab[2].size):
+                                            acc += Eab[0][t] * Eab[1][u] * Eab[2][v] * Rf(t, u, v)
+                                V[i, j] -= cc * zc * 2.0 * math.pi / p * acc
+    return S, T, V
+
+
+def int3c2e(shells, aux):
+    """(naux, n, n): (ij|P) over AO shells i, j and auxiliary shells P."""
+    n, na = nao_of(shells), nao_of(aux)
+    out = np.zeros((na, n, n))
+    offs = np.cumsum([0] + [1 if s.l == 0 else 3 for s in shells])
+    aoffs = np.cumsum([0] + [1 if s.l == 0 else 3 for s in aux])
+    for ia, A in enumerate(shells):
+        for ib, B in enumerate(shells):
+            AB = A.center - B.center
+            for ic, Cs in enumerate(aux):
+                for a, ca in _prims(A):
+                    for b, cb in _prims(B):
+                        p = a + b
+                        P = (a * A.center + b * B.center) / p
+                        for g, cg in _prims(Cs):
+                            al = p * g / (p + g)
+                            pre = 2.0 * math.pi ** 2.5 / (p * g * math.sqrt(p + g))
+                            PC = P - Cs.center
+                            for ka, la in enumerate(_CART[A.l]):
+                                for kb, lb in enumerate(_CART[B.l]):
+                                    Eab = [_hermite_e(la[d], lb[d], a, b, AB[d]) for d in range(3)]
+                                    for kc, lc in enumerate(_CART[Cs.l]):
+                                        # a single Gaussian about its own centre:
+                                        # x^0 -> E_0 = 1; x^1 -> E_0 = 0, E_1 = 1/(2g)
+                                        Ec = [np.array([1.0]) if lc[d] == 0 else
+                                              np.array([0.0, 1.0 / (2.0 * g)]) for d in range(3)]
+                                        L = sum(la) + sum(lb) + sum(lc)
+                                        Rf = _hermite_r(L, al, *PC)
+                                        acc = 0.0
+                                        for t in range(Eab[0].size):
+                                            for u in range(Eab[1].size):
+                                                for v in range(Eab[2].size):
+                                                    e1 = Eab[0][t] * Eab[1][u] * Eab[2][v]
+                                                    for tt in range(Ec[0].size):
+                                                        for uu in range(Ec[1].size):
+                                                            for vv in range(Ec[2].size):
+                                                                acc += (e1 * (-1) ** (tt + uu + vv)
+                                                                        * Ec[0][tt] * Ec[1][uu]
+                                                                        * Ec[2][vv]
+                                                                        * Rf(t + tt, u + uu, v + vv))
+                                        out[aoffs[ic] + kc, offs[ia] + ka, offs[ib] + kb] += (
+                                            ca * cb * cg * pre * acc)
+    return out
+
+
+def int2c2e(aux):
+    """(naux, naux): (P|Q) over auxiliary shells."""
+    na = nao_of(aux)
+    out = np.zeros((na, na))
+    aoffs = np.cumsum([0] + [1 if s.l == 0 else 3 for s in aux])
+    for ia, A in enumerate(aux):
+        for ib, B in enumerate(aux):
+            for a, ca in _prims(A):
+                for b, cb in _prims(B):
+                    al = a * b / (a + b)
+                    pre = 2.0 * math.pi ** 2.5 / (a * b * math.sqrt(a + b))
+                    AB = A.center - B.center
+                    for ka, la in enumerate(_CART[A.l]):
+                        for kb, lb in enumerate(_CART[B.l]):
+                            Ea = [np.array([1.0]) if la[d] == 0 else np.array([0.0, 0.5 / a])
+                                  for d in range(3)]
+                            Eb = [np.array([1.0]) if lb[d] == 0 else np.array([0.0, 0.5 / b])
+                                  for d in range(3)]
+                            Rf = _hermite_r(sum(la) + sum(lb), al, *AB)
+                            acc = 0.0
+                            for t in range(Ea[0].size):
+                                for u in range(Ea[1].size):
+                                    for v in range(Ea[2].size):
+                                        for tt in range(Eb[0].size):
+                                            for uu in range(Eb[1].size):
+                                                for vv in range(Eb[2].size):
+                                                    acc += (Ea[0][t] * Ea[1][u] * Ea[2][v]
+                                                            * (-1) ** (tt + uu + vv) * Eb[0][tt]
+                                                            * Eb[1][uu] * Eb[2][vv]
+                                                            * Rf(t + tt, u + uu, v + vv))
+                            out[aoffs[ia] + ka, aoffs[ib] + kb] += ca * cb * pre * acc
+    return out

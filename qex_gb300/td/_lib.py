@@ -33,6 +33,12 @@ SIGNATURES = {
     "qex_td_vxc_gga": (ctypes.c_int, [_i64, _i32, _v, _v, _v, _v, _sz, _v]),
     "qex_td_becke_grid": (ctypes.c_int, [_i32, _v, _v, _v, _v, _v, _v, _v, _i32, _v, _v, _i32,
                                          _i64, _v, _v, _v]),
+    "qex_td_int1e": (ctypes.c_int, [_i32, _v, _v, _v, _v, _v, _v, _i32, _i32, _v, _v, _v, _v,
+                                    _v, _v]),
+    "qex_td_int3c2e": (ctypes.c_int, [_i32, _v, _v, _v, _v, _v, _v, _i32, _i32, _v, _v, _v, _v,
+                                      _v, _v, _i32, _v, _v]),
+    "qex_td_int2c2e": (ctypes.c_int, [_i32, _v, _v, _v, _v, _v, _v, _i32, _v, _v]),
+    "qex_td_df_factors": (ctypes.c_int, [_i32, _i64, _v, _v, _v, _v]),
     "qex_td_fermi_occupations": (ctypes.c_int, [_i32, _i32, _v, _v, ctypes.c_double, _v,
                                                 ctypes.c_double, ctypes.c_double, _i32, _i32,
                                                 _v, _v, _v, _v, _v, _v]),

@@ -105,9 +105,25 @@ def ao_values(shells, coords, deriv=False):
     return (ao, grad) if deriv else ao
 
 
+def analytic_integrals(mol: Molecule3D) -> Molecule3D:
+    """Replace the model integrals by analytic ones computed on the GPU
+    (``qex_gb300.td.integrals``): S, h1e = T + V_nuc, and density-fitted
+    Coulomb factors over an even-tempered auxiliary basis."""
+    from . import integrals
+
+    S, T, V = integrals.int1e(mol)
+    B = integrals.df_factors(mol)
+    mol.s1e = S.cpu().numpy()
+    mol.h1e = (T + V).cpu().numpy()
+    mol.eri_factors = B.cpu().numpy()
+    return mol
+
+
 def synthetic_molecule(num_atoms: int, seed: int = 0, points_per_atom: int = 620,
                        with_integrals: bool = True, grid: str = "cloud",
-                       level: int = 3) -> Molecule3D:
+                       level: int = 3, integrals: str = "model") -> Molecule3D:
+    """``integrals``: "model" (the documented quadrature model above) or
+    "analytic" (Gaussian integrals and density fitting on the GPU)."""
     rng = np.random.default_rng(seed)
     names = rng.choice(["H", "C", "N", "O"], size=num_atoms, p=[0.4, 0.2, 0.2, 0.2])
     Z = np.array([ELEMENTS[x] for x in names], dtype=np.float64)
@@ -176,4 +192,8 @@ def synthetic_molecule(num_atoms: int, seed: int = 0, points_per_atom: int = 620
             g = np.exp(-beta * ((coords - R) ** 2).sum(-1))
             fac[p] = 0.3 * (ao.T @ ((weights * g)[:, None] * ao))
         mol.eri_factors = fac
+        if integrals == "analytic":
+            analytic_integrals(mol)
+        elif integrals != "model":
+            raise ValueError(f"integrals must be 'model' or 'analytic', got {integrals!r}")
     return mol
