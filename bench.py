@@ -434,15 +434,15 @@ def run_train_eval(args):
 def run_ints_eval(args):
     """Analytic one-electron integrals and density-fitting factors (int3c2e,
     int2c2e, Cholesky, substitution) for seeded synthetic molecules of 8 and
-    20 atoms; wall time per build (the oracle's loops are too slow to time
+    20 atoms in the s/p and the spd basis; wall time per build (the oracle's loops are too slow to time
     beside them at these sizes)."""
     import torch
 
     from qex_gb300.td import integrals, workloads
 
     out = {}
-    for na in (8, 20):
-        m = workloads.synthetic_molecule(na, seed=na, with_integrals=False)
+    for na, basis in ((8, "sp"), (20, "sp"), (8, "spd"), (20, "spd")):
+        m = workloads.synthetic_molecule(na, seed=na, with_integrals=False, basis=basis)
         aux = integrals.even_tempered_aux(m)
         for _ in range(args.warmup):
             integrals.int1e(m)
@@ -455,7 +455,7 @@ def run_ints_eval(args):
         integrals.df_factors(m, aux)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        out[f"atoms_{na}"] = {"nao": int(m.nao), "naux": int(sum(1 if s.l == 0 else 3 for s in aux)),
+        out[f"atoms_{na}_{basis}"] = {"nao": int(m.nao), "naux": int(sum(workloads.ncart(s.l) for s in aux)),
                               "int1e_ms": (t1 - t0) * 1e3, "df_ms": (t2 - t1) * 1e3}
     return {"workload": "analytic S, T, V and density-fitted Coulomb factors", **out}
 

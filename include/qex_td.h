@@ -56,10 +56,13 @@ extern "C" {
 #endif
 
 /* Shells of Cartesian contracted Gaussians: shell s has centre
- * centers[3s..3s+2], angular momentum l[s] (0 or 1), primitives
+ * centers[3s..3s+2], angular momentum l[s] (0, 1 or 2), primitives
  * [prim_offset[s], prim_offset[s+1]) of exponents / coefficients (the
  * coefficients include the primitive normalisation) and its first AO column
- * ao_offset[s].  ao is (G, nao). */
+ * ao_offset[s]; its (l+1)(l+2)/2 components follow in pyscf's Cartesian order
+ * (x, y, z; xx, xy, xz, yy, yz, zz), each the monomial times the radial sum.
+ * A shell with l outside 0..2 is skipped (its columns are left unwritten).
+ * ao is (G, nao). */
 int qex_td_eval_ao(int64_t num_points, const double* coords, int32_t num_shells,
                    const double* centers, const int32_t* l, const int32_t* prim_offset,
                    const int32_t* ao_offset, const double* exponents, const double* coefficients,
@@ -146,8 +149,9 @@ int qex_td_becke_grid(int32_t natom, const double* atom_xyz, const double* size_
                       const double* angular_nodes, const double* angular_weights, int32_t scheme,
                       int64_t num_points, double* coords, double* weights, void* stream);
 
-/* Gaussian integrals over Cartesian s/p shells (shell arrays as qex_td_eval_ao).
- * S, T, V: (nao, nao); V = -sum_C Z_C <i|1/|r - C||j>. */
+/* Gaussian integrals over Cartesian s, p and d shells (shell arrays as
+ * qex_td_eval_ao, auxiliary shells likewise).  S, T, V: (nao, nao), written
+ * exactly symmetric; V = -sum_C Z_C <i|1/|r - C||j>. */
 int qex_td_int1e(int32_t num_shells, const double* centers, const int32_t* l,
                  const int32_t* prim_offset, const int32_t* ao_offset, const double* exponents,
                  const double* coefficients, int32_t nao, int32_t natom, const double* charges,

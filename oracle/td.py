@@ -25,7 +25,7 @@ SLATER_CX = 0.75 * (3.0 / math.pi) ** (1.0 / 3.0)
 @dataclasses.dataclass
 class Shell:
     center: np.ndarray  # (3,)
-    l: int  # 0 (s) or 1 (p: x, y, z Cartesian)
+    l: int  # 0 (s), 1 (p: x, y, z) or 2 (d: xx, xy, xz, yy, yz, zz), Cartesian
     exponents: np.ndarray
     coefficients: np.ndarray  # contraction coefficients incl. primitive normalisation
 
@@ -35,8 +35,18 @@ def primitive_norm(alpha, l):
     return (2.0 * alpha / math.pi) ** 0.75 * (4.0 * alpha) ** (0.5 * l)
 
 
+def cart_components(l):
+    """Exponents (i, j, k) of the Cartesian components of angular momentum l in
+    pyscf's order: i = l..0, then j = l-i..0, k = l-i-j."""
+    return [(i, l - i - k, k) for i in range(l, -1, -1) for k in range(0, l - i + 1)]
+
+
+def ncart(l):
+    return (l + 1) * (l + 2) // 2
+
+
 def nao_of(shells):
-    return sum(1 if s.l == 0 else 3 for s in shells)
+    return sum(ncart(s.l) for s in shells)
 
 
 def eval_ao(shells, coords, deriv=0):
@@ -54,20 +64,20 @@ def eval_ao(shells, coords, deriv=0):
         r2 = np.sum(d * d, axis=1)
         e = np.exp(-np.outer(r2, s.exponents))  # (G, nprim)
         rad = e @ s.coefficients
-        drad = e @ (-2.0 * s.exponents * s.coefficients)  # d rad / d(r2) * 2 ... (x factor below)
-        if s.l == 0:
-            ao[:, k] = rad
+        drad = e @ (-2.0 * s.exponents * s.coefficients)  # (d rad / d r) / r
+        for c in cart_components(s.l):
+            mono = d[:, 0] ** c[0] * d[:, 1] ** c[1] * d[:, 2] ** c[2]
+            ao[:, k] = mono * rad
             if deriv:
-                for c in range(3):
-                    grad[c, :, k] = drad * d[:, c]
+                for q in range(3):
+                    if c[q] > 0:
+                        e_q = list(c)
+                        e_q[q] -= 1
+                        dm = c[q] * d[:, 0] ** e_q[0] * d[:, 1] ** e_q[1] * d[:, 2] ** e_q[2]
+                    else:
+                        dm = 0.0
+                    grad[q, :, k] = dm * rad + mono * drad * d[:, q]
             k += 1
-        else:
-            for c in range(3):
-                ao[:, k + c] = d[:, c] * rad
-                if deriv:
-                    for q in range(3):
-                        grad[q, :, k + c] = (rad if q == c else 0.0) + d[:, c] * drad * d[:, q]
-            k += 3
     return (ao, grad) if deriv else ao
 
 
@@ -672,7 +682,7 @@ def becke_grid(charges, positions, level=3, scheme="stratmann", size_adjust=True
 
 # ----------------------------------------------------------------------------
 # Gaussian integrals (McMurchie-Davidson; Helgaker, Joergensen, Olsen,
-# "Molecular Electronic-Structure Theory", ch. 9) for Cartesian s and p
+# "Molecular Electronic-Structure Theory", ch. 9) for Cartesian s, p and d
 # primitives: what pyscf's libcint provides to the reference (int1e_ovlp,
 # int1e_kin, int1e_nuc, int3c2e, int2c2e for density fitting,
 # qedft/train/td/hf.py:425-449 via pyscfad df_jk).
@@ -748,7 +758,9 @@ def _hermite_r(L, p, X, Y, Z):
     return lambda t, u, v: r(0, t, u, v)
 
 
-_CART = {0: [(0, 0, 0)], 1: [(1, 0, 0), (0, 1, 0), (0, 0, 1)]}
+def _self_e(l, g):
+    """Hermite expansion of x^l exp(-g x^2) about its own centre (E_t, t <= l)."""
+    return _hermite_e(l, 0, g, 0.0, 0.0)
 
 
 def _prims(shell):
@@ -760,7 +772,7 @@ def int1e(shells, charges, positions):
     over the contracted Cartesian shells."""
     n = nao_of(shells)
     S, T, V = np.zeros((n, n)), np.zeros((n, n)), np.zeros((n, n))
-    offs = np.cumsum([0] + [1 if s.l == 0 else 3 for s in shells])
+    offs = np.cumsum([0] + [ncart(s.l) for s in shells])
     pos = np.asarray(positions, dtype=np.float64).reshape(-1, 3)
     for ia, A in enumerate(shells):
         for ib, B in enumerate(shells):
@@ -769,8 +781,8 @@ def int1e(shells, charges, positions):
                 for b, cb in _prims(B):
                     p = a + b
                     P = (a * A.center + b * B.center) / p
-                    for ka, la in enumerate(_CART[A.l]):
-                        for kb, lb in enumerate(_CART[B.l]):
+                    for ka, la in enumerate(cart_components(A.l)):
+                        for kb, lb in enumerate(cart_components(B.l)):
                             Ed = [[_hermite_e(la[d], j, a, b, AB[d]) for j in range(lb[d] + 3)]
                                   for d in range(3)]
                             s1 = [Ed[d][lb[d]][0] * math.sqrt(math.pi / p) for d in range(3)]
@@ -807,8 +819,8 @@ def int3c2e(shells, aux):
     """(naux, n, n): (ij|P) over AO shells i, j and auxiliary shells P."""
     n, na = nao_of(shells), nao_of(aux)
     out = np.zeros((na, n, n))
-    offs = np.cumsum([0] + [1 if s.l == 0 else 3 for s in shells])
-    aoffs = np.cumsum([0] + [1 if s.l == 0 else 3 for s in aux])
+    offs = np.cumsum([0] + [ncart(s.l) for s in shells])
+    aoffs = np.cumsum([0] + [ncart(s.l) for s in aux])
     for ia, A in enumerate(shells):
         for ib, B in enumerate(shells):
             AB = A.center - B.center
@@ -821,14 +833,12 @@ def int3c2e(shells, aux):
                             al = p * g / (p + g)
                             pre = 2.0 * math.pi ** 2.5 / (p * g * math.sqrt(p + g))
                             PC = P - Cs.center
-                            for ka, la in enumerate(_CART[A.l]):
-                                for kb, lb in enumerate(_CART[B.l]):
+                            for ka, la in enumerate(cart_components(A.l)):
+                                for kb, lb in enumerate(cart_components(B.l)):
                                     Eab = [_hermite_e(la[d], lb[d], a, b, AB[d]) for d in range(3)]
-                                    for kc, lc in enumerate(_CART[Cs.l]):
-                                        # a single Gaussian about its own centre:
-                                        # x^0 -> E_0 = 1; x^1 -> E_0 = 0, E_1 = 1/(2g)
-                                        Ec = [np.array([1.0]) if lc[d] == 0 else
-                                              np.array([0.0, 1.0 / (2.0 * g)]) for d in range(3)]
+                                    for kc, lc in enumerate(cart_components(Cs.l)):
+                                        # a single Gaussian about its own centre
+                                        Ec = [_self_e(lc[d], g) for d in range(3)]
                                         L = sum(la) + sum(lb) + sum(lc)
                                         Rf = _hermite_r(L, al, *PC)
                                         acc = 0.0
@@ -852,7 +862,7 @@ def int2c2e(aux):
     """(naux, naux): (P|Q) over auxiliary shells."""
     na = nao_of(aux)
     out = np.zeros((na, na))
-    aoffs = np.cumsum([0] + [1 if s.l == 0 else 3 for s in aux])
+    aoffs = np.cumsum([0] + [ncart(s.l) for s in aux])
     for ia, A in enumerate(aux):
         for ib, B in enumerate(aux):
             for a, ca in _prims(A):
@@ -860,12 +870,10 @@ def int2c2e(aux):
                     al = a * b / (a + b)
                     pre = 2.0 * math.pi ** 2.5 / (a * b * math.sqrt(a + b))
                     AB = A.center - B.center
-                    for ka, la in enumerate(_CART[A.l]):
-                        for kb, lb in enumerate(_CART[B.l]):
-                            Ea = [np.array([1.0]) if la[d] == 0 else np.array([0.0, 0.5 / a])
-                                  for d in range(3)]
-                            Eb = [np.array([1.0]) if lb[d] == 0 else np.array([0.0, 0.5 / b])
-                                  for d in range(3)]
+                    for ka, la in enumerate(cart_components(A.l)):
+                        for kb, lb in enumerate(cart_components(B.l)):
+                            Ea = [_self_e(la[d], a) for d in range(3)]
+                            Eb = [_self_e(lb[d], b) for d in range(3)]
                             Rf = _hermite_r(sum(la) + sum(lb), al, *AB)
                             acc = 0.0
                             for t in range(Ea[0].size):

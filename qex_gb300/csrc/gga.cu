@@ -14,6 +14,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "cart.cuh"
 #include "qex_ks1d.h"
 #include "qex_td.h"
 
@@ -56,15 +57,18 @@ __global__ void eval_ao_d1_kernel(long long G, const double* __restrict__ coords
       drad -= 2.0 * ex[p] * t;
     }
     double* row = ao + g * nao + aooff[s];
-    if (l[s] == 0) {
-      row[0] = rad;
-      for (int q = 0; q < 3; ++q) row[(q + 1) * plane] = drad * d[q];
-    } else {
-      for (int c = 0; c < 3; ++c) {
-        row[c] = d[c] * rad;
-        for (int q = 0; q < 3; ++q)
-          row[(q + 1) * plane + c] = (q == c ? rad : 0.0) + d[c] * drad * d[q];
-      }
+    const int ls = l[s];
+    if (ls < 0 || ls > kMaxShellL) continue;
+    for (int k = 0; k < ncart(ls); ++k) {
+      int c[3];
+      cart_exponents(ls, k, c);
+      const double px = cart_pow(d[0], c[0]), py = cart_pow(d[1], c[1]), pz = cart_pow(d[2], c[2]);
+      const double m = px * py * pz;
+      row[k] = m * rad;
+      // d/dq (m rad) = (dm/dq) rad + m drad d_q
+      const double dm[3] = {cart_dpow(d[0], c[0]) * py * pz, px * cart_dpow(d[1], c[1]) * pz,
+                            px * py * cart_dpow(d[2], c[2])};
+      for (int q = 0; q < 3; ++q) row[(q + 1) * plane + k] = dm[q] * rad + m * drad * d[q];
     }
   }
 }

@@ -10,6 +10,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "cart.cuh"
 #include "ks1d_common.cuh"
 #include "qex_ks1d.h"
 #include "qex_td.h"
@@ -89,12 +90,12 @@ __global__ void eval_ao_kernel(long long G, const double* __restrict__ coords, i
     double rad = 0.0;
     for (int p = poff[s]; p < poff[s + 1]; ++p) rad += co[p] * exp(-ex[p] * r2);
     double* row = ao + g * nao + aooff[s];
-    if (l[s] == 0) {
-      row[0] = rad;
-    } else {
-      row[0] = dx * rad;
-      row[1] = dy * rad;
-      row[2] = dz * rad;
+    const int ls = l[s];
+    if (ls < 0 || ls > kMaxShellL) continue;
+    for (int k = 0; k < ncart(ls); ++k) {
+      int c[3];
+      cart_exponents(ls, k, c);
+      row[k] = cart_pow(dx, c[0]) * cart_pow(dy, c[1]) * cart_pow(dz, c[2]) * rad;
     }
   }
 }

@@ -5,7 +5,7 @@ Overlap, kinetic and nuclear-attraction matrices, the three-centre
 fitted factors B_P = sum_Q (L^-1)_PQ (Q|ij) with (P|Q) = L L^T, so that
 (ij|kl) ~ sum_P B_Pij B_Pkl: what pyscf's libcint and pyscfad's density
 fitting give the reference (``qedft/train/td/hf.py:425-449``).  The J build of
-the SCF then runs on these factors unchanged.  Cartesian s and p shells.
+the SCF then runs on these factors unchanged.  Cartesian s, p and d shells.
 """
 
 from __future__ import annotations
@@ -21,39 +21,40 @@ from .numint import _dev
 
 def shell_arrays(shells):
     """(centers, l, prim_offset, ao_offset, exponents, coefficients) of a shell list."""
-    centers = np.array([s.center for s in shells], dtype=np.float64).reshape(-1)
-    l = np.array([s.l for s in shells], dtype=np.int32)
-    poff = np.zeros(len(shells) + 1, dtype=np.int32)
-    poff[1:] = np.cumsum([len(s.exponents) for s in shells])
-    aoff = np.zeros(len(shells), dtype=np.int32)
-    aoff[1:] = np.cumsum([1 if s.l == 0 else 3 for s in shells])[:-1]
-    ex = np.concatenate([s.exponents for s in shells]).astype(np.float64)
-    co = np.concatenate([s.coefficients for s in shells]).astype(np.float64)
-    return centers, l, poff, aoff, ex, co
+    from .workloads import shell_arrays as arrays
+
+    return arrays(shells)
 
 
 def _nao(shells):
-    return sum(1 if s.l == 0 else 3 for s in shells)
+    from .workloads import ncart
+
+    return sum(ncart(s.l) for s in shells)
 
 
 def _prim_norm(alpha, l):
     return (2.0 * alpha / math.pi) ** 0.75 * (4.0 * alpha) ** (0.5 * l)
 
 
-# even-tempered auxiliary exponents (s, p) per element row: a fitting set for
-# the Coulomb term (the Weigend/def2 JK-fit sets pyscf uses are not in this image)
+# even-tempered auxiliary exponents (s, p, d) per element row: a fitting set
+# for the Coulomb term (the Weigend/def2 JK-fit sets pyscf uses are not in this
+# image); the d set is added where the orbital basis carries d shells
 AUX_S = {1: (0.15, 0.45, 1.35, 4.05), 2: (0.15, 0.45, 1.35, 4.05, 12.15, 36.45)}
 AUX_P = {1: (0.4, 1.2), 2: (0.3, 0.9, 2.7)}
+AUX_D = {1: (), 2: (0.5, 1.5, 4.5)}
 
 
 def even_tempered_aux(mol):
-    """Uncontracted normalised s and p auxiliary shells on every atom."""
+    """Uncontracted normalised s and p (and, for an orbital basis with d
+    shells, d) auxiliary shells on every atom."""
     from .workloads import Shell
 
+    with_d = any(s.l == 2 for s in mol.shells)
     out = []
     for z, R in zip(mol.charges, mol.positions):
         row = 1 if int(z) <= 2 else 2
-        for l, exps in ((0, AUX_S[row]), (1, AUX_P[row])):
+        sets = [(0, AUX_S[row]), (1, AUX_P[row])] + ([(2, AUX_D[row])] if with_d else [])
+        for l, exps in sets:
             for a in exps:
                 out.append(Shell(center=np.asarray(R, np.float64).copy(), l=l,
                                  exponents=np.array([a]), coefficients=np.array([_prim_norm(a, l)])))

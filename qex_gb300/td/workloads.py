@@ -5,7 +5,9 @@ documented synthetic model built on the molecule's own grid:
 
 * atoms H/C/N/O at random positions with a minimum separation of 1.0 Angstrom;
 * basis: Cartesian contracted Gaussians, H: 2 s shells; C, N, O: 3 s + 2 p
-  shells (1-3 primitives, exponents log-uniform in [0.1, 50]);
+  shells (1-3 primitives, exponents log-uniform in [0.1, 50]); with
+  ``basis="spd"`` C, N, O also carry one d shell (6 Cartesian components, one
+  primitive, exponent log-uniform in [0.3, 3]);
 * grid: points drawn from Gaussian clouds around the atoms, with Monte-Carlo
   importance weights 1 / (G p(r)) times a random factor in [0.9, 1.1]
   (positive random weights); or, with ``grid="becke"``, the Becke/Stratmann
@@ -57,20 +59,41 @@ class Molecule3D:
 
     @property
     def nao(self):
-        return sum(1 if s.l == 0 else 3 for s in self.shells)
+        return sum(ncart(s.l) for s in self.shells)
 
     def shell_arrays(self):
         """Flattened shell description for ``qex_td_eval_ao``."""
-        centers = np.array([s.center for s in self.shells], dtype=np.float64).reshape(-1)
-        l = np.array([s.l for s in self.shells], dtype=np.int32)
-        nprim = [len(s.exponents) for s in self.shells]
-        poff = np.zeros(len(self.shells) + 1, dtype=np.int32)
-        poff[1:] = np.cumsum(nprim)
-        aoff = np.zeros(len(self.shells), dtype=np.int32)
-        aoff[1:] = np.cumsum([1 if s.l == 0 else 3 for s in self.shells])[:-1]
-        ex = np.concatenate([s.exponents for s in self.shells]).astype(np.float64)
-        co = np.concatenate([s.coefficients for s in self.shells]).astype(np.float64)
-        return centers, l, poff, aoff, ex, co
+        return shell_arrays(self.shells)
+
+
+MAX_L = 2  # s, p and d shells
+
+
+def ncart(l):
+    """Cartesian components of a shell of angular momentum l."""
+    return (l + 1) * (l + 2) // 2
+
+
+def cart_components(l):
+    """(i, j, k) exponents of the components, pyscf's Cartesian order."""
+    return [(i, l - i - k, k) for i in range(l, -1, -1) for k in range(0, l - i + 1)]
+
+
+def shell_arrays(shells):
+    """(centers, l, prim_offset, ao_offset, exponents, coefficients) of a shell
+    list, as the GPU entry points take them; ValueError for l outside 0..2."""
+    bad = [s.l for s in shells if not 0 <= int(s.l) <= MAX_L]
+    if bad:
+        raise ValueError(f"shells with l = {bad[0]}: only s, p and d shells are supported")
+    centers = np.array([s.center for s in shells], dtype=np.float64).reshape(-1)
+    l = np.array([s.l for s in shells], dtype=np.int32)
+    poff = np.zeros(len(shells) + 1, dtype=np.int32)
+    poff[1:] = np.cumsum([len(s.exponents) for s in shells])
+    aoff = np.zeros(len(shells), dtype=np.int32)
+    aoff[1:] = np.cumsum([ncart(s.l) for s in shells])[:-1]
+    ex = np.concatenate([s.exponents for s in shells]).astype(np.float64)
+    co = np.concatenate([s.coefficients for s in shells]).astype(np.float64)
+    return centers, l, poff, aoff, ex, co
 
 
 def _prim_norm(alpha, l):
@@ -80,7 +103,7 @@ def _prim_norm(alpha, l):
 def ao_values(shells, coords, deriv=False):
     """Host AO values (and gradients) for the integral model."""
     G = coords.shape[0]
-    n = sum(1 if s.l == 0 else 3 for s in shells)
+    n = sum(ncart(s.l) for s in shells)
     ao = np.zeros((G, n))
     grad = np.zeros((3, G, n)) if deriv else None
     k = 0
@@ -90,18 +113,18 @@ def ao_values(shells, coords, deriv=False):
         e = np.exp(-np.outer(r2, s.exponents))
         rad = e @ s.coefficients
         drad = e @ (-2.0 * s.exponents * s.coefficients)
-        if s.l == 0:
-            ao[:, k] = rad
+        for c in cart_components(s.l):
+            mono = d[:, 0] ** c[0] * d[:, 1] ** c[1] * d[:, 2] ** c[2]
+            ao[:, k] = mono * rad
             if deriv:
-                grad[:, :, k] = (drad[:, None] * d).T
+                for q in range(3):
+                    dm = 0.0
+                    if c[q]:
+                        e_q = list(c)
+                        e_q[q] -= 1
+                        dm = c[q] * d[:, 0] ** e_q[0] * d[:, 1] ** e_q[1] * d[:, 2] ** e_q[2]
+                    grad[q, :, k] = dm * rad + mono * drad * d[:, q]
             k += 1
-        else:
-            for c in range(3):
-                ao[:, k + c] = d[:, c] * rad
-                if deriv:
-                    for q in range(3):
-                        grad[q, :, k + c] = (rad if q == c else 0.0) + d[:, c] * drad * d[:, q]
-            k += 3
     return (ao, grad) if deriv else ao
 
 
@@ -121,9 +144,13 @@ def analytic_integrals(mol: Molecule3D) -> Molecule3D:
 
 def synthetic_molecule(num_atoms: int, seed: int = 0, points_per_atom: int = 620,
                        with_integrals: bool = True, grid: str = "cloud",
-                       level: int = 3, integrals: str = "model") -> Molecule3D:
+                       level: int = 3, integrals: str = "model",
+                       basis: str = "sp") -> Molecule3D:
     """``integrals``: "model" (the documented quadrature model above) or
-    "analytic" (Gaussian integrals and density fitting on the GPU)."""
+    "analytic" (Gaussian integrals and density fitting on the GPU).
+    ``basis``: "sp" or "spd" (a d shell on C, N, O)."""
+    if basis not in ("sp", "spd"):
+        raise ValueError(f"basis must be 'sp' or 'spd', got {basis!r}")
     rng = np.random.default_rng(seed)
     names = rng.choice(["H", "C", "N", "O"], size=num_atoms, p=[0.4, 0.2, 0.2, 0.2])
     Z = np.array([ELEMENTS[x] for x in names], dtype=np.float64)
@@ -144,6 +171,10 @@ def synthetic_molecule(num_atoms: int, seed: int = 0, points_per_atom: int = 620
             w = rng.uniform(0.2, 1.0, npr)
             co = w * np.array([_prim_norm(a, l) for a in ex])
             shells.append(Shell(center=R.copy(), l=l, exponents=ex, coefficients=co))
+        if basis == "spd" and z != 1:
+            ex = np.exp(rng.uniform(math.log(0.3), math.log(3.0), 1))
+            shells.append(Shell(center=R.copy(), l=2, exponents=ex,
+                                coefficients=np.array([_prim_norm(ex[0], 2)])))
     G = points_per_atom * num_atoms
     sig = 1.5
     which = rng.integers(0, num_atoms, G)
