@@ -162,6 +162,15 @@ typedef struct qex_ks1d_outputs {
 int qex_ks1d_workspace_size(const qex_ks1d_options* options, int32_t num_molecules,
                             size_t* bytes);
 
+/* Workspace for this batch shape and functional.  With a KSR functional it
+ * adds num_molecules x num_iterations x max_num_grids doubles: given that
+ * much, qex_ks1d_solve evaluates the network on the output densities (the
+ * E_xc term of the recorded total energies) in one batched launch after the
+ * SCF instead of inside it.  Same results; no counterpart in the reference
+ * (its scan evaluates E_xc inside each iteration, jit_scf.py:46-72). */
+int qex_ks1d_workspace_size_xc(const qex_ks1d_options* options, const qex_xc_spec* xc,
+                               int32_t num_molecules, size_t* bytes);
+
 /* Full SCF for a batch of molecules in one launch (one warp per molecule,
  * persistent CTAs, all iterations inside the kernel). */
 int qex_ks1d_solve(const qex_ks1d_batch* batch, const qex_ks1d_options* options,

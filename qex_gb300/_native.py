@@ -122,6 +122,9 @@ class Ks1dOutputs(ctypes.Structure):
 _SIGNATURES = {
     "qex_ks1d_workspace_size": (ctypes.c_int, [ctypes.POINTER(Ks1dOptions), ctypes.c_int32,
                                                ctypes.POINTER(ctypes.c_size_t)]),
+    "qex_ks1d_workspace_size_xc": (ctypes.c_int, [ctypes.POINTER(Ks1dOptions),
+                                                  ctypes.POINTER(XcSpec), ctypes.c_int32,
+                                                  ctypes.POINTER(ctypes.c_size_t)]),
     "qex_ks1d_solve": (ctypes.c_int, [ctypes.POINTER(Ks1dBatch), ctypes.POINTER(Ks1dOptions),
                                       ctypes.POINTER(XcSpec), ctypes.POINTER(Ks1dOutputs), _c_p,
                                       ctypes.c_size_t, _c_p]),

@@ -76,6 +76,11 @@ struct Params {
   double ksr_lo, ksr_hi;
   int ksr_c;
   int ksr_slot;  // constant-memory slot holding the network for this launch
+  // KSR: (slot, iteration) rows of nmax doubles receiving the network's input
+  // on the output density; the energies then take E_xc from ksr_energy_kernel
+  // (one batched evaluation after the SCF) instead of the SCF kernel.  Null:
+  // the SCF kernel evaluates it.
+  double* ksr_defer;
   // outputs
   double* o_energy;
   double* o_gap;
@@ -1518,6 +1523,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
     double alpha = p.alpha;
     bool converged = false;
     int active = 0;
+    int last_t = 0;  // last iteration that ran (the converged branch repeats it)
     double last_energy = INFINITY, last_gap = 0.0;
     const long long rec = (long long)p.iters * off;
     const bool reflect_xc = p.reflect && p.xc_conv == QEX_XC_LOCAL;
@@ -1539,6 +1545,14 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
           if (p.o_vh) p.o_vh[r0 + i] = vh[i];
           if (p.o_vxc) p.o_vxc[r0 + i] = vxc[i];
           if (p.o_f) p.o_f[r0 + i] = vf[i];
+        }
+        if constexpr (kKsr) {
+          if (p.ksr_defer) {
+            const double* src = p.ksr_defer + ((long long)slot * p.iters + last_t) * p.nmax;
+            double* dst = p.ksr_defer + ((long long)slot * p.iters + t) * p.nmax;
+            #pragma unroll 1
+            for (int i = lane; i < N; i += kWarp) dst[i] = src[i];
+          }
         }
         continue;
       }
@@ -1616,7 +1630,16 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
       long long tsub = clock64();
       double exc;
       if constexpr (kKsr) {
-        exc = ksr_xc(p, N, dx, sm, false, nullptr, nullptr, false, lane);
+        if (p.ksr_defer && p.mode == kModeScf) {
+          // the network's input, evaluated after the SCF by ksr_energy_kernel
+          double* row = p.ksr_defer + ((long long)slot * p.iters + t) * p.nmax;
+          #pragma unroll 1
+          for (int i = lane; i < N; i += kWarp) row[i] = sm.s64a[kPad64 + i];
+          last_t = t;
+          exc = 0.0;
+        } else {
+          exc = ksr_xc(p, N, dx, sm, false, nullptr, nullptr, false, lane);
+        }
       } else {
         exc = xc_eval(p, N, dx, sm, false, nullptr, nullptr, false, lane);
       }
@@ -2127,6 +2150,12 @@ long long stride_doubles(const qex_ks1d_options* o, bool adjoint = false) {
   return (s + 31) / 32 * 32;
 }
 
+// Bytes of the deferred KSR energy rows for a batch shape.
+size_t ksr_defer_bytes(const qex_ks1d_options* o, int num_molecules) {
+  return sizeof(double) * (size_t)num_molecules * (size_t)o->num_iterations *
+         (size_t)o->max_num_grids;
+}
+
 int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_options* o,
                 const qex_xc_spec* xc, const qex_ks1d_outputs* out, void* ws, size_t ws_bytes,
                 int num_molecules) {
@@ -2203,6 +2232,13 @@ int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_opt
   qex_ks1d_workspace_size(o, num_molecules, &need);
   if (!ws || ws_bytes < need) return QEX_BAD_ARG;
   if (reinterpret_cast<uintptr_t>(ws) % 16 != 0) return QEX_BAD_ARG;  // float4 solve area
+  // KSR with a workspace of qex_ks1d_workspace_size_xc bytes: the energies'
+  // E_xc on the output densities in one batched launch after the SCF
+  if (mode == kModeScf && xc->kind == QEX_XC_KSR && out && out->total_energy) {
+    const size_t base = (need + 255) / 256 * 256;
+    if (ws_bytes >= base + ksr_defer_bytes(o, num_molecules))
+      P.ksr_defer = reinterpret_cast<double*>(static_cast<unsigned char*>(ws) + base);
+  }
   P.counter = reinterpret_cast<int*>(ws);
   P.ws = reinterpret_cast<double*>(static_cast<unsigned char*>(ws) + 256);
   P.stride = stride_doubles(o);
@@ -2219,6 +2255,32 @@ int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_opt
     if (o->external_potential_given && !b->external_potential) return QEX_BAD_ARG;
   }
   return QEX_OK;
+}
+
+// E_xc of the KSR network on the output densities the SCF kernel recorded in
+// p.ksr_defer (rows (slot, iteration)), added to the recorded total energies.
+// One warp per row with four channels' scans staged at a time: the SCF
+// kernel's register cap allows one.  The network arithmetic per channel is
+// the same as inside the SCF kernel.
+template <int C>
+__global__ void __launch_bounds__(kWarp) ksr_energy_kernel(const __grid_constant__ Params p) {
+  extern __shared__ __align__(16) float ksm[];
+  const int lane = threadIdx.x;
+  const long long rows = (long long)p.num_molecules * p.iters;
+  const bool local = (p.xc_conv == QEX_XC_LOCAL);
+  for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int slot = (int)(row / p.iters), t = (int)(row % p.iters);
+    const int b = p.order ? p.order[slot] : slot;
+    const int N = p.num_grids[b];
+    const int ne = p.num_electrons[b];
+    const double dx = p.grid_spacing[b];
+    if (N < 5 || N > p.nmax || ne < 1 || ne / 2 + 1 > p.kmax || !(dx > 0.0)) continue;
+    const double e = ksr_eval<C, false, 4>(p.ksr_w, p.ksr_slot, p.ksr_lo, p.ksr_hi, N, dx,
+                                           p.ksr_defer + row * p.nmax, local, nullptr, nullptr,
+                                           ksm, lane);
+    const double exc = warp_sum(e) * dx;
+    if (lane == 0) p.o_energy[(long long)b * p.iters + t] += exc;
+  }
 }
 
 int launch_adjoint(const Params& P, cudaStream_t stream) {
@@ -2275,7 +2337,22 @@ int launch_variant(const Params& P, cudaStream_t stream, size_t smem, int per_sm
     Params Q = P;
     Q.ksr_slot = stage.slot();
     ks1d_kernel<kBand, kRes, kKsr><<<(unsigned)grid, kWarp, smem, stream>>>(Q);
-    if (cudaGetLastError() != cudaSuccess || !stage.finish()) return QEX_CUDA_ERROR;
+    bool ok = cudaGetLastError() == cudaSuccess;
+    if (ok && Q.ksr_defer) {
+      const size_t ks = sizeof(float) * ksr_scratch_floats(Q.nmax);
+      auto fn = Q.ksr_c == 16 ? ksr_energy_kernel<16> : ksr_energy_kernel<8>;
+      ok = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ks) ==
+           cudaSuccess;
+      long long rows = (long long)Q.num_molecules * Q.iters;
+      if (rows > (1LL << 22)) rows = 1LL << 22;
+      if (ok && rows > 0) {
+        fn<<<(unsigned)rows, kWarp, ks, stream>>>(Q);
+        ok = cudaGetLastError() == cudaSuccess;
+      }
+    }
+    if (!stage.finish() || !ok) return QEX_CUDA_ERROR;
+    g_last_launches = Q.ksr_defer ? 2 : 1;
+    return QEX_OK;
   } else {
     ks1d_kernel<kBand, kRes, kKsr><<<(unsigned)grid, kWarp, smem, stream>>>(P);
     if (cudaGetLastError() != cudaSuccess) return QEX_CUDA_ERROR;
@@ -2377,6 +2454,15 @@ int qex_ks1d_workspace_size(const qex_ks1d_options* options, int32_t num_molecul
   if (rc) return rc;
   if (num_molecules < 0) return QEX_BAD_ARG;
   *bytes = 256 + sizeof(double) * (size_t)qex::stride_doubles(options) * (size_t)num_molecules;
+  return QEX_OK;
+}
+
+int qex_ks1d_workspace_size_xc(const qex_ks1d_options* options, const qex_xc_spec* xc,
+                               int32_t num_molecules, size_t* bytes) {
+  int rc = qex_ks1d_workspace_size(options, num_molecules, bytes);
+  if (rc) return rc;
+  if (xc && xc->kind == QEX_XC_KSR)
+    *bytes = (*bytes + 255) / 256 * 256 + qex::ksr_defer_bytes(options, num_molecules);
   return QEX_OK;
 }
 

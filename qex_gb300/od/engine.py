@@ -280,7 +280,7 @@ class Ks1dEngine:
         return o
 
     def solve(self, batch: PackedBatch, xc, cfg: SolveConfig, records=RECORD_ALL, out=None,
-              initial_density=None, bucketed=True, planes=None, tune=True):
+              initial_density=None, bucketed=True, planes=None, tune=True, defer_ksr=True):
         """Run the full SCF for every molecule of ``batch``.
 
         With ``bucketed`` the batch is split into runs of equal eigenpair count
@@ -288,6 +288,9 @@ class Ks1dEngine:
         forked streams; otherwise one launch covers the whole batch.
         ``planes`` overrides the placement of the FP32 solve planes
         (``qex_ks1d_options.solve_planes``: 1 resident, 2 streamed).
+        ``defer_ksr``: with a KSR functional, size the workspace so that the
+        network's energies on the output densities run as one batched launch
+        after the SCF (``qex_ks1d_workspace_size_xc``).
         """
         torch = N.require_cuda()
         functional, params = resolve(xc)
@@ -314,8 +317,14 @@ class Ks1dEngine:
             opts.max_num_grids = max(ng_max, 5)
             opts.solve_planes = planes
             nbytes = ctypes.c_size_t()
-            N.check(self.lib.qex_ks1d_workspace_size(ctypes.byref(opts), count, ctypes.byref(nbytes)),
-                    "qex_ks1d_workspace_size")
+            if defer_ksr:
+                N.check(self.lib.qex_ks1d_workspace_size_xc(ctypes.byref(opts), ctypes.byref(spec),
+                                                            count, ctypes.byref(nbytes)),
+                        "qex_ks1d_workspace_size_xc")
+            else:
+                N.check(self.lib.qex_ks1d_workspace_size(ctypes.byref(opts), count,
+                                                         ctypes.byref(nbytes)),
+                        "qex_ks1d_workspace_size")
             aligned = (nbytes.value + 255) // 256 * 256
             plans.append((start, count, opts, total, aligned))
             total += aligned

@@ -208,6 +208,33 @@ def test_trained_scf_matches_oracle_and_exact_energies(qx, golden):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("tol", [-1.0, 1e-6])
+def test_deferred_ksr_energies_match_in_kernel(qx, golden, tol):
+    """E_xc on the output densities evaluated after the SCF (one batched
+    launch) against the same term evaluated inside the SCF kernel; with a
+    convergence tolerance the converged branch repeats the last energy."""
+    qex, od = qx
+    k = golden["ksr"]
+    p = _trained(golden)
+    ms = [od.Molecule1D.from_grids(k["grids"], k["locations"][i], k["nuclear_charges"][i], 2)
+          for i in range(0, len(k["locations"]), 4)]
+    batch = od.PackedBatch(ms)
+    cfg = od.SolveConfig(num_iterations=15, convention="local", stencil=5,
+                         num_mixing_iterations=1, enforce_reflection_symmetry=True,
+                         density_mse_converge_tolerance=tol)
+    fn = qex.Partial(qex.KSRFunctional(16), params=p)
+    eng = od.engine.default_engine()
+    a = {key: v.cpu().numpy() for key, v in eng.solve(batch, fn, cfg, defer_ksr=True).items()}
+    assert eng.last_launches >= 2
+    b = {key: v.cpu().numpy() for key, v in eng.solve(batch, fn, cfg, defer_ksr=False).items()}
+    np.testing.assert_array_equal(a["final_density"], b["final_density"])
+    np.testing.assert_array_equal(a["converged"], b["converged"])
+    np.testing.assert_allclose(a["energy"], b["energy"], atol=1e-12, rtol=0)
+    if tol > 0:
+        assert a["converged"][:, -1].any()
+
+
+@pytest.mark.gpu
 def test_ragged_ksr_batch_matches_oracle(qx):
     """Random molecules on 257- and 513-point grids (each on its own grid, one
     launch), amplitude and local conventions."""
