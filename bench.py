@@ -431,6 +431,37 @@ def run_train_eval(args):
             "grad_norm": float(np.linalg.norm(grad))}
 
 
+def run_eigh_eval(args):
+    """Generalized eigensolves F C = S C e (batch 1) at the basis sizes of the
+    3D configuration: core Hamiltonian and overlap from the analytic
+    integrals of seeded molecules (s/p and spd bases).  Median wall time per
+    solve over ``--steps`` repeats and the residual max|F C - S C e| / max|F|."""
+    import torch
+
+    from qex_gb300.td import eigh, integrals, workloads
+
+    out = {}
+    for na, basis in ((8, "sp"), (20, "sp"), (20, "spd"), (21, "spd")):
+        m = workloads.synthetic_molecule(na, seed=na, with_integrals=False, basis=basis)
+        S, T, V = integrals.int1e(m)
+        F = T + V
+        for _ in range(max(args.warmup, 1)):
+            w, C = eigh.generalized_eigh(F, S)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(max(args.steps, 3)):
+            t0 = time.perf_counter()
+            w, C = eigh.generalized_eigh(F, S)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        res = (F @ C - S @ C * w[None, :]).abs().max().item() / F.abs().max().item()
+        ev = torch.linalg.eigvalsh(S)
+        out[f"atoms_{na}_{basis}"] = {"nao": int(m.nao), "ms": float(np.median(times)) * 1e3,
+                                      "residual": res,
+                                      "overlap_condition": float(ev[-1] / ev[0])}
+    return {"workload": "generalized eigensolve, core Hamiltonian and overlap", **out}
+
+
 def run_ints_eval(args):
     """Analytic one-electron integrals and density-fitting factors (int3c2e,
     int2c2e, Cholesky, substitution) for seeded synthetic molecules of 8 and
@@ -739,6 +770,8 @@ def main():
                     help="time only the molecular grid build")
     ap.add_argument("--train-eval", action="store_true",
                     help="time only one training-loss value and gradient")
+    ap.add_argument("--eigh-eval", action="store_true",
+                    help="time the 3D generalized eigensolver at the configuration's basis sizes")
     ap.add_argument("--ints-eval", action="store_true",
                     help="time only the analytic integrals and density fitting")
     ap.add_argument("--serving-rates", type=float, nargs="*", default=[1000.0, 5000.0])
@@ -754,6 +787,12 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         torch.distributed.init_process_group("nccl")
+    if args.eigh_eval:
+        from qex_gb300 import _native
+
+        _native.load()
+        print(json.dumps({"eigh_eval": run_eigh_eval(args)}), flush=True)
+        return
     if args.ints_eval:
         from qex_gb300 import _native
 

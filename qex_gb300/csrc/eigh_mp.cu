@@ -17,7 +17,9 @@
 //   3. Ascending order (stable), eigenvectors in columns.
 // Overlaps whose FP32 Cholesky fails or whose pivots spread beyond 1e5 take a
 // stage 1 with the factor and the transformation in FP64 (the Jacobi stays
-// FP32).  Matrices that are not numerically SPD even in FP64, or that the
+// FP32); so does every matrix with n > 128 (up to 240), whose FP32 C alone
+// stays in shared memory while the rotations accumulate transposed in global
+// memory.  Matrices that are not numerically SPD even in FP64, or that the
 // check of the last refinement step rejects, keep the FP64 Jacobi path of
 // td.cu, which applies the reference's shift
 // (qedft/train/td/generalized_eigensolver.py:264-330).
@@ -48,6 +50,18 @@ __device__ inline float block_sumf(float v, float* red) {
   return s;
 }
 
+__device__ inline double block_max(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s = fmax(s, red[i]);
+  __syncthreads();
+  return s;
+}
+
 __device__ inline double block_sum(double v, double* red) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -61,7 +75,11 @@ __device__ inline double block_sum(double v, double* red) {
 }
 
 // Parallel cyclic Jacobi (round-robin pairs) in FP32 on the symmetric C (n x n,
-// shared memory); U (shared, set to I by the caller) accumulates the rotations.
+// shared memory); U (set to I by the caller) accumulates the rotations.  With
+// kUT, U is stored transposed (row p of U^T is column p of U), so the rotation
+// of its columns p, q walks two contiguous rows: the layout for U in global
+// memory when n is beyond what shared memory holds.
+template <bool kUT>
 __device__ void jacobi32(int n, float* C, float* U, float* cs, int* pq, float* red) {
   const long long nn = (long long)n * n;
   const int m = (n + 1) & ~1;
@@ -130,10 +148,12 @@ __device__ void jacobi32(int n, float* C, float* U, float* cs, int* pq, float* r
         float xp = C[(long long)i * n + p], xq = C[(long long)i * n + q];
         C[(long long)i * n + p] = c * xp - s * xq;
         C[(long long)i * n + q] = s * xp + c * xq;
-        xp = U[(long long)i * n + p];
-        xq = U[(long long)i * n + q];
-        U[(long long)i * n + p] = c * xp - s * xq;
-        U[(long long)i * n + q] = s * xp + c * xq;
+        const long long up = kUT ? (long long)p * n + i : (long long)i * n + p;
+        const long long uq = kUT ? (long long)q * n + i : (long long)i * n + q;
+        xp = U[up];
+        xq = U[uq];
+        U[up] = c * xp - s * xq;
+        U[uq] = s * xp + c * xq;
       }
       __syncthreads();
     }
@@ -227,7 +247,7 @@ __global__ void __launch_bounds__(kThreads) eigh32_kernel(int n, const double* _
     U[e] = (i == j) ? 1.0f : 0.0f;
   }
   __syncthreads();
-  jacobi32(n, C, U, cs, pq, red);
+  jacobi32<false>(n, C, U, cs, pq, red);
   // X = L^-T U: column j solves L^T x = u_j (back substitution)
   double* Xb = X + b * nn;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
@@ -310,8 +330,8 @@ __global__ void __launch_bounds__(kThreads) eigh32_fp64factor_kernel(
     U[e] = (i == j) ? 1.0f : 0.0f;
   }
   __syncthreads();
-  jacobi32(n, C, U, cs, pq, red);
-  // X = L^-T U in FP64 (column j per thread; Cd reused as the output)
+  jacobi32<false>(n, C, U, cs, pq, red);
+  // X = L^-T U in FP64 (column j per thread)
   double* Xb = X + b * nn;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     for (int i = n - 1; i >= 0; --i) {
@@ -322,6 +342,157 @@ __global__ void __launch_bounds__(kThreads) eigh32_fp64factor_kernel(
   }
   __syncthreads();
   if (threadIdx.x == 0) ok[b] = 2;
+}
+
+// ---------------------------------------------------------------------------
+// Stage 1 beyond the shared-memory FP32 solver (n > 128): the same
+// mathematics as eigh32_fp64factor_kernel in four launches, so that the
+// triangular solves spread over the GPU (a warp per vector) instead of
+// running as serial chains on one SM.  ok[b]: 3 after the Cholesky, 4 after
+// the Jacobi, 2 once X is formed.
+// ---------------------------------------------------------------------------
+constexpr int kVecWarps = 8;          // warps per CTA of the per-vector kernels
+constexpr int kMaxLargeN = 240;       // vector staging in shared memory
+
+// S = L L^T (FP64, one CTA per matrix), C64 <- A.  A and S are symmetric.
+__global__ void __launch_bounds__(kThreads) chol64_kernel(int n, const double* __restrict__ A,
+                                                          const double* __restrict__ S,
+                                                          double* __restrict__ L64,
+                                                          double* __restrict__ C64,
+                                                          int* __restrict__ ok) {
+  const int b = blockIdx.x;
+  __shared__ double piv;
+  const long long nn = (long long)n * n;
+  double* L = L64 + b * nn;
+  double* Cd = C64 + b * nn;
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    Cd[e] = A[b * nn + e];
+    L[e] = S[b * nn + e];
+  }
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      const double d = L[(long long)k * n + k];
+      piv = d;
+      L[(long long)k * n + k] = d > 0.0 ? sqrt(d) : 0.0;
+    }
+    __syncthreads();
+    if (!(piv > 0.0)) return;  // not SPD: ok stays 0, the FP64 Jacobi path applies the shift
+    const double lkk = L[(long long)k * n + k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) L[(long long)i * n + k] /= lkk;
+    __syncthreads();
+    const int r = n - k - 1;
+    for (long long e = threadIdx.x; e < (long long)r * r; e += blockDim.x) {
+      const int i = k + 1 + (int)(e / r), j = k + 1 + (int)(e % r);
+      if (j <= i) L[(long long)i * n + j] -= L[(long long)i * n + k] * L[(long long)j * n + k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) ok[b] = 3;
+}
+
+__device__ __forceinline__ double warp_sum64(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Forward substitution v <- L^-1 v for every column (rows = 0) or every row
+// (rows = 1) of C64: C <- L^-1 C, then C <- C L^-T.  A warp per vector, the
+// vector staged in shared memory, the dot products split over the lanes.
+__global__ void __launch_bounds__(kVecWarps * 32) tri_fwd_kernel(int n, int batch,
+                                                                 const double* __restrict__ L64,
+                                                                 double* __restrict__ C64,
+                                                                 const int* __restrict__ ok,
+                                                                 int rows) {
+  __shared__ double vec[kVecWarps][kMaxLargeN];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long gw = (long long)blockIdx.x * kVecWarps + w;
+  if (gw >= (long long)batch * n) return;
+  const int b = (int)(gw / n), j = (int)(gw % n);
+  if (ok[b] != 3) return;
+  const long long nn = (long long)n * n;
+  const double* L = L64 + b * nn;
+  double* Cb = C64 + b * nn;
+  const long long base = rows ? (long long)j * n : j;
+  const long long stride = rows ? 1 : n;
+  double* v = vec[w];
+  for (int i = lane; i < n; i += 32) v[i] = Cb[base + i * stride];
+  __syncwarp();
+  for (int i = 0; i < n; ++i) {
+    const double* Li = L + (long long)i * n;
+    double s = 0.0;
+    for (int k = lane; k < i; k += 32) s = fma(Li[k], v[k], s);
+    s = warp_sum64(s);
+    const double x = (v[i] - s) / Li[i];
+    __syncwarp();
+    if (lane == 0) v[i] = x;
+    __syncwarp();
+  }
+  for (int i = lane; i < n; i += 32) Cb[base + i * stride] = v[i];
+}
+
+// Jacobi of C (FP32, C in shared memory), U^T accumulated in global memory.
+__global__ void __launch_bounds__(kThreads) jacobi_large_kernel(int n,
+                                                                const double* __restrict__ C64,
+                                                                float* __restrict__ U32,
+                                                                int* __restrict__ ok) {
+  const int b = blockIdx.x;
+  if (ok[b] != 3) return;
+  extern __shared__ float sm[];
+  const long long nn = (long long)n * n;
+  const int m = (n + 1) & ~1;
+  float* C = sm;
+  float* cs = C + nn;
+  int* pq = reinterpret_cast<int*>(cs + m);
+  float* red = reinterpret_cast<float*>(pq + m);
+  float* U = U32 + b * nn;
+  const double* Cd = C64 + b * nn;
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    C[e] = (float)(0.5 * (Cd[e] + Cd[(long long)j * n + i]));
+    U[e] = (i == j) ? 1.0f : 0.0f;
+  }
+  __syncthreads();
+  jacobi32<true>(n, C, U, cs, pq, red);
+  __syncthreads();
+  if (threadIdx.x == 0) ok[b] = 4;
+}
+
+// X[:, j] = L^-T u_j (backward substitution, FP64), u_j = row j of U^T.
+__global__ void __launch_bounds__(kVecWarps * 32) tri_back_kernel(int n, int batch,
+                                                                  const double* __restrict__ L64,
+                                                                  const float* __restrict__ U32,
+                                                                  double* __restrict__ X,
+                                                                  const int* __restrict__ ok) {
+  __shared__ double vec[kVecWarps][kMaxLargeN];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long gw = (long long)blockIdx.x * kVecWarps + w;
+  if (gw >= (long long)batch * n) return;
+  const int b = (int)(gw / n), j = (int)(gw % n);
+  if (ok[b] != 4) return;
+  const long long nn = (long long)n * n;
+  const double* L = L64 + b * nn;
+  const float* u = U32 + b * nn + (long long)j * n;
+  double* v = vec[w];
+  for (int i = lane; i < n; i += 32) v[i] = (double)u[i];
+  __syncwarp();
+  for (int i = n - 1; i >= 0; --i) {
+    double s = 0.0;
+    for (int k = i + 1 + lane; k < n; k += 32) s = fma(L[(long long)k * n + i], v[k], s);
+    s = warp_sum64(s);
+    const double x = (v[i] - s) / L[(long long)i * n + i];
+    __syncwarp();
+    if (lane == 0) v[i] = x;
+    __syncwarp();
+  }
+  double* Xb = X + b * nn;
+  for (int i = lane; i < n; i += 32) Xb[(long long)i * n + j] = v[i];
+}
+
+__global__ void large_done_kernel(int batch, int* __restrict__ ok) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < batch; b += gridDim.x * blockDim.x)
+    if (ok[b] == 4) ok[b] = 2;
 }
 
 // Batched split-K FP64 GEMM partials: P[b][kc] = op(A_b)[:, kc chunk] B_b[kc chunk, :]
@@ -437,7 +608,35 @@ __global__ void __launch_bounds__(kThreads) refine_update_kernel(int n, const do
   // last step: the X it refines must already be accurate to ~1e-7 (it is
   // unless S is too ill-conditioned for the FP32 solve), so that this step
   // reaches the FP64 floor; otherwise hand the matrix to the FP64 path
-  if (check && threadIdx.x == 0 && !(rn <= 1e-14 && od <= 1e-14 * an)) ok[b] = 0;
+  // checks 2 and 3 also bound, for every pair, how far the diagonal of T is
+  // from the eigenvalues of its 2 x 2 block (an unresolved near-degenerate
+  // pair leaves both off by ~T_ij^2 / gap although |T - D|_F is small)
+  double pe = 0.0;
+  if (check >= 2) {
+    for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+      const int i = (int)(e / n), j = (int)(e % n);
+      if (i == j) continue;
+      const double d = 0.5 * fabs(lb[j] - lb[i]), t2 = Tb[e] * Tb[e];
+      const double q = d + sqrt(fma(d, d, t2));
+      if (q > 0.0) pe = fmax(pe, t2 / q);
+    }
+    pe = block_max(pe, red);
+  }
+  // check 1: this step decides; 2 and 3: the last two steps, either passing
+  // suffices (at the FP64 floor of an ill-conditioned S, |R| fluctuates from
+  // step to step by orders of magnitude)
+  if (check && threadIdx.x == 0 && ok[b] != 0) {
+    const bool pass = rn <= 1e-14 && od <= 1e-14 * an && (check < 2 || pe <= 1e-12 * sqrt(an));
+    if (check == 1) {
+      if (!pass) ok[b] = 0;
+    } else if (check == 2) {
+      if (!pass) ok[b] |= 8;
+    } else if (pass) {
+      ok[b] &= ~8;
+    } else if (ok[b] & 8) {
+      ok[b] = 0;
+    }
+  }
   for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
     const int i = (int)(e / n), j = (int)(e % n);
     double v;
@@ -448,6 +647,99 @@ __global__ void __launch_bounds__(kThreads) refine_update_kernel(int n, const do
       v = (fabs(gap) > delta) ? (Tb[e] + lb[j] * Rb[e]) / gap : 0.5 * Rb[e];
     }
     Eb[e] = v;
+  }
+}
+
+// Rayleigh-Ritz on strongly mixed pairs: T = X^T A X of a nearly
+// S-orthonormal X; the pairs (i, j) with |t_ij| > 1e-3 |t_ii - t_jj| (a mixing
+// angle above ~1e-3) are rotated by FP64 Jacobi rotations (three sweeps over
+// the pair list, in a fixed order) applied to T and to the columns of X.  The
+// FP32 start cannot resolve pairs closer than ~1e-7 |C|; their first-order
+// corrections would be O(1), outside the refinement's convergence region (and
+// pairs inside its cluster threshold are never separated at all).  At most
+// kMaxPairs pairs (else nothing is done).
+constexpr int kMaxPairs = 512;
+
+__global__ void __launch_bounds__(kThreads) cluster_jacobi_kernel(int n, double* __restrict__ T,
+                                                                  double* __restrict__ X,
+                                                                  const int* __restrict__ ok) {
+  const int b = blockIdx.x;
+  if (!ok[b]) return;
+  __shared__ int cnt[kThreads];
+  __shared__ int pi[kMaxPairs], pj[kMaxPairs];
+  __shared__ double rot[2];
+  __shared__ int npair;
+  const long long nn = (long long)n * n;
+  double* Tb = T + b * nn;
+  double* Xb = X + b * nn;
+  // pair list in (i, j) order: counts per row, prefix, fill (n <= kThreads)
+  auto mixed = [&](int i, int j) {
+    return fabs(Tb[(long long)i * n + j]) >
+           1e-3 * fabs(Tb[(long long)i * n + i] - Tb[(long long)j * n + j]);
+  };
+  const int i0 = threadIdx.x;
+  int c = 0;
+  if (i0 < n)
+    for (int j = i0 + 1; j < n; ++j) c += mixed(i0, j);
+  cnt[threadIdx.x] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int t = 0; t < (int)blockDim.x; ++t) {
+      const int v = cnt[t];
+      cnt[t] = acc;
+      acc += v;
+    }
+    npair = acc;
+  }
+  __syncthreads();
+  if (npair > kMaxPairs || npair == 0) return;
+  if (i0 < n) {
+    int q = cnt[i0];
+    for (int j = i0 + 1; j < n; ++j)
+      if (mixed(i0, j)) {
+        pi[q] = i0;
+        pj[q] = j;
+        ++q;
+      }
+  }
+  __syncthreads();
+  const int np = npair;
+  for (int sweep = 0; sweep < 3; ++sweep) {
+    for (int q = 0; q < np; ++q) {
+      const int i = pi[q], j = pj[q];
+      if (threadIdx.x == 0) {
+        const double tij = Tb[(long long)i * n + j];
+        double cc = 1.0, ss = 0.0;
+        if (tij != 0.0) {
+          const double tau = (Tb[(long long)j * n + j] - Tb[(long long)i * n + i]) / (2.0 * tij);
+          const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(fma(tau, tau, 1.0)));
+          cc = 1.0 / sqrt(fma(t, t, 1.0));
+          ss = t * cc;
+        }
+        rot[0] = cc;
+        rot[1] = ss;
+      }
+      __syncthreads();
+      const double cc = rot[0], ss = rot[1];
+      if (ss != 0.0) {
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {  // columns i, j of T and X
+          const double ti = Tb[(long long)k * n + i], tj = Tb[(long long)k * n + j];
+          Tb[(long long)k * n + i] = cc * ti - ss * tj;
+          Tb[(long long)k * n + j] = ss * ti + cc * tj;
+          const double xi = Xb[(long long)k * n + i], xj = Xb[(long long)k * n + j];
+          Xb[(long long)k * n + i] = cc * xi - ss * xj;
+          Xb[(long long)k * n + j] = ss * xi + cc * xj;
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {  // rows i, j of T
+          const double ti = Tb[(long long)i * n + k], tj = Tb[(long long)j * n + k];
+          Tb[(long long)i * n + k] = cc * ti - ss * tj;
+          Tb[(long long)j * n + k] = ss * ti + cc * tj;
+        }
+      }
+      __syncthreads();
+    }
   }
 }
 
@@ -482,21 +774,29 @@ namespace qex_mp_host {
 
 using namespace qex_mp;
 
-constexpr int kMaxN = 128;  // 3 n^2 FP32 matrices in shared memory
+constexpr int kMaxSmemN = 128;  // eigh32_kernel: 3 n^2 FP32 matrices in shared memory
+constexpr int kMaxN = 240;      // beyond kMaxSmemN: C alone in shared memory (checked at launch)
+static_assert(kMaxN <= kMaxLargeN, "per-vector kernels stage up to kMaxLargeN entries");
 
 int ksplit_of(int n) { return (n + kKC - 1) / kKC; }
 
 // Doubles of the mixed-precision area per matrix: As, Ss, X, X', T, R, E
 // (7 n^2), split-K partials (ksplit n^2), lambda (n), the FP64 factor and
-// transformed matrix of the fallback stage 1 (2 n^2), one spare.
+// transformed matrix of the FP64-factor stage (2 n^2), one spare; beyond
+// kMaxSmemN also U^T in FP32 (n^2 floats).
 long long area_doubles(int n) {
   const long long nn = (long long)n * n;
-  return (9 + ksplit_of(n)) * nn + n + 1;
+  return (9 + ksplit_of(n)) * nn + n + 1 + (n > kMaxSmemN ? (nn + 1) / 2 + 1 : 0);
 }
 
 size_t smem_factor64(int n) {
   const int m = (n + 1) & ~1;
   return sizeof(float) * (2 * (size_t)n * n + 2 * (size_t)m + 33);
+}
+
+size_t smem_factor64_large(int n) {
+  const int m = (n + 1) & ~1;
+  return sizeof(float) * ((size_t)n * n + 2 * (size_t)m + 33);
 }
 
 size_t smem32(int n) {
@@ -523,11 +823,19 @@ void gemm(cudaStream_t s, int batch, int n, bool ta, const double* A, const doub
 
 // Host entry used by qex_td_gen_eigh: runs the mixed-precision solver on the
 // batch and leaves ok[b] = 0 for matrices that need the FP64 path.  Returns
-// false when n is beyond the shared-memory solver (then nothing was launched).
+// false when n is beyond the solver (n > 240, or C does not fit in shared
+// memory; then nothing was launched).
 bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double* w, double* V,
                      int32_t* status, double* area, int* ok_out, cudaStream_t s) {
   using namespace qex_mp_host;
   if (n > kMaxN) return false;
+  const bool large = n > kMaxSmemN;
+  if (large) {
+    int dev = 0, max_optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (smem_factor64_large(n) + 64 > (size_t)max_optin) return false;  // + static shared
+  }
   const long long nn = (long long)n * n;
   const long long per = (long long)batch * nn;
   double* As = area;
@@ -544,22 +852,51 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
   int* ok = ok_out;
   const int eb = (int)((per + 255) / 256 < 4096 ? (per + 255) / 256 : 4096);
   sym_kernel<<<eb, 256, 0, s>>>(batch, n, A, S, As, Ss);
-  const size_t sm = smem32(n);
-  cudaFuncSetAttribute(eigh32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  eigh32_kernel<<<batch, kThreads, sm, s>>>(n, As, Ss, X, ok);
-  // overlaps too ill-conditioned for the FP32 Cholesky: FP64 factor, FP32 Jacobi
-  const size_t sm64 = smem_factor64(n);
-  cudaFuncSetAttribute(eigh32_fp64factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sm64);
-  eigh32_fp64factor_kernel<<<batch, kThreads, sm64, s>>>(n, As, Ss, X, L64, C64, ok);
-  for (int it = 0; it < kRefineSteps; ++it) {
+  if (!large) {
+    const size_t sm = smem32(n);
+    cudaFuncSetAttribute(eigh32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    eigh32_kernel<<<batch, kThreads, sm, s>>>(n, As, Ss, X, ok);
+    // overlaps too ill-conditioned for the FP32 Cholesky: FP64 factor, FP32 Jacobi
+    const size_t sm64 = smem_factor64(n);
+    cudaFuncSetAttribute(eigh32_fp64factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm64);
+    eigh32_fp64factor_kernel<<<batch, kThreads, sm64, s>>>(n, As, Ss, X, L64, C64, ok);
+  } else {
+    // every matrix: FP64 factor and transformation, FP32 Jacobi with C in
+    // shared memory and U^T in global memory, FP64 back-transformation
+    float* U32 = reinterpret_cast<float*>(C64 + per);
+    cudaMemsetAsync(ok, 0, sizeof(int) * (size_t)batch, s);
+    chol64_kernel<<<batch, kThreads, 0, s>>>(n, As, Ss, L64, C64, ok);
+    const long long vecs = (long long)batch * n;
+    const unsigned vb = (unsigned)((vecs + kVecWarps - 1) / kVecWarps);
+    tri_fwd_kernel<<<vb, kVecWarps * 32, 0, s>>>(n, batch, L64, C64, ok, 0);  // C <- L^-1 C
+    tri_fwd_kernel<<<vb, kVecWarps * 32, 0, s>>>(n, batch, L64, C64, ok, 1);  // C <- C L^-T
+    const size_t sml = smem_factor64_large(n);
+    cudaFuncSetAttribute(jacobi_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sml);
+    jacobi_large_kernel<<<batch, kThreads, sml, s>>>(n, C64, U32, ok);
+    tri_back_kernel<<<vb, kVecWarps * 32, 0, s>>>(n, batch, L64, U32, X, ok);
+    large_done_kernel<<<(batch + 255) / 256, 256, 0, s>>>(batch, ok);
+  }
+  // four steps; beyond the shared-memory solver six, with a Rayleigh-Ritz
+  // pass on strongly mixed pairs after the first and the last two checked
+  // (either passing suffices)
+  const int steps = large ? kRefineSteps + 2 : kRefineSteps;
+  for (int it = 0; it < steps; ++it) {
+    if (large && it == 1) {
+      gemm(s, batch, n, false, As, X, P, nullptr, false, 1.0, T);  // T = A X
+      gemm(s, batch, n, true, X, T, P, nullptr, false, 1.0, E);    // E <- X^T A X
+      cluster_jacobi_kernel<<<batch, kThreads, 0, s>>>(n, E, X, ok);
+    }
     gemm(s, batch, n, false, Ss, X, P, nullptr, false, 1.0, T);   // T = S X
     gemm(s, batch, n, true, X, T, P, nullptr, true, -1.0, R);     // R = I - X^T S X
     gemm(s, batch, n, false, As, X, P, nullptr, false, 1.0, T);   // T = A X
     gemm(s, batch, n, true, X, T, P, nullptr, false, 1.0, E);     // E <- X^T A X
     // move X^T A X into T and build the correction in E
     cudaMemcpyAsync(T, E, sizeof(double) * per, cudaMemcpyDeviceToDevice, s);
-    refine_update_kernel<<<batch, kThreads, 0, s>>>(n, As, R, T, E, lam, ok, it == kRefineSteps - 1);
+    const int check = !large ? (it == steps - 1 ? 1 : 0)
+                             : (it == steps - 2 ? 2 : (it == steps - 1 ? 3 : 0));
+    refine_update_kernel<<<batch, kThreads, 0, s>>>(n, As, R, T, E, lam, ok, check);
     gemm(s, batch, n, false, X, E, P, X, false, 1.0, X2);         // X' = X + X E
     double* t = X;
     X = X2;

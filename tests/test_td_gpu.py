@@ -56,7 +56,7 @@ def test_rho_lda_vxc(td, mols):
                                    atol=1e-12 * np.abs(vmat_r).max())
 
 
-@pytest.mark.parametrize("n", [1, 4, 17, 33, 64])
+@pytest.mark.parametrize("n", [1, 4, 17, 33, 64, 150, 231])
 def test_generalized_eigh(td, n):
     torch, eigh, numint, scf, W = td
     rng = np.random.default_rng(n)
@@ -73,6 +73,26 @@ def test_generalized_eigh(td, n):
         # eigenvectors: S-orthonormal and A V = S V diag(w)
         np.testing.assert_allclose(V[b].T @ S[b] @ V[b], np.eye(n), atol=1e-10)
         np.testing.assert_allclose(A[b] @ V[b], S[b] @ V[b] * w[b][None, :], atol=1e-9)
+
+
+@pytest.mark.parametrize("na", [20, 21])
+def test_generalized_eigh_large_basis(td, na):
+    """Core Hamiltonian and overlap of 20- and 21-atom molecules in the spd
+    basis (nao 157 and 224, overlap condition 5e5 and 3e6): the solver
+    beyond the shared-memory FP32 stage against the oracle."""
+    torch, eigh, numint, scf, W = td
+    from qex_gb300.td import integrals
+
+    m = W.synthetic_molecule(na, seed=na, with_integrals=False, basis="spd")
+    S, T, V = integrals.int1e(m)
+    F = T + V
+    w, C, st = eigh.generalized_eigh(F, S, return_status=True)
+    assert int(_host(st)) == 0
+    Fh, Sh, w, C = _host(F), _host(S), _host(w), _host(C)
+    wr, _ = o.generalized_eigh(Fh, Sh)
+    np.testing.assert_allclose(w, wr, atol=1e-9 * np.abs(wr).max(), rtol=0)
+    assert np.abs(Fh @ C - Sh @ C * w[None, :]).max() < 1e-9 * np.abs(Fh).max()
+    np.testing.assert_allclose(C.T @ Sh @ C, np.eye(m.nao), atol=1e-8)
 
 
 def test_generalized_eigh_spd_shift(td):
