@@ -52,6 +52,50 @@ def test_version_and_workspace_size_without_gpu():
     assert lib.qex_ks1d_workspace_size(ctypes.byref(o), 4, ctypes.byref(nb)) == N.QEX_BAD_ARG
 
 
+def test_ksr_workspace_adds_deferred_energy_rows_without_gpu():
+    """qex_ks1d_workspace_size_xc: the base size for every functional but KSR,
+    which adds num_molecules x num_iterations x max_num_grids doubles (the
+    output-density rows evaluated after the SCF)."""
+    from qex_gb300 import _native as N
+
+    lib = N.load()
+    o = N.Ks1dOptions(stencil=5, interaction=0, interaction_a=1.071295, interaction_b=1 / 2.385345,
+                      num_iterations=15, alpha=0.5, alpha_decay=0.9, num_mixing_iterations=1,
+                      density_mse_converge_tolerance=-1.0, max_num_grids=513,
+                      max_num_electrons=2, max_nuclei=2)
+    base, xc_size = ctypes.c_size_t(), ctypes.c_size_t()
+    assert lib.qex_ks1d_workspace_size(ctypes.byref(o), 64, ctypes.byref(base)) == 0
+    spec = N.XcSpec(kind=N.QEX_XC_LDA_EXP_COULOMB)
+    assert lib.qex_ks1d_workspace_size_xc(ctypes.byref(o), ctypes.byref(spec), 64,
+                                          ctypes.byref(xc_size)) == 0
+    assert xc_size.value == base.value
+    spec = N.XcSpec(kind=N.QEX_XC_KSR, ksr_channels=16)
+    assert lib.qex_ks1d_workspace_size_xc(ctypes.byref(o), ctypes.byref(spec), 64,
+                                          ctypes.byref(xc_size)) == 0
+    aligned = (base.value + 255) // 256 * 256
+    assert xc_size.value == aligned + 8 * 64 * 15 * 513
+    o.stencil = 4
+    assert lib.qex_ks1d_workspace_size_xc(ctypes.byref(o), ctypes.byref(spec), 64,
+                                          ctypes.byref(xc_size)) == N.QEX_BAD_ARG
+
+
+def test_shell_arrays_reject_f_shells():
+    import numpy as np
+
+    from qex_gb300.td import workloads
+
+    sh = [workloads.Shell(center=np.zeros(3), l=l, exponents=np.array([1.0]),
+                          coefficients=np.array([1.0])) for l in (0, 1, 2)]
+    centers, l, poff, aoff, ex, co = workloads.shell_arrays(sh)
+    assert list(aoff) == [0, 1, 4] and list(poff) == [0, 1, 2, 3]
+    assert workloads.cart_components(2) == [(2, 0, 0), (1, 1, 0), (1, 0, 1), (0, 2, 0), (0, 1, 1),
+                                            (0, 0, 2)]
+    sh.append(workloads.Shell(center=np.zeros(3), l=3, exponents=np.array([1.0]),
+                              coefficients=np.array([1.0])))
+    with pytest.raises(ValueError):
+        workloads.shell_arrays(sh)
+
+
 def test_xc_resolution_rejects_arbitrary_callables():
     from qex_gb300.xc import Partial, PowerXC, resolve
 
