@@ -1,7 +1,8 @@
 /*
  * qex_probe.h -- pipe-throughput probe used as the roofline denominator of
- * the 1D SCF kernel (FP64 FMA throughput is not part of the driver-measured
- * peaks).  No counterpart in the reference.
+ * the 1D SCF kernel (the machine's measured peaks cover HBM copy bandwidth and
+ * bf16 GEMM throughput, not FP64 FMA throughput).  No counterpart in the
+ * reference.
  */
 #ifndef QEX_PROBE_H_
 #define QEX_PROBE_H_
