@@ -177,6 +177,7 @@ def vxc_matrix(ao, weights, vrho):
 
 
 GGA_CODES = ("PBE_X", "GGA_X_PBE")
+_LDA_CODES = ("LDA", "LDA_X", "SLATER", "LDA,VWN", "SLATER,VWN")
 
 
 def eval_ao_deriv1(mol, coords=None):
@@ -261,8 +262,90 @@ def nr_rks(ao, weights, dm, xc_code="LDA"):
         exc, vrho, nelec, excsum = eval_xc_nn(rho, xc_code, weights)
         return nelec, excsum, vxc_matrix(ao, weights, vrho)
     code = xc_code.upper().replace(" ", "")
-    if code not in ("LDA", "LDA_X", "SLATER", "LDA,VWN", "SLATER,VWN"):
+    if code not in _LDA_CODES:
         raise NotImplementedError(f"xc_code {xc_code!r}: the GPU path implements the LDA exchange "
                                   "(with or without VWN correlation) and the neural functional")
     exc, vrho, nelec, excsum = eval_xc_lda(rho, weights, vwn=code.endswith("VWN"))
     return nelec, excsum, vxc_matrix(ao, weights, vrho)
+
+
+class NumInt:
+    """The reference's ``NumInt`` interface (``qedft/train/td/numint.py:16-273``
+    ``nr_rks``, and ``eval_rho`` / ``eval_xc`` of ``:276-400``) over the GPU
+    kernels.
+
+    ``mol``: a molecule with Cartesian shells (``shells``, ``nao``,
+    ``shell_arrays()``, e.g. ``workloads.Molecule3D``).  ``grids``: anything
+    with ``coords`` (G, 3) and ``weights`` (G,), such as
+    ``qex_gb300.td.grids.Grids`` after ``build()`` or the molecule itself.
+    ``xc_code``: "LDA" / "LDA_X" / "SLATER" (Slater exchange), "LDA,VWN" (the
+    reference's default), "PBE_X" (GGA), or a code containing "NN" with the
+    network passed as ``params`` (a ``NeuralXC`` or its flax parameter tree).
+    ``dms``: one (nao, nao) density matrix or a stack of them; the results are
+    per matrix, unwrapped for a single one, as the reference returns them.
+    ``relativity``, ``hermi``, ``max_memory`` and ``verbose`` are accepted for
+    the reference's signature; the GPU path holds the whole grid at once.
+    """
+
+    @staticmethod
+    def _functional(xc_code, params):
+        if isinstance(xc_code, NeuralXC):
+            return xc_code
+        if isinstance(xc_code, str) and "NN" in xc_code.upper():
+            if params is None:
+                raise ValueError(f"xc_code {xc_code!r} needs the network as params")
+            return params if isinstance(params, NeuralXC) else NeuralXC(params)
+        return xc_code
+
+    @staticmethod
+    def _code(xc):
+        return xc.upper().replace(" ", "") if isinstance(xc, str) else None
+
+    def nr_rks(self, mol, grids, xc_code, dms, relativity=0, hermi=0, max_memory=2000,
+               verbose=None, params=None):
+        torch = N.require_cuda()
+        xc = self._functional(xc_code, params)
+        gga = self._code(xc) in GGA_CODES
+        ao = eval_ao_deriv1(mol, grids.coords) if gga else eval_ao(mol, grids.coords)
+        d = _dev(dms, torch.float64)
+        single = d.dim() == 2
+        parts = [nr_rks(ao, grids.weights, dm, xc) for dm in (d[None] if single else d)]
+        nelec, excsum, vmat = ([p[k] for p in parts] for k in range(3))
+        if single:
+            return nelec[0], excsum[0], vmat[0]
+        return nelec, excsum, vmat
+
+    def eval_rho(self, mol, ao, dm, non0tab=None, xctype="LDA", hermi=0, verbose=None):
+        """rho (LDA, from (G, nao) AO values) or rho and its gradient (GGA, from
+        the (4, G, nao) values and derivatives)."""
+        kind = xctype.upper()
+        if kind == "LDA":
+            return eval_rho(ao, dm)
+        if kind == "GGA":
+            return eval_rho_gga(ao, dm)
+        raise NotImplementedError(f"xctype {xctype!r}: the GPU path evaluates LDA and GGA densities")
+
+    @staticmethod
+    def eval_xc(xc_code, rho, spin=0, relativity=0, deriv=1, verbose=None, params=None,
+                weights=None):
+        """(exc, (vrho, None, None, None), None, None) of an LDA or neural
+        functional (``qedft/train/td/xc.py:57-87``); ValueError unless deriv == 1,
+        as the reference.  The global neural form needs the grid ``weights``."""
+        if deriv != 1:
+            raise ValueError("eval_xc: deriv should be set to 1.")
+        if spin != 0:
+            raise NotImplementedError("spin-polarised functionals are not on the GPU path")
+        xc = NumInt._functional(xc_code, params)
+        if isinstance(xc, NeuralXC):
+            if xc.is_global:
+                raise NotImplementedError("the global network's exc is one number: use nr_rks")
+            exc, vrho = eval_xc_nn(rho, xc)
+        elif NumInt._code(xc) in _LDA_CODES:
+            torch = N.require_cuda()
+            r = _dev(rho, torch.float64)
+            w = torch.ones_like(r) if weights is None else weights
+            exc, vrho, _, _ = eval_xc_lda(r, w, vwn=NumInt._code(xc).endswith("VWN"))
+        else:
+            raise NotImplementedError(f"eval_xc for {xc_code!r}: LDA and neural functionals "
+                                      "(GGA through nr_rks)")
+        return exc, (vrho, None, None, None), None, None

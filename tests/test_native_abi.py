@@ -96,6 +96,19 @@ def test_shell_arrays_reject_f_shells():
         workloads.shell_arrays(sh)
 
 
+def test_numint_interface_checks_without_gpu():
+    """The reference's eval_xc rule (deriv must be 1) and a neural xc_code
+    without its network are rejected before any device work."""
+    import numpy as np
+
+    from qex_gb300.td.numint import NumInt
+
+    with pytest.raises(ValueError):
+        NumInt.eval_xc("LDA", np.ones(4), deriv=0)
+    with pytest.raises(ValueError):
+        NumInt.eval_xc("NN-LDA", np.ones(4), deriv=1)
+
+
 def test_xc_resolution_rejects_arbitrary_callables():
     from qex_gb300.xc import Partial, PowerXC, resolve
 

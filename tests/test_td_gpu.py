@@ -252,3 +252,40 @@ def test_lda_vwn_matches_oracle(td, mols):
     e_ref, _, _ = o.scf(m, max_cycle=12, vwn=True)
     np.testing.assert_allclose(_host(res.energies), e_ref, atol=1e-5, rtol=0)
     assert abs(_host(res.energies)[-1] - e_ref[-1]) < 1e-8
+
+
+def test_numint_class_mirrors_reference_interface(td):
+    """NumInt.nr_rks(mol, grids, xc_code, dms, ...) with the reference's
+    signature and return convention (per matrix for a stack, unwrapped for a
+    single one) against the oracle; eval_rho / eval_xc with its deriv rule."""
+    torch, eigh, numint, scf, W = td
+    m = W.synthetic_molecule(3, seed=1, basis="spd")
+    e0, c0 = o.generalized_eigh(m.h1e, m.s1e)
+    dm = o.make_rdm1(c0, o.get_occ(m.nelectron, e0))
+    dms = np.stack([dm, 0.5 * dm])
+    ni = numint.NumInt()
+    nelec, excsum, vmat = ni.nr_rks(m, m, "LDA,VWN", dms)
+    assert len(vmat) == 2
+    ao_r, grad_r = o.eval_ao(m.shells, m.coords, deriv=1)
+    for k, d in enumerate(dms):
+        n_r, e_r, v_r = o.nr_rks_lda(ao_r, m.weights, d, vwn=True)
+        assert abs(float(nelec[k]) - n_r) < 1e-10 * max(1.0, abs(n_r))
+        assert abs(float(excsum[k]) - e_r) < 1e-10 * max(1.0, abs(e_r))
+        np.testing.assert_allclose(_host(vmat[k]), v_r, rtol=0, atol=1e-10 * np.abs(v_r).max())
+    n1, e1, v1 = ni.nr_rks(m, m, "PBE_X", dm)
+    ao4_r = np.concatenate([ao_r[None], grad_r], axis=0)
+    n_r, e_r, v_r = o.nr_rks_gga(ao4_r, m.weights, dm)
+    assert abs(float(n1) - n_r) < 1e-10 * max(1.0, abs(n_r))
+    assert abs(float(e1) - e_r) < 1e-10 * max(1.0, abs(e_r))
+    np.testing.assert_allclose(_host(v1), v_r, rtol=0, atol=1e-10 * np.abs(v_r).max())
+    ao = numint.eval_ao(m)
+    rho = ni.eval_rho(m, ao, dm)
+    rho_r = o.eval_rho(ao_r, dm)
+    np.testing.assert_allclose(_host(rho), rho_r, rtol=1e-11, atol=1e-12 * np.abs(rho_r).max())
+    with pytest.raises(ValueError):
+        ni.eval_xc("LDA", rho, deriv=2)
+    exc, (vrho, vsigma, _, _), fxc, kxc = ni.eval_xc("LDA,VWN", rho)
+    assert vsigma is None and fxc is None and kxc is None
+    _, _, v_ref = o.nr_rks_lda(ao_r, m.weights, dm, vwn=True)
+    np.testing.assert_allclose(_host(numint.vxc_matrix(ao, m.weights, vrho)), v_ref, rtol=0,
+                               atol=1e-10 * np.abs(v_ref).max())
