@@ -1,0 +1,79 @@
+"""CPU tests of the serving layer's host logic: the seeded request streams
+(Poisson arrivals, the 1D/3D mix) and the latency summary (p50/p99, the
+converged count, the 1D/3D split).  The GPU admission and the served-equals-
+alone identity are in ``test_serving_gpu.py``."""
+
+import numpy as np
+
+from qex_gb300 import serving
+
+
+def test_poisson_arrivals_are_seeded_sorted_and_inside_the_window():
+    a = serving.poisson_arrivals(500.0, 2.0, seed=3)
+    b = serving.poisson_arrivals(500.0, 2.0, seed=3)
+    np.testing.assert_array_equal(a, b)
+    assert np.all(np.diff(a) >= 0.0) and a[0] >= 0.0 and a[-1] <= 2.0
+    # count ~ Poisson(1000): within 5 standard deviations
+    assert abs(a.size - 1000) < 5 * np.sqrt(1000)
+
+
+def test_mixed_requests_fraction_shape_and_reproducibility():
+    arr = np.linspace(0.0, 1.0, 4000)
+    keys = ["a", "b", "c"]
+    reqs = serving.mixed_requests(arr, keys, frac3d=0.2, seed=5)
+    again = serving.mixed_requests(arr, keys, frac3d=0.2, seed=5)
+    assert [r.graph3d for r in reqs] == [r.graph3d for r in again]
+    n3 = sum(r.is3d for r in reqs)
+    assert abs(n3 / len(reqs) - 0.2) < 0.03
+    assert {r.graph3d for r in reqs if r.is3d} == set(keys)
+    for r in reqs:
+        if r.is3d:
+            assert r.molecule is None
+        else:
+            m = r.molecule
+            assert m.num_grids == 513 and m.num_electrons == 2
+            loc = np.asarray(m.locations)
+            assert np.isclose(loc[0], -loc[1]) and 0.5 <= loc[1] <= 1.5
+    assert [r.rid for r in reqs] == list(range(len(arr)))
+    assert all(r.arrival == t for r, t in zip(reqs, arr))
+    # no resident 3D molecules: every request is 1D
+    assert not any(r.is3d for r in serving.mixed_requests(arr[:50], [], seed=1))
+
+
+def test_config1_requests_match_the_plain_configuration():
+    reqs = serving.config1_requests([0.0, 0.5, 1.0], seed=2)
+    for r in reqs:
+        m = r.molecule
+        assert m.num_grids == 513 and m.grid_spacing == 0.08
+        assert list(m.nuclear_charges) == [1.0, 1.0] and m.num_electrons == 2
+        assert not r.is3d
+
+
+def _done(rid, arrival, latency, dE, status=0, graph=None):
+    r = serving.Request(rid=rid, molecule=None, arrival=arrival, graph3d=graph)
+    r.start = arrival
+    r.finish = arrival + latency
+    r.energies = np.array([-1.0, -1.0 + dE])
+    r.status = status
+    return r
+
+
+def test_latency_summary_percentiles_converged_count_and_split():
+    lat = np.linspace(0.001, 0.1, 100)
+    reqs = []
+    for i, l in enumerate(lat):
+        dE = 1e-9 if i % 4 else 1e-6        # every fourth not converged
+        status = 0x1 if i == 1 else 0        # a flagged solve does not count
+        reqs.append(_done(i, 0.01 * i, l, dE, status, graph="m" if i % 5 == 0 else None))
+    s = serving.latency_summary(reqs)
+    assert s["requests"] == 100
+    assert s["converged"] == 100 - 25 - 1
+    np.testing.assert_allclose(s["p50_ms"], np.percentile(lat, 50) * 1e3)
+    np.testing.assert_allclose(s["p99_ms"], np.percentile(lat, 99) * 1e3)
+    span = max(r.finish for r in reqs) - min(r.arrival for r in reqs)
+    np.testing.assert_allclose(s["solves_per_s"], 100 / span)
+    assert s["3d"]["requests"] == 20 and s["1d"]["requests"] == 80
+    assert s["1d"]["span_s"] == s["span_s"]
+    # a per-molecule flag (here the degenerate-frontier bit) also excludes it
+    r = _done(0, 0.0, 0.01, 1e-9, status=0x100)
+    assert serving.latency_summary([r, _done(1, 0.0, 0.02, 1e-9)])["converged"] == 1
