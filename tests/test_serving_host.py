@@ -77,3 +77,32 @@ def test_latency_summary_percentiles_converged_count_and_split():
     # a per-molecule flag (here the degenerate-frontier bit) also excludes it
     r = _done(0, 0.0, 0.01, 1e-9, status=0x100)
     assert serving.latency_summary([r, _done(1, 0.0, 0.02, 1e-9)])["converged"] == 1
+
+
+def test_plan_tuner_key_is_the_shape_histogram():
+    """The launch-plan cache key: molecules per (grid size, eigenpair count)
+    class plus the XC kind and the solve options, independent of order."""
+    import dataclasses
+
+    from qex_gb300.od.autotune import PlanTuner
+    from qex_gb300.od.engine import SolveConfig
+
+    @dataclasses.dataclass
+    class M:
+        num_electrons: int
+
+    @dataclasses.dataclass
+    class B:
+        num_grids_host: list
+        molecules: list
+
+    cfg = SolveConfig()
+    a = B([513, 257, 513], [M(2), M(3), M(2)])
+    b = B([257, 513, 513], [M(3), M(2), M(2)])
+    ka, kb = PlanTuner.key(a, 3, cfg), PlanTuner.key(b, 3, cfg)
+    assert ka == kb
+    assert ka[0] == ((257, 2, 1), (513, 2, 2))
+    assert PlanTuner.key(a, 4, cfg) != ka
+    assert PlanTuner.key(a, 3, dataclasses.replace(cfg, stencil=3)) != ka
+    c = B([513, 257, 513], [M(4), M(3), M(2)])  # one molecule moves to K = 3
+    assert PlanTuner.key(c, 3, cfg) != ka
