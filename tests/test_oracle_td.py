@@ -135,3 +135,83 @@ def test_vwn5_correlation_known_values_and_derivative():
     np.testing.assert_allclose(((rho + h) * ep - (rho - h) * em) / (2 * h), v, rtol=0, atol=1e-8)
     e0, v0 = o.vwn5_c(np.zeros(3))
     assert (e0 == 0).all() and (v0 == 0).all()
+
+
+def _pad(f, s, pad, idx=None):
+    real = f.shape[0]
+    idx = np.arange(real) if idx is None else np.asarray(idx)
+    F = np.zeros((pad, pad))
+    S = np.zeros((pad, pad))
+    F[np.ix_(idx, idx)] = f
+    S[np.ix_(idx, idx)] = s
+    mask = np.zeros(pad, dtype=bool)
+    mask[idx] = True
+    return F, S, mask
+
+
+def test_masked_eigh_reference_edge_cases():
+    # tests/test_generalized_eigh_padded.py:59-172 (cases) and :280-310 (checks:
+    # the lowest eigenvalue of the masked solve against the unpadded one)
+    rng = np.random.default_rng(43)
+    g = rng.normal(size=(3, 3))
+    s_ill = np.eye(3)
+    s_ill[0, 0] = 1e-8
+    cases = {
+        "degenerate": (np.diag([1.0, 2.0, 2.0, 3.0]), np.eye(4), 6),
+        "ill_conditioned": (g @ g.T / 2, s_ill, 5),
+        "negative_eigenvalues": (np.diag([-2.0, 1.0, 3.0]), np.eye(3), 5),
+        "zero_eigenvalues": (np.diag([0.0, 1.0, 2.0]), np.eye(3), 5),
+    }
+    for name, (f, s, pad) in cases.items():
+        F, S, mask = _pad(f, s, pad)
+        w_ref, _ = o.generalized_eigh(f, s)
+        w, v = o.masked_generalized_eigh(F, S, mask)
+        assert abs(w[0] - w_ref[0]) < 1e-5, name
+        np.testing.assert_allclose(w[f.shape[0]:], 0.0, atol=0)
+    # the reference's slot sorting: the padded slots solve F = S = 1e-12, i.e.
+    # eigenvalue 1, and the mask is applied per eigenvalue slot, so the real
+    # slots hold the lowest values of the whole padded spectrum (real
+    # eigenvalues above 1 are displaced); hence its checks of w[0] alone
+    for name in ("degenerate", "negative_eigenvalues", "zero_eigenvalues"):
+        f, s, pad = cases[name]
+        real = f.shape[0]
+        w, _ = o.masked_generalized_eigh(*_pad(f, s, pad))
+        whole = np.sort(np.concatenate([np.diag(f), np.ones(pad - real)]))
+        np.testing.assert_allclose(w[:real], whole[:real], atol=1e-12)
+
+
+def test_masked_eigh_non_contiguous_mask():
+    # tests/test_generalized_eigh_padded.py:176-228 and :353-384: real slots
+    # 0, 2, 4 of 5; the lowest eigenvalue against the solve of the submatrices
+    rng = np.random.default_rng(44)
+    a, b = rng.normal(size=(3, 3)), rng.normal(size=(3, 3))
+    f = a @ a.T / 2
+    s = b @ b.T / 2 + 5.0 * np.eye(3)
+    F, S, mask = _pad(f, s, 5, idx=[0, 2, 4])
+    w_ref, _ = o.generalized_eigh(f, s)
+    w, v = o.masked_generalized_eigh(F, S, mask)
+    assert abs(np.sort(w)[-3:][0] - w_ref[0]) < 1e-5
+    # the eigenvectors vanish on the padded basis functions
+    np.testing.assert_allclose(v[~mask], 0.0, atol=0)
+
+
+def test_masked_eigh_independent_of_padding_values_and_large_pad():
+    # tests/test_generalized_eigh_padded.py:387-425 (padding filled with 100)
+    # and :482-526 (3 real of 20)
+    rng = np.random.default_rng(46)
+    f, s, F, S, mask = _padded_case(rng, 3, 5)
+    w1, v1 = o.masked_generalized_eigh(F, S, mask)
+    F2, S2 = F.copy(), S.copy()
+    F2[3:, 3:] = 100.0
+    S2[3:, 3:] = 100.0
+    w2, v2 = o.masked_generalized_eigh(F2, S2, mask)
+    np.testing.assert_allclose(w1[:3], w2[:3], atol=1e-10)
+    np.testing.assert_allclose(np.abs(v1[:3, :3]), np.abs(v2[:3, :3]), atol=1e-8)
+    a, b = rng.normal(size=(3, 3)), rng.normal(size=(3, 3))
+    f = (a + a.T) / 2
+    s = b @ b.T / 2 + 5.0 * np.eye(3)
+    F, S, mask = _pad(f, s, 20)
+    w_ref, _ = o.generalized_eigh(f, s)
+    w, _ = o.masked_generalized_eigh(F, S, mask)
+    np.testing.assert_allclose(w[:3], w_ref, atol=1e-10)
+    np.testing.assert_allclose(w[3:], 0.0, atol=0)
