@@ -477,8 +477,12 @@ def get_occ(nelectron, mo_energy):
 
 
 def make_rdm1(mo_coeff, mo_occ):
-    """D = C diag(occ) C^T (``qedft/train/td/hf.py:303-308``)."""
-    return np.einsum("ij,j,kj->ik", mo_coeff, mo_occ, mo_coeff)
+    """D = C_occ diag(occ) C_occ^H over the orbitals with occ > 0
+    (``qedft/train/td/hf.py:303-308``)."""
+    mo_occ = np.asarray(mo_occ)
+    sel = mo_occ > 0
+    mocc = np.asarray(mo_coeff)[:, sel]
+    return (mocc * mo_occ[sel]) @ mocc.conj().T
 
 
 class DIIS:

@@ -215,3 +215,34 @@ def test_masked_eigh_independent_of_padding_values_and_large_pad():
     w, _ = o.masked_generalized_eigh(F, S, mask)
     np.testing.assert_allclose(w[:3], w_ref, atol=1e-10)
     np.testing.assert_allclose(w[3:], 0.0, atol=0)
+
+
+def _rdm1_explicit(c, occ):
+    # tests/test_make_rdm1.py:10-40: C[:, occ > 0] diag(occ) C[:, occ > 0]^H
+    sel = occ > 0
+    return np.dot(c[:, sel] * occ[sel], c[:, sel].conj().T)
+
+
+def test_make_rdm1_reference_cases():
+    # tests/test_make_rdm1.py:99-193: random sizes, complex coefficients,
+    # fractional occupations, hermiticity and trace
+    rng = np.random.default_rng(0)
+    for n, k in ((4, 2), (6, 3), (8, 4)):
+        c = rng.normal(size=(n, n))
+        occ = np.zeros(n)
+        occ[:k] = 2.0
+        np.testing.assert_allclose(o.make_rdm1(c, occ), _rdm1_explicit(c, occ), atol=1e-14)
+    c = rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4))
+    occ = np.array([2.0, 2.0, 0.0, 0.0])
+    dm = o.make_rdm1(c, occ)
+    np.testing.assert_allclose(dm, _rdm1_explicit(c, occ), atol=1e-14)
+    np.testing.assert_allclose(dm, dm.conj().T, atol=1e-14)
+    c = rng.normal(size=(4, 4))
+    occ = np.array([1.5, 0.5, 0.0, 0.0])
+    dm = o.make_rdm1(c, occ)
+    np.testing.assert_allclose(dm, _rdm1_explicit(c, occ), atol=1e-14)
+    q = np.linalg.qr(rng.normal(size=(4, 4)))[0]
+    assert abs(np.trace(o.make_rdm1(q, np.array([2.0, 2.0, 0.0, 0.0]))) - 4.0) < 1e-12
+    # unoccupied (or negative) slots do not enter
+    occ = np.array([2.0, 0.0, -1.0, 0.0])
+    np.testing.assert_allclose(o.make_rdm1(c, occ), 2.0 * np.outer(c[:, 0], c[:, 0]), atol=1e-14)
