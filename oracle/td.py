@@ -480,9 +480,9 @@ def make_rdm1(mo_coeff, mo_occ):
     """D = C_occ diag(occ) C_occ^H over the orbitals with occ > 0
     (``qedft/train/td/hf.py:303-308``)."""
     mo_occ = np.asarray(mo_occ)
-    sel = mo_occ > 0
-    mocc = np.asarray(mo_coeff)[:, sel]
-    return (mocc * mo_occ[sel]) @ mocc.conj().T
+    c = np.asarray(mo_coeff)
+    # the non-positive slots enter with weight 0 (same sum as the selection)
+    return np.einsum("ij,j,kj->ik", c, np.where(mo_occ > 0, mo_occ, 0.0), c.conj())
 
 
 class DIIS:
