@@ -60,7 +60,10 @@ extern "C" {
  *   W1[t][c][o] (3 C C; tap t applies to the point at offset t - 1),
  *   W2[t][c][o] (3 C C), W3[c] (C),
  *   eta (C - 1): widths minval + (maxval - minval) * sigmoid(eta),
- *   the self-interaction width (1). */
+ *   the self-interaction width (1).
+ * The network is staged into a constant-memory slot per call, so a KSR call
+ * (qex_ks1d_solve* or qex_ksr1d_eval) on a stream that is being captured into
+ * a CUDA graph is refused with QEX_BAD_ARG. */
 #define QEX_KSR_CHANNELS 16
 #define QEX_KSR_NUM_PARAMS(c) (6 * (c) * (c) + 2 * (c))
 
@@ -184,9 +187,11 @@ int qex_ks1d_solve(const qex_ks1d_batch* batch, const qex_ks1d_options* options,
  * whose memory is budgeted up front) or a runtime that forbids allocation on
  * its hot path.  Its scratch is a fixed 16 MiB device array inside this
  * library; a batch whose qex_ks1d_workspace_size exceeds 16 MiB is rejected
- * with QEX_OOM before anything is launched.  The first call on each device
- * looks up the array's device address (cudaGetSymbolAddress), so make that
- * first call before any stream capture.  Every call shares the one array:
+ * with QEX_OOM before anything is launched.  Each call outside stream
+ * capture looks up the array's device address on the current device
+ * (cudaGetSymbolAddress), which stays valid across a device reset; a call
+ * under capture reuses the address of the last call outside capture, so make
+ * the first call on each device before any stream capture.  Every call shares the one array:
  * calls that overlap on the GPU (other streams, other host threads) race and
  * corrupt each other's results; serialise them.  The array keeps the last
  * call's contents; what must start at zero (the work counter) is cleared by

@@ -447,8 +447,10 @@ def get_fractional_occupations_jax_stable(mo_energy, n_electrons, theta, frac_mu
     n = e.size
     n_double = int(np.floor(n_electrons / 2.0))
     rem = n_electrons - 2.0 * n_double
-    homo = max(n_double - 1, 0)
-    lumo = min(n_double + (1 if rem > 0 else 0), n - 1)
+    # jnp indexing clamps out-of-range indices (fermi.py:422-427): more than
+    # 2n electrons take the highest orbital for both
+    homo = min(max(n_double - 1, 0), n - 1)
+    lumo = max(min(n_double + (1 if rem > 0 else 0), n - 1), 0)
     default_mu = 0.5 * (e[homo] + e[lumo])
     mu = default_mu if frac_mu is None else float(frac_mu)
     for _ in range(min(int(frac_max_steps), 100)):
@@ -480,9 +482,11 @@ def make_rdm1(mo_coeff, mo_occ):
     """D = C_occ diag(occ) C_occ^H over the orbitals with occ > 0
     (``qedft/train/td/hf.py:303-308``)."""
     mo_occ = np.asarray(mo_occ)
-    c = np.asarray(mo_coeff)
-    # the non-positive slots enter with weight 0 (same sum as the selection)
-    return np.einsum("ij,j,kj->ik", c, np.where(mo_occ > 0, mo_occ, 0.0), c.conj())
+    sel = mo_occ > 0
+    mocc = np.asarray(mo_coeff)[:, sel]
+    # the unoccupied columns are dropped, not weighted by 0: a non-finite
+    # entry there (padding of a masked eigensolve) does not reach D
+    return (mocc * mo_occ[sel]) @ mocc.conj().T
 
 
 class DIIS:

@@ -9,9 +9,11 @@
 // re-stage it in stream order.  A slot that changes hands is first waited on
 // (the previous owner's last launch), so concurrent launches on different
 // streams with different weights never share a slot while one of them runs.
-// Under stream capture a device-to-device copy is captured with the launch and
-// no cross-stream wait is added (run captured graphs on the stream that
-// captured them); a host-to-device copy cannot be captured and is refused.
+// Staging is refused under stream capture: a graph that replays a slot's copy
+// and launch later would hold the slot outside this table's ownership rules,
+// and another stream given the slot meanwhile could overwrite the weights
+// while the graph runs.  Callers return QEX_BAD_ARG for a launch attempted
+// under capture (capturing_refused()).
 //
 // Internal linkage throughout: each translation unit has its own constant
 // arrays, and the staging code must write the array its kernels read.
@@ -51,8 +53,10 @@ class ConstStage {
       return;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) return;
-    capturing_ = cap != cudaStreamCaptureStatusNone;
-    if (capturing_ && kind != cudaMemcpyDeviceToDevice) return;
+    if (cap != cudaStreamCaptureStatusNone) {
+      capturing_ = true;
+      return;
+    }
     auto& t = slots.tab[dev_];
     int s = -1;
     for (int i = 0; i < kSlots; ++i)
@@ -63,7 +67,7 @@ class ConstStage {
       if (!t.used[s]) {
         if (cudaEventCreateWithFlags(&t.done[s], cudaEventDisableTiming) != cudaSuccess) return;
         t.used[s] = true;
-      } else if (!capturing_ && cudaStreamWaitEvent(stream, t.done[s], 0) != cudaSuccess) {
+      } else if (cudaStreamWaitEvent(stream, t.done[s], 0) != cudaSuccess) {
         return;
       }
       t.owner[s] = stream;
@@ -74,10 +78,11 @@ class ConstStage {
     slot_ = s;
   }
   int slot() const { return slot_; }
+  // True when the stream was capturing: nothing was staged.
+  bool capturing_refused() const { return capturing_; }
   // Call after the launch that reads the slot.
   bool finish() {
     if (slot_ < 0) return false;
-    if (capturing_) return true;
     return cudaEventRecord(slots_.tab[dev_].done[slot_], stream_) == cudaSuccess;
   }
 

@@ -18,6 +18,7 @@
 // theta sum 2 [f ln f + (1-f) ln(1-f)] (0 ln 0 taken as 0), the final loss.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <math_constants.h>
 #include <stdint.h>
 
 #include "qex_ks1d.h"
@@ -97,11 +98,27 @@ __global__ void __launch_bounds__(kThreads) fermi_kernel(const __grid_constant__
   const double N = p.nelec[b];
   double theta = p.theta;
 
-  // start
-  const int n_double = (int)floor(N / 2.0);
-  const double rem = N - 2.0 * n_double;
-  const int homo = max(n_double - 1, 0);
-  const int lumo = min(n_double + (rem > 0.0 ? 1 : 0), n - 1);
+  // An electron count that is negative or not finite has no occupations: the
+  // molecule's status says so and its outputs are NaN (the block takes this
+  // branch as a whole, since N is one value per block).
+  if (!(N >= 0.0) || !isfinite(N)) {
+    for (int i = threadIdx.x; i < n; i += kThreads) p.occ[(long long)b * n + i] = CUDART_NAN;
+    if (threadIdx.x == 0) {
+      if (p.mu_out) p.mu_out[b] = CUDART_NAN;
+      if (p.entr) p.entr[b] = CUDART_NAN;
+      if (p.loss) p.loss[b] = CUDART_NAN;
+      if (p.status) p.status[b] = QEX_BAD_ARG;
+    }
+    return;
+  }
+  // start.  HOMO and LUMO indices are clamped into [0, n) as the reference's
+  // array lookup clamps them (fermi.py:422-427): more than 2n electrons take
+  // the highest orbital for both.
+  const double nd = floor(N / 2.0);
+  const double rem = N - 2.0 * nd;
+  const int n_double = (int)fmin(nd, (double)n);
+  const int homo = min(max(n_double - 1, 0), n - 1);
+  const int lumo = max(min(n_double + (rem > 0.0 ? 1 : 0), n - 1), 0);
   const double mid = 0.5 * (e[homo] + e[lumo]);
   double mu;
   if (p.mu_in) {

@@ -2333,6 +2333,7 @@ int launch_variant(const Params& P, cudaStream_t stream, size_t smem, int per_sm
   if (e != cudaSuccess) return QEX_CUDA_ERROR;
   if constexpr (kKsr) {
     auto stage = ksr_stage(P.ksr_w, 6 * P.ksr_c * P.ksr_c + 2 * P.ksr_c, stream);
+    if (stage.capturing_refused()) return QEX_BAD_ARG;
     if (stage.slot() < 0) return QEX_CUDA_ERROR;
     Params Q = P;
     Q.ksr_slot = stage.slot();
@@ -2426,13 +2427,18 @@ void* g_static_address[kStaticMaxDevices] = {};
 
 // Device address of the scratch array on the current device.  Host code may
 // not use the array's name as a pointer (it is a host-side stand-in), so the
-// address is looked up once per device, with that device current.
-int static_scratch_address(void** out) {
+// address is looked up with that device current.  Outside stream capture it
+// is looked up on every call (cheap), so a device reset or a new primary
+// context never leaves a stale address behind; under capture the address
+// from the last call outside capture is used.
+int static_scratch_address(cudaStream_t stream, void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return QEX_CUDA_ERROR;
   if (dev < 0 || dev >= kStaticMaxDevices) return QEX_BAD_ARG;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) return QEX_CUDA_ERROR;
   std::lock_guard<std::mutex> lock(g_static_mutex);
-  if (!g_static_address[dev]) {
+  if (cap == cudaStreamCaptureStatusNone || !g_static_address[dev]) {
     void* ptr = nullptr;
     if (cudaGetSymbolAddress(&ptr, qex_static_scratch) != cudaSuccess || !ptr) {
       return QEX_CUDA_ERROR;
@@ -2485,7 +2491,7 @@ int qex_ks1d_solve_static(const qex_ks1d_batch* batch, const qex_ks1d_options* o
   if (rc) return rc;
   if (need > kStaticScratchBytes) return QEX_OOM;  // batch too large for the fixed scratch
   void* scratch = nullptr;
-  rc = static_scratch_address(&scratch);
+  rc = static_scratch_address(static_cast<cudaStream_t>(stream), &scratch);
   if (rc) return rc;
   qex::Params P;
   rc = qex::fill_params(P, qex::kModeScf, batch, options, xc, outputs, scratch,

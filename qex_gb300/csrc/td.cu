@@ -379,7 +379,7 @@ __global__ void make_rdm1_kernel(int batch, int n, const double* __restrict__ C,
     double s = 0.0;
     for (int k = 0; k < n; ++k) {
       const double o = ob[k];
-      if (o != 0.0) s = fma(o * Cb[(long long)i * n + k], Cb[(long long)j * n + k], s);
+      if (o > 0.0) s = fma(o * Cb[(long long)i * n + k], Cb[(long long)j * n + k], s);
     }
     D[e] = s;
   }

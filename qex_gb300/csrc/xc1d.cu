@@ -210,6 +210,7 @@ int qex_ksr1d_eval(int32_t num_molecules, int32_t max_num_grids, const int32_t* 
   const cudaStream_t s = static_cast<cudaStream_t>(stream);
   auto stage =
       ksr_stage(xc->ksr_params, 6 * xc->ksr_channels * xc->ksr_channels + 2 * xc->ksr_channels, s);
+  if (stage.capturing_refused()) return QEX_BAD_ARG;
   if (stage.slot() < 0) return QEX_CUDA_ERROR;
   P.slot = stage.slot();
   ksr1d_kernel<<<num_molecules, kWarp, smem, s>>>(P);

@@ -2,7 +2,7 @@
 
 Run from the repository root (needs the read-only reference tree):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the reference source tree>
 
 Writes ``tests/golden/ks1d_reference_data.npz`` (small slices of the
 reference's shipped datasets, ``data/od/{h2,h2_h2,h4}``) and
@@ -69,7 +69,9 @@ def oracle_cases():
 
 
 def main(argv):
-    ref = pathlib.Path(argv[1] if len(argv) > 1 else "/root/reference")
+    if len(argv) != 2:
+        raise SystemExit(f"usage: python {argv[0]} <path of the reference source tree>")
+    ref = pathlib.Path(argv[1])
     np.savez_compressed(OUT / "ks1d_reference_data.npz", **reference_slices(ref))
     np.savez_compressed(OUT / "ks1d_oracle.npz", **oracle_cases())
     print("wrote", OUT / "ks1d_reference_data.npz", OUT / "ks1d_oracle.npz")

@@ -2,7 +2,7 @@
 
 Run from the repository root (needs the read-only reference tree):
 
-    python tests/golden/make_ksr_golden.py /root/reference
+    python tests/golden/make_ksr_golden.py <path of the reference source tree>
 
 Stores
   * the trained global-local conv network shipped at ``data/od/h2/h2_optimal.pkl``
@@ -45,7 +45,9 @@ SCF_ROWS = (8, 16, 24, 40)
 
 
 def main(argv):
-    ref = pathlib.Path(argv[1] if len(argv) > 1 else "/root/reference")
+    if len(argv) != 2:
+        raise SystemExit(f"usage: python {argv[0]} <path of the reference source tree>")
+    ref = pathlib.Path(argv[1])
     d = ref / "data" / "od" / "h2"
     with open(d / "h2_optimal.pkl", "rb") as fh:
         tree = _ArrayUnpickler(fh).load()

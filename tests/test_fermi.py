@@ -138,3 +138,30 @@ def test_scf_with_fermi_occupations_matches_oracle(fermi):
         np.testing.assert_allclose(res.energies.cpu().numpy(), e_r, atol=1e-8, rtol=0)
         np.testing.assert_allclose(res.entropic_energy.cpu().numpy(), s_r, atol=1e-10, rtol=0)
         assert abs(float(res.mo_occ.sum()) - m.nelectron) < 1e-8
+
+
+@pytest.mark.gpu
+def test_more_electrons_than_slots_and_bad_counts(fermi):
+    """More than 2n electrons: HOMO and LUMO clamp to the highest orbital, as
+    the reference's array lookup clamps them (fermi.py:422-427); a negative or
+    non-finite electron count sets the molecule's status to QEX_BAD_ARG and
+    leaves its neighbours in the batch untouched."""
+    import torch
+
+    from qex_gb300 import _native as N
+
+    e = np.array([-1.0, -0.5, 0.3])
+    occ, entr, mu, _ = fermi.get_fractional_occupations_jax_stable(e, 10.0, 0.1, None, 0.9,
+                                                                   0.6, 100)
+    occ_r, entr_r, mu_r, _ = o.get_fractional_occupations_jax_stable(e, 10.0, 0.1, None, 0.9,
+                                                                     0.6, 100)
+    np.testing.assert_allclose(occ.cpu().numpy(), occ_r, atol=1e-12, rtol=0)
+    assert abs(float(mu) - mu_r) <= 1e-12 * max(1.0, abs(mu_r))
+    es = torch.as_tensor(np.stack([e, e, e]))
+    occ, entr, mu, loss, st = fermi._run(es, torch.as_tensor([2.0, -1.0, float("nan")]), 0.1,
+                                         None, 0.9, 0.6, 100, 2)
+    st = st.cpu().numpy()
+    assert st[0] == 0 and st[1] == N.QEX_BAD_ARG and st[2] == N.QEX_BAD_ARG
+    occ_r, _, _, _ = o.get_fractional_occupations_jax_stable(e, 2.0, 0.1, None, 0.9, 0.6, 100)
+    np.testing.assert_allclose(occ[0].cpu().numpy(), occ_r, atol=1e-12, rtol=0)
+    assert bool(torch.isnan(occ[1:]).all())

@@ -246,3 +246,9 @@ def test_make_rdm1_reference_cases():
     # unoccupied (or negative) slots do not enter
     occ = np.array([2.0, 0.0, -1.0, 0.0])
     np.testing.assert_allclose(o.make_rdm1(c, occ), 2.0 * np.outer(c[:, 0], c[:, 0]), atol=1e-14)
+    # a non-finite unoccupied column (padding of a masked eigensolve) is dropped
+    c_nan = c.copy()
+    c_nan[:, 3] = np.nan
+    c_nan[1, 2] = np.inf
+    np.testing.assert_allclose(o.make_rdm1(c_nan, occ), 2.0 * np.outer(c[:, 0], c[:, 0]),
+                               atol=1e-14)

@@ -56,6 +56,17 @@ def test_rho_lda_vxc(td, mols):
                                    atol=1e-12 * np.abs(vmat_r).max())
 
 
+def test_make_rdm1_selects_positive_occupations(td):
+    """hf.py:303-308 keeps the orbitals with occ > 0: zero and negative
+    occupations do not enter D (a fractional and a negative one here)."""
+    torch, eigh, numint, scf, W = td
+    rng = np.random.default_rng(5)
+    c = rng.normal(size=(6, 6))
+    for occ in (np.array([2.0, 1.5, 0.0, -1.0, 0.5, 0.0]), np.array([2.0, 2.0, 2.0, 0, 0, 0])):
+        np.testing.assert_allclose(_host(scf.make_rdm1(c, occ)), o.make_rdm1(c, occ),
+                                   atol=1e-14, rtol=0)
+
+
 @pytest.mark.parametrize("n", [1, 4, 17, 33, 64, 150, 231])
 def test_generalized_eigh(td, n):
     torch, eigh, numint, scf, W = td
