@@ -77,8 +77,41 @@ enum qex_xc_kind {
   QEX_XC_LDA_EXP_COULOMB = 1, /* exponential-Coulomb uniform-gas LDA */
   QEX_XC_POWER = 2,           /* f(n) = coefficient * (n + shift)^power */
   QEX_XC_WINDOW_MLP = 3,      /* FP32 window-17 MLP, two SiLU layers of 16 */
-  QEX_XC_KSR = 4              /* FP32 global-local conv network (whole-grid functional) */
+  QEX_XC_KSR = 4,             /* FP32 global-local conv network (whole-grid functional) */
+  QEX_XC_LOCAL_MLP = 5,       /* FP32 dense network per grid point (LocalMLP) */
+  QEX_XC_GLOBAL_MLP = 6       /* FP32 dense network on the whole density (GlobalMLP) */
 };
+
+/* Dense XC networks of qedft/models/networks.py:83-138 (LocalMLP, GlobalMLP;
+ * stax stacks of qedft/models/classical/classical_models.py:77-224):
+ *   x -> [Dense(H), activation] x L -> Dense(1),  x = n / normalization,
+ * with x = n_i per grid point (local) or the whole density (global, whose
+ * input size is nn_inputs = the grid size of every molecule).  The wrappers of
+ * qedft/models/wrappers.py:162-217 are flags: QEX_NN_SELF_INTERACTION
+ * (u_i = beta (-v_H[n]_i / 2) + (1 - beta) g_i, beta = exp(-((dx sum n - 1) /
+ * width)^2), v_H with the default exponential Coulomb interaction) and
+ * QEX_NN_NEGATIVITY (f = -swish(u)); a global network's values are its mean
+ * over the grid (per-point values f_i / N).  Packed FP32 parameters in a
+ * DEVICE buffer, 16-byte aligned, hidden width padded to Hp = nn_width (a
+ * multiple of 8, at most 128) with zero weights: W1 (nn_inputs x Hp), b1 (Hp),
+ * then per further hidden layer W (Hp x Hp), b (Hp), then Wout (Hp), then
+ * {bout, width, 0, 0}: QEX_NN_NUM_PARAMS floats.  The network runs in FP32,
+ * the wrappers and sums in FP64.  Neither has an adjoint step. */
+enum qex_nn_activation {
+  QEX_NN_TANH = 0,
+  QEX_NN_RELU = 1,
+  QEX_NN_SOFTPLUS = 2,
+  QEX_NN_SIGMOID = 3,
+  QEX_NN_ELU = 4,
+  QEX_NN_LEAKY_RELU = 5, /* negative slope 0.01 */
+  QEX_NN_SELU = 6,
+  QEX_NN_GELU = 7        /* tanh approximation */
+};
+#define QEX_NN_SELF_INTERACTION 1
+#define QEX_NN_NEGATIVITY 2
+#define QEX_NN_MAX_WIDTH 128
+#define QEX_NN_NUM_PARAMS(inputs, hp, layers) \
+  ((inputs) * (hp) + (hp) + ((layers) - 1) * ((hp) * (hp) + (hp)) + (hp) + 4)
 
 enum qex_xc_convention {
   QEX_XC_AMPLITUDE = 0, /* qedft: E = dx sum f, v = dE/dn (scf.py:32-76) */
@@ -95,6 +128,12 @@ typedef struct qex_xc_spec {
   const float* ksr_params;          /* DEVICE pointer, QEX_KSR_NUM_PARAMS(ksr_channels) floats */
   double ksr_minval, ksr_maxval;    /* range of the global-convolution widths */
   int32_t ksr_channels;             /* 16 or 8 (QEX_XC_KSR) */
+  const float* nn_params;           /* DEVICE pointer, QEX_NN_NUM_PARAMS floats (LOCAL/GLOBAL_MLP) */
+  int32_t nn_width;                 /* padded hidden width Hp: multiple of 8, <= 128 */
+  int32_t nn_layers;                /* hidden layers L >= 1 */
+  int32_t nn_activation;            /* enum qex_nn_activation */
+  int32_t nn_inputs;                /* 1 (local) or the grid size (global) */
+  int32_t nn_flags;                 /* QEX_NN_SELF_INTERACTION | QEX_NN_NEGATIVITY */
 } qex_xc_spec;
 
 typedef struct qex_ks1d_options {

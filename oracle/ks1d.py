@@ -473,6 +473,110 @@ class KSRGlobalConv(PointwiseXC):
         return dn
 
 
+_NN_ACTIVATIONS = {
+    # name: (f(z), f'(z)), the stax layers of qedft/models/classical/classical_models.py:37-47
+    "tanh": (np.tanh, lambda z: 1.0 - np.tanh(z) ** 2),
+    "relu": (lambda z: np.maximum(z, 0.0), lambda z: (z > 0).astype(z.dtype)),
+    "softplus": (lambda z: np.logaddexp(z, 0.0), lambda z: 0.5 * (1.0 + np.tanh(0.5 * z))),
+    "sigmoid": (lambda z: 0.5 * (1.0 + np.tanh(0.5 * z)),
+                lambda z: 0.25 * (1.0 - np.tanh(0.5 * z) ** 2)),
+    "elu": (lambda z: np.where(z > 0, z, np.expm1(np.minimum(z, 0.0))),
+            lambda z: np.where(z > 0, 1.0, np.exp(np.minimum(z, 0.0)))),
+    "leaky_relu": (lambda z: np.where(z >= 0, z, 0.01 * z), lambda z: np.where(z >= 0, 1.0, 0.01)),
+    "selu": (lambda z: 1.0507009873554805 * np.where(
+        z > 0, z, 1.6732632423543772 * np.expm1(np.minimum(z, 0.0))),
+             lambda z: 1.0507009873554805 * np.where(
+        z > 0, 1.0, 1.6732632423543772 * np.exp(np.minimum(z, 0.0)))),
+    "gelu": (lambda z: 0.5 * z * (1.0 + np.tanh(0.7978845608028654 * (z + 0.044715 * z ** 3))),
+             lambda z: (0.5 * (1.0 + np.tanh(0.7978845608028654 * (z + 0.044715 * z ** 3)))
+                        + 0.5 * z * (1.0 - np.tanh(0.7978845608028654 * (z + 0.044715 * z ** 3)) ** 2)
+                        * 0.7978845608028654 * (1.0 + 3 * 0.044715 * z * z))),
+}
+
+
+class DenseNetworkXC(PointwiseXC):
+    """The reference's dense XC networks with their wrappers.
+
+    Network: x -> [Dense(H), activation] x L -> Dense(1), x = n / norm
+    (``build_mlp_layers``, ``qedft/models/classical/classical_models.py:77-115``):
+      * local (``build_local_mlp``, :123-174; ``LocalMLP``,
+        ``qedft/models/networks.py:83-109``): g_i = MLP(n_i / norm) per point;
+      * global (``build_global_mlp``, :177-224; ``GlobalMLP``, networks.py:112-138):
+        g = MLP(n / norm) on the whole density.
+    Wrappers (``qedft/models/wrappers.py:162-217``), in the reference's order:
+      * self-interaction (jax_dft ``wrap_network_with_self_interaction_layer``
+        with exponential_coulomb): u_i = beta (-v_H[n]_i / 2) + (1 - beta) g_i,
+        beta = exp(-((dx sum n - 1) / width)^2);
+      * negativity (jax_dft ``negativity_transform``): f = -swish(u);
+      * global networks: the mean of f over the grid (``global_apply_fn``),
+        returned here as per-point values f_i / N (their sum is the scalar).
+    ``layers``: [(W (in, out), b (out,)), ...] of the Dense layers; ``dtype``
+    is the network's arithmetic (float32 as on the GPU, or float64); the
+    wrappers run in float64.
+    """
+
+    def __init__(self, grids, layers, activation="tanh", normalization=2.0, local=True,
+                 self_interaction=False, negativity=True, width=1.0, dtype=np.float64):
+        self.grids = np.asarray(grids, dtype=np.float64)
+        self.dx = get_dx(self.grids)
+        self.layers = [(np.asarray(w, dtype), np.asarray(b, dtype).reshape(-1)) for w, b in layers]
+        self.act, self.dact = _NN_ACTIVATIONS[activation]
+        self.norm = float(normalization)
+        self.local, self.si, self.neg = bool(local), bool(self_interaction), bool(negativity)
+        self.width = float(width)
+        self.dtype = dtype
+
+    def _network(self, n64):
+        """g (per point, or a scalar) and its input gradient (per point)."""
+        x = (n64.astype(self.dtype) / self.dtype(self.norm))
+        x = x[:, None] if self.local else x[None, :]
+        zs, a = [], x
+        for w, b in self.layers[:-1]:
+            z = a @ w + b
+            zs.append(z)
+            a = self.act(z)
+        w, b = self.layers[-1]
+        g = (a @ w + b)[:, 0]
+        # reverse pass of the scalar outputs (one row per point, or one row)
+        d = np.broadcast_to(w[:, 0], a.shape).astype(self.dtype)
+        for li in range(len(zs) - 1, -1, -1):
+            d = d * self.dact(zs[li])
+            d = d @ self.layers[li][0].T
+        gx = d / self.dtype(self.norm)
+        if self.local:
+            return g.astype(np.float64), gx[:, 0].astype(np.float64)
+        return float(g[0]), gx[0].astype(np.float64)
+
+    def _forward(self, density):
+        n = np.asarray(density, np.float64)
+        g, gx = self._network(n)
+        q = float(np.sum(n) * self.dx)
+        beta = math.exp(-((q - 1.0) / self.width) ** 2) if self.si else 0.0
+        vh = get_hartree_potential(n, self.grids, exponential_coulomb) if self.si else 0.0
+        u = -0.5 * beta * vh + (1.0 - beta) * g if self.si else g * np.ones_like(n)
+        if self.neg:
+            s = 1.0 / (1.0 + np.exp(-u))
+            f, fp = -u * s, -(s + u * s * (1.0 - s))
+        else:
+            f, fp = u, np.ones_like(u)
+        scale = 1.0 if self.local else 1.0 / n.size
+        return f * scale, (g, gx, q, beta, vh, fp * scale)
+
+    def values(self, density):
+        return self._forward(density)[0]
+
+    def vjp(self, density, cotangent):
+        _, (g, gx, q, beta, vh, fps) = self._forward(density)
+        c = np.asarray(cotangent, np.float64) * fps
+        keep = (1.0 - beta) if self.si else 1.0
+        out = keep * (c * gx if self.local else np.sum(c) * gx)
+        if self.si:
+            dbeta = beta * (-2.0 * (q - 1.0) / self.width ** 2) * self.dx
+            out = out - 0.5 * beta * get_hartree_potential(c, self.grids, exponential_coulomb)
+            out = out + float(np.dot(c, -0.5 * vh - g)) * dbeta
+        return out
+
+
 def ksr_params_from_tree(tree, minval=0.1, maxval=2.385345):
     """The dict form of ``KSRGlobalConv`` params from the stax parameter tree of
     ``create_ksr_model_from_config`` (the nesting of ``data/od/h2/h2_optimal.pkl``:

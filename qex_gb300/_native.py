@@ -28,6 +28,13 @@ QEX_XC_LDA_EXP_COULOMB = 1
 QEX_XC_POWER = 2
 QEX_XC_WINDOW_MLP = 3
 QEX_XC_KSR = 4
+QEX_XC_LOCAL_MLP = 5
+QEX_XC_GLOBAL_MLP = 6
+QEX_NN_ACTIVATIONS = {"tanh": 0, "relu": 1, "softplus": 2, "sigmoid": 3, "elu": 4,
+                      "leaky_relu": 5, "selu": 6, "gelu": 7}
+QEX_NN_SELF_INTERACTION = 1
+QEX_NN_NEGATIVITY = 2
+QEX_NN_MAX_WIDTH = 128
 QEX_XC_AMPLITUDE = 0
 QEX_XC_LOCAL = 1
 
@@ -60,6 +67,12 @@ class XcSpec(ctypes.Structure):
         ("ksr_minval", ctypes.c_double),
         ("ksr_maxval", ctypes.c_double),
         ("ksr_channels", ctypes.c_int32),
+        ("nn_params", _c_p),
+        ("nn_width", ctypes.c_int32),
+        ("nn_layers", ctypes.c_int32),
+        ("nn_activation", ctypes.c_int32),
+        ("nn_inputs", ctypes.c_int32),
+        ("nn_flags", ctypes.c_int32),
     ]
 
 

@@ -24,6 +24,7 @@
 // td.cu, which applies the reference's shift
 // (qedft/train/td/generalized_eigensolver.py:264-330).
 #include <cuda_runtime.h>
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 
@@ -459,6 +460,339 @@ __global__ void __launch_bounds__(kThreads) jacobi_large_kernel(int n,
   if (threadIdx.x == 0) ok[b] = 4;
 }
 
+// ---------------------------------------------------------------------------
+// FP32 eigenvectors of C beyond kMaxSmemN by tridiagonal reduction (in place
+// of the one-CTA Jacobi, whose n - 1 synchronised rounds per sweep made it the
+// bulk of a solve at nao 150-240):
+//   tridiag_kernel: Householder reduction C = Q T Q^T in shared memory (one
+//     CTA per matrix; the reflectors v_k go to HV row k, d / e / tau to tri);
+//   tri_eig_kernel: all eigenvalues of T by Sturm bisection (a thread per
+//     eigenvalue) and its eigenvectors by inverse iteration with partial
+//     pivoting, the vectors of a cluster (gaps below 1e-5 |T|) computed by one
+//     thread in turn and orthogonalised against each other (Gram-Schmidt),
+//     LAPACK stein's scheme;
+//   tri_back_kernel32: u_j = H_0 ... H_{n-3} z_j over many CTAs, written as
+//     row j of U^T (the layout jacobi_large_kernel produced).
+// Scratch (per matrix, from the refinement's areas, idle in stage 1): HV
+// (n x n floats), tri (d, e, tau, lambda: 4 n floats), and the inverse
+// iteration's factors and vectors (6 n^2 floats, element i of thread j's
+// array at [i n + j], so that threads stepping i together read contiguously).
+// ---------------------------------------------------------------------------
+__device__ inline float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* __restrict__ C64,
+                                                           double* __restrict__ HVws,
+                                                           double* __restrict__ TRIws,
+                                                           const int* __restrict__ ok) {
+  const int b = blockIdx.x;
+  if (ok[b] != 3) return;
+  extern __shared__ float sm[];
+  const long long nn = (long long)n * n;
+  float* C = sm;
+  float* v = C + nn;
+  float* p = v + n;
+  float* red = p + n;
+  float* HV = reinterpret_cast<float*>(HVws + b * nn);
+  float* d = reinterpret_cast<float*>(TRIws + b * nn);
+  float* e = d + n;
+  float* tau = e + n;
+  const double* Cd = C64 + b * nn;
+  for (long long el = threadIdx.x; el < nn; el += blockDim.x) {
+    const int i = (int)(el / n), j = (int)(el % n);
+    C[el] = (float)(0.5 * (Cd[el] + Cd[(long long)j * n + i]));
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int k = 0; k < n - 2; ++k) {
+    const int m = n - k - 1;  // x = C[k+1 .. n-1][k] (= row k right of the diagonal)
+    float sq = 0.0f;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      const float x = C[(long long)k * n + k + 1 + i];
+      v[i] = x;
+      if (i > 0) sq = fmaf(x, x, sq);
+    }
+    sq = block_sumf(sq, red);
+    const float x0 = v[0];
+    float alpha = x0, t = 0.0f;
+    if (sq > 0.0f) {
+      const float nrm = sqrtf(fmaf(x0, x0, sq));
+      alpha = x0 >= 0.0f ? -nrm : nrm;
+      const float v0 = x0 - alpha;
+      t = 2.0f / fmaf(v0, v0, sq);
+    }
+    __syncthreads();  // every thread has read v[0]
+    if (threadIdx.x == 0) {
+      v[0] = (t != 0.0f) ? x0 - alpha : 1.0f;
+      d[k] = C[(long long)k * n + k];
+      e[k] = alpha;
+      tau[k] = t;
+    }
+    __syncthreads();
+    if (t != 0.0f) {
+      // p = tau A v over the trailing block, a warp per row
+      for (int r = warp; r < m; r += nw) {
+        const float* row = C + (long long)(k + 1 + r) * n + k + 1;
+        float a = 0.0f;
+        for (int c = lane; c < m; c += 32) a = fmaf(row[c], v[c], a);
+        a = warp_sumf(a);
+        if (lane == 0) p[r] = t * a;
+      }
+      __syncthreads();
+      float q = 0.0f;
+      for (int i = threadIdx.x; i < m; i += blockDim.x) q = fmaf(v[i], p[i], q);
+      q = block_sumf(q, red);
+      const float K = 0.5f * t * q;
+      for (int i = threadIdx.x; i < m; i += blockDim.x) p[i] = fmaf(-K, v[i], p[i]);  // w
+      __syncthreads();
+      // A <- A - v w^T - w v^T
+      for (int r = warp; r < m; r += nw) {
+        float* row = C + (long long)(k + 1 + r) * n + k + 1;
+        const float vr = v[r], wr = p[r];
+        for (int c = lane; c < m; c += 32) row[c] -= fmaf(vr, p[c], wr * v[c]);
+      }
+    }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) HV[(long long)k * n + k + 1 + i] = v[i];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (n >= 2) {
+      d[n - 2] = C[(long long)(n - 2) * n + n - 2];
+      e[n - 2] = C[(long long)(n - 1) * n + n - 2];
+      tau[n - 2] = 0.0f;
+    }
+    d[n - 1] = C[(long long)(n - 1) * n + n - 1];
+    e[n - 1] = 0.0f;
+    tau[n - 1] = 0.0f;
+  }
+}
+
+// Number of eigenvalues of T below sigma (signs of the L D L^T pivots).
+__device__ inline int sturm_count32(int n, const float* d, const float* e2, float sigma,
+                                    float pivmin) {
+  float q = d[0] - sigma;
+  if (fabsf(q) < pivmin) q = -pivmin;
+  int c = q < 0.0f;
+  for (int i = 1; i < n; ++i) {
+    q = d[i] - sigma - e2[i - 1] / q;
+    if (fabsf(q) < pivmin) q = -pivmin;
+    c += q < 0.0f;
+  }
+  return c;
+}
+
+__global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __restrict__ TRIws,
+                                                           double* __restrict__ INVws, int ks,
+                                                           const int* __restrict__ ok) {
+  const int b = blockIdx.x;
+  if (ok[b] != 3) return;
+  __shared__ float ds[kMaxLargeN], es[kMaxLargeN], e2[kMaxLargeN], lam[kMaxLargeN];
+  const long long nn = (long long)n * n;
+  const float* d = reinterpret_cast<const float*>(TRIws + b * nn);
+  const float* e = d + n;
+  float* W = reinterpret_cast<float*>(INVws + b * (long long)ks * nn);
+  float* Lm = W;                 // multipliers
+  float* U0 = W + nn;            // U diagonal, first and second superdiagonals
+  float* U1 = W + 2 * nn;
+  float* U2 = W + 3 * nn;
+  float* PV = W + 4 * nn;        // 1 where rows i and i+1 were swapped
+  float* X = W + 5 * nn;         // eigenvector of eigenvalue j in column j
+  float lo = 3.0e38f, hi = -3.0e38f, nrm = 0.0f, emax = 0.0f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float di = d[i], ei = (i < n - 1) ? e[i] : 0.0f, ep = i > 0 ? e[i - 1] : 0.0f;
+    ds[i] = di;
+    es[i] = ei;
+    e2[i] = ei * ei;
+    const float r = fabsf(ei) + fabsf(ep);
+    lo = fminf(lo, di - r);
+    hi = fmaxf(hi, di + r);
+    nrm = fmaxf(nrm, fabsf(di) + r);
+    emax = fmaxf(emax, ei * ei);
+  }
+  // block min / max
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    nrm = fmaxf(nrm, __shfl_xor_sync(0xffffffffu, nrm, o));
+    emax = fmaxf(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+  }
+  __shared__ float r4[4][32];
+  if ((threadIdx.x & 31) == 0) {
+    r4[0][threadIdx.x >> 5] = lo;
+    r4[1][threadIdx.x >> 5] = hi;
+    r4[2][threadIdx.x >> 5] = nrm;
+    r4[3][threadIdx.x >> 5] = emax;
+  }
+  __syncthreads();
+  lo = r4[0][0];
+  hi = r4[1][0];
+  nrm = r4[2][0];
+  emax = r4[3][0];
+  for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+    lo = fminf(lo, r4[0][w]);
+    hi = fmaxf(hi, r4[1][w]);
+    nrm = fmaxf(nrm, r4[2][w]);
+    emax = fmaxf(emax, r4[3][w]);
+  }
+  nrm = fmaxf(nrm, 1e-30f);
+  const float pivmin = 1.2e-38f * fmaxf(1.0f, emax);
+  const float span = fmaxf(hi - lo, nrm * 1e-6f);
+  lo -= 2.0f * FLT_EPSILON * span + pivmin;
+  hi += 2.0f * FLT_EPSILON * span + pivmin;
+  // eigenvalue j by bisection (ascending)
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    float a = lo, c = hi;
+    for (int it = 0; it < 80; ++it) {
+      const float mid = 0.5f * (a + c);
+      if (mid <= a || mid >= c || c - a <= 2.0f * FLT_EPSILON * fmaxf(fabsf(a), fabsf(c)) + pivmin)
+        break;
+      if (sturm_count32(n, ds, e2, mid, pivmin) > j) {
+        c = mid;
+      } else {
+        a = mid;
+      }
+    }
+    lam[j] = 0.5f * (a + c);
+  }
+  __syncthreads();
+  // inverse iteration; a cluster's first thread computes its vectors in turn
+  const float ctol = 1e-5f * nrm;
+  const float sep = 10.0f * FLT_EPSILON * nrm;
+  const float tiny = FLT_EPSILON * nrm;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    if (j > 0 && lam[j] - lam[j - 1] <= ctol) continue;  // not the first of its cluster
+    int end = j;
+    while (end + 1 < n && lam[end + 1] - lam[end] <= ctol) ++end;
+    float lprev = -3.0e38f;
+    for (int mbr = j; mbr <= end; ++mbr) {
+      float lm = lam[mbr];
+      if (mbr > j && lm - lprev < sep) lm = lprev + sep;
+      lprev = lm;
+      // T - lm I = P L U (partial pivoting); column j of the factor arrays
+      float ra = ds[0] - lm, rb = n > 1 ? es[0] : 0.0f, rc = 0.0f;
+      for (int i = 0; i < n - 1; ++i) {
+        const float ci = es[i], an = ds[i + 1] - lm, bn = (i + 1 < n - 1) ? es[i + 1] : 0.0f;
+        const long long q = (long long)i * n + j;
+        if (fabsf(ci) > fabsf(ra)) {
+          const float l = ra / ci;
+          U0[q] = ci;
+          U1[q] = an;
+          U2[q] = bn;
+          Lm[q] = l;
+          PV[q] = 1.0f;
+          ra = rb - l * an;
+          rb = rc - l * bn;
+        } else {
+          const float piv = fabsf(ra) < tiny ? copysignf(tiny, ra) : ra;
+          const float l = ci / piv;
+          U0[q] = piv;
+          U1[q] = rb;
+          U2[q] = rc;
+          Lm[q] = l;
+          PV[q] = 0.0f;
+          ra = an - l * rb;
+          rb = bn - l * rc;
+        }
+        rc = 0.0f;
+      }
+      {
+        const long long q = (long long)(n - 1) * n + j;
+        U0[q] = fabsf(ra) < tiny ? copysignf(tiny, ra) : ra;
+        U1[q] = 0.0f;
+        U2[q] = 0.0f;
+      }
+      // start vector: a fixed pseudo-random pattern
+      for (int i = 0; i < n; ++i)
+        X[(long long)i * n + mbr] = 1.0f + 0.25f * (float)((i * 7919 + mbr * 104729) % 17) / 17.0f;
+      for (int it = 0; it < 3; ++it) {
+        // x <- U^-1 L^-1 P x
+        for (int i = 0; i < n - 1; ++i) {
+          const long long q = (long long)i * n + j;
+          float xi = X[(long long)i * n + mbr], xn = X[(long long)(i + 1) * n + mbr];
+          if (PV[q] != 0.0f) {
+            const float t = xi;
+            xi = xn;
+            xn = t;
+          }
+          X[(long long)i * n + mbr] = xi;
+          X[(long long)(i + 1) * n + mbr] = xn - Lm[q] * xi;
+        }
+        float x1 = 0.0f, x2 = 0.0f, amax = 0.0f;
+        for (int i = n - 1; i >= 0; --i) {
+          const long long q = (long long)i * n + j;
+          const float xi = (X[(long long)i * n + mbr] - U1[q] * x1 - U2[q] * x2) / U0[q];
+          X[(long long)i * n + mbr] = xi;
+          x2 = x1;
+          x1 = xi;
+          amax = fmaxf(amax, fabsf(xi));
+        }
+        // scale, orthogonalise against the cluster's earlier vectors, normalise
+        const float sc = amax > 0.0f ? 1.0f / amax : 1.0f;
+        for (int i = 0; i < n; ++i) X[(long long)i * n + mbr] *= sc;
+        for (int o = j; o < mbr; ++o) {
+          float dot = 0.0f;
+          for (int i = 0; i < n; ++i)
+            dot = fmaf(X[(long long)i * n + o], X[(long long)i * n + mbr], dot);
+          for (int i = 0; i < n; ++i)
+            X[(long long)i * n + mbr] = fmaf(-dot, X[(long long)i * n + o], X[(long long)i * n + mbr]);
+        }
+        float ss = 0.0f;
+        for (int i = 0; i < n; ++i) {
+          const float xi = X[(long long)i * n + mbr];
+          ss = fmaf(xi, xi, ss);
+        }
+        const float inv = ss > 0.0f ? rsqrtf(ss) : 0.0f;
+        for (int i = 0; i < n; ++i) X[(long long)i * n + mbr] *= inv;
+      }
+    }
+  }
+}
+
+// u_j = H_0 H_1 ... H_{n-3} z_j for the eigenvectors z_j of T (column j of
+// the inverse iteration's X), a warp per vector; row j of U^T receives u_j.
+__global__ void __launch_bounds__(kVecWarps * 32) tri_back_kernel32(int n, int batch,
+                                                                    const double* __restrict__ HVws,
+                                                                    const double* __restrict__ TRIws,
+                                                                    const double* __restrict__ INVws,
+                                                                    int ks,
+                                                                    float* __restrict__ U32,
+                                                                    const int* __restrict__ ok) {
+  __shared__ float z[kVecWarps][kMaxLargeN];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long gw = (long long)blockIdx.x * kVecWarps + w;
+  if (gw >= (long long)batch * n) return;
+  const int b = (int)(gw / n), j = (int)(gw % n);
+  if (ok[b] != 3) return;
+  const long long nn = (long long)n * n;
+  const float* HV = reinterpret_cast<const float*>(HVws + b * nn);
+  const float* tau = reinterpret_cast<const float*>(TRIws + b * nn) + 2 * n;
+  const float* X = reinterpret_cast<const float*>(INVws + b * (long long)ks * nn) + 5 * nn;
+  float* zz = z[w];
+  for (int i = lane; i < n; i += 32) zz[i] = X[(long long)i * n + j];
+  __syncwarp();
+  for (int k = n - 3; k >= 0; --k) {
+    const float t = tau[k];
+    if (t == 0.0f) continue;
+    const float* v = HV + (long long)k * n;
+    float a = 0.0f;
+    for (int i = k + 1 + lane; i < n; i += 32) a = fmaf(v[i], zz[i], a);
+    a = t * warp_sumf(a);
+    for (int i = k + 1 + lane; i < n; i += 32) zz[i] = fmaf(-a, v[i], zz[i]);
+    __syncwarp();
+  }
+  float* u = U32 + b * nn + (long long)j * n;
+  for (int i = lane; i < n; i += 32) u[i] = zz[i];
+}
+
+__global__ void stage_done_kernel(int batch, int* __restrict__ ok, int from, int to) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < batch; b += gridDim.x * blockDim.x)
+    if (ok[b] == from) ok[b] = to;
+}
+
 // X[:, j] = L^-T u_j (backward substitution, FP64), u_j = row j of U^T.
 __global__ void __launch_bounds__(kVecWarps * 32) tri_back_kernel(int n, int batch,
                                                                   const double* __restrict__ L64,
@@ -799,6 +1133,10 @@ size_t smem_factor64_large(int n) {
   return sizeof(float) * ((size_t)n * n + 2 * (size_t)m + 33);
 }
 
+size_t smem_tridiag(int n) {
+  return sizeof(float) * ((size_t)n * n + 2 * (size_t)n + 32);
+}
+
 size_t smem32(int n) {
   const int m = (n + 1) & ~1;
   return sizeof(float) * (3 * (size_t)n * n + 2 * (size_t)m + 35);
@@ -835,6 +1173,7 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (smem_factor64_large(n) + 64 > (size_t)max_optin) return false;  // + static shared
+    if (smem_tridiag(n) + 64 > (size_t)max_optin) return false;
   }
   const long long nn = (long long)n * n;
   const long long per = (long long)batch * nn;
@@ -871,10 +1210,16 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     const unsigned vb = (unsigned)((vecs + kVecWarps - 1) / kVecWarps);
     tri_fwd_kernel<<<vb, kVecWarps * 32, 0, s>>>(n, batch, L64, C64, ok, 0);  // C <- L^-1 C
     tri_fwd_kernel<<<vb, kVecWarps * 32, 0, s>>>(n, batch, L64, C64, ok, 1);  // C <- C L^-T
-    const size_t sml = smem_factor64_large(n);
-    cudaFuncSetAttribute(jacobi_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sml);
-    jacobi_large_kernel<<<batch, kThreads, sml, s>>>(n, C64, U32, ok);
+    // eigenvectors of C in FP32: Householder tridiagonalisation, bisection and
+    // inverse iteration, back-transformation (scratch: T, R and P, idle until
+    // the refinement)
+    const size_t smt = smem_tridiag(n);
+    cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+    tridiag_kernel<<<batch, kThreads, smt, s>>>(n, C64, T, R, ok);
+    const int ks = ksplit_of(n);
+    tri_eig_kernel<<<batch, kThreads, 0, s>>>(n, R, P, ks, ok);
+    tri_back_kernel32<<<vb, kVecWarps * 32, 0, s>>>(n, batch, T, R, P, ks, U32, ok);
+    stage_done_kernel<<<(batch + 255) / 256, 256, 0, s>>>(batch, ok, 3, 4);
     tri_back_kernel<<<vb, kVecWarps * 32, 0, s>>>(n, batch, L64, U32, X, ok);
     large_done_kernel<<<(batch + 255) / 256, 256, 0, s>>>(batch, ok);
   }

@@ -31,6 +31,7 @@
 
 #include "ks1d_common.cuh"
 #include "ksr_device.cuh"
+#include "nn_device.cuh"
 #include "xc_device.cuh"
 #include "qex_ks1d.h"
 
@@ -109,6 +110,11 @@ struct Params {
   int planes;             // qex_ks1d_options.solve_planes
   int* counter;
   MlpParams mlp;
+  // dense networks (QEX_XC_LOCAL_MLP / GLOBAL_MLP): the network, its shared
+  // FP32 floats per warp and 4 nmax-double scratch vectors per slot
+  NnNet nn;
+  int nn_floats;
+  double* nn_ws;
 };
 
 // Workspace vectors (each nmax doubles) per molecule.
@@ -134,7 +140,7 @@ __host__ __device__ inline long long ruw_doubles(int nmax, int kmax) {
 // resident: the FP32 solve planes live in shared memory (small batches, where
 // occupancy is not limited by shared memory) instead of streaming through the ring.
 __host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax, bool adjoint = false,
-                                                  bool resident = false) {
+                                                  bool resident = false, int nn_floats = 0) {
   SmemLayout L;
   L.nstr = ((nmax + 31) / 32) * 32 + 1;
   size_t off = 0;
@@ -148,6 +154,7 @@ __host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax, bool adjoi
   L.f32 = off;
   size_t xc_floats = 2 * (size_t)(nmax + 2 * kPadMlp) + (size_t)kMlpScratch * kWarp;
   if (ksr_scratch_floats(nmax) > xc_floats) xc_floats = ksr_scratch_floats(nmax);
+  if ((size_t)nn_floats > xc_floats) xc_floats = (size_t)nn_floats;
   size_t hart_floats = 2 * (size_t)nmax + 2;  // one FP64 scan vector
   // FP32 diagonal, then the ring of the streamed solves (16-byte aligned)
   const size_t ring_off = ((size_t)L.nstr + 3) / 4 * 4;
@@ -379,8 +386,15 @@ __device__ inline void flip_avg_global(double* v, int N, int lane) {
 // Returns E_xc (already multiplied by dx).  With reflect_xc the functional is
 // symmetrised (local convention, jax_dft kohn_sham_iteration): the staged
 // density must already be flip-averaged; outputs are flip-averaged here.
+__device__ __noinline__ double nn_xc(const Params& p, int N, double dx, const Smem& sm,
+                                     bool want_v, double* vout, double* frec, bool reflect_xc,
+                                     double* nnws, int lane);
+
 __device__ __noinline__ double xc_eval(const Params& p, int N, double dx, const Smem& sm, bool want_v,
-                          double* vout, double* frec, bool reflect_xc, int lane) {
+                          double* vout, double* frec, bool reflect_xc, int lane,
+                          double* nnws = nullptr) {
+  if (p.xc_kind == QEX_XC_LOCAL_MLP || p.xc_kind == QEX_XC_GLOBAL_MLP)
+    return nn_xc(p, N, dx, sm, want_v, vout, frec, reflect_xc, nnws, lane);
   const double* n = sm.s64a + kPad64;
   const bool local = (p.xc_conv == QEX_XC_LOCAL);
   double e = 0.0;
@@ -479,6 +493,28 @@ __device__ __noinline__ double xc_eval(const Params& p, int N, double dx, const 
     if (frec) flip_avg_global(frec, N, lane);
   }
   return warp_sum(e) * dx;
+}
+
+// The dense networks (LocalMLP / GlobalMLP with their wrappers) on the
+// density staged in sm.s64a; FP32 network in sm.f32, four scratch vectors of
+// nmax doubles at nnws.  Same contract as xc_eval.
+__device__ __noinline__ double nn_xc(const Params& p, int N, double dx, const Smem& sm,
+                                     bool want_v, double* vout, double* frec, bool reflect_xc,
+                                     double* nnws, int lane) {
+  const double* n = sm.s64a + kPad64;
+  const bool local = (p.xc_conv == QEX_XC_LOCAL);
+  double* g = nnws;
+  double* gp = nnws + p.nmax;
+  double* vs = nnws + 2LL * p.nmax;
+  double* c = nnws + 3LL * p.nmax;
+  const double e = nn_xc_eval(p.nn, p.xc_kind, N, dx, local, n, want_v, vout, frec, sm.f32, g,
+                              gp, vs, c, lane);
+  __syncwarp();
+  if (reflect_xc) {
+    if (want_v) flip_avg_global(vout, N, lane);
+    if (frec) flip_avg_global(frec, N, lane);
+  }
+  return e;
 }
 
 // The KSR functional's counterpart of xc_eval, called from the kernel body
@@ -1420,7 +1456,7 @@ template <int kBand, bool kRes, bool kKsr>
 __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__ Params p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x;
-  const SmemLayout L = smem_layout(p.nmax, p.kmax, false, kRes);
+  const SmemLayout L = smem_layout(p.nmax, p.kmax, false, kRes, p.nn_floats);
   Smem sm = carve(smem_raw, L);
   if (p.xc_kind == QEX_XC_WINDOW_MLP) stage_mlp_weights(p.mlp, sm.mlpw, lane, kWarp);
   __syncwarp();
@@ -1438,7 +1474,8 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
     const double x0 = p.grid_start[b];
     const double dx = p.grid_spacing[b];
     const int K = ne / 2 + 1;
-    if (N < 5 || N > p.nmax || ne < 1 || K > p.kmax || !(dx > 0.0)) {
+    if (N < 5 || N > p.nmax || ne < 1 || K > p.kmax || !(dx > 0.0) ||
+        (p.xc_kind == QEX_XC_GLOBAL_MLP && N != p.nn.inputs)) {
       if (lane == 0 && p.o_status) p.o_status[b] = QEX_BAD_ARG;
       continue;
     }
@@ -1456,6 +1493,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
     double* kt = ws + (long long)VKT * p.nmax;
     double* diffs = ws + (long long)VDIFF * p.nmax;
     double* X = diffs + (long long)p.mix_slots * p.nmax;
+    double* const nnws = p.nn_ws ? p.nn_ws + 4LL * slot * p.nmax : nullptr;
     int flags = 0;
     EigStats est = {};
     long long tmol = clock64();
@@ -1582,7 +1620,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
       if constexpr (kKsr) {
         ksr_xc(p, N, dx, sm, true, vxc, vf, reflect_xc, lane);
       } else {
-        xc_eval(p, N, dx, sm, true, vxc, vf, reflect_xc, lane);
+        xc_eval(p, N, dx, sm, true, vxc, vf, reflect_xc, lane, nnws);
       }
       // |dv_KS|_inf in FP32, rounded up: it only sizes brackets and picks the
       // warm route, both of which are verified
@@ -1641,7 +1679,7 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
           exc = ksr_xc(p, N, dx, sm, false, nullptr, nullptr, false, lane);
         }
       } else {
-        exc = xc_eval(p, N, dx, sm, false, nullptr, nullptr, false, lane);
+        exc = xc_eval(p, N, dx, sm, false, nullptr, nullptr, false, lane, nnws);
       }
       lap(est, tsub, 14);
       const double energy = tee - eks + eh + exc + eext;
@@ -2150,6 +2188,11 @@ long long stride_doubles(const qex_ks1d_options* o, bool adjoint = false) {
   return (s + 31) / 32 * 32;
 }
 
+// Bytes of the dense networks' scratch vectors (4 per slot) for a batch shape.
+size_t nn_tail_bytes(const qex_ks1d_options* o, int num_molecules) {
+  return sizeof(double) * 4 * (size_t)num_molecules * (size_t)o->max_num_grids;
+}
+
 // Bytes of the deferred KSR energy rows for a batch shape.
 size_t ksr_defer_bytes(const qex_ks1d_options* o, int num_molecules) {
   return sizeof(double) * (size_t)num_molecules * (size_t)o->num_iterations *
@@ -2199,10 +2242,16 @@ int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_opt
   P.xc_shift = xc->shift;
   P.lda_A = xc->lda_amplitude;
   P.lda_kappa = xc->lda_kappa;
-  if (xc->kind < QEX_XC_NONE || xc->kind > QEX_XC_KSR) return QEX_BAD_ARG;
+  if (xc->kind < QEX_XC_NONE || xc->kind > QEX_XC_GLOBAL_MLP) return QEX_BAD_ARG;
   if (xc->convention != QEX_XC_AMPLITUDE && xc->convention != QEX_XC_LOCAL) return QEX_BAD_ARG;
   if (xc->kind == QEX_XC_WINDOW_MLP) {
     if (!fill_mlp_params(P.mlp, xc)) return QEX_BAD_ARG;
+  }
+  if (is_nn_kind(xc->kind)) {
+    rc = fill_nn(P.nn, xc);
+    if (rc) return rc;
+    if (xc->kind == QEX_XC_GLOBAL_MLP && xc->nn_inputs > o->max_num_grids) return QEX_BAD_ARG;
+    P.nn_floats = (int)nn_smem_floats(xc->kind, xc->nn_width, xc->nn_layers, o->max_num_grids);
   }
   if (xc->kind == QEX_XC_KSR) {
     if (!xc->ksr_params || reinterpret_cast<uintptr_t>(xc->ksr_params) % 16 != 0) return QEX_BAD_ARG;
@@ -2238,6 +2287,13 @@ int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_opt
     const size_t base = (need + 255) / 256 * 256;
     if (ws_bytes >= base + ksr_defer_bytes(o, num_molecules))
       P.ksr_defer = reinterpret_cast<double*>(static_cast<unsigned char*>(ws) + base);
+  }
+  // dense networks: their scratch vectors follow the base workspace
+  // (qex_ks1d_workspace_size_xc bytes in all)
+  if (is_nn_kind(xc->kind)) {
+    const size_t base = (need + 255) / 256 * 256;
+    if (ws_bytes < base + nn_tail_bytes(o, num_molecules)) return QEX_BAD_ARG;
+    P.nn_ws = reinterpret_cast<double*>(static_cast<unsigned char*>(ws) + base);
   }
   P.counter = reinterpret_cast<int*>(ws);
   P.ws = reinterpret_cast<double*>(static_cast<unsigned char*>(ws) + 256);
@@ -2384,8 +2440,8 @@ int launch(const Params& P, cudaStream_t stream) {
   int sms = 0, max_optin = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t smem_s = smem_layout(P.nmax, P.kmax, false, false).total;
-  const size_t smem_r = smem_layout(P.nmax, P.kmax, false, true).total;
+  const size_t smem_s = smem_layout(P.nmax, P.kmax, false, false, P.nn_floats).total;
+  const size_t smem_r = smem_layout(P.nmax, P.kmax, false, true, P.nn_floats).total;
   const bool band2 = (P.stencil == 5);
   if (P.xc_kind == QEX_XC_KSR) {
     // the KSR instantiation streams its solve planes (one variant per stencil)
@@ -2469,6 +2525,8 @@ int qex_ks1d_workspace_size_xc(const qex_ks1d_options* options, const qex_xc_spe
   if (rc) return rc;
   if (xc && xc->kind == QEX_XC_KSR)
     *bytes = (*bytes + 255) / 256 * 256 + qex::ksr_defer_bytes(options, num_molecules);
+  if (xc && qex::is_nn_kind(xc->kind))
+    *bytes = (*bytes + 255) / 256 * 256 + qex::nn_tail_bytes(options, num_molecules);
   return QEX_OK;
 }
 

@@ -11,6 +11,7 @@
 
 #include "ks1d_common.cuh"
 #include "ksr_device.cuh"
+#include "nn_device.cuh"
 #include "qex_xc1d.h"
 #include "xc_device.cuh"
 
@@ -165,6 +166,42 @@ __global__ void __launch_bounds__(kWarp) ksr1d_kernel(const __grid_constant__ Ks
   if (lane == 0 && p.energy) p.energy[b] = e * dx;
 }
 
+struct NnEvalParams {
+  int num_molecules;
+  const int32_t* num_grids;
+  const int64_t* offsets;
+  const double* spacing;
+  const double* density;
+  double* values;
+  double* potential;
+  double* energy;
+  int kind, conv;
+  NnNet net;
+  double* scratch;  // 4 vectors per molecule: molecule b at 4 * offsets[b]
+};
+
+// Dense networks (LocalMLP / GlobalMLP): one warp per molecule, the
+// warp-level evaluation shared with the SCF kernel.
+__global__ void __launch_bounds__(kWarp) nn1d_kernel(const __grid_constant__ NnEvalParams p) {
+  extern __shared__ __align__(16) float nsm[];
+  const int b = blockIdx.x;
+  const int lane = threadIdx.x;
+  if (b >= p.num_molecules) return;
+  const int N = p.num_grids[b];
+  if (N < 1 || (p.kind == QEX_XC_GLOBAL_MLP && N != p.net.inputs)) {
+    if (lane == 0 && p.energy) p.energy[b] = nan("");
+    return;
+  }
+  const long long off = p.offsets[b];
+  const double dx = p.spacing[b];
+  double* sc = p.scratch + 4 * off;
+  const double e = nn_xc_eval(p.net, p.kind, N, dx, p.conv == QEX_XC_LOCAL, p.density + off,
+                              p.potential != nullptr, p.potential ? p.potential + off : nullptr,
+                              p.values ? p.values + off : nullptr, nsm, sc, sc + N, sc + 2 * N,
+                              sc + 3 * N, lane);
+  if (lane == 0 && p.energy) p.energy[b] = e;
+}
+
 }  // namespace
 }  // namespace qex
 
@@ -223,6 +260,7 @@ int qex_xc1d_workspace_size(int64_t total_points, const qex_xc_spec* xc, size_t*
   *bytes = (xc->kind == QEX_XC_WINDOW_MLP)
                ? sizeof(float) * QEX_MLP_WINDOW * (size_t)total_points
                : 0;
+  if (qex::is_nn_kind(xc->kind)) *bytes = sizeof(double) * 4 * (size_t)total_points;
   return QEX_OK;
 }
 
@@ -235,6 +273,38 @@ int qex_xc1d_eval(int32_t num_molecules, int64_t total_points, const int32_t* nu
   if (num_molecules < 0 || !xc) return QEX_BAD_ARG;
   if (num_molecules == 0) return QEX_OK;
   if (!num_grids || !grid_offsets || !grid_spacing || !density) return QEX_BAD_ARG;
+  if (is_nn_kind(xc->kind)) {
+    if (xc->convention != QEX_XC_AMPLITUDE && xc->convention != QEX_XC_LOCAL) return QEX_BAD_ARG;
+    NnEvalParams Q;
+    memset(&Q, 0, sizeof(Q));
+    if (fill_nn(Q.net, xc) != QEX_OK) return QEX_BAD_ARG;
+    size_t need = 0;
+    qex_xc1d_workspace_size(total_points, xc, &need);
+    if (!workspace || workspace_bytes < need) return QEX_BAD_ARG;
+    Q.num_molecules = num_molecules;
+    Q.num_grids = num_grids;
+    Q.offsets = grid_offsets;
+    Q.spacing = grid_spacing;
+    Q.density = density;
+    Q.values = values;
+    Q.potential = potential;
+    Q.energy = energy;
+    Q.kind = xc->kind;
+    Q.conv = xc->convention;
+    Q.scratch = static_cast<double*>(workspace);
+    // the global network's input size is the grid size of every molecule
+    const size_t smem =
+        sizeof(float) * (size_t)nn_smem_floats(xc->kind, xc->nn_width, xc->nn_layers, xc->nn_inputs);
+    int dev = 0, max_optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return QEX_CUDA_ERROR;
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (smem > (size_t)max_optin) return QEX_BAD_ARG;
+    if (cudaFuncSetAttribute(nn1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return QEX_CUDA_ERROR;
+    nn1d_kernel<<<num_molecules, kWarp, smem, static_cast<cudaStream_t>(stream)>>>(Q);
+    return cudaGetLastError() == cudaSuccess ? QEX_OK : QEX_CUDA_ERROR;
+  }
   if (xc->kind < QEX_XC_NONE || xc->kind > QEX_XC_WINDOW_MLP) return QEX_BAD_ARG;
   XcParams P;
   memset(&P, 0, sizeof(P));

@@ -18,7 +18,7 @@ from typing import Protocol
 import numpy as np
 
 from . import _native as N
-from .xc import LDAExpCoulomb, Partial, WindowMLPFunctional, XCFunctional
+from .xc import LDAExpCoulomb, NeuralMLPFunctional, Partial, WindowMLPFunctional, XCFunctional
 
 
 class KohnShamNetwork(Protocol):
@@ -77,6 +77,148 @@ class WindowMLP:
         return init_fn, apply_fn
 
 
+def glorot_normal(rng, fan_in, fan_out, dtype=np.float32):
+    """jax.nn.initializers.glorot_normal (stax ``Dense``'s default): a normal
+    truncated at two standard deviations, variance 2 / (fan_in + fan_out)."""
+    std = np.sqrt(2.0 / (fan_in + fan_out)) / 0.87962566103423978
+    w = rng.normal(0.0, std, size=(fan_in, fan_out))
+    bad = np.abs(w) > 2.0 * std
+    while bad.any():
+        w[bad] = rng.normal(0.0, std, size=int(bad.sum()))
+        bad = np.abs(w) > 2.0 * std
+    return w.astype(dtype)
+
+
+def dense_stack_params(rng, fan_in, n_neurons, n_layers, n_outputs=1):
+    """stax.serial([Dense(n_neurons), activation] x n_layers, Dense(n_outputs))
+    parameters (``qedft/models/classical/classical_models.py:77-115``):
+    (W, b) per Dense layer (Glorot-normal W, normal(1e-6) b), () per activation."""
+    g = _rng(rng)
+    params = []
+    fin = fan_in
+    for _ in range(n_layers):
+        params.append((glorot_normal(g, fin, n_neurons),
+                       (g.normal(0.0, 1e-6, n_neurons)).astype(np.float32)))
+        params.append(())
+        fin = n_neurons
+    params.append((glorot_normal(g, fin, n_outputs), (g.normal(0.0, 1e-6, n_outputs)).astype(np.float32)))
+    return params
+
+
+class _DenseNetwork:
+    """(init_fn, apply_fn) of a bare dense stack; apply_fn evaluates it on the
+    GPU (no wrappers).  ``template`` is the unwrapped functional."""
+
+    def __init__(self, template: NeuralMLPFunctional, fan_in):
+        self.template, self.fan_in = template, int(fan_in)
+
+    def init_fn(self, rng, input_shape=None):
+        params = dense_stack_params(rng, self.fan_in, self.template.n_neurons,
+                                    self.template.n_layers)
+        out = (input_shape[:-1] + (1,)) if input_shape and self.template.local else (1,)
+        return out, params
+
+    def apply_fn(self, params, inputs, **kwargs):
+        from .od.xc_eval import xc_energy_and_potential
+
+        n = np.asarray(inputs, dtype=np.float64).reshape(-1)
+        t = self.template
+        bare = NeuralMLPFunctional(t.local, t.n_neurons, t.n_layers, t.activation,
+                                   t.normalization, False, False, n.size)
+        _, _, vals = xc_energy_and_potential(n, Partial(bare, params=params),
+                                             np.arange(n.size) * 1.0, "amplitude")
+        return vals if t.local else np.array([vals.sum()])
+
+    def __iter__(self):
+        return iter((self.init_fn, self.apply_fn))
+
+
+class LocalMLP:
+    """``qedft/models/networks.py:83-109``: the dense network applied at every
+    grid point to n_i / density_normalization_factor
+    (``build_local_mlp``, ``qedft/models/classical/classical_models.py:123-174``).
+    Default config: n_neurons 64, n_layers 3, tanh, normalization 2.0, wrapped
+    with the negativity transform (``wrap_with_negative_transform``)."""
+
+    def __init__(self, config_dict: dict | None = None):
+        self.config = {"network_type": "mlp", "wrap_self_interaction": False,
+                       "wrap_with_negative_transform": True, "use_amplitude_encoding": False}
+        if config_dict is not None:
+            self.config.update(config_dict)
+        if self.config.get("use_amplitude_encoding") is True:
+            raise ValueError("Set use_amplitude_encoding to False.")
+
+    def build_network(self, grids):
+        if grids is None:
+            raise ValueError("grids must be provided for local MLP")
+        t = NeuralMLPFunctional(True, self.config.get("n_neurons", 64),
+                                self.config.get("n_layers", 3),
+                                self.config.get("activation", "tanh"),
+                                self.config.get("density_normalization_factor", 2.0),
+                                False, False, 1)
+        return _DenseNetwork(t, 1)
+
+
+class GlobalMLP:
+    """``qedft/models/networks.py:112-138``: the dense network on the whole
+    density vector / density_normalization_factor, one scalar out
+    (``build_global_mlp``, ``classical_models.py:177-224``).  Default config:
+    network_type "mlp_ksr" (amplitude encoding), n_neurons 64, n_layers 3,
+    tanh, normalization 2.0, wrapped with the self-interaction layer and the
+    negativity transform."""
+
+    def __init__(self, config_dict: dict | None = None):
+        self.config = {"network_type": "mlp_ksr", "wrap_self_interaction": True,
+                       "wrap_with_negative_transform": True, "use_amplitude_encoding": True}
+        if config_dict is not None:
+            self.config.update(config_dict)
+        if self.config.get("use_amplitude_encoding") is False:
+            raise ValueError("Set use_amplitude_encoding to True.")
+
+    def build_network(self, grids):
+        if grids is None:
+            raise ValueError("grids must be provided for global MLP")
+        n = int(np.asarray(grids).shape[0])
+        t = NeuralMLPFunctional(False, self.config.get("n_neurons", 64),
+                                self.config.get("n_layers", 3),
+                                self.config.get("activation", "tanh"),
+                                self.config.get("density_normalization_factor", 2.0),
+                                False, False, n)
+        return _DenseNetwork(t, n)
+
+
+# network types whose functional is global (amplitude encoded), qedft/models/wrappers.py:170-178
+_GLOBAL_TYPES = ("gadqc", "gadqc_with_mlp", "conv_dqc", "conv_adqc", "mlp_ksr", "conv_dqc_tfm",
+                 "conv_adqc_tfm")
+
+
+def _wrap_dense(network: _DenseNetwork, grids, config):
+    """``wrap_network`` (``qedft/models/wrappers.py:162-217``) for the dense
+    networks: self-interaction, then negativity, then (global types) the mean."""
+    t = network.template
+    is_global = config.get("network_type") in _GLOBAL_TYPES
+    if is_global == t.local:
+        raise ValueError(f"network_type {config.get('network_type')!r} does not match a "
+                         f"{'local' if t.local else 'global'} network")
+    si = bool(config.get("wrap_self_interaction", False))
+    neg = bool(config.get("wrap_with_negative_transform", False))
+    functional = NeuralMLPFunctional(t.local, t.n_neurons, t.n_layers, t.activation,
+                                     t.normalization, si, neg, t.num_inputs)
+    n = int(np.asarray(grids).shape[0])
+
+    def init_fn(rng, **kwargs):
+        # the local network is initialised with input_shape (-1, N, 1), the
+        # global one with (1,) (wrappers.py:62-75); the Dense shapes follow the fan-in
+        _, params = network.init_fn(rng, (-1, n, 1) if t.local else (1,))
+        if si:
+            params = [(), ((), params), (np.array(1.0, np.float32),)]
+        if neg:
+            params = [params, ()]
+        return params
+
+    return init_fn, _XCEnergyDensityFn(functional)
+
+
 class LDA:
     """The exponential-Coulomb LDA as a (parameter-free) network."""
 
@@ -112,12 +254,20 @@ class _XCEnergyDensityFn:
 def build_xc_functional(network, grids, config: dict | None = None):
     """(init_fn(rng) -> params, xc_energy_density_fn(density, params)).
 
-    Mirrors ``qedft/models/wrappers.py:267-299``.  The self-interaction and
-    negativity wrappers of ``wrap_network`` are not part of the GPU path.
+    Mirrors ``qedft/models/wrappers.py:267-299``.  For the dense networks
+    (``LocalMLP``, ``GlobalMLP``) the config's ``wrap_self_interaction`` and
+    ``wrap_with_negative_transform`` wrappers and the global mean are part of
+    the GPU functional; the fixed-shape window MLP and the LDA take none.
     """
     config = dict(config or {})
+    if isinstance(network, tuple) and isinstance(getattr(network[1], "__self__", None),
+                                                 _DenseNetwork):
+        network = network[1].__self__  # (init_fn, apply_fn) unpacked from build_network
+    if isinstance(network, _DenseNetwork):
+        return _wrap_dense(network, grids, config)
     if config.get("wrap_self_interaction") or config.get("wrap_with_negative_transform"):
-        raise NotImplementedError("self-interaction / negativity wrappers are not on the GPU path")
+        raise NotImplementedError("the self-interaction / negativity wrappers apply to the dense "
+                                  "networks (LocalMLP, GlobalMLP) and the KSR model")
     net_init, net_apply = network
     functional = getattr(net_apply, "functional", None)
     if not isinstance(functional, XCFunctional):

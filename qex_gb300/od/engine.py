@@ -317,7 +317,7 @@ class Ks1dEngine:
             opts.max_num_grids = max(ng_max, 5)
             opts.solve_planes = planes
             nbytes = ctypes.c_size_t()
-            if defer_ksr:
+            if defer_ksr or functional.kind in (N.QEX_XC_LOCAL_MLP, N.QEX_XC_GLOBAL_MLP):
                 N.check(self.lib.qex_ks1d_workspace_size_xc(ctypes.byref(opts), ctypes.byref(spec),
                                                             count, ctypes.byref(nbytes)),
                         "qex_ks1d_workspace_size_xc")
@@ -375,8 +375,9 @@ class Ks1dEngine:
         out = self.allocate_outputs(batch, c1, ("energy", "gap", "density", "hartree_potential",
                                                 "xc_potential", "xc_energy_density"))
         nbytes = ctypes.c_size_t()
-        N.check(self.lib.qex_ks1d_workspace_size(ctypes.byref(opts), batch.size, ctypes.byref(nbytes)),
-                "qex_ks1d_workspace_size")
+        N.check(self.lib.qex_ks1d_workspace_size_xc(ctypes.byref(opts), ctypes.byref(spec),
+                                                    batch.size, ctypes.byref(nbytes)),
+                "qex_ks1d_workspace_size_xc")
         ws = self.workspace.get(nbytes.value)
         cb = batch.c_batch(external_potential=external_potential)
         co = self._c_outputs(out)

@@ -193,6 +193,106 @@ class KSRFunctional(XCFunctional):
         return s, buf
 
 
+class NeuralMLPFunctional(XCFunctional):
+    """The reference's dense XC networks with their wrappers, FP32 on the GPU.
+
+    ``local=True``: LocalMLP (``qedft/models/networks.py:83-109``,
+    ``build_local_mlp`` at ``qedft/models/classical/classical_models.py:123-174``),
+    g_i = MLP(n_i / norm) at every grid point.  ``local=False``: GlobalMLP
+    (``networks.py:112-138``, ``build_global_mlp`` at ``classical_models.py:177-224``),
+    one g = MLP(n / norm) from the whole density (input size = the grid size).
+    Wrappers (``qedft/models/wrappers.py:162-217``): ``self_interaction``
+    (jax_dft's layer, u_i = beta (-v_H[n]_i / 2) + (1 - beta) g_i) and
+    ``negativity`` (f = -swish(u)); a global network's output is the mean of
+    f over the grid.  The network is [Dense(n_neurons), activation] x
+    n_layers, Dense(1).
+
+    ``params`` is the stax parameter tree the wrapped network's ``init_fn``
+    returns (see ``qex_gb300.networks.LocalMLP`` / ``GlobalMLP``).
+    """
+
+    def __init__(self, local=True, n_neurons=64, n_layers=3, activation="tanh",
+                 normalization=2.0, self_interaction=False, negativity=True, num_inputs=1):
+        if activation not in N.QEX_NN_ACTIVATIONS:
+            raise ValueError(f"activation {activation!r} is not on the GPU path "
+                             f"(one of {sorted(N.QEX_NN_ACTIVATIONS)})")
+        if not 1 <= int(n_neurons) <= N.QEX_NN_MAX_WIDTH or int(n_layers) < 1:
+            raise ValueError(f"the GPU networks take 1..{N.QEX_NN_MAX_WIDTH} neurons and "
+                             "at least one hidden layer")
+        self.local = bool(local)
+        self.kind = N.QEX_XC_LOCAL_MLP if self.local else N.QEX_XC_GLOBAL_MLP
+        self.n_neurons, self.n_layers = int(n_neurons), int(n_layers)
+        self.activation = activation
+        self.normalization = float(normalization)
+        self.self_interaction, self.negativity = bool(self_interaction), bool(negativity)
+        self.num_inputs = 1 if self.local else int(num_inputs)
+        self.width_padded = (self.n_neurons + 7) // 8 * 8
+        self._dev = None
+
+    def dense_layers(self, params):
+        """[(W, b), ...] of the Dense layers and the self-interaction width
+        (1.0 without the layer) from the wrapped network's parameter tree."""
+        tree = params
+        if self.negativity:
+            tree = tree[0]  # stax.serial(network, negativity_transform())
+        width = 1.0
+        if self.self_interaction:
+            # stax.serial(FanOut(2), parallel(Identity, network), self_interaction_layer)
+            width = float(np.asarray(tree[2][0]))
+            tree = tree[1][1]
+        dense = [layer for layer in tree if len(layer) == 2]
+        if len(dense) != self.n_layers + 1:
+            raise ValueError(f"expected {self.n_layers + 1} Dense layers, got {len(dense)}")
+        return [(np.asarray(w), np.asarray(b)) for w, b in dense], width
+
+    def pack(self, params) -> np.ndarray:
+        layers, width = self.dense_layers(params)
+        H, Hp, nin = self.n_neurons, self.width_padded, self.num_inputs
+        parts = []
+        for li, (w, b) in enumerate(layers[:-1]):
+            fin = nin if li == 0 else H
+            w = np.asarray(w, np.float32).reshape(fin, H)
+            wp = np.zeros((fin if li == 0 else Hp, Hp), np.float32)
+            wp[:fin, :H] = w
+            bp = np.zeros(Hp, np.float32)
+            bp[:H] = np.asarray(b, np.float32).reshape(H)
+            parts += [wp.reshape(-1), bp]
+        wo, bo = layers[-1]
+        wop = np.zeros(Hp, np.float32)
+        wop[:H] = np.asarray(wo, np.float32).reshape(H)
+        tail = np.array([float(np.asarray(bo).reshape(-1)[0]), width, 0.0, 0.0], np.float32)
+        flat = np.concatenate(parts + [wop, tail])
+        assert flat.size == nin * Hp + Hp + (self.n_layers - 1) * (Hp * Hp + Hp) + Hp + 4
+        return np.ascontiguousarray(flat)
+
+    def device_params(self, params):
+        torch = N.require_cuda()
+        flat = self.pack(params)
+        key = flat.tobytes()
+        if self._dev is None or self._dev[0] != key or self._dev[1].device != torch.device(
+                "cuda", torch.cuda.current_device()):
+            self._dev = (key, torch.as_tensor(flat, device="cuda"))
+        return self._dev[1]
+
+    def spec(self, params, convention):
+        if params is None:
+            raise ValueError("NeuralMLPFunctional needs params")
+        if not self.local and convention != N.QEX_XC_AMPLITUDE:
+            raise ValueError("a global network is an amplitude-encoded functional "
+                             "(kohn_sham_amplitude_encoded)")
+        s, _ = super().spec(params, convention)
+        buf = self.device_params(params)
+        s.nn_params = buf.data_ptr()
+        s.nn_width = self.width_padded
+        s.nn_layers = self.n_layers
+        s.nn_activation = N.QEX_NN_ACTIVATIONS[self.activation]
+        s.nn_inputs = self.num_inputs
+        s.nn_flags = ((N.QEX_NN_SELF_INTERACTION if self.self_interaction else 0)
+                      | (N.QEX_NN_NEGATIVITY if self.negativity else 0))
+        s.normalization = self.normalization
+        return s, buf
+
+
 class Partial:
     """Minimal stand-in for ``jax.tree_util.Partial``: a functional with bound
     keyword arguments (``params``), as built at ``qedft/train/od/train.py:102-105``."""
