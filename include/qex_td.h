@@ -44,6 +44,19 @@
  *   qex_td_coulomb        <- J = einsum('ijkl,kl->ij', eri, dm),
  *                            qedft/train/td/scf_functions_masked.py:152, with the
  *                            ERI in factored form (ij|kl) = sum_P B_Pij B_Pkl
+ *   qex_td_fock_energy    <- get_fock without DIIS (h1e + vhf, qedft/train/td/hf.py:360-404)
+ *                            fused with energy_tot (tr(D h) + 1/2 tr(D J) + E_xc + E_nuc,
+ *                            qedft/train/td/scf_functions_masked.py:243-265)
+ *   qex_td_orbital_gradient <- norm of mf.get_grad(mo_coeff, mo_occ, fock) (pyscf RHF
+ *                            gradient 2 C_vir^T F C_occ), qedft/train/td/hf.py:81-84
+ *   qex_td_scf_check      <- the stop rule |E - E_last| < conv_tol and |g| < conv_tol_grad,
+ *                            qedft/train/td/hf.py:93-96 (results latched at the first
+ *                            converged cycle, as the reference's loop breaks there)
+ *   qex_td_aufbau_occ     <- get_occ, qedft/train/td/hf.py:602-607 and
+ *                            qedft/train/td/scf_functions_masked.py:176-186
+ *   qex_td_mask_pad, qex_td_mask_sort
+ *                         <- the padding and slot sorting of masked_generalized_eigh,
+ *                            qedft/train/td/generalized_eigensolver_masked.py:19-89
  */
 #ifndef QEX_TD_H_
 #define QEX_TD_H_
@@ -218,6 +231,47 @@ size_t qex_td_nn_xc_global_workspace_size(int64_t num_points, int32_t hidden);
 int qex_td_nn_xc_global(int64_t num_points, int32_t hidden, const double* rho,
                         const double* weights, const float* params, double scale, double* vrho,
                         double* sums, void* workspace, size_t workspace_bytes, void* stream);
+
+/* F = h1e + J + V (fock may be NULL) and energy[0] = sum_ij D_ij h_ji +
+ * 1/2 sum_ij D_ij J_ij + excsum[0] + energy_nuc (excsum a device scalar, may be
+ * NULL for 0).  One CTA, fixed-order sums. */
+int qex_td_fock_energy(int32_t n, const double* h1e, const double* J, const double* V,
+                       const double* dm, const double* excsum, double energy_nuc, double* fock,
+                       double* energy, void* stream);
+
+/* norm[0] = |g|_2, g_ai = 2 (C^T F C)_ai over virtual a (mo_occ == 0 or below)
+ * and occupied i (mo_occ > 0).  Workspace of the queried size. */
+size_t qex_td_orbital_gradient_workspace_size(int32_t n);
+int qex_td_orbital_gradient(int32_t n, const double* mo_coeff, const double* mo_occ,
+                            const double* fock, double* norm, void* workspace,
+                            size_t workspace_bytes, void* stream);
+
+/* Convergence of cycle `cycle`: E = energies[cycle], E_last = energies[cycle-1]
+ * (energy_init[0] for cycle 0).  state (3 ints, zeroed before cycle 0):
+ * [0] converged, [1] first converged cycle, [2] cycles run up to it.  Until
+ * the first converged cycle (included) the cycle's dm, mo_energy, mo_coeff,
+ * mo_occ and energy are copied to the *_out buffers; after it they are left
+ * alone, so the outputs are those of the cycle at which the reference's loop
+ * stops, or of the last cycle when it never converges. */
+int qex_td_scf_check(int32_t cycle, int32_t n, const double* energies, const double* energy_init,
+                     const double* gnorm, double conv_tol, double conv_tol_grad, int32_t* state,
+                     const double* dm, const double* mo_energy, const double* mo_coeff,
+                     const double* mo_occ, double* dm_out, double* mo_energy_out,
+                     double* mo_coeff_out, double* mo_occ_out, double* energy_out, void* stream);
+
+/* Aufbau occupations for a batch of spectra (batch, n): 2 in the lowest
+ * nelectron / 2 orbitals (ties by index), 0 elsewhere. */
+int qex_td_aufbau_occ(int32_t batch, int32_t n, const double* mo_energy, int32_t nelectron,
+                      double* mo_occ, void* stream);
+
+/* Masked eigenproblem set-up and ordering (mask: n bytes, 1 = kept):
+ * mask_pad writes F and S restricted to the kept block with 1e-12 on padded
+ * diagonals; mask_sort orders eigenpairs by (mask ? w : 1e12), stably, zeroes
+ * the padded eigenvalues and the padded rows and columns of V. */
+int qex_td_mask_pad(int32_t n, const double* fock, const double* s1e, const uint8_t* mask,
+                    double* fock_out, double* s1e_out, void* stream);
+int qex_td_mask_sort(int32_t n, const double* w, const double* V, const uint8_t* mask,
+                     double* w_out, double* V_out, void* stream);
 
 #ifdef __cplusplus
 }

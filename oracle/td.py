@@ -532,15 +532,28 @@ def energy_tot(dm, h1e, J, exc, e_nuc):
     return float(np.einsum("ij,ji->", dm, h1e) + 0.5 * np.einsum("ij,ij->", dm, J) + exc + e_nuc)
 
 
+def orbital_gradient_norm(mo_coeff, mo_occ, fock):
+    """|g|, g = 2 C_vir^T F C_occ: pyscf's RHF ``get_grad`` as the reference's
+    loop calls it (``qedft/train/td/hf.py:81-84``; occupied = mo_occ > 0)."""
+    occ = np.asarray(mo_occ) > 0
+    g = 2.0 * mo_coeff[:, ~occ].T @ fock @ mo_coeff[:, occ]
+    return float(np.linalg.norm(g))
+
+
 def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, nn=None, vwn=False, fermi=None,
-        gga=False):
+        gga=False, stop=None):
     """Fixed-cycle SCF of ``qedft/train/td/scf_functions_masked.py:907-967`` with
     the low-rank Coulomb model and the LDA exchange, or with ``nn = (flat,
     scale, dtype)`` the neural functional.  ``fermi`` (a dict: theta, mode
     "stable" (default) / "jax" / "optimize", max_steps, step_grad, mu_shift, mu) replaces
     the aufbau occupations by Fermi-Dirac ones (``qedft/train/td/fermi.py``);
     the per-cycle entropic energies are then returned as a fourth value.
-    ``gga=True`` uses the GGA branch with PBE exchange (``nr_rks_gga``)."""
+    ``gga=True`` uses the GGA branch with PBE exchange (``nr_rks_gga``).
+    ``stop = (conv_tol, conv_tol_grad)``: the loop of ``qedft/train/td/hf.py:47-110``
+    instead, which stops at the first cycle with |E - E_last| < conv_tol and
+    |g| < conv_tol_grad (E_last of cycle 0 = the initial guess's energy); it
+    returns a dict (e_tot, dm, mo_energy, mo_occ, converged, cycles, energies,
+    grad_norms)."""
     ao, w = mol.ao, mol.weights
     if gga:
         ao = eval_ao(mol.shells, mol.coords, deriv=1)
@@ -577,8 +590,10 @@ def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, nn=None, vwn=Fals
     J = coulomb_lowrank(mol.eri_factors, dm)
     _, exc, vxc = rks(ao, w, dm)
     vhf = J + vxc
+    e_last = energy_tot(dm, h1e, J, exc, mol.energy_nuc)
     diis = DIIS(diis_max_vec)
-    energies, entropic = [], []
+    energies, entropic, gnorms = [], [], []
+    converged = False
     for cycle in range(max_cycle):
         fock = h1e + vhf
         if cycle >= diis_start_cycle:
@@ -591,6 +606,16 @@ def scf(mol, max_cycle=30, diis_max_vec=8, diis_start_cycle=1, nn=None, vwn=Fals
         _, exc, vxc = rks(ao, w, dm)
         vhf = J + vxc
         energies.append(energy_tot(dm, h1e, J, exc, mol.energy_nuc))
+        if stop is not None:
+            gnorms.append(orbital_gradient_norm(mo_c, occ, h1e + vhf))
+            if abs(energies[-1] - e_last) < stop[0] and gnorms[-1] < stop[1]:
+                converged = True
+                break
+            e_last = energies[-1]
+    if stop is not None:
+        return {"e_tot": energies[-1], "dm": dm, "mo_energy": mo_e, "mo_occ": occ,
+                "converged": converged, "cycles": len(energies),
+                "energies": np.array(energies), "grad_norms": np.array(gnorms)}
     if fermi is not None:
         return np.array(energies), dm, mo_e, np.array(entropic)
     return np.array(energies), dm, mo_e

@@ -43,6 +43,8 @@ class Request:
     density: np.ndarray | None = None
     status: int = 0
     graph3d: object = None  # 3D request: key of a resident CapturedScf
+    e_tot: float | None = None  # 3D: energy at the cycle the stop rule was met (else the last)
+    converged3d: bool = False   # 3D: the reference's stop rule (|dE|, |g|) was met
 
     @property
     def is3d(self):
@@ -151,9 +153,13 @@ class ScfServer:
         with torch.cuda.stream(stream):
             res = g.replay()
             host = {"energy": torch.empty(res.energies.shape, dtype=torch.float64, pin_memory=True),
-                    "status": torch.empty(res.status.shape, dtype=torch.int32, pin_memory=True)}
+                    "status": torch.empty(res.status.shape, dtype=torch.int32, pin_memory=True),
+                    "e_tot": torch.empty(1, dtype=torch.float64, pin_memory=True),
+                    "state": torch.empty(3, dtype=torch.int32, pin_memory=True)}
             host["energy"].copy_(res.energies, non_blocking=True)
             host["status"].copy_(res.status, non_blocking=True)
+            host["e_tot"].copy_(res.e_tot, non_blocking=True)
+            host["state"].copy_(res.converged, non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(stream)
         self.busy3d.add(req.graph3d)
@@ -167,6 +173,8 @@ class ScfServer:
             r.finish = now
             r.energies = launch.host["energy"].numpy().copy()
             r.status = int(np.bitwise_or.reduce(launch.host["status"].numpy()))
+            r.e_tot = float(launch.host["e_tot"].numpy()[0])
+            r.converged3d = bool(launch.host["state"].numpy()[0])
             self.busy3d.discard(launch.graph3d)
             return
         energy = launch.host["energy"].numpy()
@@ -261,6 +269,8 @@ def serve_plain(xc, cfg: SolveConfig, requests: Sequence[Request],
             res = run_scf(molecules3d[r.graph3d], max_cycle)
             r.energies = res.energies.cpu().numpy()
             r.status = int(np.bitwise_or.reduce(res.status.cpu().numpy()))
+            r.e_tot = float(res.e_tot.cpu().numpy()[0])
+            r.converged3d = bool(res.converged.cpu().numpy()[0])
             r.finish = time.perf_counter() - t0
             continue
         batch = PackedBatch([r.molecule], sort=False)
@@ -303,8 +313,11 @@ def latency_summary(reqs: Sequence[Request], duration: float | None = None) -> d
 def _summary(reqs: Sequence[Request], duration: float | None = None) -> dict:
     lat = np.array([r.latency for r in reqs])
     span = duration if duration else (max(r.finish for r in reqs) - min(r.arrival for r in reqs))
-    conv = [r for r in reqs if r.energies is not None and abs(r.energies[-1] - r.energies[-2]) < 1e-8
-            and (r.status & 0xFFFF) == 0]
+    # 1D: |E_T - E_T-1| < 1e-8 Ha with the status clear; 3D: the reference's
+    # stop rule (|dE| < conv_tol and |g| < conv_tol_grad) met on the device
+    conv = [r for r in reqs if (r.converged3d if r.is3d else (
+        r.energies is not None and abs(r.energies[-1] - r.energies[-2]) < 1e-8))
+        and (r.status & 0xFFFF) == 0]
     return {
         "requests": len(reqs),
         "converged": len(conv),

@@ -51,6 +51,14 @@ SIGNATURES = {
                                            _sz, _v]),
     "qex_td_nn_xc": (ctypes.c_int, [_i64, _i32, _v, _v, _v, ctypes.c_double, _v, _v, _v, _v,
                                     _sz, _v]),
+    "qex_td_fock_energy": (ctypes.c_int, [_i32, _v, _v, _v, _v, _v, ctypes.c_double, _v, _v, _v]),
+    "qex_td_orbital_gradient_workspace_size": (_sz, [_i32]),
+    "qex_td_orbital_gradient": (ctypes.c_int, [_i32, _v, _v, _v, _v, _v, _sz, _v]),
+    "qex_td_scf_check": (ctypes.c_int, [_i32, _i32, _v, _v, _v, ctypes.c_double, ctypes.c_double,
+                                        _v, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v]),
+    "qex_td_aufbau_occ": (ctypes.c_int, [_i32, _i32, _v, _i32, _v, _v]),
+    "qex_td_mask_pad": (ctypes.c_int, [_i32, _v, _v, _v, _v, _v, _v]),
+    "qex_td_mask_sort": (ctypes.c_int, [_i32, _v, _v, _v, _v, _v, _v]),
 }
 
 _lib = None

@@ -38,20 +38,21 @@ def generalized_eigh(A, B, *, eps: float = 1.0e-12, return_status: bool = False)
 
 
 def masked_generalized_eigh(fock, s1e, mask):
-    """Padded/masked solve with the reference's padding and sorting rules."""
+    """Padded/masked solve with the reference's padding and sorting rules
+    (``qex_td_mask_pad``, the solve, ``qex_td_mask_sort``)."""
     torch = N.require_cuda()
-    fock = _dev(fock, torch.float64)
-    s1e = _dev(s1e, torch.float64)
-    mask = _dev(mask, torch.bool)
+    L = _lib.lib()
+    fock = _dev(fock, torch.float64).contiguous()
+    s1e = _dev(s1e, torch.float64).contiguous()
+    mask8 = _dev(mask, torch.bool).to(torch.uint8).contiguous()
     n = fock.shape[-1]
-    m2 = mask[:, None] & mask[None, :]
-    eye = torch.eye(n, dtype=torch.bool, device="cuda")
-    padd = (~mask)[:, None] & eye
-    f = torch.where(m2, fock, 0.0) + torch.where(padd, 1e-12, 0.0)
-    s = torch.where(m2, s1e, torch.where(padd, 1e-12, 0.0))
+    f = torch.empty_like(fock)
+    s = torch.empty_like(s1e)
+    N.check(L.qex_td_mask_pad(n, _lib.p(fock), _lib.p(s1e), _lib.p(mask8), _lib.p(f), _lib.p(s),
+                              _lib.stream()), "qex_td_mask_pad")
     w, v = generalized_eigh(f, s)
-    key = torch.where(mask, w, torch.full_like(w, 1e12))
-    order = torch.sort(key, stable=True).indices
-    w = w[order] * mask[order].to(w.dtype)
-    v = torch.where(m2[:, order], v[:, order], 0.0)
-    return w, v
+    w_out = torch.empty_like(w)
+    v_out = torch.empty_like(v)
+    N.check(L.qex_td_mask_sort(n, _lib.p(w), _lib.p(v.contiguous()), _lib.p(mask8), _lib.p(w_out),
+                               _lib.p(v_out), _lib.stream()), "qex_td_mask_sort")
+    return w_out, v_out
