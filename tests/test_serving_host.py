@@ -55,6 +55,8 @@ def _done(rid, arrival, latency, dE, status=0, graph=None):
     r.finish = arrival + latency
     r.energies = np.array([-1.0, -1.0 + dE])
     r.status = status
+    if graph is not None:  # a 3D result carries the device's stop-rule flag
+        r.converged3d = dE < 1e-8
     return r
 
 
