@@ -485,6 +485,142 @@ def run_train_eval(args):
             "grad_norm": float(np.linalg.norm(grad))}
 
 
+def run_config3(args, steps=3):
+    """The differentiation configuration: loss and gradient with respect to the
+    FP32 window-MLP parameters of 256 H2-type molecules (unit charges,
+    separation ~ U[0.5, 3.0] bohr), 513 points, 15 unrolled iterations,
+    checkpoints every 5, loss sum (E - E_t)^2 + 0.1 sum |n - n_t|^2 dx with
+    targets from the LDA solve; the hand-written adjoint on the GPU."""
+    import torch
+
+    import qex_gb300
+    from qex_gb300.od import adjoint, engine as eng
+    from qex_gb300.xc import Partial
+
+    rng = np.random.default_rng(args.seed + 3)
+    B, T = 256, 15
+    mols = [eng.Molecule1D(num_grids=513, grid_spacing=0.08, locations=[-r / 2, r / 2],
+                           nuclear_charges=[1.0, 1.0], num_electrons=2)
+            for r in rng.uniform(0.5, 3.0, B)]
+    batch = eng.PackedBatch(mols, sort=False)
+    cfg = eng.SolveConfig(num_iterations=T, alpha=0.5, alpha_decay=0.9, num_mixing_iterations=1,
+                          convention="local", stencil=5)
+    out = eng.default_engine().solve(batch, qex_gb300.LDAExpCoulomb(), cfg,
+                                     records=("energy", "final_density"))
+    te = out["energy"][:, -1].cpu().numpy()
+    tn = out["final_density"].cpu().numpy()
+    params, xc_fn = mlp_params(0)
+    xc = Partial(xc_fn, params=params)
+    adj = adjoint.Ks1dAdjoint()
+    res = adj.value_and_grad(batch, xc, cfg, te, tn, density_weight=0.1, checkpoint_every=5)
+    times = []
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = adj.value_and_grad(batch, xc, cfg, te, tn, density_weight=0.1, checkpoint_every=5)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    t = sorted(times)[len(times) // 2]
+    return {"workload": f"loss and gradient, {B} H2-type molecules, 513 points, window MLP (FP32), "
+                        f"{T} iterations, checkpoints every 5, loss sum (E-E_t)^2 + "
+                        "0.1 sum |n-n_t|^2 dx", "s_per_step": t,
+            "molecule_gradients_per_s": B / t, "loss": float(res.loss),
+            "grad_norm": float(np.linalg.norm(res.grad))}
+
+
+def td_flops(G, n, naux, nocc, hidden=None):
+    """Algorithmic work of one 3D SCF cycle (per the 3D roofline of the
+    measurement plan): FP64 GEMM-shaped work 4 G n^2 (rho and Vxc) +
+    4 naux n^2 (J) + 4 n^3 (DIIS error) + 2 n^2 k (rdm1), the eigensolve
+    2 n^3 + 4/3 n^3 + 4 n^2 (k + 1); FP32 network work 4 G H + 4 H^2 for a
+    global [H, H, 1] network (forward and backward)."""
+    w64 = 4.0 * G * n * n + 4.0 * naux * n * n + 4.0 * n ** 3 + 2.0 * n * n * nocc
+    w64 += 2.0 * n ** 3 + 4.0 / 3.0 * n ** 3 + 4.0 * n * n * (nocc + 1)
+    w32 = 0.0 if hidden is None else 4.0 * G * hidden + 4.0 * hidden * hidden
+    return w64, w32
+
+
+def run_td(args, peak64, peak32, cycles=30):
+    """The 3D configuration at its shapes: synthetic molecules of 8 (s/p basis),
+    14 and 20 atoms (s/p/d), Gaussian-cloud grids of 1240, ~42k and 200k points
+    with positive random weights, analytic one-electron integrals and
+    density-fitted Coulomb factors built on the GPU; LDA exchange and the global
+    neural functional [512, 512, 1]; DIIS depth 8, 30 cycles, the reference's
+    stop rule latched on the device; each SCF captured as one CUDA graph and
+    replayed.  Beside it the oracle (NumPy FP64) on the host: the full SCF of the
+    smallest molecule, two cycles of the others (scaled to 30)."""
+    import torch
+
+    from oracle import td as otd
+    from qex_gb300.td import graph, numint, workloads
+
+    cases = ((8, "sp", 155), (14, "spd", 3000), (20, "spd", 10000))
+    out = {"workload": "3D numint SCF, synthetic H/C/N/O molecules, analytic integrals and "
+                       "density-fitted J on the GPU, DIIS 8, 30 cycles (CUDA graph)"}
+    cpu_total = 0.0
+    for na, basis, ppa in cases:
+        dev, mol = workloads.device_molecule(na, seed=100 + na, points_per_atom=ppa, basis=basis)
+        G, n = dev.weights.numel(), dev.nao
+        naux = int(dev.eri_factors.shape[0])
+        nocc = dev.nelectron // 2
+        row = {"atoms": na, "basis": basis, "nao": n, "grid_points": G, "naux": naux}
+        for label, xc in (("lda", "LDA"),
+                          ("global_mlp_512", numint.NeuralXC(
+                              numint.NeuralXC.init(hidden=512, seed=1, inputs=G), scale=1e-2))):
+            cap = graph.CapturedScf(dev, max_cycle=cycles, xc=xc)
+            stream = torch.cuda.current_stream()
+            times = []
+            for _ in range(max(3, args.steps)):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                res = cap.replay()
+                e1.record(stream)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1) / 1e3)
+            t = sorted(times)[len(times) // 2]
+            st = res.converged.cpu().numpy()
+            w64, w32 = td_flops(G, n, naux, nocc, 512 if label != "lda" else None)
+            bound = cycles * (w64 / (peak64 * 1e12) + (w32 / (peak32 * 1e12) if peak32 else 0.0))
+            row[label] = {"ms_per_solve": t * 1e3, "solves_per_s": 1.0 / t,
+                          "converged": bool(st[0]), "converged_cycle": int(st[1]) + 1,
+                          "e_tot": float(res.e_tot.cpu()[0]),
+                          "roofline": {"bound": "fp64 (+fp32 network)", "frac": bound / t,
+                                       "fp64_flops_per_cycle": w64, "fp32_flops_per_cycle": w32}}
+            del cap
+            torch.cuda.empty_cache()
+        # oracle on the host: the LDA SCF
+        hm = workloads.Molecule3D(charges=mol.charges, positions=mol.positions, shells=mol.shells,
+                                  coords=mol.coords, weights=mol.weights,
+                                  nelectron=mol.nelectron)
+        hm.ao = dev.ao.cpu().numpy()
+        hm.s1e = dev.s1e.cpu().numpy()
+        hm.h1e = dev.h1e.cpu().numpy()
+        hm.eri_factors = dev.eri_factors.cpu().numpy()
+        hm.energy_nuc = dev.energy_nuc
+        k = cycles if na == cases[0][0] else 2
+        t0 = time.perf_counter()
+        e_ref = otd.scf(hm, max_cycle=k)[0]
+        dt = (time.perf_counter() - t0) * cycles / k
+        cpu_total += dt
+        row["cpu_baseline"] = {"s_per_solve": dt, "cores": host_cores(), "kind": "port",
+                               "sample": f"{k} cycles of the oracle's LDA SCF"
+                                         + ("" if k == cycles else f", scaled to {cycles}")}
+        if k == cycles:
+            row["lda"]["parity_vs_oracle_e_tot_fixed_cycles"] = float(
+                abs(e_ref[-1] - float(graph_last_energy(dev, cycles))))
+        out[f"atoms_{na}_{basis}"] = row
+        del dev
+        torch.cuda.empty_cache()
+    return out
+
+
+def graph_last_energy(dev, cycles):
+    """Energy of the last cycle of a host-launched LDA SCF (no stop rule)."""
+    from qex_gb300.td import scf
+
+    return scf.run_scf(dev, cycles).energies[-1].cpu()
+
+
 def run_eigh_eval(args):
     """Generalized eigensolves F C = S C e (batch 1) at the basis sizes of the
     3D configuration: core Hamiltonian and overlap from the analytic
@@ -685,6 +821,8 @@ def run_ours(args, rank, world):
     serving = None
     if world == 1 and not args.no_serving:
         serving = run_serving(args)
+    config3 = run_config3(args) if world == 1 and not args.no_ksr else None
+    td = run_td(args, peak64, peak32) if world == 1 and not args.no_td else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
@@ -720,6 +858,10 @@ def run_ours(args, rank, world):
         line["ksr"] = ksr
     if serving is not None:
         line["serving"] = serving
+    if config3 is not None:
+        line["differentiation"] = config3
+    if td is not None:
+        line["numint_3d"] = td
     return line
 
 
@@ -786,6 +928,65 @@ def run_serving_mix(args, xc, cfg):
     return out
 
 
+def run_serve_eval(args):
+    """The serving configuration as specified: Poisson streams of
+    ``--serve-seconds`` (default 60 s) at each rate of ``--serve-rates``
+    (default 100 ... 5000 req/s) mixing 80% plain-configuration 1D solves and
+    20% 3D solves over a population of 64 synthetic molecules of nao 4-117
+    (s/p basis), each arriving as a new molecule the first time (grid, AO
+    values, analytic integrals and density fitting on the GPU, then the
+    captured SCF graph: inside that request's latency); admission by free HBM.
+    Then the saturated capacity of the served and the plain forms for 1D
+    requests (all arrivals at t = 0)."""
+    import qex_gb300
+    from qex_gb300 import serving as sv
+    from qex_gb300.od import engine as eng
+    from qex_gb300.td import workloads
+
+    cfg = eng.SolveConfig(num_iterations=20, alpha=0.5, alpha_decay=0.9, num_mixing_iterations=1,
+                          convention="local", stencil=3)
+    xc = qex_gb300.LDAExpCoulomb()
+    rng = np.random.default_rng(5)
+    keys = [(int(rng.integers(2, 14)), 1000 + i) for i in range(64)]
+
+    def build(key):
+        return workloads.device_molecule(key[0], seed=key[1], points_per_atom=620)[0]
+
+    out = {"workload": "Poisson mix, 80% 1D (513 points, H2-like, exp-Coulomb LDA, 3-point "
+                       "kinetic, 20 iterations), 20% 3D SCF (LDA, DIIS 8, 30 cycles, stop rule) "
+                       "over 64 molecules of 2-13 atoms, new molecules built inside the "
+                       "request's latency; admission by free HBM",
+           "seconds": args.serve_seconds}
+    server = sv.ScfServer(xc, cfg, max_inflight=16, max_batch=1024, builder3d=build)
+    server.serve(sv.mixed_requests(sv.poisson_arrivals(200, 0.2, seed=1), keys[:2], 0.5, seed=1))
+    for rate in args.serve_rates:
+        arr = sv.poisson_arrivals(rate, args.serve_seconds, seed=int(rate) + 11)
+        reqs = sv.mixed_requests(arr, keys, frac3d=0.2, seed=int(rate) + 11)
+        server = sv.ScfServer(xc, cfg, max_inflight=16, max_batch=1024, builder3d=build)
+        done = server.serve(reqs)
+        s = sv.latency_summary(done)
+        s["launches"] = server.launches
+        s["molecules_built"] = server.built3d
+        out[f"served_rate_{int(rate)}"] = s
+        del server
+    # saturated capacity, 1D
+    n_cap = 20000
+    reqs = sv.config1_requests(np.zeros(n_cap), seed=3)
+    server = sv.ScfServer(xc, cfg, max_inflight=16, max_batch=1024)
+    t0 = time.perf_counter()
+    server.serve(reqs)
+    dt = time.perf_counter() - t0
+    out["served_capacity_1d"] = {"requests": n_cap, "s": dt, "solves_per_s": n_cap / dt}
+    n_plain = 300
+    reqs = sv.config1_requests(np.zeros(n_plain), seed=4)
+    t0 = time.perf_counter()
+    sv.serve_plain(xc, cfg, reqs)
+    dt = time.perf_counter() - t0
+    out["plain_capacity_1d"] = {"requests": n_plain, "s": dt, "solves_per_s": n_plain / dt}
+    out["capacity_ratio_1d"] = out["served_capacity_1d"]["solves_per_s"] / (n_plain / dt)
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
@@ -831,6 +1032,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-ksr", action="store_true")
+    ap.add_argument("--no-td", action="store_true", help="skip the 3D configuration")
+    ap.add_argument("--td-only", action="store_true", help="time only the 3D configuration")
     ap.add_argument("--ksr-only", action="store_true",
                     help="time only the KSR SCF workload (profiling)")
     ap.add_argument("--ksr-eval", action="store_true",
@@ -845,6 +1048,11 @@ def main():
                     help="time the 3D generalized eigensolver at the configuration's basis sizes")
     ap.add_argument("--ints-eval", action="store_true",
                     help="time only the analytic integrals and density fitting")
+    ap.add_argument("--serve-eval", action="store_true",
+                    help="the serving configuration as specified (60 s streams per rate)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-rates", type=float, nargs="*",
+                    default=[100.0, 200.0, 500.0, 1000.0, 2000.0, 5000.0])
     ap.add_argument("--serving-rates", type=float, nargs="*", default=[1000.0, 5000.0])
     ap.add_argument("--serving-seconds", type=float, default=1.0)
     ap.add_argument("--mix-rates", type=float, nargs="*", default=[100.0, 200.0])
@@ -858,6 +1066,19 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         torch.distributed.init_process_group("nccl")
+    if args.serve_eval:
+        from qex_gb300 import _native
+
+        _native.load()
+        print(json.dumps({"serve_eval": run_serve_eval(args)}), flush=True)
+        return
+    if args.td_only:
+        from qex_gb300 import _native
+
+        _native.load()
+        peak64, peak32 = _native.measure_fma_peak()
+        print(json.dumps({"numint_3d": run_td(args, peak64, peak32)}), flush=True)
+        return
     if args.eigh_eval:
         from qex_gb300 import _native
 

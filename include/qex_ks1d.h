@@ -134,6 +134,12 @@ typedef struct qex_xc_spec {
   int32_t nn_activation;            /* enum qex_nn_activation */
   int32_t nn_inputs;                /* 1 (local) or the grid size (global) */
   int32_t nn_flags;                 /* QEX_NN_SELF_INTERACTION | QEX_NN_NEGATIVITY */
+  /* QEX_XC_WINDOW_MLP only: a DEVICE pointer to the same QEX_MLP_NUM_PARAMS
+   * parameters in FP64 (16-byte aligned), or NULL.  Given, the network runs in
+   * FP64 in the SCF and in the adjoint step: a checking mode in which the
+   * adjoint's gradient can be compared with finite differences without the
+   * FP32 network's rounding.  mlp_params_host must still be given. */
+  const double* mlp_params64;
 } qex_xc_spec;
 
 typedef struct qex_ks1d_options {

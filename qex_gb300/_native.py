@@ -73,6 +73,7 @@ class XcSpec(ctypes.Structure):
         ("nn_activation", ctypes.c_int32),
         ("nn_inputs", ctypes.c_int32),
         ("nn_flags", ctypes.c_int32),
+        ("mlp_params64", _c_p),
     ]
 
 

@@ -28,6 +28,7 @@
 #include <string.h>
 
 #include <mutex>
+#include <type_traits>
 
 #include "ks1d_common.cuh"
 #include "ksr_device.cuh"
@@ -110,6 +111,10 @@ struct Params {
   int planes;             // qex_ks1d_options.solve_planes
   int* counter;
   MlpParams mlp;
+  // window MLP in FP64 (a checking mode): 577 doubles in global memory, and
+  // 1 / normalization in FP64; null: the FP32 network of `mlp`
+  const double* mlp_w64;
+  double mlp_norm_inv64;
   // dense networks (QEX_XC_LOCAL_MLP / GLOBAL_MLP): the network, its shared
   // FP32 floats per warp and 4 nmax-double scratch vectors per slot
   NnNet nn;
@@ -390,6 +395,78 @@ __device__ __noinline__ double nn_xc(const Params& p, int N, double dx, const Sm
                                      bool want_v, double* vout, double* frec, bool reflect_xc,
                                      double* nnws, int lane);
 
+// Window MLP on the density staged in sm.s64a: the network input n / norm
+// with 8 zeros either side and the v_xc accumulator (one window offset at a
+// time: distinct addresses per lane, so no atomics are needed) in the FP32
+// area, in the network's arithmetic T.  Returns this lane's share of
+// sum f n (local) or sum f (amplitude); vout gets v_xc, frec the values.
+template <typename T>
+__device__ inline double mlp_xc(const Params& p, const T* W, T ninv, int N, double dx,
+                                const Smem& sm, bool want_v, double* vout, double* frec,
+                                int lane) {
+  const double* n = sm.s64a + kPad64;
+  const bool local = (p.xc_conv == QEX_XC_LOCAL);
+  double e = 0.0;
+  T* n32 = reinterpret_cast<T*>(sm.f32);
+  T* vacc = n32 + (p.nmax + 2 * kPadMlp);
+  #pragma unroll 1
+  for (int i = lane; i < N + 2 * kPadMlp; i += kWarp) {
+    int k = i - kPadMlp;
+    n32[i] = (k >= 0 && k < N) ? (T)n[k] * ninv : T(0);
+    vacc[i] = T(0);
+  }
+  __syncwarp();
+  T* scr = vacc + (p.nmax + 2 * kPadMlp) + lane;  // per-lane MLP scratch, stride 32
+  const int rounds = (N + kWarp - 1) / kWarp;
+  for (int r = 0; r < rounds; ++r) {
+    const int i = r * kWarp + lane;
+    const bool act = i < N;
+    // inactive lanes evaluate a harmless all-zero window
+    const T* win = act ? (n32 + i) : (n32 + N + kPadMlp);
+    T f;
+    if (want_v) {
+      f = mlp_point<true>(W, win, act ? 1 : 0, scr, kWarp);
+    } else {
+      f = mlp_point<false>(W, win, act ? 1 : 0, scr, kWarp);
+    }
+    double ni = act ? n[i] : 0.0;
+    if (act) {
+      if (local) {
+        e = fma((double)f, ni, e);
+      } else {
+        e += (double)f;
+      }
+      if (frec) frec[i] = (double)f;
+    }
+    if (want_v) {
+      const T up = local ? (T)ni * ninv : ninv;
+      __syncwarp();
+      for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
+        if (act) vacc[i + k] += up * scr[k * kWarp];
+        __syncwarp();
+      }
+      if (act && local) vacc[i + kPadMlp] += f;
+      __syncwarp();
+    }
+  }
+  if (want_v) {
+    #pragma unroll 1
+    for (int i = lane; i < N; i += kWarp) {
+      double v = (double)vacc[i + kPadMlp];
+      vout[i] = local ? v : dx * v;
+    }
+  }
+  return e;
+}
+
+// The FP64 network (checking mode), out of line: its registers stay off the
+// FP32 path's.
+__device__ __noinline__ double mlp_xc64(const Params& p, int N, double dx, const Smem& sm,
+                                        bool want_v, double* vout, double* frec, int lane) {
+  return mlp_xc<double>(p, p.mlp_w64, p.mlp_norm_inv64, N, dx, sm, want_v, vout, frec, lane);
+}
+
+
 __device__ __noinline__ double xc_eval(const Params& p, int N, double dx, const Smem& sm, bool want_v,
                           double* vout, double* frec, bool reflect_xc, int lane,
                           double* nnws = nullptr) {
@@ -433,59 +510,8 @@ __device__ __noinline__ double xc_eval(const Params& p, int N, double dx, const 
       if (frec) frec[i] = f;
     }
   } else {
-    // Window MLP: stage n / norm as FP32 with 8 zeros either side; v_xc
-    // contributions are accumulated in FP32 shared memory, one window offset
-    // at a time (distinct addresses per lane, so no atomics are needed).
-    float* n32 = sm.f32;
-    float* vacc = sm.f32 + (p.nmax + 2 * kPadMlp);
-    const float ninv = p.mlp.norm_inv;
-    #pragma unroll 1
-    for (int i = lane; i < N + 2 * kPadMlp; i += kWarp) {
-      int k = i - kPadMlp;
-      n32[i] = (k >= 0 && k < N) ? (float)n[k] * ninv : 0.0f;
-      vacc[i] = 0.0f;
-    }
-    __syncwarp();
-    float* scr = vacc + (p.nmax + 2 * kPadMlp) + lane;  // per-lane MLP scratch, stride 32
-    const int rounds = (N + kWarp - 1) / kWarp;
-    for (int r = 0; r < rounds; ++r) {
-      const int i = r * kWarp + lane;
-      const bool act = i < N;
-      // inactive lanes evaluate a harmless all-zero window
-      const float* win = act ? (n32 + i) : (n32 + N + kPadMlp);
-      float f;
-      if (want_v) {
-        f = mlp_point<true>(sm.mlpw, win, act ? 1 : 0, scr, kWarp);
-      } else {
-        f = mlp_point<false>(sm.mlpw, win, act ? 1 : 0, scr, kWarp);
-      }
-      double ni = act ? n[i] : 0.0;
-      if (act) {
-        if (local) {
-          e = fma((double)f, ni, e);
-        } else {
-          e += (double)f;
-        }
-        if (frec) frec[i] = (double)f;
-      }
-      if (want_v) {
-        const float up = local ? (float)ni * ninv : ninv;
-        __syncwarp();
-        for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
-          if (act) vacc[i + k] += up * scr[k * kWarp];
-          __syncwarp();
-        }
-        if (act && local) vacc[i + kPadMlp] += f;
-        __syncwarp();
-      }
-    }
-    if (want_v) {
-      #pragma unroll 1
-      for (int i = lane; i < N; i += kWarp) {
-        double v = (double)vacc[i + kPadMlp];
-        vout[i] = local ? v : dx * v;
-      }
-    }
+    e = p.mlp_w64 ? mlp_xc64(p, N, dx, sm, want_v, vout, frec, lane)
+                  : mlp_xc<float>(p, sm.mlpw, p.mlp.norm_inv, N, dx, sm, want_v, vout, frec, lane);
   }
   __syncwarp();
   if (reflect_xc) {
@@ -1937,26 +1963,25 @@ __device__ int sternheimer(const Params& p, int N, double dx, int ne, const doub
 //   n32 / u32: padded FP32 windows (density / norm, direction / norm)
 //   ybar_i = ya[i] * yscale, dybar_i = with_tangent ? n[i] : 0
 //   xbar scattered into gacc (FP32, padded), dy added to gn (FP64) if with_tangent.
-__device__ void mlp_adjoint_pass(const Params& p, int N, const float* n32, const float* u32,
+template <typename T>
+__device__ void mlp_adjoint_pass(const T* W, T ninv, int N, const T* n32, const T* u32,
                                  bool with_tangent, const double* ya, double yscale,
-                                 const double* nvec, float* gacc, double* gn, float* rec,
-                                 const Smem& sm, double* acc, int lane) {
-  const float ninv = p.mlp.norm_inv;
+                                 const double* nvec, T* gacc, double* gn, T* rec, double* acc,
+                                 int lane) {
   const int rounds = (N + kWarp - 1) / kWarp;
-  const float* zero_win = n32 + N + kPadMlp;  // 8+ zeros
+  const T* zero_win = n32 + N + kPadMlp;  // 8+ zeros
   for (int r = 0; r < rounds; ++r) {
     const int i = r * kWarp + lane;
     const bool act = i < N;
-    const float* win = act ? (n32 + i) : zero_win;
-    const float* twin = (act && with_tangent) ? (u32 + i) : zero_win;
+    const T* win = act ? (n32 + i) : zero_win;
+    const T* twin = (act && with_tangent) ? (u32 + i) : zero_win;
     // inactive lanes (and the tangent of a pass without one) read a single
     // zero element with stride 0
     const int stride = act ? 1 : 0;
     const int tstride = (act && with_tangent) ? 1 : 0;
-    const float ybar = act ? (float)(ya[i] * yscale) : 0.0f;
-    const float dybar = (act && with_tangent) ? (float)nvec[i] : 0.0f;
-    const float dy = mlp_dual_reverse(sm.mlpw, win, stride, twin, tstride, ybar, dybar,
-                                      rec + lane, kWarp);
+    const T ybar = act ? (T)(ya[i] * yscale) : T(0);
+    const T dybar = (act && with_tangent) ? (T)nvec[i] : T(0);
+    const T dy = mlp_dual_reverse(W, win, stride, twin, tstride, ybar, dybar, rec + lane, kWarp);
     __syncwarp();
     mlp_param_grad_round(rec, lane, acc);
     for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
@@ -1968,11 +1993,12 @@ __device__ void mlp_adjoint_pass(const Params& p, int N, const float* n32, const
   }
 }
 
-template <int kBand>
+template <int kBand, bool kNet64>
 __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_constant__ Params p) {
+  using T = typename std::conditional<kNet64, double, float>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x;
-  const SmemLayout L = smem_layout(p.nmax, p.kmax, true);
+  const SmemLayout L = smem_layout(p.nmax, p.kmax, true, false, p.nn_floats);
   Smem sm = carve(smem_raw, L);
   stage_mlp_weights(p.mlp, sm.mlpw, lane, kWarp);
   __syncwarp();
@@ -2049,10 +2075,19 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
     density_from_orbitals(p, N, dx, ne, K, X, nout, sm, tee, gap, lane);
     const double gE = p.a_genergy ? p.a_genergy[b] : 0.0;
     const double at = p.a_alpha;
-    float* n32 = sm.f32;
-    float* u32 = n32 + (p.nmax + 2 * kPadMlp);
-    float* gacc = u32 + (p.nmax + 2 * kPadMlp);
-    float* rec = gacc + (p.nmax + 2 * kPadMlp);
+    T* n32 = reinterpret_cast<T*>(sm.f32);
+    T* u32 = n32 + (p.nmax + 2 * kPadMlp);
+    T* gacc = u32 + (p.nmax + 2 * kPadMlp);
+    T* rec = gacc + (p.nmax + 2 * kPadMlp);
+    const T* W;
+    T ninv;
+    if constexpr (kNet64) {
+      W = p.mlp_w64;
+      ninv = p.mlp_norm_inv64;
+    } else {
+      W = sm.mlpw;
+      ninv = p.mlp.norm_inv;
+    }
     double acc[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) acc[q] = 0.0;
@@ -2087,16 +2122,15 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
         __syncwarp();
         sm_out = t1;
       }
-      const float ninv = p.mlp.norm_inv;
       #pragma unroll 1
       for (int i = lane; i < N + 2 * kPadMlp; i += kWarp) {
         const int k = i - kPadMlp;
-        n32[i] = (k >= 0 && k < N) ? (float)sm_out[k] * ninv : 0.0f;
-        gacc[i] = 0.0f;
+        n32[i] = (k >= 0 && k < N) ? (T)sm_out[k] * ninv : T(0);
+        gacc[i] = T(0);
       }
       __syncwarp();
       // ybar_i = gE dx s_i (local convention E_xc = dx sum eps_i s_i); no tangent
-      mlp_adjoint_pass(p, N, n32, n32, false, sm_out, gE * dx, sm_out, gacc, gn, rec, sm, acc,
+      mlp_adjoint_pass(W, ninv, N, n32, n32, false, sm_out, gE * dx, sm_out, gacc, gn, rec, acc,
                        lane);
     }
     // ---- gv = chi gm
@@ -2124,17 +2158,16 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
         uv = vxc;
         xg = t2;
       }
-      const float ninv = p.mlp.norm_inv;
       #pragma unroll 1
       for (int i = lane; i < N + 2 * kPadMlp; i += kWarp) {
         const int k = i - kPadMlp;
-        n32[i] = (k >= 0 && k < N) ? (float)sv[k] * ninv : 0.0f;
-        u32[i] = (k >= 0 && k < N) ? (float)uv[k] * ninv : 0.0f;
-        gacc[i] = 0.0f;
+        n32[i] = (k >= 0 && k < N) ? (T)sv[k] * ninv : T(0);
+        u32[i] = (k >= 0 && k < N) ? (T)uv[k] * ninv : T(0);
+        gacc[i] = T(0);
       }
       __syncwarp();
       // local convention: v_xc(n) . u = sum_i [eps_i u_i + n_i D eps_i[u window]]
-      mlp_adjoint_pass(p, N, n32, u32, true, uv, 1.0, sv, gacc, xg, rec, sm, acc, lane);
+      mlp_adjoint_pass(W, ninv, N, n32, u32, true, uv, 1.0, sv, gacc, xg, rec, acc, lane);
       #pragma unroll 1
       for (int i = lane; i < N; i += kWarp) xg[i] += (double)gacc[i + kPadMlp];
       __syncwarp();
@@ -2246,6 +2279,13 @@ int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_opt
   if (xc->convention != QEX_XC_AMPLITUDE && xc->convention != QEX_XC_LOCAL) return QEX_BAD_ARG;
   if (xc->kind == QEX_XC_WINDOW_MLP) {
     if (!fill_mlp_params(P.mlp, xc)) return QEX_BAD_ARG;
+    if (xc->mlp_params64) {
+      if (reinterpret_cast<uintptr_t>(xc->mlp_params64) % 16 != 0) return QEX_BAD_ARG;
+      P.mlp_w64 = xc->mlp_params64;
+      P.mlp_norm_inv64 = 1.0 / xc->normalization;
+      // the FP64 windows, accumulator and per-lane scratch in the FP32 area
+      P.nn_floats = 2 * (2 * (o->max_num_grids + 2 * kPadMlp) + kMlpScratch * kWarp);
+    }
   }
   if (is_nn_kind(xc->kind)) {
     rc = fill_nn(P.nn, xc);
@@ -2339,10 +2379,28 @@ __global__ void __launch_bounds__(kWarp) ksr_energy_kernel(const __grid_constant
   }
 }
 
+template <int kBand, bool kNet64>
+int launch_adjoint_variant(const Params& P, cudaStream_t stream, size_t smem, int sms) {
+  auto fn = ks1d_adjoint_kernel<kBand, kNet64>;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return QEX_CUDA_ERROR;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kWarp, smem);
+  if (per_sm < 1) per_sm = 1;
+  long long grid = (long long)sms * per_sm;
+  if (grid > P.num_molecules) grid = P.num_molecules;
+  if (cudaMemsetAsync(P.counter, 0, sizeof(int), stream) != cudaSuccess) return QEX_CUDA_ERROR;
+  fn<<<(unsigned)grid, kWarp, smem, stream>>>(P);
+  if (cudaGetLastError() != cudaSuccess) return QEX_CUDA_ERROR;
+  g_last_launches = 1;
+  return QEX_OK;
+}
+
 int launch_adjoint(const Params& P, cudaStream_t stream) {
   g_last_launches = 0;
   if (P.num_molecules == 0) return QEX_OK;
-  const SmemLayout L = smem_layout(P.nmax, P.kmax, true);
+  const SmemLayout L = smem_layout(P.nmax, P.kmax, true, false, P.nn_floats);
   const size_t smem = L.total;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return QEX_CUDA_ERROR;
@@ -2350,32 +2408,12 @@ int launch_adjoint(const Params& P, cudaStream_t stream) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if ((int)smem > max_optin) return QEX_BAD_ARG;
-  cudaError_t e;
-  int per_sm = 0;
-  if (P.stencil == 5) {
-    e = cudaFuncSetAttribute(ks1d_adjoint_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return QEX_CUDA_ERROR;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks1d_adjoint_kernel<2>, kWarp, smem);
-  } else {
-    e = cudaFuncSetAttribute(ks1d_adjoint_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return QEX_CUDA_ERROR;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks1d_adjoint_kernel<1>, kWarp, smem);
-  }
-  if (per_sm < 1) per_sm = 1;
-  long long grid = (long long)sms * per_sm;
-  if (grid > P.num_molecules) grid = P.num_molecules;
-  e = cudaMemsetAsync(P.counter, 0, sizeof(int), stream);
-  if (e != cudaSuccess) return QEX_CUDA_ERROR;
-  if (P.stencil == 5) {
-    ks1d_adjoint_kernel<2><<<(unsigned)grid, kWarp, smem, stream>>>(P);
-  } else {
-    ks1d_adjoint_kernel<1><<<(unsigned)grid, kWarp, smem, stream>>>(P);
-  }
-  if (cudaGetLastError() != cudaSuccess) return QEX_CUDA_ERROR;
-  g_last_launches = 1;
-  return QEX_OK;
+  const bool net64 = P.mlp_w64 != nullptr;
+  if (P.stencil == 5)
+    return net64 ? launch_adjoint_variant<2, true>(P, stream, smem, sms)
+                 : launch_adjoint_variant<2, false>(P, stream, smem, sms);
+  return net64 ? launch_adjoint_variant<1, true>(P, stream, smem, sms)
+               : launch_adjoint_variant<1, false>(P, stream, smem, sms);
 }
 
 template <int kBand, bool kRes, bool kKsr>
@@ -2613,6 +2651,8 @@ int qex_ks1d_adjoint_step(const qex_ks1d_batch* batch, const qex_ks1d_options* o
                         batch->num_molecules);
   if (rc) return rc;
   P.stride = qex::stride_doubles(&o, true);
+  if (P.mlp_w64)  // FP64 windows and per-lane records of the adjoint's MLP passes
+    P.nn_floats = 2 * (3 * (o.max_num_grids + 2 * qex::kPadMlp) + qex::kMlpRec * qex::kWarp);
   P.dens_in = density_in;
   P.a_gnext = grad_density_next;
   P.a_genergy = grad_energy;

@@ -89,9 +89,19 @@ __device__ inline void lda_exp_coulomb(double n, const LdaConsts& c, double& eps
   if (kDeriv) deps_dn = (dex + dec) * c.pik;
 }
 
-__device__ inline float silu_d(float z, float& d) {
-  float s = __fdividef(1.0f, 1.0f + __expf(-z));  // 0 when exp(-z) overflows: silu -> 0
-  d = s * (1.0f + z * (1.0f - s));
+// The window MLP runs in FP32 (the configuration's network arithmetic) or, as
+// a checking mode, in FP64 (weights then read from global memory).
+__device__ inline float mlp_fma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ inline double mlp_fma(double a, double b, double c) { return fma(a, b, c); }
+__device__ inline float mlp_sigmoid(float z) {
+  return __fdividef(1.0f, 1.0f + __expf(-z));  // 0 when exp(-z) overflows: silu -> 0
+}
+__device__ inline double mlp_sigmoid(double z) { return 1.0 / (1.0 + exp(-z)); }
+
+template <typename T>
+__device__ inline T silu_d(T z, T& d) {
+  const T s = mlp_sigmoid(z);
+  d = s * (T(1) + z * (T(1) - s));
   return z * s;
 }
 
@@ -115,28 +125,38 @@ __device__ inline void mlp_load4(const float* W, int off, float& a, float& b, fl
   d = r.w;
 }
 
-template <bool kGrad>
-__device__ inline float mlp_point(const float* W, const float* win, int wstride, float* scr,
-                                  int ss) {
-  float z[QEX_MLP_HIDDEN];
+// FP64 weights (global memory, 16-byte aligned)
+__device__ inline void mlp_load4(const double* W, int off, double& a, double& b, double& c,
+                                 double& d) {
+  const double2 r0 = __ldg(reinterpret_cast<const double2*>(W + off));
+  const double2 r1 = __ldg(reinterpret_cast<const double2*>(W + off + 2));
+  a = r0.x;
+  b = r0.y;
+  c = r1.x;
+  d = r1.y;
+}
+
+template <bool kGrad, typename T>
+__device__ inline T mlp_point(const T* W, const T* win, int wstride, T* scr, int ss) {
+  T z[QEX_MLP_HIDDEN];
 #pragma unroll
   for (int q = 0; q < 4; ++q) mlp_load4(W, 272 + 4 * q, z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
 #pragma unroll 1
   for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
-    const float x = win[k * wstride];
+    const T x = win[k * wstride];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      float a, b, c, d;
+      T a, b, c, d;
       mlp_load4(W, 16 * k + 4 * q, a, b, c, d);
-      z[4 * q] = fmaf(x, a, z[4 * q]);
-      z[4 * q + 1] = fmaf(x, b, z[4 * q + 1]);
-      z[4 * q + 2] = fmaf(x, c, z[4 * q + 2]);
-      z[4 * q + 3] = fmaf(x, d, z[4 * q + 3]);
+      z[4 * q] = mlp_fma(x, a, z[4 * q]);
+      z[4 * q + 1] = mlp_fma(x, b, z[4 * q + 1]);
+      z[4 * q + 2] = mlp_fma(x, c, z[4 * q + 2]);
+      z[4 * q + 3] = mlp_fma(x, d, z[4 * q + 3]);
     }
   }
 #pragma unroll
   for (int h = 0; h < QEX_MLP_HIDDEN; ++h) {
-    float d;
+    T d;
     scr[h * ss] = silu_d(z[h], d);  // h1
     scr[(16 + h) * ss] = d;         // d1
   }
@@ -144,60 +164,60 @@ __device__ inline float mlp_point(const float* W, const float* win, int wstride,
   for (int q = 0; q < 4; ++q) mlp_load4(W, 544 + 4 * q, z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
 #pragma unroll 1
   for (int k = 0; k < QEX_MLP_HIDDEN; ++k) {
-    const float x = scr[k * ss];
+    const T x = scr[k * ss];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      float a, b, c, d;
+      T a, b, c, d;
       mlp_load4(W, 288 + 16 * k + 4 * q, a, b, c, d);
-      z[4 * q] = fmaf(x, a, z[4 * q]);
-      z[4 * q + 1] = fmaf(x, b, z[4 * q + 1]);
-      z[4 * q + 2] = fmaf(x, c, z[4 * q + 2]);
-      z[4 * q + 3] = fmaf(x, d, z[4 * q + 3]);
+      z[4 * q] = mlp_fma(x, a, z[4 * q]);
+      z[4 * q + 1] = mlp_fma(x, b, z[4 * q + 1]);
+      z[4 * q + 2] = mlp_fma(x, c, z[4 * q + 2]);
+      z[4 * q + 3] = mlp_fma(x, d, z[4 * q + 3]);
     }
   }
-  float out = W[576];
-  float g2[QEX_MLP_HIDDEN];
+  T out = W[576];
+  T g2[QEX_MLP_HIDDEN];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    float w3[4];
+    T w3[4];
     mlp_load4(W, 560 + 4 * q, w3[0], w3[1], w3[2], w3[3]);
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      float d;
-      float a = silu_d(z[4 * q + e], d);
-      out = fmaf(a, w3[e], out);
+      T d;
+      T a = silu_d(z[4 * q + e], d);
+      out = mlp_fma(a, w3[e], out);
       g2[4 * q + e] = w3[e] * d;
     }
   }
   if (kGrad) {
 #pragma unroll 1
     for (int k = 0; k < QEX_MLP_HIDDEN; ++k) {
-      float a = 0.0f;
+      T a = T(0);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        float r0, r1, r2, r3;
+        T r0, r1, r2, r3;
         mlp_load4(W, 288 + 16 * k + 4 * q, r0, r1, r2, r3);
-        a = fmaf(r0, g2[4 * q], a);
-        a = fmaf(r1, g2[4 * q + 1], a);
-        a = fmaf(r2, g2[4 * q + 2], a);
-        a = fmaf(r3, g2[4 * q + 3], a);
+        a = mlp_fma(r0, g2[4 * q], a);
+        a = mlp_fma(r1, g2[4 * q + 1], a);
+        a = mlp_fma(r2, g2[4 * q + 2], a);
+        a = mlp_fma(r3, g2[4 * q + 3], a);
       }
       scr[(16 + k) * ss] = a * scr[(16 + k) * ss];  // g1 = (W2 g2) * d1, over d1
     }
-    float g1[QEX_MLP_HIDDEN];
+    T g1[QEX_MLP_HIDDEN];
 #pragma unroll
     for (int h = 0; h < QEX_MLP_HIDDEN; ++h) g1[h] = scr[(16 + h) * ss];
 #pragma unroll 1
     for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
-      float a = 0.0f;
+      T a = T(0);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        float r0, r1, r2, r3;
+        T r0, r1, r2, r3;
         mlp_load4(W, 16 * k + 4 * q, r0, r1, r2, r3);
-        a = fmaf(r0, g1[4 * q], a);
-        a = fmaf(r1, g1[4 * q + 1], a);
-        a = fmaf(r2, g1[4 * q + 2], a);
-        a = fmaf(r3, g1[4 * q + 3], a);
+        a = mlp_fma(r0, g1[4 * q], a);
+        a = mlp_fma(r1, g1[4 * q + 1], a);
+        a = mlp_fma(r2, g1[4 * q + 2], a);
+        a = mlp_fma(r3, g1[4 * q + 3], a);
       }
       scr[k * ss] = a;  // h1 / d1 slots are dead here
     }
@@ -215,47 +235,48 @@ __device__ inline float mlp_point(const float* W, const float* win, int wstride,
 // Returns dy.
 constexpr int kMlpRec = 164;
 
-__device__ inline float silu_dd(float z, float& d1, float& d2) {
-  float s = __fdividef(1.0f, 1.0f + __expf(-z));  // 0 when exp(-z) overflows: silu -> 0
-  d1 = s * (1.0f + z * (1.0f - s));
-  d2 = s * (1.0f - s) * (2.0f + z * (1.0f - 2.0f * s));
+template <typename T>
+__device__ inline T silu_dd(T z, T& d1, T& d2) {
+  const T s = mlp_sigmoid(z);
+  d1 = s * (T(1) + z * (T(1) - s));
+  d2 = s * (T(1) - s) * (T(2) + z * (T(1) - T(2) * s));
   return z * s;
 }
 
-__device__ inline float mlp_dual_reverse(const float* W, const float* win, int wstride,
-                                         const float* twin, int tstride, float ybar, float dybar,
-                                         float* rec, int rs) {
-  float z[QEX_MLP_HIDDEN], dz[QEX_MLP_HIDDEN];
+template <typename T>
+__device__ inline T mlp_dual_reverse(const T* W, const T* win, int wstride, const T* twin,
+                                     int tstride, T ybar, T dybar, T* rec, int rs) {
+  T z[QEX_MLP_HIDDEN], dz[QEX_MLP_HIDDEN];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     mlp_load4(W, 272 + 4 * q, z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
-    dz[4 * q] = dz[4 * q + 1] = dz[4 * q + 2] = dz[4 * q + 3] = 0.0f;
+    dz[4 * q] = dz[4 * q + 1] = dz[4 * q + 2] = dz[4 * q + 3] = T(0);
   }
 #pragma unroll 1
   for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
-    const float x = win[k * wstride], t = twin[k * tstride];
+    const T x = win[k * wstride], t = twin[k * tstride];
     rec[k * rs] = x;
     rec[(17 + k) * rs] = t;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      float a, b, c, d;
+      T a, b, c, d;
       mlp_load4(W, 16 * k + 4 * q, a, b, c, d);
-      z[4 * q] = fmaf(x, a, z[4 * q]);
-      z[4 * q + 1] = fmaf(x, b, z[4 * q + 1]);
-      z[4 * q + 2] = fmaf(x, c, z[4 * q + 2]);
-      z[4 * q + 3] = fmaf(x, d, z[4 * q + 3]);
-      dz[4 * q] = fmaf(t, a, dz[4 * q]);
-      dz[4 * q + 1] = fmaf(t, b, dz[4 * q + 1]);
-      dz[4 * q + 2] = fmaf(t, c, dz[4 * q + 2]);
-      dz[4 * q + 3] = fmaf(t, d, dz[4 * q + 3]);
+      z[4 * q] = mlp_fma(x, a, z[4 * q]);
+      z[4 * q + 1] = mlp_fma(x, b, z[4 * q + 1]);
+      z[4 * q + 2] = mlp_fma(x, c, z[4 * q + 2]);
+      z[4 * q + 3] = mlp_fma(x, d, z[4 * q + 3]);
+      dz[4 * q] = mlp_fma(t, a, dz[4 * q]);
+      dz[4 * q + 1] = mlp_fma(t, b, dz[4 * q + 1]);
+      dz[4 * q + 2] = mlp_fma(t, c, dz[4 * q + 2]);
+      dz[4 * q + 3] = mlp_fma(t, d, dz[4 * q + 3]);
     }
   }
   // layer 1 activations: h1, dh1 to records; keep s1', s1'' * dz1 for the reverse
-  float s1p[QEX_MLP_HIDDEN], s1q[QEX_MLP_HIDDEN];
+  T s1p[QEX_MLP_HIDDEN], s1q[QEX_MLP_HIDDEN];
 #pragma unroll
   for (int h = 0; h < QEX_MLP_HIDDEN; ++h) {
-    float d1, d2;
-    const float a = silu_dd(z[h], d1, d2);
+    T d1, d2;
+    const T a = silu_dd(z[h], d1, d2);
     rec[(66 + h) * rs] = a;
     rec[(82 + h) * rs] = d1 * dz[h];
     s1p[h] = d1;
@@ -264,41 +285,41 @@ __device__ inline float mlp_dual_reverse(const float* W, const float* win, int w
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     mlp_load4(W, 544 + 4 * q, z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
-    dz[4 * q] = dz[4 * q + 1] = dz[4 * q + 2] = dz[4 * q + 3] = 0.0f;
+    dz[4 * q] = dz[4 * q + 1] = dz[4 * q + 2] = dz[4 * q + 3] = T(0);
   }
 #pragma unroll 1
   for (int k = 0; k < QEX_MLP_HIDDEN; ++k) {
-    const float x = rec[(66 + k) * rs], t = rec[(82 + k) * rs];
+    const T x = rec[(66 + k) * rs], t = rec[(82 + k) * rs];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      float a, b, c, d;
+      T a, b, c, d;
       mlp_load4(W, 288 + 16 * k + 4 * q, a, b, c, d);
-      z[4 * q] = fmaf(x, a, z[4 * q]);
-      z[4 * q + 1] = fmaf(x, b, z[4 * q + 1]);
-      z[4 * q + 2] = fmaf(x, c, z[4 * q + 2]);
-      z[4 * q + 3] = fmaf(x, d, z[4 * q + 3]);
-      dz[4 * q] = fmaf(t, a, dz[4 * q]);
-      dz[4 * q + 1] = fmaf(t, b, dz[4 * q + 1]);
-      dz[4 * q + 2] = fmaf(t, c, dz[4 * q + 2]);
-      dz[4 * q + 3] = fmaf(t, d, dz[4 * q + 3]);
+      z[4 * q] = mlp_fma(x, a, z[4 * q]);
+      z[4 * q + 1] = mlp_fma(x, b, z[4 * q + 1]);
+      z[4 * q + 2] = mlp_fma(x, c, z[4 * q + 2]);
+      z[4 * q + 3] = mlp_fma(x, d, z[4 * q + 3]);
+      dz[4 * q] = mlp_fma(t, a, dz[4 * q]);
+      dz[4 * q + 1] = mlp_fma(t, b, dz[4 * q + 1]);
+      dz[4 * q + 2] = mlp_fma(t, c, dz[4 * q + 2]);
+      dz[4 * q + 3] = mlp_fma(t, d, dz[4 * q + 3]);
     }
   }
   // layer 2, output, and the reverse of the output layer
-  float dy = 0.0f;
-  float zb2[QEX_MLP_HIDDEN], dzb2[QEX_MLP_HIDDEN];
+  T dy = T(0);
+  T zb2[QEX_MLP_HIDDEN], dzb2[QEX_MLP_HIDDEN];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    float w3[4];
+    T w3[4];
     mlp_load4(W, 560 + 4 * q, w3[0], w3[1], w3[2], w3[3]);
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const int h = 4 * q + e;
-      float d1, d2;
-      const float h2 = silu_dd(z[h], d1, d2);
-      const float dh2 = d1 * dz[h];
-      dy = fmaf(w3[e], dh2, dy);
+      T d1, d2;
+      const T h2 = silu_dd(z[h], d1, d2);
+      const T dh2 = d1 * dz[h];
+      dy = mlp_fma(w3[e], dh2, dy);
       rec[(130 + h) * rs] = ybar * h2 + dybar * dh2;  // w3bar
-      const float hb2 = ybar * w3[e], dhb2 = dybar * w3[e];
+      const T hb2 = ybar * w3[e], dhb2 = dybar * w3[e];
       zb2[h] = hb2 * d1 + dhb2 * d2 * dz[h];
       dzb2[h] = dhb2 * d1;
       rec[(98 + h) * rs] = zb2[h];
@@ -309,28 +330,28 @@ __device__ inline float mlp_dual_reverse(const float* W, const float* win, int w
   // reverse of layer 2: hbar1 = W2 zbar2, dhbar1 = W2 dzbar2
 #pragma unroll 1
   for (int k = 0; k < QEX_MLP_HIDDEN; ++k) {
-    float hb = 0.0f, dhb = 0.0f;
+    T hb = T(0), dhb = T(0);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      float r0, r1, r2, r3;
+      T r0, r1, r2, r3;
       mlp_load4(W, 288 + 16 * k + 4 * q, r0, r1, r2, r3);
-      hb = fmaf(r0, zb2[4 * q], hb);
-      hb = fmaf(r1, zb2[4 * q + 1], hb);
-      hb = fmaf(r2, zb2[4 * q + 2], hb);
-      hb = fmaf(r3, zb2[4 * q + 3], hb);
-      dhb = fmaf(r0, dzb2[4 * q], dhb);
-      dhb = fmaf(r1, dzb2[4 * q + 1], dhb);
-      dhb = fmaf(r2, dzb2[4 * q + 2], dhb);
-      dhb = fmaf(r3, dzb2[4 * q + 3], dhb);
+      hb = mlp_fma(r0, zb2[4 * q], hb);
+      hb = mlp_fma(r1, zb2[4 * q + 1], hb);
+      hb = mlp_fma(r2, zb2[4 * q + 2], hb);
+      hb = mlp_fma(r3, zb2[4 * q + 3], hb);
+      dhb = mlp_fma(r0, dzb2[4 * q], dhb);
+      dhb = mlp_fma(r1, dzb2[4 * q + 1], dhb);
+      dhb = mlp_fma(r2, dzb2[4 * q + 2], dhb);
+      dhb = mlp_fma(r3, dzb2[4 * q + 3], dhb);
     }
     // zbar1 = hbar1 s1' + dhbar1 s1'' dz1 ; dzbar1 = dhbar1 s1'
     rec[(34 + k) * rs] = hb;   // temporarily hbar1
     rec[(50 + k) * rs] = dhb;  // temporarily dhbar1
   }
-  float zb1[QEX_MLP_HIDDEN];
+  T zb1[QEX_MLP_HIDDEN];
 #pragma unroll
   for (int h = 0; h < QEX_MLP_HIDDEN; ++h) {
-    const float hb = rec[(34 + h) * rs], dhb = rec[(50 + h) * rs];
+    const T hb = rec[(34 + h) * rs], dhb = rec[(50 + h) * rs];
     zb1[h] = hb * s1p[h] + dhb * s1q[h];
     rec[(34 + h) * rs] = zb1[h];
     rec[(50 + h) * rs] = dhb * s1p[h];
@@ -338,15 +359,15 @@ __device__ inline float mlp_dual_reverse(const float* W, const float* win, int w
   // xbar = W1 zbar1
 #pragma unroll 1
   for (int k = 0; k < QEX_MLP_WINDOW; ++k) {
-    float a = 0.0f;
+    T a = T(0);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      float r0, r1, r2, r3;
+      T r0, r1, r2, r3;
       mlp_load4(W, 16 * k + 4 * q, r0, r1, r2, r3);
-      a = fmaf(r0, zb1[4 * q], a);
-      a = fmaf(r1, zb1[4 * q + 1], a);
-      a = fmaf(r2, zb1[4 * q + 2], a);
-      a = fmaf(r3, zb1[4 * q + 3], a);
+      a = mlp_fma(r0, zb1[4 * q], a);
+      a = mlp_fma(r1, zb1[4 * q + 1], a);
+      a = mlp_fma(r2, zb1[4 * q + 2], a);
+      a = mlp_fma(r3, zb1[4 * q + 3], a);
     }
     rec[(147 + k) * rs] = a;
   }
@@ -355,13 +376,14 @@ __device__ inline float mlp_dual_reverse(const float* W, const float* win, int w
 
 // Parameter gradient of one round: sum over the 32 lanes' records, parameter p
 // handled by lane p % 32 into acc[p / 32] (FP64 accumulators).
-__device__ inline void mlp_param_grad_round(const float* recbase, int lane, double* acc) {
+template <typename T>
+__device__ inline void mlp_param_grad_round(const T* recbase, int lane, double* acc) {
   // recbase: records of lane l at recbase[f * 32 + l]
 #pragma unroll
   for (int q = 0; q < 19; ++q) {
     const int pidx = lane + 32 * q;
     if (pidx >= 577) break;
-    float s = 0.0f;
+    T s = T(0);
     if (pidx < 272) {
       const int a = pidx >> 4, h = pidx & 15;
       for (int l = 0; l < 32; ++l)

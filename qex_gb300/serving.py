@@ -8,10 +8,15 @@ different times run concurrently on the GPU; each request's density,
 eigenvectors and mixing history stay in its batch's device workspace until
 the solve ends.  A 3D request replays its molecule's captured SCF graph
 (``qex_gb300.td.graph.CapturedScf``: integrals, density matrix and DIIS
-history resident on the device) on a free stream.  Admission is by device
-memory: a 1D batch is admitted only while the bytes of all in-flight batches
-(workspace + outputs) plus the resident 3D graphs stay under
-``memory_budget_bytes``.  Latency is arrival -> result on the host.
+history resident on the device) on a free stream; a 3D request for a
+molecule that is not resident is admitted by building it first (grid, AO
+values and integrals on the GPU, then the captured graph), and that set-up is
+part of its latency.  Admission is by device memory: a batch is admitted only
+while its estimated bytes fit the free HBM the driver reports
+(``cudaMemGetInfo``, through ``torch.cuda.mem_get_info``, plus the memory the
+allocator caches but does not use) less a safety margin, or, when
+``memory_budget_bytes`` is given, while the in-flight batches and resident 3D
+graphs stay under that budget.  Latency is arrival -> result on the host.
 
 The reference has no serving layer; it solves one molecule (or one vmap'd
 batch of equal-shape molecules) per call (``qedft/train/od/train.py:84-125``),
@@ -91,8 +96,9 @@ class ScfServer:
     """Continuous batching of 1D SCF requests over a pool of CUDA streams."""
 
     def __init__(self, xc, cfg: SolveConfig, max_inflight: int = 16, max_batch: int = 512,
-                 memory_budget_bytes: int = 8 << 30, engine: Ks1dEngine | None = None,
-                 graphs3d: dict | None = None):
+                 memory_budget_bytes: int | None = None, engine: Ks1dEngine | None = None,
+                 graphs3d: dict | None = None, builder3d=None, max_cycle3d: int = 30,
+                 hbm_margin_bytes: int = 2 << 30):
         self.torch = N.require_cuda()
         self.xc = xc
         self.cfg = cfg
@@ -110,6 +116,32 @@ class ScfServer:
         self.busy3d = set()
         self.in_use = 0
         self.launches = 0
+        # builder3d(key) -> molecule: how a 3D request for a molecule that is
+        # not resident is built (its graph is then captured and kept)
+        self.builder3d = builder3d
+        self.max_cycle3d = max_cycle3d
+        self.margin = hbm_margin_bytes
+        self.built3d = 0
+
+    def _fits(self, nbytes: int) -> bool:
+        """Admission test: the fixed budget when given, else the free HBM."""
+        if self.budget is not None:
+            return self.in_use + self.resident + nbytes <= self.budget
+        free, _ = self.torch.cuda.mem_get_info()
+        cached = self.torch.cuda.memory_reserved() - self.torch.cuda.memory_allocated()
+        return nbytes <= free + cached - self.margin
+
+    def _ensure3d(self, key):
+        """Make the molecule of a 3D request resident (build + capture) if needed."""
+        if key in self.graphs3d:
+            return
+        from .td.graph import CapturedScf
+
+        mol = self.builder3d(key)
+        g = CapturedScf(mol, max_cycle=self.max_cycle3d)
+        self.graphs3d[key] = g
+        self.resident += g.nbytes
+        self.built3d += 1
 
     def _bytes_for(self, batch: PackedBatch, opts) -> int:
         nb = ctypes.c_size_t()
@@ -216,6 +248,11 @@ class ScfServer:
                     break
                 if r.graph3d in self.busy3d:
                     continue
+                if r.graph3d not in self.graphs3d:
+                    if self.builder3d is None:
+                        raise KeyError(f"3D molecule {r.graph3d!r} is not resident")
+                    self._ensure3d(r.graph3d)  # set-up inside this request's latency
+                    now = time.perf_counter() - t0
                 inflight.append(self._launch3d(r, free.pop(), now))
                 pending.remove(r)
             while free and any(not q.is3d for q in pending):
@@ -224,10 +261,9 @@ class ScfServer:
                 # admission by device memory: halve the batch until it fits the
                 # free budget; a single request that does not fit waits for
                 # in-flight batches to finish (or runs alone on an idle GPU)
-                base = self.in_use + self.resident
-                while len(take) > 1 and base + self._estimate(take) > self.budget:
+                while len(take) > 1 and not self._fits(self._estimate(take)):
                     take = take[: len(take) // 2]
-                if base + self._estimate(take) > self.budget and inflight:
+                if not self._fits(self._estimate(take)) and inflight:
                     break
                 L = self._launch(take, free.pop(), now)
                 self.in_use += L.nbytes

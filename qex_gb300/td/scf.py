@@ -33,6 +33,24 @@ def get_occ(nelectron, mo_energy, out=None):
     return occ
 
 
+def orbital_gradient_norm(mo_coeff, mo_occ, fock):
+    """|g| with g = 2 C_vir^T F C_occ (pyscf's RHF ``get_grad``, as the
+    reference's loop calls it at ``qedft/train/td/hf.py:81-84``), as a (1,)
+    device tensor."""
+    torch = N.require_cuda()
+    L = _lib.lib()
+    C = _dev(mo_coeff, torch.float64).contiguous()
+    occ = _dev(mo_occ, torch.float64).contiguous()
+    F = _dev(fock, torch.float64).contiguous()
+    n = C.shape[0]
+    out = torch.empty(1, dtype=torch.float64, device="cuda")
+    ws = torch.empty(L.qex_td_orbital_gradient_workspace_size(n), dtype=torch.uint8, device="cuda")
+    N.check(L.qex_td_orbital_gradient(n, _lib.p(C), _lib.p(occ), _lib.p(F), _lib.p(out),
+                                      _lib.p(ws), ws.numel(), _lib.stream()),
+            "qex_td_orbital_gradient")
+    return out
+
+
 def make_rdm1(mo_coeff, mo_occ):
     """D = C diag(occ) C^T (batched when C is (batch, n, n))."""
     torch = N.require_cuda()

@@ -228,3 +228,28 @@ def synthetic_molecule(num_atoms: int, seed: int = 0, points_per_atom: int = 620
         elif integrals != "model":
             raise ValueError(f"integrals must be 'model' or 'analytic', got {integrals!r}")
     return mol
+
+
+def device_molecule(num_atoms: int, seed: int = 0, points_per_atom: int = 620,
+                    basis: str = "sp"):
+    """A synthetic molecule of the 3D configuration built on the GPU, for the
+    sizes where the host model integrals are too slow (nao up to ~220, G up to
+    2e5): geometry, shells and the Gaussian-cloud grid with positive random
+    weights from ``synthetic_molecule``; AO values (``qex_td_eval_ao``), S,
+    h1e = T + V_nuc (``qex_td_int1e``) and the density-fitted Coulomb factors
+    (``qex_td_int3c2e`` / ``int2c2e`` / ``df_factors``) on the device.
+    Returns (``graph.DeviceMolecule3D``, the host ``Molecule3D`` description)."""
+    from . import integrals
+    from .graph import DeviceMolecule3D
+    from .numint import _dev, eval_ao
+
+    import torch
+
+    mol = synthetic_molecule(num_atoms, seed=seed, points_per_atom=points_per_atom,
+                             with_integrals=False, basis=basis)
+    ao = eval_ao(mol)
+    S, T, V = integrals.int1e(mol)
+    B = integrals.df_factors(mol)
+    dev = DeviceMolecule3D(ao, _dev(np.asarray(mol.weights, np.float64), torch.float64), S, T + V,
+                           B, int(mol.nelectron), float(mol.energy_nuc))
+    return dev, mol

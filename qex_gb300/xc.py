@@ -88,8 +88,13 @@ class WindowMLPFunctional(XCFunctional):
 
     kind = N.QEX_XC_WINDOW_MLP
 
-    def __init__(self, normalization=2.0):
+    def __init__(self, normalization=2.0, precision="fp32"):
+        if precision not in ("fp32", "fp64"):
+            raise ValueError("precision is 'fp32' (the configuration's network) or 'fp64' "
+                             "(a checking mode)")
         self.normalization = float(normalization)
+        self.precision = precision
+        self._dev = None
 
     @staticmethod
     def flatten(params) -> np.ndarray:
@@ -125,7 +130,25 @@ class WindowMLPFunctional(XCFunctional):
         flat = self.flatten(params)
         s.normalization = self.normalization
         s.mlp_params_host = flat.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        if self.precision == "fp64":
+            # the parameters in FP64 as given (not rounded to FP32): the network
+            # then runs in FP64 in the SCF and in the adjoint step
+            torch = N.require_cuda()
+            flat64 = self.flatten64(params)
+            key = flat64.tobytes()
+            if self._dev is None or self._dev[0] != key:
+                self._dev = (key, torch.as_tensor(flat64, device="cuda"))
+            s.mlp_params64 = self._dev[1].data_ptr()
+            return s, (flat, self._dev[1])
         return s, flat  # keep the host buffer alive for the call
+
+    @staticmethod
+    def flatten64(params) -> np.ndarray:
+        (w1, b1), (w2, b2), (w3, b3) = params
+        flat = np.concatenate([np.asarray(a, np.float64).reshape(-1)
+                               for a in (w1, b1, w2, b2, w3, b3)])
+        assert flat.size == N.MLP_NUM_PARAMS
+        return np.ascontiguousarray(flat)
 
 
 class KSRFunctional(XCFunctional):
