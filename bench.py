@@ -1046,6 +1046,8 @@ def main():
                     help="time only one training-loss value and gradient")
     ap.add_argument("--eigh-eval", action="store_true",
                     help="time the 3D generalized eigensolver at the configuration's basis sizes")
+    ap.add_argument("--probe", action="store_true",
+                    help="measure the FP64/FP32 FMA and FP64 tensor-core (DMMA) throughput")
     ap.add_argument("--ints-eval", action="store_true",
                     help="time only the analytic integrals and density fitting")
     ap.add_argument("--serve-eval", action="store_true",
@@ -1066,6 +1068,16 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         torch.distributed.init_process_group("nccl")
+    if args.probe:
+        from qex_gb300 import _native
+
+        _native.load()
+        f64, f32 = _native.measure_fma_peak()
+        d1, d2 = _native.measure_dmma_peak()
+        print(json.dumps({"probe": {"fp64_fma_tflops": f64, "fp32_fma_tflops": f32,
+                                    "dmma_m8n8k4_tflops": d1, "dmma_m16n8k16_tflops": d2}}),
+              flush=True)
+        return
     if args.serve_eval:
         from qex_gb300 import _native
 

@@ -20,6 +20,13 @@ size_t qex_probe_workspace_size(void);
 int qex_probe_fma_peak(double* fp64_tflops, double* fp32_tflops, void* workspace,
                        size_t workspace_bytes, void* stream);
 
+/* Measures FP64 tensor-core (DMMA, mma.sync) throughput in TFLOP/s for the
+ * m8n8k4 and m16n8k16 shapes with the same grid; synchronises the stream.
+ * Used to decide whether the FP64 contractions of the 3D path belong on the
+ * tensor pipe. */
+int qex_probe_dmma_peak(double* m8n8k4_tflops, double* m16n8k16_tflops, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -153,6 +153,9 @@ _SIGNATURES = {
     "qex_probe_fma_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_double), _c_p, ctypes.c_size_t,
                                           _c_p]),
+    "qex_probe_dmma_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_double), _c_p, ctypes.c_size_t,
+                                           _c_p]),
     "qex_version": (ctypes.c_char_p, []),
     "qex_last_launch_count": (ctypes.c_int, []),
 }
@@ -190,6 +193,17 @@ def measure_fma_peak():
     check(lib.qex_probe_fma_peak(ctypes.byref(f64), ctypes.byref(f32), ws.data_ptr(), ws.numel(),
                                  torch.cuda.current_stream().cuda_stream), "qex_probe_fma_peak")
     return f64.value, f32.value
+
+
+def measure_dmma_peak():
+    """(m8n8k4, m16n8k16) FP64 tensor-core MMA throughput in TFLOP/s."""
+    torch = require_cuda()
+    lib = load()
+    ws = torch.empty(lib.qex_probe_workspace_size(), dtype=torch.uint8, device="cuda")
+    a, b = ctypes.c_double(), ctypes.c_double()
+    check(lib.qex_probe_dmma_peak(ctypes.byref(a), ctypes.byref(b), ws.data_ptr(), ws.numel(),
+                                  torch.cuda.current_stream().cuda_stream), "qex_probe_dmma_peak")
+    return a.value, b.value
 
 
 def declared_symbols():

@@ -103,3 +103,30 @@ def test_mixed_1d_3d_stream_equals_alone(srv):
                                  for r in three[:2]], molecules3d=mols3, max_cycle=12)
     for a, b in zip(plain, three[:2]):
         np.testing.assert_array_equal(a.energies, b.energies)
+
+
+def test_new_3d_molecules_built_on_admission(srv):
+    """3D requests for molecules that are not resident are admitted by building
+    them (GPU integrals, then the captured graph) inside the request; the
+    result equals the molecule solved alone; admission by free HBM."""
+    qex, serving, eng, cfg = srv
+    from qex_gb300.td import scf, workloads
+
+    keys = [(2, 21), (3, 22)]
+    built = {}
+
+    def build(key):
+        built[key] = workloads.device_molecule(key[0], seed=key[1])[0]
+        return built[key]
+
+    reqs = serving.mixed_requests(serving.poisson_arrivals(200.0, 0.1, seed=9), keys,
+                                  frac3d=0.4, seed=9)
+    server = serving.ScfServer(qex.LDAExpCoulomb(), cfg, max_inflight=4, max_batch=16,
+                               builder3d=build)
+    done = server.serve(reqs, realtime=False)
+    three = [r for r in done if r.is3d]
+    assert three and server.built3d == len({r.graph3d for r in three})
+    for r in three:
+        alone = scf.run_scf(built[r.graph3d], max_cycle=30)
+        np.testing.assert_array_equal(r.energies, alone.energies.cpu().numpy())
+        assert r.e_tot == float(alone.e_tot.cpu()[0]) and r.converged3d

@@ -352,3 +352,53 @@ def test_numint_class_mirrors_reference_interface(td):
     _, _, v_ref = o.nr_rks_lda(ao_r, m.weights, dm, vwn=True)
     np.testing.assert_allclose(_host(numint.vxc_matrix(ao, m.weights, vrho)), v_ref, rtol=0,
                                atol=1e-10 * np.abs(v_ref).max())
+
+
+def _host_copy(dev, mol):
+    """The oracle's host molecule of a GPU-built one (same integrals)."""
+    from qex_gb300.td import workloads
+
+    hm = workloads.Molecule3D(charges=mol.charges, positions=mol.positions, shells=mol.shells,
+                              coords=mol.coords, weights=mol.weights, nelectron=mol.nelectron)
+    hm.ao = _host(dev.ao)
+    hm.s1e = _host(dev.s1e)
+    hm.h1e = _host(dev.h1e)
+    hm.eri_factors = _host(dev.eri_factors)
+    hm.energy_nuc = dev.energy_nuc
+    return hm
+
+
+def test_scf_at_nao_above_120_matches_oracle(td):
+    """The 3D configuration's larger shapes: 14 atoms in the s/p/d basis (nao
+    above 120) with analytic integrals and density fitting built on the GPU,
+    LDA exchange, DIIS 8: the converged energy (the reference's stop rule) and
+    the last of 20 fixed cycles within 1e-8 Ha of the oracle."""
+    torch, eigh, numint, scf, W = td
+    dev, mol = W.device_molecule(14, seed=7, points_per_atom=620, basis="spd")
+    assert dev.nao > 120
+    hm = _host_copy(dev, mol)
+    res = scf.run_scf(dev, max_cycle=20)
+    ref = o.scf(hm, max_cycle=20, stop=(1e-10, 1e-5))
+    st = _host(res.converged)
+    assert bool(st[0]) == ref["converged"]
+    assert abs(float(_host(res.e_tot)[0]) - ref["e_tot"]) < 1e-8
+    e_fixed, _, _ = o.scf(hm, max_cycle=20)
+    assert abs(_host(res.energies)[-1] - e_fixed[-1]) < 1e-8
+    assert (_host(res.status) == 0).all()
+
+
+def test_scf_with_global_network_512_matches_oracle(td):
+    """The global neural functional at the configuration's width (512, 512, 1)
+    in the SCF (FP32 network on the GPU, the oracle's network in FP32 as
+    well): final energy within 1e-8 Ha, trajectory within the DIIS bound."""
+    torch, eigh, numint, scf, W = td
+    dev, mol = W.device_molecule(6, seed=3, points_per_atom=300, basis="sp")
+    G = dev.weights.numel()
+    params = numint.NeuralXC.init(hidden=512, seed=4, inputs=G)
+    f = numint.NeuralXC(params, scale=1e-2)
+    hm = _host_copy(dev, mol)
+    res = scf.run_scf(dev, max_cycle=15, xc=f)
+    e_ref, _, _ = o.scf(hm, max_cycle=15, nn=(f.flat, 1e-2, np.float32, 512))
+    e = _host(res.energies)
+    np.testing.assert_allclose(e, e_ref, atol=1e-5, rtol=0)
+    assert abs(e[-1] - e_ref[-1]) < 1e-8, abs(e[-1] - e_ref[-1])
