@@ -119,36 +119,24 @@ class Ks1dAdjoint:
         ws.argtypes = [ctypes.POINTER(N.Ks1dOptions), ctypes.c_int32,
                        ctypes.POINTER(ctypes.c_size_t)]
 
-    def value_and_grad(self, batch: PackedBatch, xc, cfg: SolveConfig, target_energy,
-                       target_density, density_weight: float = 0.1,
-                       checkpoint_every: int = 5, loss=None,
-                       initial_density=None) -> AdjointResult:
-        """Loss and gradient; ``loss`` is a ``Config3Loss`` (the default, with
-        ``density_weight``) or a ``TrajectoryLoss``.  Reflection symmetry
-        (``cfg.enforce_reflection_symmetry``) is differentiated as well.
-        ``initial_density`` (packed) defaults to the non-interacting density
-        of v_ext (jax_dft ``get_initial_density(..., 'noninteracting')``)."""
+    def forward(self, batch: PackedBatch, xc, cfg: SolveConfig, checkpoint_every: int = 5,
+                initial_density=None):
+        """The forward half of a ``jax.custom_vjp`` (``fwd``): the unrolled SCF
+        with checkpoints.  Returns ((energies (B, T), final mixed density
+        (packed)), residuals); the residuals are the checkpointed input
+        densities of every ``checkpoint_every``-iteration segment, from which
+        ``backward`` recomputes the iterates.  ``initial_density`` (packed)
+        defaults to the non-interacting density of v_ext (jax_dft
+        ``get_initial_density(..., 'noninteracting')``)."""
         torch = N.require_cuda()
         if cfg.convention != "local" or cfg.num_mixing_iterations != 1:
             raise ValueError("the adjoint covers the local convention with one mixing difference")
         if cfg.density_mse_converge_tolerance > 0:
             raise ValueError("the adjoint differentiates the fixed-iteration SCF "
                              "(density_mse_converge_tolerance <= 0)")
-        if loss is None:
-            loss = Config3Loss(density_weight)
-        functional, params = resolve(xc)
-        spec, keep = functional.spec(params, _convention(cfg))
         dev = batch.device
         T = int(cfg.num_iterations)
         B = batch.size
-        dx = torch.as_tensor(np.repeat(np.array([m.grid_spacing for m in batch.molecules]),
-                                       batch.num_grids_host), device=dev)
-        t_e = torch.as_tensor(np.asarray(target_energy, np.float64), device=dev)
-        t_n = torch.as_tensor(np.asarray(target_density, np.float64), device=dev)
-        ne_host = np.array([m.num_electrons for m in batch.molecules], dtype=np.float64)
-        ne = torch.as_tensor(ne_host, device=dev)
-        ne_pts = torch.as_tensor(np.repeat(ne_host, batch.num_grids_host), device=dev)
-
         if initial_density is not None:
             n0 = torch.as_tensor(np.asarray(initial_density, np.float64), device=dev).contiguous()
         else:
@@ -158,28 +146,44 @@ class Ks1dAdjoint:
                                      bucketed=False)
             n0, _, _, _ = self.engine.noninteracting(batch, out1["external_potential"],
                                                      cfg.stencil)
-
-        def segment(n_start, t0, steps, records):
-            c = SolveConfig(**{**dataclasses.asdict(cfg), "num_iterations": steps,
-                               "alpha": cfg.alpha * cfg.alpha_decay ** t0})
-            return self.engine.solve(batch, xc, c, records=records, initial_density=n_start,
-                                     bucketed=False)
-
-        # ---- forward with checkpoints
         checkpoints = {}
         energies = torch.empty((B, T), dtype=torch.float64, device=dev)
         n = n0
         for t0 in range(0, T, checkpoint_every):
             steps = min(checkpoint_every, T - t0)
             checkpoints[t0] = n
-            out = segment(n, t0, steps, ("energy", "final_density"))
+            out = self._segment(batch, xc, cfg, n, t0, steps, ("energy", "final_density"))
             energies[:, t0:t0 + steps] = out["energy"]
             n = out["final_density"].clone()
-        status = out["status"].clone()
-        loss_value = loss.value(energies, n, t_e, t_n, dx, ne, ne_pts)
+        residuals = {"batch": batch, "xc": xc, "cfg": cfg, "checkpoints": checkpoints,
+                     "checkpoint_every": checkpoint_every, "status": out["status"].clone()}
+        return (energies, n), residuals
 
-        # ---- backward
-        gnext = loss.grad_density(n, t_n, dx, ne_pts, B).contiguous()
+    def _segment(self, batch, xc, cfg, n_start, t0, steps, records):
+        c = SolveConfig(**{**dataclasses.asdict(cfg), "num_iterations": steps,
+                           "alpha": cfg.alpha * cfg.alpha_decay ** t0})
+        return self.engine.solve(batch, xc, c, records=records, initial_density=n_start,
+                                 bucketed=False)
+
+    def backward(self, residuals, cotangents):
+        """The backward half of a ``jax.custom_vjp`` (``bwd``): cotangents
+        (g_energies (B, T) or None, g_final_density (packed) or None) -> the
+        gradient with respect to the window-MLP parameters (flat, 577 FP64),
+        by one ``qex_ks1d_adjoint_step`` launch per iteration, each segment's
+        iterates recomputed from its checkpoint."""
+        torch = N.require_cuda()
+        batch, xc, cfg = residuals["batch"], residuals["xc"], residuals["cfg"]
+        checkpoints, every = residuals["checkpoints"], residuals["checkpoint_every"]
+        functional, params = resolve(xc)
+        spec, keep = functional.spec(params, _convention(cfg))
+        dev = batch.device
+        T = int(cfg.num_iterations)
+        B = batch.size
+        P = batch.total_points
+        g_e, g_n = cotangents
+        gnext = (torch.zeros(P, dtype=torch.float64, device=dev) if g_n is None else
+                 torch.as_tensor(g_n, dtype=torch.float64, device=dev).clone().contiguous())
+        g_e = None if g_e is None else torch.as_tensor(g_e, dtype=torch.float64, device=dev)
         genergy = torch.zeros(B, dtype=torch.float64, device=dev)
         gtheta = torch.zeros((B, N.MLP_NUM_PARAMS), dtype=torch.float64, device=dev)
         gn = torch.empty_like(gnext)
@@ -191,12 +195,12 @@ class Ks1dAdjoint:
         st = torch.zeros(B, dtype=torch.int32, device=dev)
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         cb = batch.c_batch()
-        P = batch.total_points
         for t0 in sorted(checkpoints, reverse=True):
-            steps = min(checkpoint_every, T - t0)
+            steps = min(every, T - t0)
             # recompute the segment's per-iteration input densities
             if steps > 1:
-                rec = segment(checkpoints[t0], t0, steps - 1, ("density",))["density"]
+                rec = self._segment(batch, xc, cfg, checkpoints[t0], t0, steps - 1,
+                                    ("density",))["density"]
                 dens_rec = rec  # (steps-1) x packed, molecule-major
             inputs = [checkpoints[t0]]
             for k in range(1, steps):
@@ -208,10 +212,10 @@ class Ks1dAdjoint:
                 inputs.append(x)
             for k in range(steps - 1, -1, -1):
                 t = t0 + k
-                genergy.zero_()
-                ge = loss.grad_energy(t, energies, t_e, ne)
-                if ge is not None:
-                    genergy.copy_(ge)
+                if g_e is None:
+                    genergy.zero_()
+                else:
+                    genergy.copy_(g_e[:, t])
                 alpha_t = cfg.alpha * cfg.alpha_decay ** t
                 rc = self.lib.qex_ks1d_adjoint_step(
                     ctypes.byref(cb), ctypes.byref(opts), ctypes.byref(spec),
@@ -225,6 +229,56 @@ class Ks1dAdjoint:
         grad = gtheta.sum(dim=0)
         torch.cuda.current_stream().synchronize()
         del keep
-        return AdjointResult(loss=loss_value, grad=grad.cpu().numpy(),
-                             energies=energies.cpu().numpy(),
-                             final_density=n.cpu().numpy(), status=status.cpu().numpy())
+        return grad.cpu().numpy()
+
+    def value_and_grad(self, batch: PackedBatch, xc, cfg: SolveConfig, target_energy,
+                       target_density, density_weight: float = 0.1,
+                       checkpoint_every: int = 5, loss=None,
+                       initial_density=None) -> AdjointResult:
+        """Loss and gradient; ``loss`` is a ``Config3Loss`` (the default, with
+        ``density_weight``) or a ``TrajectoryLoss``.  Reflection symmetry
+        (``cfg.enforce_reflection_symmetry``) is differentiated as well.
+        ``forward`` then ``backward`` with the loss's cotangents."""
+        torch = N.require_cuda()
+        if loss is None:
+            loss = Config3Loss(density_weight)
+        dev = batch.device
+        B = batch.size
+        dx = torch.as_tensor(np.repeat(np.array([m.grid_spacing for m in batch.molecules]),
+                                       batch.num_grids_host), device=dev)
+        t_e = torch.as_tensor(np.asarray(target_energy, np.float64), device=dev)
+        t_n = torch.as_tensor(np.asarray(target_density, np.float64), device=dev)
+        ne_host = np.array([m.num_electrons for m in batch.molecules], dtype=np.float64)
+        ne = torch.as_tensor(ne_host, device=dev)
+        ne_pts = torch.as_tensor(np.repeat(ne_host, batch.num_grids_host), device=dev)
+        (energies, n), res = self.forward(batch, xc, cfg, checkpoint_every, initial_density)
+        loss_value = loss.value(energies, n, t_e, t_n, dx, ne, ne_pts)
+        T = energies.shape[1]
+        g_e = torch.zeros((B, T), dtype=torch.float64, device=dev)
+        for t in range(T):
+            ge = loss.grad_energy(t, energies, t_e, ne)
+            if ge is not None:
+                g_e[:, t] = ge
+        g_n = loss.grad_density(n, t_n, dx, ne_pts, B).contiguous()
+        grad = self.backward(res, (g_e, g_n))
+        return AdjointResult(loss=loss_value, grad=grad, energies=energies.cpu().numpy(),
+                             final_density=n.cpu().numpy(), status=res["status"].cpu().numpy())
+
+
+def scf_fwd(xc, batch: PackedBatch, cfg: SolveConfig, checkpoint_every: int = 5,
+            initial_density=None, adjoint: Ks1dAdjoint | None = None):
+    """``fwd`` of ``jax.custom_vjp`` over the unrolled SCF (the reference
+    differentiates ``jax.lax.scan`` at ``qedft/train/od/jit_scf.py:184-211``
+    with ``jax.value_and_grad`` at ``qedft/train/od/trainer.py:139-143``):
+    ((energies, final density), residuals)."""
+    adj = adjoint or Ks1dAdjoint()
+    out, res = adj.forward(batch, xc, cfg, checkpoint_every, initial_density)
+    res["adjoint"] = adj
+    return out, res
+
+
+def scf_bwd(residuals, cotangents):
+    """``bwd`` of ``jax.custom_vjp``: (g_energies, g_final_density) -> the
+    parameter gradient (flat window-MLP order, 577 FP64)."""
+    return residuals["adjoint"].backward(residuals, cotangents)
+
