@@ -803,6 +803,10 @@ def run_ours(args, rank, world):
                "sample": f"{cn} molecules of the same workload, reference algorithm (dense "
                          f"eigh, materialised Hartree kernel), {cconv} converged, {dt:.1f} s wall",
                "total_solves_per_s": cn / dt}
+        # one core (one process), a smaller sample of the same molecules
+        dt1, c1, n1, _ = cpu_sample(mols, params, args.iters, min(8, sample), 1)
+        cpu["single_core"] = {"value": c1 / dt1, "total_solves_per_s": n1 / dt1, "cores": 1,
+                              "sample": f"first {n1} molecules, {c1} converged, {dt1:.1f} s"}
         _, _, _, ref64 = cpu_sample(mols, params, args.iters, sample, cores, np.float64)
         dens = batch.split(out["final_density"].cpu().numpy())
         parity, selfc, full = parity_summary(mols, energy, status, dens, ref32, ref64)
