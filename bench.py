@@ -646,9 +646,22 @@ def run_eigh_eval(args):
             times.append(time.perf_counter() - t0)
         res = (F @ C - S @ C * w[None, :]).abs().max().item() / F.abs().max().item()
         ev = torch.linalg.eigvalsh(S)
+        # the host LAPACK solve of the same problem (SciPy eigh(F, S), all host threads)
+        import scipy.linalg
+
+        Fh, Sh = F.cpu().numpy(), S.cpu().numpy()
+        host = []
+        for _ in range(max(args.steps, 3)):
+            t0 = time.perf_counter()
+            wh = scipy.linalg.eigh(Fh, Sh, eigvals_only=False)[0]
+            host.append(time.perf_counter() - t0)
         out[f"atoms_{na}_{basis}"] = {"nao": int(m.nao), "ms": float(np.median(times)) * 1e3,
                                       "residual": res,
-                                      "overlap_condition": float(ev[-1] / ev[0])}
+                                      "overlap_condition": float(ev[-1] / ev[0]),
+                                      "host_scipy_ms": float(np.median(host)) * 1e3,
+                                      "host_cores": host_cores(),
+                                      "max_abs_eigenvalue_diff_vs_host": float(
+                                          np.abs(np.sort(wh) - w.cpu().numpy()).max())}
     return {"workload": "generalized eigensolve, core Hamiltonian and overlap", **out}
 
 
