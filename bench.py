@@ -579,11 +579,15 @@ def run_td(args, peak64, peak32, cycles=30):
                 times.append(e0.elapsed_time(e1) / 1e3)
             t = sorted(times)[len(times) // 2]
             st = res.converged.cpu().numpy()
+            en = res.energies.cpu().numpy()
             w64, w32 = td_flops(G, n, naux, nocc, 512 if label != "lda" else None)
             bound = cycles * (w64 / (peak64 * 1e12) + (w32 / (peak32 * 1e12) if peak32 else 0.0))
             row[label] = {"ms_per_solve": t * 1e3, "solves_per_s": 1.0 / t,
                           "converged": bool(st[0]), "converged_cycle": int(st[1]) + 1,
                           "e_tot": float(res.e_tot.cpu()[0]),
+                          "last_abs_dE": float(abs(en[-1] - en[-2])),
+                          "last_grad_norm": float(res.grad_norms.cpu()[-1]),
+                          "eigh_path": getattr(cap, "eigh_path", None),
                           "roofline": {"bound": "fp64 (+fp32 network)", "frac": bound / t,
                                        "fp64_flops_per_cycle": w64, "fp32_flops_per_cycle": w32}}
             del cap
@@ -631,7 +635,10 @@ def run_eigh_eval(args):
     from qex_gb300.td import eigh, integrals, workloads
 
     out = {}
-    for na, basis in ((8, "sp"), (20, "sp"), (20, "spd"), (21, "spd")):
+    cases = ((8, "sp"), (20, "sp"), (20, "spd"), (21, "spd"))
+    if args.eigh_atoms:
+        cases = tuple(c for c in cases if c[0] in args.eigh_atoms)
+    for na, basis in cases:
         m = workloads.synthetic_molecule(na, seed=na, with_integrals=False, basis=basis)
         S, T, V = integrals.int1e(m)
         F = T + V
@@ -645,7 +652,7 @@ def run_eigh_eval(args):
             torch.cuda.synchronize()
             times.append(time.perf_counter() - t0)
         res = (F @ C - S @ C * w[None, :]).abs().max().item() / F.abs().max().item()
-        ev = torch.linalg.eigvalsh(S)
+        ev = np.linalg.eigvalsh(S.cpu().numpy())
         # the host LAPACK solve of the same problem (SciPy eigh(F, S), all host threads)
         import scipy.linalg
 
@@ -655,7 +662,14 @@ def run_eigh_eval(args):
             t0 = time.perf_counter()
             wh = scipy.linalg.eigh(Fh, Sh, eigvals_only=False)[0]
             host.append(time.perf_counter() - t0)
+        # the other path of the mixed-precision solver at this size (autotuner candidates)
+        from qex_gb300.td.eigh import tune_path
+
+        eigh._PATHS.pop(int(m.nao), None)
+        best, path_ms = tune_path(F, S)
         out[f"atoms_{na}_{basis}"] = {"nao": int(m.nao), "ms": float(np.median(times)) * 1e3,
+                                      "path_ms": {str(k): v for k, v in path_ms.items()},
+                                      "tuned_path": best,
                                       "residual": res,
                                       "overlap_condition": float(ev[-1] / ev[0]),
                                       "host_scipy_ms": float(np.median(host)) * 1e3,
@@ -1061,6 +1075,8 @@ def main():
                     help="time only the molecular grid build")
     ap.add_argument("--train-eval", action="store_true",
                     help="time only one training-loss value and gradient")
+    ap.add_argument("--eigh-atoms", type=int, nargs="*", default=None,
+                    help="restrict --eigh-eval to the molecules of these atom counts")
     ap.add_argument("--eigh-eval", action="store_true",
                     help="time the 3D generalized eigensolver at the configuration's basis sizes")
     ap.add_argument("--probe", action="store_true",

@@ -232,6 +232,15 @@ int qex_td_nn_xc_global(int64_t num_points, int32_t hidden, const double* rho,
                         const double* weights, const float* params, double scale, double* vrho,
                         double* sums, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Path of qex_td_gen_eigh for matrices of size n (1 <= n <= 240), a tuning
+ * knob with no counterpart in the reference: 0 the default (FP32 solve in
+ * shared memory up to n = 128, the FP64 factor and tridiagonal stage beyond),
+ * 1 the shared-memory FP32 solve (n <= 128), 2 the FP64 factor and
+ * tridiagonal stage.  Both are refined in FP64 to the same accuracy; the
+ * faster one depends on n.  Process-wide; not synchronised with calls in
+ * flight. */
+int qex_td_gen_eigh_set_path(int32_t n, int32_t path);
+
 /* F = h1e + J + V (fock may be NULL) and energy[0] = sum_ij D_ij h_ji +
  * 1/2 sum_ij D_ij J_ij + excsum[0] + energy_nuc (excsum a device scalar, may be
  * NULL for 0).  One CTA, fixed-order sums. */

@@ -24,6 +24,8 @@
 // td.cu, which applies the reference's shift
 // (qedft/train/td/generalized_eigensolver.py:264-330).
 #include <cuda_runtime.h>
+
+#include <atomic>
 #include <float.h>
 #include <math.h>
 #include <stdint.h>
@@ -1120,8 +1122,14 @@ int ksplit_of(int n) { return (n + kKC - 1) / kKC; }
 // kMaxSmemN also U^T in FP32 (n^2 floats).
 long long area_doubles(int n) {
   const long long nn = (long long)n * n;
-  return (9 + ksplit_of(n)) * nn + n + 1 + (n > kMaxSmemN ? (nn + 1) / 2 + 1 : 0);
+  // U^T in FP32 is reserved at every size: the path of a size is selectable
+  return (9 + ksplit_of(n)) * nn + n + 1 + (nn + 1) / 2 + 1;
 }
+
+// Path per matrix size: 0 the default (shared-memory FP32 solve up to
+// kMaxSmemN, the FP64 factor and tridiagonal stage beyond), 1 the
+// shared-memory solve, 2 the FP64 factor and tridiagonal stage.
+std::atomic<int> g_path[kMaxN + 1];
 
 size_t smem_factor64(int n) {
   const int m = (n + 1) & ~1;
@@ -1167,7 +1175,8 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
                      int32_t* status, double* area, int* ok_out, cudaStream_t s) {
   using namespace qex_mp_host;
   if (n > kMaxN) return false;
-  const bool large = n > kMaxSmemN;
+  const int path = g_path[n].load(std::memory_order_relaxed);
+  const bool large = (path == 2 || n > kMaxSmemN) && !(path == 1 && n <= kMaxSmemN);
   if (large) {
     int dev = 0, max_optin = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
@@ -1248,6 +1257,14 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     X2 = t;
   }
   sort_out_kernel<<<batch, 256, sizeof(int) * n, s>>>(n, lam, X, ok, w, V, status);
+  return true;
+}
+
+// Selects the path of matrices of size n (see g_path); false when n is beyond
+// the mixed-precision solver or path is unknown.
+bool qex_mp_set_path(int n, int path) {
+  if (n < 1 || n > qex_mp_host::kMaxN || path < 0 || path > 2) return false;
+  qex_mp_host::g_path[n].store(path, std::memory_order_relaxed);
   return true;
 }
 

@@ -19,6 +19,7 @@
 bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double* w, double* V,
                      int32_t* status, double* area, int* ok_out, cudaStream_t s);
 long long qex_mp_area_doubles(int n);
+bool qex_mp_set_path(int n, int path);
 
 namespace {
 
@@ -858,6 +859,10 @@ size_t qex_td_gen_eigh_workspace_size(int32_t batch, int32_t n) {
   // FP64 path (L, C, U), then the mixed-precision area and its ok flags
   return sizeof(double) * (3 * (size_t)n * n + (size_t)qex_mp_area_doubles(n)) * (size_t)batch +
          sizeof(int) * (size_t)batch;
+}
+
+int qex_td_gen_eigh_set_path(int32_t n, int32_t path) {
+  return qex_mp_set_path(n, path) ? QEX_OK : QEX_BAD_ARG;
 }
 
 int qex_td_gen_eigh(int32_t batch, int32_t n, const double* A, const double* S, double* w,

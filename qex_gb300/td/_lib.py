@@ -59,6 +59,7 @@ SIGNATURES = {
     "qex_td_aufbau_occ": (ctypes.c_int, [_i32, _i32, _v, _i32, _v, _v]),
     "qex_td_mask_pad": (ctypes.c_int, [_i32, _v, _v, _v, _v, _v, _v]),
     "qex_td_mask_sort": (ctypes.c_int, [_i32, _v, _v, _v, _v, _v, _v]),
+    "qex_td_gen_eigh_set_path": (ctypes.c_int, [_i32, _i32]),
 }
 
 _lib = None

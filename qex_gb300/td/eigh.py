@@ -37,6 +37,50 @@ def generalized_eigh(A, B, *, eps: float = 1.0e-12, return_status: bool = False)
     return (w, V, st) if return_status else (w, V)
 
 
+_PATHS = {}  # n -> (selected path, {path: ms})
+
+
+def set_path(n: int, path: int) -> None:
+    """Select the mixed-precision solver's path for matrices of size n: 0 the
+    default, 1 the shared-memory FP32 solve (n <= 128), 2 the FP64 factor and
+    tridiagonal stage (``qex_td_gen_eigh_set_path``)."""
+    N.check(_lib.lib().qex_td_gen_eigh_set_path(int(n), int(path)), "qex_td_gen_eigh_set_path")
+
+
+def tune_path(A, B, repeats: int = 3):
+    """Autotune the eigensolver path for the size of (A, B): time each
+    candidate path on this pair (CUDA events, median of ``repeats`` after one
+    warm-up) and keep the faster for that size.  Both paths refine to the same
+    FP64 accuracy.  Cached per size; returns (path, {path: ms})."""
+    torch = N.require_cuda()
+    A = _dev(A, torch.float64)
+    n = A.shape[-1]
+    if n in _PATHS:
+        return _PATHS[n]
+    if n > 240:
+        _PATHS[n] = (0, {})
+        return _PATHS[n]
+    cands = (1, 2) if n <= 128 else (2,)
+    timings = {}
+    stream = torch.cuda.current_stream()
+    for path in cands:
+        set_path(n, path)
+        generalized_eigh(A, B)
+        ts = []
+        for _ in range(repeats):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            generalized_eigh(A, B)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        timings[path] = sorted(ts)[len(ts) // 2]
+    best = min(timings, key=timings.get)
+    set_path(n, best)
+    _PATHS[n] = (best, timings)
+    return _PATHS[n]
+
+
 def masked_generalized_eigh(fock, s1e, mask):
     """Padded/masked solve with the reference's padding and sorting rules
     (``qex_td_mask_pad``, the solve, ``qex_td_mask_sort``)."""

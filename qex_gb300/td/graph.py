@@ -52,10 +52,15 @@ class DeviceMolecule3D:
 class CapturedScf:
     """One molecule's ``run_scf(max_cycle)`` captured as a CUDA graph."""
 
-    def __init__(self, mol, max_cycle: int = 30, xc="LDA"):
+    def __init__(self, mol, max_cycle: int = 30, xc="LDA", tune_eigh: bool = True):
         torch = N.require_cuda()
         self.max_cycle = max_cycle
         self.mol = mol if isinstance(mol, DeviceMolecule3D) else DeviceMolecule3D.from_host(mol)
+        if tune_eigh:
+            # the eigensolver path for this basis size, timed on the core Hamiltonian
+            from .eigh import tune_path
+
+            self.eigh_path = tune_path(self.mol.h1e, self.mol.s1e)
         before = torch.cuda.memory_allocated()
         # warm-up outside the capture: kernel attributes, allocator pools
         side = torch.cuda.Stream()

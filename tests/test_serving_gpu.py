@@ -129,4 +129,5 @@ def test_new_3d_molecules_built_on_admission(srv):
     for r in three:
         alone = scf.run_scf(built[r.graph3d], max_cycle=30)
         np.testing.assert_array_equal(r.energies, alone.energies.cpu().numpy())
-        assert r.e_tot == float(alone.e_tot.cpu()[0]) and r.converged3d
+        assert r.e_tot == float(alone.e_tot.cpu()[0])
+        assert r.converged3d == bool(alone.converged.cpu()[0])
