@@ -555,6 +555,8 @@ def run_td(args, peak64, peak32, cycles=30):
     from qex_gb300.td import graph, numint, workloads
 
     cases = ((8, "sp", 155), (14, "spd", 3000), (20, "spd", 10000))
+    if args.td_atoms:
+        cases = tuple(c for c in cases if c[0] in args.td_atoms)
     out = {"workload": "3D numint SCF, synthetic H/C/N/O molecules, analytic integrals and "
                        "density-fitted J on the GPU, DIIS 8, 30 cycles (CUDA graph)"}
     cpu_total = 0.0
@@ -966,7 +968,9 @@ def run_serve_eval(args):
     20% 3D solves over a population of 64 synthetic molecules of nao 4-117
     (s/p basis), each arriving as a new molecule the first time (grid, AO
     values, analytic integrals and density fitting on the GPU, then the
-    captured SCF graph: inside that request's latency); admission by free HBM.
+    captured SCF graph: inside that request's latency); admission by free HBM;
+    a stream is cut 10 s after its last arrival (requests still waiting are
+    reported as unserved).
     Then the saturated capacity of the served and the plain forms for 1D
     requests (all arrivals at t = 0)."""
     import qex_gb300
@@ -993,8 +997,10 @@ def run_serve_eval(args):
     for rate in args.serve_rates:
         arr = sv.poisson_arrivals(rate, args.serve_seconds, seed=int(rate) + 11)
         reqs = sv.mixed_requests(arr, keys, frac3d=0.2, seed=int(rate) + 11)
-        server = sv.ScfServer(xc, cfg, max_inflight=16, max_batch=1024, builder3d=build)
-        done = server.serve(reqs)
+        server = sv.ScfServer(xc, cfg, max_inflight=32, max_batch=1024, builder3d=build)
+        # an overloaded stream is cut 10 s after its last arrival: what waits
+        # then is reported as unserved
+        done = server.serve(reqs, deadline=args.serve_seconds + 10.0)
         s = sv.latency_summary(done)
         s["launches"] = server.launches
         s["molecules_built"] = server.built3d
@@ -1065,6 +1071,8 @@ def main():
     ap.add_argument("--no-ksr", action="store_true")
     ap.add_argument("--no-td", action="store_true", help="skip the 3D configuration")
     ap.add_argument("--td-only", action="store_true", help="time only the 3D configuration")
+    ap.add_argument("--td-atoms", type=int, nargs="*", default=None,
+                    help="restrict the 3D configuration to the molecules of these atom counts")
     ap.add_argument("--ksr-only", action="store_true",
                     help="time only the KSR SCF workload (profiling)")
     ap.add_argument("--ksr-eval", action="store_true",

@@ -365,6 +365,7 @@ __global__ void __launch_bounds__(kThreads) chol64_kernel(int n, const double* _
                                                           int* __restrict__ ok) {
   const int b = blockIdx.x;
   __shared__ double piv;
+  __shared__ double colk[kMaxLargeN];  // column k of L below the diagonal
   const long long nn = (long long)n * n;
   double* L = L64 + b * nn;
   double* Cd = C64 + b * nn;
@@ -373,6 +374,7 @@ __global__ void __launch_bounds__(kThreads) chol64_kernel(int n, const double* _
     L[e] = S[b * nn + e];
   }
   __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int k = 0; k < n; ++k) {
     if (threadIdx.x == 0) {
       const double d = L[(long long)k * n + k];
@@ -381,13 +383,18 @@ __global__ void __launch_bounds__(kThreads) chol64_kernel(int n, const double* _
     }
     __syncthreads();
     if (!(piv > 0.0)) return;  // not SPD: ok stays 0, the FP64 Jacobi path applies the shift
-    const double lkk = L[(long long)k * n + k];
-    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) L[(long long)i * n + k] /= lkk;
+    const double inv = 1.0 / L[(long long)k * n + k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) {
+      const double v = L[(long long)i * n + k] * inv;
+      L[(long long)i * n + k] = v;
+      colk[i] = v;
+    }
     __syncthreads();
-    const int r = n - k - 1;
-    for (long long e = threadIdx.x; e < (long long)r * r; e += blockDim.x) {
-      const int i = k + 1 + (int)(e / r), j = k + 1 + (int)(e % r);
-      if (j <= i) L[(long long)i * n + j] -= L[(long long)i * n + k] * L[(long long)j * n + k];
+    // trailing lower triangle: a warp per row, lanes along the row
+    for (int i = k + 1 + warp; i < n; i += nw) {
+      const double lik = colk[i];
+      double* row = L + (long long)i * n;
+      for (int j = k + 1 + lane; j <= i; j += 32) row[j] = fma(-lik, colk[j], row[j]);
     }
     __syncthreads();
   }
@@ -409,6 +416,7 @@ __global__ void __launch_bounds__(kVecWarps * 32) tri_fwd_kernel(int n, int batc
                                                                  const int* __restrict__ ok,
                                                                  int rows) {
   __shared__ double vec[kVecWarps][kMaxLargeN];
+  __shared__ double rdiag[kVecWarps][kMaxLargeN];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long gw = (long long)blockIdx.x * kVecWarps + w;
   if (gw >= (long long)batch * n) return;
@@ -420,14 +428,17 @@ __global__ void __launch_bounds__(kVecWarps * 32) tri_fwd_kernel(int n, int batc
   const long long base = rows ? (long long)j * n : j;
   const long long stride = rows ? 1 : n;
   double* v = vec[w];
-  for (int i = lane; i < n; i += 32) v[i] = Cb[base + i * stride];
+  double* rd = rdiag[w];
+  for (int i = lane; i < n; i += 32) {
+    v[i] = Cb[base + i * stride];
+    rd[i] = 1.0 / L[(long long)i * n + i];
+  }
   __syncwarp();
+  // column-oriented substitution: once x_i is known, the lanes update the
+  // remaining entries with column i of L (no reduction on the dependent chain)
   for (int i = 0; i < n; ++i) {
-    const double* Li = L + (long long)i * n;
-    double s = 0.0;
-    for (int k = lane; k < i; k += 32) s = fma(Li[k], v[k], s);
-    s = warp_sum64(s);
-    const double x = (v[i] - s) / Li[i];
+    const double x = v[i] * rd[i];
+    for (int k = i + 1 + lane; k < n; k += 32) v[k] = fma(-L[(long long)k * n + i], x, v[k]);
     __syncwarp();
     if (lane == 0) v[i] = x;
     __syncwarp();
@@ -497,28 +508,37 @@ __global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* 
   float* C = sm;
   float* v = C + nn;
   float* p = v + n;
-  float* red = p + n;
+  float* red = p + n;  // 32 floats
   float* HV = reinterpret_cast<float*>(HVws + b * nn);
   float* d = reinterpret_cast<float*>(TRIws + b * nn);
   float* e = d + n;
   float* tau = e + n;
   const double* Cd = C64 + b * nn;
-  for (long long el = threadIdx.x; el < nn; el += blockDim.x) {
-    const int i = (int)(el / n), j = (int)(el % n);
-    C[el] = (float)(0.5 * (Cd[el] + Cd[(long long)j * n + i]));
-  }
-  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  // C in FP32, rows read coalesced, then symmetrised in shared memory
+  for (int i = warp; i < n; i += nw)
+    for (int j = lane; j < n; j += 32) C[(long long)i * n + j] = (float)Cd[(long long)i * n + j];
+  __syncthreads();
+  for (int i = warp; i < n; i += nw)
+    for (int j = i + 1 + lane; j < n; j += 32) {
+      const float a = 0.5f * (C[(long long)i * n + j] + C[(long long)j * n + i]);
+      C[(long long)i * n + j] = a;
+      C[(long long)j * n + i] = a;
+    }
+  __syncthreads();
+  // four block barriers per step: the reflector's norm, the complete v, the
+  // product p = tau A v with v.p, the rank-2 update
   for (int k = 0; k < n - 2; ++k) {
     const int m = n - k - 1;  // x = C[k+1 .. n-1][k] (= row k right of the diagonal)
+    const float* xk = C + (long long)k * n + k + 1;
     float sq = 0.0f;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-      const float x = C[(long long)k * n + k + 1 + i];
-      v[i] = x;
-      if (i > 0) sq = fmaf(x, x, sq);
-    }
-    sq = block_sumf(sq, red);
-    const float x0 = v[0];
+    for (int i = 1 + threadIdx.x; i < m; i += blockDim.x) sq = fmaf(xk[i], xk[i], sq);
+    sq = warp_sumf(sq);
+    if (lane == 0) red[warp] = sq;
+    __syncthreads();
+    sq = 0.0f;
+    for (int w = 0; w < nw; ++w) sq += red[w];
+    const float x0 = xk[0];
     float alpha = x0, t = 0.0f;
     if (sq > 0.0f) {
       const float nrm = sqrtf(fmaf(x0, x0, sq));
@@ -526,35 +546,35 @@ __global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* 
       const float v0 = x0 - alpha;
       t = 2.0f / fmaf(v0, v0, sq);
     }
-    __syncthreads();  // every thread has read v[0]
+    for (int i = threadIdx.x; i < m; i += blockDim.x)
+      v[i] = i == 0 ? ((t != 0.0f) ? x0 - alpha : 1.0f) : xk[i];
     if (threadIdx.x == 0) {
-      v[0] = (t != 0.0f) ? x0 - alpha : 1.0f;
       d[k] = C[(long long)k * n + k];
       e[k] = alpha;
       tau[k] = t;
     }
     __syncthreads();
     if (t != 0.0f) {
-      // p = tau A v over the trailing block, a warp per row
+      // p = tau A v over the trailing block, a warp per row; v.p per warp
+      float vp = 0.0f;
       for (int r = warp; r < m; r += nw) {
         const float* row = C + (long long)(k + 1 + r) * n + k + 1;
         float a = 0.0f;
         for (int c = lane; c < m; c += 32) a = fmaf(row[c], v[c], a);
-        a = warp_sumf(a);
-        if (lane == 0) p[r] = t * a;
+        a = t * warp_sumf(a);
+        if (lane == 0) p[r] = a;
+        vp = fmaf(v[r], a, vp);
       }
+      if (lane == 0) red[32 + warp] = vp;
       __syncthreads();
       float q = 0.0f;
-      for (int i = threadIdx.x; i < m; i += blockDim.x) q = fmaf(v[i], p[i], q);
-      q = block_sumf(q, red);
+      for (int w = 0; w < nw; ++w) q += red[32 + w];
       const float K = 0.5f * t * q;
-      for (int i = threadIdx.x; i < m; i += blockDim.x) p[i] = fmaf(-K, v[i], p[i]);  // w
-      __syncthreads();
-      // A <- A - v w^T - w v^T
+      // A <- A - v w^T - w v^T with w = p - K v formed on the fly
       for (int r = warp; r < m; r += nw) {
         float* row = C + (long long)(k + 1 + r) * n + k + 1;
-        const float vr = v[r], wr = p[r];
-        for (int c = lane; c < m; c += 32) row[c] -= fmaf(vr, p[c], wr * v[c]);
+        const float vr = v[r], wr = fmaf(-K, vr, p[r]);
+        for (int c = lane; c < m; c += 32) row[c] -= fmaf(vr, fmaf(-K, v[c], p[c]), wr * v[c]);
       }
     }
     for (int i = threadIdx.x; i < m; i += blockDim.x) HV[(long long)k * n + k + 1 + i] = v[i];
@@ -579,13 +599,17 @@ __device__ inline int sturm_count32(int n, const float* d, const float* e2, floa
   if (fabsf(q) < pivmin) q = -pivmin;
   int c = q < 0.0f;
   for (int i = 1; i < n; ++i) {
-    q = d[i] - sigma - e2[i - 1] / q;
+    q = d[i] - sigma - __fdividef(e2[i - 1], q);
     if (fabsf(q) < pivmin) q = -pivmin;
     c += q < 0.0f;
   }
   return c;
 }
 
+// kSmemX: the vectors under inverse iteration live in shared memory (every
+// step of a solve reads the value the previous step wrote; from global memory
+// that is an L2 round trip per step), copied to INV at the end.
+template <bool kSmemX>
 __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __restrict__ TRIws,
                                                            double* __restrict__ INVws, int ks,
                                                            const int* __restrict__ ok) {
@@ -601,7 +625,9 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
   float* U1 = W + 2 * nn;
   float* U2 = W + 3 * nn;
   float* PV = W + 4 * nn;        // 1 where rows i and i+1 were swapped
-  float* X = W + 5 * nn;         // eigenvector of eigenvalue j in column j
+  float* Xg = W + 5 * nn;        // eigenvector of eigenvalue j in column j
+  extern __shared__ float xsm[];
+  float* X = kSmemX ? xsm : Xg;
   float lo = 3.0e38f, hi = -3.0e38f, nrm = 0.0f, emax = 0.0f;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const float di = d[i], ei = (i < n - 1) ? e[i] : 0.0f, ep = i > 0 ? e[i - 1] : 0.0f;
@@ -680,7 +706,7 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
         const float ci = es[i], an = ds[i + 1] - lm, bn = (i + 1 < n - 1) ? es[i + 1] : 0.0f;
         const long long q = (long long)i * n + j;
         if (fabsf(ci) > fabsf(ra)) {
-          const float l = ra / ci;
+          const float l = __fdividef(ra, ci);
           U0[q] = ci;
           U1[q] = an;
           U2[q] = bn;
@@ -690,7 +716,7 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
           rb = rc - l * bn;
         } else {
           const float piv = fabsf(ra) < tiny ? copysignf(tiny, ra) : ra;
-          const float l = ci / piv;
+          const float l = __fdividef(ci, piv);
           U0[q] = piv;
           U1[q] = rb;
           U2[q] = rc;
@@ -726,7 +752,7 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
         float x1 = 0.0f, x2 = 0.0f, amax = 0.0f;
         for (int i = n - 1; i >= 0; --i) {
           const long long q = (long long)i * n + j;
-          const float xi = (X[(long long)i * n + mbr] - U1[q] * x1 - U2[q] * x2) / U0[q];
+          const float xi = __fdividef(X[(long long)i * n + mbr] - U1[q] * x1 - U2[q] * x2, U0[q]);
           X[(long long)i * n + mbr] = xi;
           x2 = x1;
           x1 = xi;
@@ -751,6 +777,10 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
         for (int i = 0; i < n; ++i) X[(long long)i * n + mbr] *= inv;
       }
     }
+  }
+  if (kSmemX) {
+    __syncthreads();
+    for (long long e = threadIdx.x; e < nn; e += blockDim.x) Xg[e] = X[e];
   }
 }
 
@@ -802,6 +832,7 @@ __global__ void __launch_bounds__(kVecWarps * 32) tri_back_kernel(int n, int bat
                                                                   double* __restrict__ X,
                                                                   const int* __restrict__ ok) {
   __shared__ double vec[kVecWarps][kMaxLargeN];
+  __shared__ double rdiag[kVecWarps][kMaxLargeN];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long gw = (long long)blockIdx.x * kVecWarps + w;
   if (gw >= (long long)batch * n) return;
@@ -811,13 +842,18 @@ __global__ void __launch_bounds__(kVecWarps * 32) tri_back_kernel(int n, int bat
   const double* L = L64 + b * nn;
   const float* u = U32 + b * nn + (long long)j * n;
   double* v = vec[w];
-  for (int i = lane; i < n; i += 32) v[i] = (double)u[i];
+  double* rd = rdiag[w];
+  for (int i = lane; i < n; i += 32) {
+    v[i] = (double)u[i];
+    rd[i] = 1.0 / L[(long long)i * n + i];
+  }
   __syncwarp();
+  // L^T x = u from the bottom: once x_i is known, the lanes update the
+  // entries above it with row i of L (contiguous)
   for (int i = n - 1; i >= 0; --i) {
-    double s = 0.0;
-    for (int k = i + 1 + lane; k < n; k += 32) s = fma(L[(long long)k * n + i], v[k], s);
-    s = warp_sum64(s);
-    const double x = (v[i] - s) / L[(long long)i * n + i];
+    const double x = v[i] * rd[i];
+    const double* Li = L + (long long)i * n;
+    for (int k = lane; k < i; k += 32) v[k] = fma(-Li[k], x, v[k]);
     __syncwarp();
     if (lane == 0) v[i] = x;
     __syncwarp();
@@ -909,59 +945,111 @@ __global__ void sym_kernel(int batch, int n, const double* __restrict__ A,
   }
 }
 
-// Refinement step: lambda_i = t_ii / (1 - r_ii), delta, correction E.
-__global__ void __launch_bounds__(kThreads) refine_update_kernel(int n, const double* __restrict__ A,
-                                                                 const double* __restrict__ R,
-                                                                 const double* __restrict__ T,
-                                                                 double* __restrict__ E,
-                                                                 double* __restrict__ lam,
-                                                                 int* __restrict__ ok, int check) {
-  __shared__ double red[kThreads / 32];
-  const int b = blockIdx.x;
+// Refinement step, part 1: per 8-row block of every matrix (grid (row blocks,
+// matrices), a warp per row) lambda_i = t_ii / (1 - r_ii) and the block's
+// partial sums of |T - D|_F^2, |A|_F^2 and |R|_F^2 (in `part`, 4 doubles per
+// block, a fixed summation order).
+__global__ void __launch_bounds__(256) refine_partials_kernel(int n, const double* __restrict__ A,
+                                                              const double* __restrict__ R,
+                                                              const double* __restrict__ T,
+                                                              double* __restrict__ lam,
+                                                              double* __restrict__ part) {
+  __shared__ double red[3][8];
+  const int b = blockIdx.y, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + warp;
   const long long nn = (long long)n * n;
-  const double* Ab = A + b * nn;
-  const double* Rb = R + b * nn;
-  const double* Tb = T + b * nn;
-  double* Eb = E + b * nn;
-  double* lb = lam + (long long)b * n;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    lb[i] = Tb[(long long)i * n + i] / (1.0 - Rb[(long long)i * n + i]);
+  double od = 0.0, an = 0.0, rn = 0.0;
+  if (i < n) {
+    const double* tr = T + b * nn + (long long)i * n;
+    const double* ar = A + b * nn + (long long)i * n;
+    const double* rr = R + b * nn + (long long)i * n;
+    const double li = tr[i] / (1.0 - rr[i]);
+    if (lane == 0) lam[(long long)b * n + i] = li;
+    for (int j = lane; j < n; j += 32) {
+      const double d = tr[j] - (i == j ? li : 0.0);
+      od = fma(d, d, od);
+      an = fma(ar[j], ar[j], an);
+      rn = fma(rr[j], rr[j], rn);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    od += __shfl_xor_sync(0xffffffffu, od, o);
+    an += __shfl_xor_sync(0xffffffffu, an, o);
+    rn += __shfl_xor_sync(0xffffffffu, rn, o);
+  }
+  if (lane == 0) {
+    red[0][warp] = od;
+    red[1][warp] = an;
+    red[2][warp] = rn;
   }
   __syncthreads();
-  double od = 0.0, an = 0.0, rn = 0.0;
-  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
-    const int i = (int)(e / n), j = (int)(e % n);
-    const double d = Tb[e] - (i == j ? lb[i] : 0.0);
-    od = fma(d, d, od);
-    an = fma(Ab[e], Ab[e], an);
-    rn = fma(Rb[e], Rb[e], rn);
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[threadIdx.x][w];
+    part[((long long)b * gridDim.x + blockIdx.x) * 4 + threadIdx.x] = t;
   }
-  od = block_sum(od, red);
-  an = block_sum(an, red);
-  rn = block_sum(rn, red);
-  // Frobenius norms bound the 2-norms of Ogita and Aishima's threshold
-  const double delta = 2.0 * (sqrt(od) + sqrt(an) * sqrt(rn));
-  // last step: the X it refines must already be accurate to ~1e-7 (it is
-  // unless S is too ill-conditioned for the FP32 solve), so that this step
-  // reaches the FP64 floor; otherwise hand the matrix to the FP64 path
-  // checks 2 and 3 also bound, for every pair, how far the diagonal of T is
-  // from the eigenvalues of its 2 x 2 block (an unresolved near-degenerate
-  // pair leaves both off by ~T_ij^2 / gap although |T - D|_F is small)
+}
+
+// The pairwise check of the last two steps: per block the largest
+// t_ij^2 / (d + sqrt(d^2 + t_ij^2)), d = |lambda_j - lambda_i| / 2 (slot 3).
+__global__ void __launch_bounds__(256) refine_pairs_kernel(int n, const double* __restrict__ T,
+                                                           const double* __restrict__ lam,
+                                                           double* __restrict__ part) {
+  __shared__ double red[8];
+  const int b = blockIdx.y, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + warp;
+  const long long nn = (long long)n * n;
   double pe = 0.0;
-  if (check >= 2) {
-    for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
-      const int i = (int)(e / n), j = (int)(e % n);
-      if (i == j) continue;
-      const double d = 0.5 * fabs(lb[j] - lb[i]), t2 = Tb[e] * Tb[e];
+  if (i < n) {
+    const double* tr = T + b * nn + (long long)i * n;
+    const double* lb = lam + (long long)b * n;
+    const double li = lb[i];
+    for (int j = lane; j < n; j += 32) {
+      if (j == i) continue;
+      const double d = 0.5 * fabs(lb[j] - li), t2 = tr[j] * tr[j];
       const double q = d + sqrt(fma(d, d, t2));
       if (q > 0.0) pe = fmax(pe, t2 / q);
     }
-    pe = block_max(pe, red);
   }
-  // check 1: this step decides; 2 and 3: the last two steps, either passing
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) pe = fmax(pe, __shfl_xor_sync(0xffffffffu, pe, o));
+  if (lane == 0) red[warp] = pe;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int w = 0; w < 8; ++w) m = fmax(m, red[w]);
+    part[((long long)b * gridDim.x + blockIdx.x) * 4 + 3] = m;
+  }
+}
+
+// Refinement step, part 2 (a thread per matrix): Ogita and Aishima's
+// threshold delta (delta[b]) from the partial sums and the acceptance checks.
+__global__ void refine_final_kernel(int batch, int blocks, const double* __restrict__ part,
+                                    double* __restrict__ delta_out, int* __restrict__ ok,
+                                    int check) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  double od = 0.0, an = 0.0, rn = 0.0, pe = 0.0;
+  for (int k = 0; k < blocks; ++k) {
+    const double* q = part + ((long long)b * blocks + k) * 4;
+    od += q[0];
+    an += q[1];
+    rn += q[2];
+    if (check >= 2) pe = fmax(pe, q[3]);
+  }
+  // Frobenius norms bound the 2-norms of Ogita and Aishima's threshold
+  delta_out[b] = 2.0 * (sqrt(od) + sqrt(an) * sqrt(rn));
+  // last step: the X it refines must already be accurate to ~1e-7 (it is
+  // unless S is too ill-conditioned for the FP32 solve), so that this step
+  // reaches the FP64 floor; otherwise hand the matrix to the FP64 path.
+  // Checks 2 and 3 also bound, for every pair, how far the diagonal of T is
+  // from the eigenvalues of its 2 x 2 block (an unresolved near-degenerate
+  // pair leaves both off by ~T_ij^2 / gap although |T - D|_F is small).
+  // Check 1: this step decides; 2 and 3: the last two steps, either passing
   // suffices (at the FP64 floor of an ill-conditioned S, |R| fluctuates from
-  // step to step by orders of magnitude)
-  if (check && threadIdx.x == 0 && ok[b] != 0) {
+  // step to step by orders of magnitude).
+  if (check && ok[b] != 0) {
     const bool pass = rn <= 1e-14 && od <= 1e-14 * an && (check < 2 || pe <= 1e-12 * sqrt(an));
     if (check == 1) {
       if (!pass) ok[b] = 0;
@@ -973,16 +1061,33 @@ __global__ void __launch_bounds__(kThreads) refine_update_kernel(int n, const do
       ok[b] = 0;
     }
   }
-  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
-    const int i = (int)(e / n), j = (int)(e % n);
+}
+
+// Refinement step, part 2: the correction E over the GPU (a warp per row,
+// grid (rows / 8, matrices)).
+__global__ void __launch_bounds__(256) refine_e_kernel(int n, const double* __restrict__ R,
+                                                       const double* __restrict__ T,
+                                                       const double* __restrict__ lam,
+                                                       const double* __restrict__ delta,
+                                                       double* __restrict__ E) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const long long nn = (long long)n * n;
+  const double* rr = R + b * nn + (long long)i * n;
+  const double* tr = T + b * nn + (long long)i * n;
+  double* er = E + b * nn + (long long)i * n;
+  const double* lb = lam + (long long)b * n;
+  const double li = lb[i], dl = delta[b];
+  for (int j = lane; j < n; j += 32) {
     double v;
     if (i == j) {
-      v = 0.5 * Rb[e];
+      v = 0.5 * rr[j];
     } else {
-      const double gap = lb[j] - lb[i];
-      v = (fabs(gap) > delta) ? (Tb[e] + lb[j] * Rb[e]) / gap : 0.5 * Rb[e];
+      const double gap = lb[j] - li;
+      v = (fabs(gap) > dl) ? (tr[j] + lb[j] * rr[j]) / gap : 0.5 * rr[j];
     }
-    Eb[e] = v;
+    er[j] = v;
   }
 }
 
@@ -1123,7 +1228,8 @@ int ksplit_of(int n) { return (n + kKC - 1) / kKC; }
 long long area_doubles(int n) {
   const long long nn = (long long)n * n;
   // U^T in FP32 is reserved at every size: the path of a size is selectable
-  return (9 + ksplit_of(n)) * nn + n + 1 + (nn + 1) / 2 + 1;
+  // ... then delta and the refinement's partial sums (4 per 8-row block)
+  return (9 + ksplit_of(n)) * nn + n + 1 + (nn + 1) / 2 + 1 + 4 * ((n + 7) / 8);
 }
 
 // Path per matrix size: 0 the default (shared-memory FP32 solve up to
@@ -1142,7 +1248,7 @@ size_t smem_factor64_large(int n) {
 }
 
 size_t smem_tridiag(int n) {
-  return sizeof(float) * ((size_t)n * n + 2 * (size_t)n + 32);
+  return sizeof(float) * ((size_t)n * n + 2 * (size_t)n + 64);
 }
 
 size_t smem32(int n) {
@@ -1177,8 +1283,9 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
   if (n > kMaxN) return false;
   const int path = g_path[n].load(std::memory_order_relaxed);
   const bool large = (path == 2 || n > kMaxSmemN) && !(path == 1 && n <= kMaxSmemN);
+  int max_optin = 0;
   if (large) {
-    int dev = 0, max_optin = 0;
+    int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (smem_factor64_large(n) + 64 > (size_t)max_optin) return false;  // + static shared
@@ -1197,6 +1304,9 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
   double* lam = P + (long long)ksplit_of(n) * per;
   double* L64 = lam + (long long)batch * n;
   double* C64 = L64 + per;
+  // one double per matrix after the FP32 U^T area (within the area's spare)
+  double* dlt = reinterpret_cast<double*>(reinterpret_cast<float*>(C64 + per) + ((per + 1) & ~1LL));
+  double* part = dlt + batch;  // 4 per 8-row block of every matrix
   int* ok = ok_out;
   const int eb = (int)((per + 255) / 256 < 4096 ? (per + 255) / 256 : 4096);
   sym_kernel<<<eb, 256, 0, s>>>(batch, n, A, S, As, Ss);
@@ -1226,7 +1336,14 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
     tridiag_kernel<<<batch, kThreads, smt, s>>>(n, C64, T, R, ok);
     const int ks = ksplit_of(n);
-    tri_eig_kernel<<<batch, kThreads, 0, s>>>(n, R, P, ks, ok);
+    const size_t smx = sizeof(float) * (size_t)n * n;
+    if (smx + 8192 <= (size_t)max_optin &&
+        cudaFuncSetAttribute(tri_eig_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smx) == cudaSuccess) {
+      tri_eig_kernel<true><<<batch, kThreads, smx, s>>>(n, R, P, ks, ok);
+    } else {
+      tri_eig_kernel<false><<<batch, kThreads, 0, s>>>(n, R, P, ks, ok);
+    }
     tri_back_kernel32<<<vb, kVecWarps * 32, 0, s>>>(n, batch, T, R, P, ks, U32, ok);
     stage_done_kernel<<<(batch + 255) / 256, 256, 0, s>>>(batch, ok, 3, 4);
     tri_back_kernel<<<vb, kVecWarps * 32, 0, s>>>(n, batch, L64, U32, X, ok);
@@ -1250,7 +1367,13 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     cudaMemcpyAsync(T, E, sizeof(double) * per, cudaMemcpyDeviceToDevice, s);
     const int check = !large ? (it == steps - 1 ? 1 : 0)
                              : (it == steps - 2 ? 2 : (it == steps - 1 ? 3 : 0));
-    refine_update_kernel<<<batch, kThreads, 0, s>>>(n, As, R, T, E, lam, ok, check);
+    const dim3 rgrid((unsigned)((n + 7) / 8), (unsigned)batch);
+    refine_partials_kernel<<<rgrid, 256, 0, s>>>(n, As, R, T, lam, part);
+    if (check >= 2) refine_pairs_kernel<<<rgrid, 256, 0, s>>>(n, T, lam, part);
+    refine_final_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, (n + 7) / 8, part, dlt, ok,
+                                                            check);
+    refine_e_kernel<<<dim3((unsigned)((n + 7) / 8), (unsigned)batch), 256, 0, s>>>(n, R, T, lam, dlt,
+                                                                                  E);
     gemm(s, batch, n, false, X, E, P, X, false, 1.0, X2);         // X' = X + X E
     double* t = X;
     X = X2;

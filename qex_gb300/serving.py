@@ -11,7 +11,10 @@ the solve ends.  A 3D request replays its molecule's captured SCF graph
 history resident on the device) on a free stream; a 3D request for a
 molecule that is not resident is admitted by building it first (grid, AO
 values and integrals on the GPU, then the captured graph), and that set-up is
-part of its latency.  Admission is by device memory: a batch is admitted only
+part of its latency.  The streams split into a 1D share and a 3D share
+(``max_inflight3d``), so that neither kind of backlog holds back the other,
+and at most one new 3D molecule is built per pass of the loop.  Admission is
+by device memory: a batch is admitted only
 while its estimated bytes fit the free HBM the driver reports
 (``cudaMemGetInfo``, through ``torch.cuda.mem_get_info``, plus the memory the
 allocator caches but does not use) less a safety margin, or, when
@@ -98,7 +101,7 @@ class ScfServer:
     def __init__(self, xc, cfg: SolveConfig, max_inflight: int = 16, max_batch: int = 512,
                  memory_budget_bytes: int | None = None, engine: Ks1dEngine | None = None,
                  graphs3d: dict | None = None, builder3d=None, max_cycle3d: int = 30,
-                 hbm_margin_bytes: int = 2 << 30):
+                 hbm_margin_bytes: int = 2 << 30, max_inflight3d: int | None = None):
         self.torch = N.require_cuda()
         self.xc = xc
         self.cfg = cfg
@@ -108,6 +111,15 @@ class ScfServer:
         self.max_batch = max_batch
         self.budget = memory_budget_bytes
         self.streams = [self.torch.cuda.Stream() for _ in range(max_inflight)]
+        # the streams split into a 1D share and a 3D share, so that a 3D
+        # backlog (seconds of replays) never holds back the 1D batches and
+        # the reverse; without 3D molecules 1D has every stream
+        has3d = bool(graphs3d) or builder3d is not None
+        if max_inflight3d is None:
+            max_inflight3d = max_inflight // 2 if has3d else 0
+        if has3d and not 1 <= max_inflight3d < max_inflight:
+            raise ValueError("with 3D molecules, 1 <= max_inflight3d < max_inflight")
+        self.max_inflight3d = max_inflight3d
         self.functional, self.params = resolve(xc)
         self.spec, self._keep = self.functional.spec(self.params, _convention(cfg))
         # resident 3D molecules (captured SCF graphs) hold their memory throughout
@@ -219,60 +231,99 @@ class ScfServer:
             r.status = int(status[i])
         self.in_use -= launch.nbytes
 
-    def serve(self, requests: Sequence[Request], realtime: bool = True) -> List[Request]:
-        """Serve ``requests`` (sorted by arrival) and return them completed."""
+    def serve(self, requests: Sequence[Request], realtime: bool = True,
+              deadline: float | None = None) -> List[Request]:
+        """Serve ``requests`` (sorted by arrival) and return them.
+
+        With ``deadline`` (seconds from the start), nothing new is launched
+        after it: the work in flight completes and the requests still waiting
+        are returned unserved (``finish`` NaN), as a load test of an
+        overloaded server reports them.
+
+        Pending 1D requests wait in one FIFO, pending 3D requests in one FIFO
+        per molecule (a molecule's graph replays one request at a time), so
+        each pass of the loop costs O(batch + molecules) however long the
+        backlog grows."""
+        import collections
+
         reqs = sorted(requests, key=lambda r: r.arrival)
-        pending: List[Request] = []
+        pending1d = collections.deque()
+        pending3d = collections.OrderedDict()  # molecule -> deque of requests
         inflight: List[_Launch] = []
-        free = list(self.streams)
+        free = list(self.streams[self.max_inflight3d:])
+        free3d = list(self.streams[: self.max_inflight3d])
         nxt = 0
         t0 = time.perf_counter()
         done = 0
         while done < len(reqs):
             now = time.perf_counter() - t0
-            if not realtime and not pending and not inflight and nxt < len(reqs):
+            if deadline is not None and now > deadline:
+                for L in inflight:
+                    L.event.synchronize()
+                    self._retire(L, time.perf_counter() - t0)
+                break
+            if (not realtime and not pending1d and not pending3d and not inflight
+                    and nxt < len(reqs)):
                 now = reqs[nxt].arrival
             while nxt < len(reqs) and reqs[nxt].arrival <= now:
-                pending.append(reqs[nxt])
+                r = reqs[nxt]
+                if r.is3d:
+                    pending3d.setdefault(r.graph3d, collections.deque()).append(r)
+                else:
+                    pending1d.append(r)
                 nxt += 1
             for L in list(inflight):
                 if L.event.query():
                     self._retire(L, time.perf_counter() - t0)
                     done += len(L.requests)
                     inflight.remove(L)
-                    free.append(L.stream)
-            # 3D requests: a replay of the molecule's graph on a free stream
-            # (one replay of a graph at a time: its results are static tensors)
-            for r in [q for q in pending if q.is3d]:
-                if not free:
-                    break
-                if r.graph3d in self.busy3d:
-                    continue
-                if r.graph3d not in self.graphs3d:
-                    if self.builder3d is None:
-                        raise KeyError(f"3D molecule {r.graph3d!r} is not resident")
-                    self._ensure3d(r.graph3d)  # set-up inside this request's latency
-                    now = time.perf_counter() - t0
-                inflight.append(self._launch3d(r, free.pop(), now))
-                pending.remove(r)
-            while free and any(not q.is3d for q in pending):
-                p1d = [q for q in pending if not q.is3d]
-                take = p1d[: self.max_batch]
-                # admission by device memory: halve the batch until it fits the
-                # free budget; a single request that does not fit waits for
-                # in-flight batches to finish (or runs alone on an idle GPU)
-                while len(take) > 1 and not self._fits(self._estimate(take)):
-                    take = take[: len(take) // 2]
-                if not self._fits(self._estimate(take)) and inflight:
-                    break
-                L = self._launch(take, free.pop(), now)
-                self.in_use += L.nbytes
-                inflight.append(L)
-                taken = set(id(q) for q in take)
-                pending = [q for q in pending if id(q) not in taken]
+                    (free3d if L.graph3d is not None else free).append(L.stream)
+            self._launch1d(pending1d, free, inflight, now)
+            # 3D requests: a replay of the molecule's graph on a free 3D stream
+            # (one replay of a graph at a time: its results are static tensors);
+            # the molecule whose oldest request arrived first goes first.  At
+            # most one new molecule is built per pass (a build takes a while):
+            # the 1D requests that arrived meanwhile launch at the next pass.
+            if pending3d and free3d:
+                order = sorted((q[0].arrival, k) for k, q in pending3d.items()
+                               if k not in self.busy3d)
+                built = False
+                for _, key in order:
+                    if not free3d:
+                        break
+                    if key not in self.graphs3d:
+                        if self.builder3d is None:
+                            raise KeyError(f"3D molecule {key!r} is not resident")
+                        if built:
+                            continue
+                        self._ensure3d(key)  # set-up inside this request's latency
+                        built = True
+                        now = time.perf_counter() - t0
+                    q = pending3d[key]
+                    r = q.popleft()
+                    if not q:
+                        del pending3d[key]
+                    inflight.append(self._launch3d(r, free3d.pop(), now))
             if realtime:
                 time.sleep(0.0002)
         return reqs
+
+    def _launch1d(self, pending1d, free, inflight, now):
+        """Launch the pending 1D requests in batches while streams are free."""
+        while free and pending1d:
+            take = [pending1d[i] for i in range(min(self.max_batch, len(pending1d)))]
+            # admission by device memory: halve the batch until it fits; a
+            # single request that does not fit waits for in-flight batches
+            # to finish (or runs alone on an idle GPU)
+            while len(take) > 1 and not self._fits(self._estimate(take)):
+                take = take[: len(take) // 2]
+            if not self._fits(self._estimate(take)) and inflight:
+                break
+            L = self._launch(take, free.pop(), now)
+            self.in_use += L.nbytes
+            inflight.append(L)
+            for _ in range(len(take)):
+                pending1d.popleft()
 
     def _estimate(self, reqs: Sequence[Request]) -> int:
         n = sum(r.molecule.num_grids for r in reqs)
@@ -340,13 +391,17 @@ def mixed_requests(arrivals, keys3d: Sequence, frac3d: float = 0.2, seed: int = 
 def latency_summary(reqs: Sequence[Request], duration: float | None = None) -> dict:
     out = _summary(reqs, duration)
     if any(r.is3d for r in reqs) and not all(r.is3d for r in reqs):
-        span = out["span_s"]
+        span = out.get("span_s")
         out["1d"] = _summary([r for r in reqs if not r.is3d], span)
         out["3d"] = _summary([r for r in reqs if r.is3d], span)
     return out
 
 
 def _summary(reqs: Sequence[Request], duration: float | None = None) -> dict:
+    unserved = sum(1 for r in reqs if not np.isfinite(r.finish))
+    reqs = [r for r in reqs if np.isfinite(r.finish)]
+    if not reqs:
+        return {"requests": 0, "unserved": unserved}
     lat = np.array([r.latency for r in reqs])
     span = duration if duration else (max(r.finish for r in reqs) - min(r.arrival for r in reqs))
     # 1D: |E_T - E_T-1| < 1e-8 Ha with the status clear; 3D: the reference's
@@ -356,6 +411,7 @@ def _summary(reqs: Sequence[Request], duration: float | None = None) -> dict:
         and (r.status & 0xFFFF) == 0]
     return {
         "requests": len(reqs),
+        "unserved": unserved,
         "converged": len(conv),
         "solves_per_s": len(reqs) / span if span > 0 else float("nan"),
         "converged_solves_per_s": len(conv) / span if span > 0 else float("nan"),

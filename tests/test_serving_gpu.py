@@ -131,3 +131,40 @@ def test_new_3d_molecules_built_on_admission(srv):
         np.testing.assert_array_equal(r.energies, alone.energies.cpu().numpy())
         assert r.e_tot == float(alone.e_tot.cpu()[0])
         assert r.converged3d == bool(alone.converged.cpu()[0])
+
+
+def test_deadline_reports_unserved_requests(srv):
+    """An overloaded stream cut at its deadline: work in flight completes, the
+    requests still waiting come back unserved and the summary counts them."""
+    qex, serving, eng, cfg = srv
+    reqs = serving.config1_requests(np.zeros(64), seed=2)
+    server = serving.ScfServer(qex.LDAExpCoulomb(), cfg, max_inflight=1, max_batch=4)
+    done = server.serve(reqs, realtime=False, deadline=0.0)
+    served = [r for r in done if np.isfinite(r.finish)]
+    assert len(served) <= 4 and len(served) + sum(1 for r in done if r.energies is None) == 64
+    s = serving.latency_summary(done)
+    assert s["unserved"] == 64 - len(served)
+
+
+def test_3d_backlog_does_not_hold_back_1d(srv):
+    """The streams split into a 1D and a 3D share: with a backlog of replays of
+    one 3D molecule (they run one at a time), the 1D requests that arrive
+    beside it are all served long before the backlog drains."""
+    qex, serving, eng, cfg = srv
+    from qex_gb300.td import graph, workloads
+
+    graphs = {"a": graph.CapturedScf(workloads.synthetic_molecule(3, seed=4), max_cycle=12)}
+    three = [serving.Request(i, None, 0.0, graph3d="a") for i in range(40)]
+    one = serving.config1_requests(np.zeros(32), seed=5)
+    for i, r in enumerate(one):
+        r.rid = 100 + i
+    server = serving.ScfServer(qex.LDAExpCoulomb(), cfg, max_inflight=4, max_batch=16,
+                               graphs3d=graphs)
+    assert server.max_inflight3d == 2
+    done = server.serve(three + one, realtime=False)
+    fin1 = max(r.finish for r in done if not r.is3d)
+    fin3 = sorted(r.finish for r in done if r.is3d)
+    assert fin1 < fin3[len(fin3) // 2], (fin1, fin3[len(fin3) // 2])
+    with pytest.raises(ValueError):
+        serving.ScfServer(qex.LDAExpCoulomb(), cfg, max_inflight=2, graphs3d=graphs,
+                          max_inflight3d=2)
