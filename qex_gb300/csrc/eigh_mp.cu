@@ -349,56 +349,152 @@ __global__ void __launch_bounds__(kThreads) eigh32_fp64factor_kernel(
 
 // ---------------------------------------------------------------------------
 // Stage 1 beyond the shared-memory FP32 solver (n > 128): the same
-// mathematics as eigh32_fp64factor_kernel in four launches, so that the
-// triangular solves spread over the GPU (a warp per vector) instead of
-// running as serial chains on one SM.  ok[b]: 3 after the Cholesky, 4 after
-// the Jacobi, 2 once X is formed.
+// mathematics as eigh32_fp64factor_kernel in several launches, so that the
+// Cholesky and the triangular solves spread over the GPU (tiles, a warp per
+// vector) instead of running as serial chains on one SM.  ok[b]: 3 after the
+// Cholesky, 4 after the eigenvectors of C, 2 once X is formed.
 // ---------------------------------------------------------------------------
 constexpr int kVecWarps = 8;          // warps per CTA of the per-vector kernels
 constexpr int kMaxLargeN = 240;       // vector staging in shared memory
 
-// S = L L^T (FP64, one CTA per matrix), C64 <- A.  A and S are symmetric.
-__global__ void __launch_bounds__(kThreads) chol64_kernel(int n, const double* __restrict__ A,
-                                                          const double* __restrict__ S,
-                                                          double* __restrict__ L64,
-                                                          double* __restrict__ C64,
-                                                          int* __restrict__ ok) {
+// ---------------------------------------------------------------------------
+// Blocked FP64 Cholesky S = L L^T over the GPU (right-looking, panels of
+// kCholNb columns).  Per panel: chol_diag_kernel factors the diagonal block
+// (one CTA per matrix, one barrier per column), chol_panel_kernel solves the
+// rows below it against that block (a warp per row, the row's entries on the
+// lanes), chol_update_kernel subtracts the panel's outer product from the
+// trailing lower triangle (kCholTile x kCholTile tiles, a CTA each).  A
+// matrix whose pivot is not positive drops ok to 0 and is skipped from then
+// on (the FP64 Jacobi path applies the reference's shift).  Only the lower
+// triangle of L is written.
+// ---------------------------------------------------------------------------
+constexpr int kCholNb = 32;
+constexpr int kCholTile = 16;
+
+// 1 / sqrt(x) from the FP32 estimate and two Newton steps (FP64 accuracy;
+// an FP64 square root and divide cost ~10 dependent FP64 operations).
+__device__ __forceinline__ double rsqrt64(double x) {
+  if (!(x > 1e-30 && x < 1e30)) return 1.0 / sqrt(x);
+  double y = (double)rsqrtf((float)x);
+  const double h = 0.5 * x;
+  y = y * fma(-h * y, y, 1.5);
+  return y * fma(-h * y, y, 1.5);
+}
+
+__global__ void chol_init_kernel(int batch, int n, const double* __restrict__ A,
+                                 const double* __restrict__ S, double* __restrict__ C64,
+                                 double* __restrict__ L64, int* __restrict__ ok) {
+  const long long tot = (long long)batch * n * n;
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (long long e = g; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    C64[e] = A[e];
+    L64[e] = S[e];
+  }
+  for (long long b = g; b < batch; b += (long long)gridDim.x * blockDim.x) ok[b] = 3;
+}
+
+__global__ void __launch_bounds__(128) chol_diag_kernel(int n, int p0, double* __restrict__ L64,
+                                                        int* __restrict__ ok) {
   const int b = blockIdx.x;
-  __shared__ double piv;
-  __shared__ double colk[kMaxLargeN];  // column k of L below the diagonal
-  const long long nn = (long long)n * n;
-  double* L = L64 + b * nn;
-  double* Cd = C64 + b * nn;
-  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
-    Cd[e] = A[b * nn + e];
-    L[e] = S[b * nn + e];
+  if (ok[b] != 3) return;
+  const int w = min(kCholNb, n - p0);
+  __shared__ double D[kCholNb][kCholNb + 1];   // the block, updated in place (unscaled columns)
+  __shared__ double Lo[kCholNb][kCholNb + 1];  // the factor's columns
+  double* L = L64 + (long long)b * n * n;
+  for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+    const int i = e / w, j = e % w;
+    D[i][j] = L[(long long)(p0 + i) * n + p0 + j];
   }
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int k = 0; k < n; ++k) {
-    if (threadIdx.x == 0) {
-      const double d = L[(long long)k * n + k];
-      piv = d;
-      L[(long long)k * n + k] = d > 0.0 ? sqrt(d) : 0.0;
+  for (int j = 0; j < w; ++j) {
+    const double dj = D[j][j];
+    if (!(dj > 0.0)) {
+      if (threadIdx.x == 0) ok[b] = 0;
+      return;  // dj is the same for every thread: the whole CTA leaves
     }
-    __syncthreads();
-    if (!(piv > 0.0)) return;  // not SPD: ok stays 0, the FP64 Jacobi path applies the shift
-    const double inv = 1.0 / L[(long long)k * n + k];
-    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) {
-      const double v = L[(long long)i * n + k] * inv;
-      L[(long long)i * n + k] = v;
-      colk[i] = v;
-    }
-    __syncthreads();
-    // trailing lower triangle: a warp per row, lanes along the row
-    for (int i = k + 1 + warp; i < n; i += nw) {
-      const double lik = colk[i];
-      double* row = L + (long long)i * n;
-      for (int j = k + 1 + lane; j <= i; j += 32) row[j] = fma(-lik, colk[j], row[j]);
+    const double r = rsqrt64(dj), r2 = r * r;
+    // column j of the factor; the trailing block loses D[:, j] D[:, j]^T / dj
+    for (int i = j + threadIdx.x; i < w; i += blockDim.x) Lo[i][j] = D[i][j] * r;
+    const int m = w - j - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int i = j + 1 + e / m, l = j + 1 + e % m;
+      if (l <= i) D[i][l] = fma(-D[i][j] * r2, D[l][j], D[i][l]);
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) ok[b] = 3;
+  for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+    const int i = e / w, j = e % w;
+    if (j <= i) L[(long long)(p0 + i) * n + p0 + j] = Lo[i][j];
+  }
+}
+
+// Rows below the panel: x L_pp^T = a, a warp per row (lane l holds a_l).
+__global__ void __launch_bounds__(256) chol_panel_kernel(int n, int p0, double* __restrict__ L64,
+                                                         const int* __restrict__ ok) {
+  const int b = blockIdx.y;
+  if (ok[b] != 3) return;
+  const int w = min(kCholNb, n - p0);
+  __shared__ double D[kCholNb][kCholNb + 1];
+  __shared__ double rd[kCholNb];
+  double* L = L64 + (long long)b * n * n;
+  for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+    const int i = e / w, j = e % w;
+    D[i][j] = (j <= i) ? L[(long long)(p0 + i) * n + p0 + j] : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x < w) rd[threadIdx.x] = 1.0 / D[threadIdx.x][threadIdx.x];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = p0 + w + blockIdx.x * 8 + warp;
+  if (i >= n) return;
+  double a = (lane < w) ? L[(long long)i * n + p0 + lane] : 0.0;
+  for (int j = 0; j < w; ++j) {
+    const double xj = __shfl_sync(0xffffffffu, a, j) * rd[j];
+    if (lane == j) {
+      a = xj;
+    } else if (lane > j && lane < w) {
+      a = fma(-xj, D[lane][j], a);
+    }
+  }
+  if (lane < w) L[(long long)i * n + p0 + lane] = a;
+}
+
+// Trailing update L_ij -= sum_l L_il L_jl (l over the panel) on the tile
+// (ti, tj), tj <= ti, of the trailing lower triangle; a thread per entry.
+__global__ void __launch_bounds__(kCholTile * kCholTile) chol_update_kernel(
+    int n, int p0, double* __restrict__ L64, const int* __restrict__ ok) {
+  const int b = blockIdx.y;
+  if (ok[b] != 3) return;
+  const int w = min(kCholNb, n - p0);
+  const int t0 = p0 + w;
+  int x = blockIdx.x, ti = 0;
+  while (x > ti) {
+    x -= ti + 1;
+    ++ti;
+  }
+  const int tj = x;
+  __shared__ double Pi[kCholTile][kCholNb + 1], Pj[kCholTile][kCholNb + 1];
+  double* L = L64 + (long long)b * n * n;
+  for (int e = threadIdx.x; e < kCholTile * w; e += blockDim.x) {
+    const int r = e / w, l = e % w;
+    const int ri = t0 + ti * kCholTile + r, rj = t0 + tj * kCholTile + r;
+    Pi[r][l] = ri < n ? L[(long long)ri * n + p0 + l] : 0.0;
+    Pj[r][l] = rj < n ? L[(long long)rj * n + p0 + l] : 0.0;
+  }
+  __syncthreads();
+  const int r = threadIdx.x / kCholTile, c = threadIdx.x % kCholTile;
+  const int i = t0 + ti * kCholTile + r, j = t0 + tj * kCholTile + c;
+  if (i >= n || j > i) return;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int l = 0;
+  for (; l + 3 < w; l += 4) {
+    s0 = fma(Pi[r][l], Pj[c][l], s0);
+    s1 = fma(Pi[r][l + 1], Pj[c][l + 1], s1);
+    s2 = fma(Pi[r][l + 2], Pj[c][l + 2], s2);
+    s3 = fma(Pi[r][l + 3], Pj[c][l + 3], s3);
+  }
+  for (; l < w; ++l) s0 = fma(Pi[r][l], Pj[c][l], s0);
+  L[(long long)i * n + j] -= (s0 + s1) + (s2 + s3);
 }
 
 __device__ __forceinline__ double warp_sum64(double v) {
@@ -506,9 +602,8 @@ __global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* 
   extern __shared__ float sm[];
   const long long nn = (long long)n * n;
   float* C = sm;
-  float* v = C + nn;
-  float* p = v + n;
-  float* red = p + n;  // 32 floats
+  float* p = C + nn;  // p, then p2 (n floats each)
+  float* red = p + 2 * n;  // 64 floats
   float* HV = reinterpret_cast<float*>(HVws + b * nn);
   float* d = reinterpret_cast<float*>(TRIws + b * nn);
   float* e = d + n;
@@ -526,58 +621,106 @@ __global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* 
       C[(long long)j * n + i] = a;
     }
   __syncthreads();
-  // four block barriers per step: the reflector's norm, the complete v, the
-  // product p = tau A v with v.p, the rank-2 update
+  // Three block barriers per step.  The reflector of step k is row k right of
+  // the diagonal, x = C[k][k+1 ..], with its first entry replaced by
+  // v0 = x0 - alpha (read in place, never copied); the sum of squares of
+  // x[1 ..] comes from the previous step's update (red[48]).  Then: the
+  // product p = tau A v column by column (a thread per column, the rows in
+  // two halves, partial sums in p and p2) | p and v.p | the rank-2 update,
+  // which also sums the squares of the next step's x.
+  constexpr int kNw = kThreads / 32;
+  float* p2 = p + n;
+  if (n > 2) {
+    float s0 = 0.0f;
+    if (warp == 0)
+      for (int c = 2 + lane; c < n; c += 32) s0 = fmaf(C[c], C[c], s0);
+    s0 = warp_sumf(s0);
+    if (threadIdx.x == 0) red[48] = s0;
+  }
+  __syncthreads();
   for (int k = 0; k < n - 2; ++k) {
-    const int m = n - k - 1;  // x = C[k+1 .. n-1][k] (= row k right of the diagonal)
+    const int m = n - k - 1;
     const float* xk = C + (long long)k * n + k + 1;
-    float sq = 0.0f;
-    for (int i = 1 + threadIdx.x; i < m; i += blockDim.x) sq = fmaf(xk[i], xk[i], sq);
-    sq = warp_sumf(sq);
-    if (lane == 0) red[warp] = sq;
-    __syncthreads();
-    sq = 0.0f;
-    for (int w = 0; w < nw; ++w) sq += red[w];
+    const float sq = red[48];
     const float x0 = xk[0];
     float alpha = x0, t = 0.0f;
     if (sq > 0.0f) {
       const float nrm = sqrtf(fmaf(x0, x0, sq));
       alpha = x0 >= 0.0f ? -nrm : nrm;
-      const float v0 = x0 - alpha;
-      t = 2.0f / fmaf(v0, v0, sq);
+      const float u0 = x0 - alpha;
+      t = 2.0f / fmaf(u0, u0, sq);
     }
-    for (int i = threadIdx.x; i < m; i += blockDim.x)
-      v[i] = i == 0 ? ((t != 0.0f) ? x0 - alpha : 1.0f) : xk[i];
+    const float v0 = (t != 0.0f) ? x0 - alpha : 1.0f;
     if (threadIdx.x == 0) {
       d[k] = C[(long long)k * n + k];
       e[k] = alpha;
       tau[k] = t;
     }
-    __syncthreads();
+    for (int i = threadIdx.x; i < m; i += blockDim.x)
+      HV[(long long)k * n + k + 1 + i] = i == 0 ? v0 : xk[i];
+    float* A = C + (long long)(k + 1) * n + k + 1;  // trailing block, row stride n
     if (t != 0.0f) {
-      // p = tau A v over the trailing block, a warp per row; v.p per warp
-      float vp = 0.0f;
-      for (int r = warp; r < m; r += nw) {
-        const float* row = C + (long long)(k + 1 + r) * n + k + 1;
-        float a = 0.0f;
-        for (int c = lane; c < m; c += 32) a = fmaf(row[c], v[c], a);
-        a = t * warp_sumf(a);
-        if (lane == 0) p[r] = a;
-        vp = fmaf(v[r], a, vp);
+      {
+        const int c = threadIdx.x & 255, h = threadIdx.x >> 8;
+        const int half = (m + 1) >> 1, r0 = h * half, r1 = min(m, r0 + half);
+        if (c < m) {
+          float a0 = 0.0f, a1 = 0.0f;
+          int r = r0;
+          if (r == 0) {
+            a0 = A[c] * v0;
+            r = 1;
+          }
+          for (; r + 1 < r1; r += 2) {
+            a0 = fmaf(A[(long long)r * n + c], xk[r], a0);
+            a1 = fmaf(A[(long long)(r + 1) * n + c], xk[r + 1], a1);
+          }
+          if (r < r1) a0 = fmaf(A[(long long)r * n + c], xk[r], a0);
+          (h ? p2 : p)[c] = a0 + a1;
+        }
       }
+      __syncthreads();
+      float vp = 0.0f;
+      if (threadIdx.x < m) {
+        const int c = threadIdx.x;
+        const float pc = t * (p[c] + p2[c]);
+        p[c] = pc;
+        vp = (c == 0 ? v0 : xk[c]) * pc;
+      }
+      vp = warp_sumf(vp);
       if (lane == 0) red[32 + warp] = vp;
       __syncthreads();
       float q = 0.0f;
-      for (int w = 0; w < nw; ++w) q += red[32 + w];
+#pragma unroll
+      for (int w = 0; w < kNw; ++w) q += red[32 + w];
       const float K = 0.5f * t * q;
-      // A <- A - v w^T - w v^T with w = p - K v formed on the fly
+      // A <- A - v w^T - w v^T with w = p - K v formed on the fly; the warp
+      // of row 0 also sums the squares of its new entries 2 .. (next step)
       for (int r = warp; r < m; r += nw) {
-        float* row = C + (long long)(k + 1 + r) * n + k + 1;
-        const float vr = v[r], wr = fmaf(-K, vr, p[r]);
-        for (int c = lane; c < m; c += 32) row[c] -= fmaf(vr, fmaf(-K, v[c], p[c]), wr * v[c]);
+        float* row = A + (long long)r * n;
+        const float vr = r == 0 ? v0 : xk[r], wr = fmaf(-K, vr, p[r]);
+        float s2 = 0.0f;
+        for (int c = lane; c < m; c += 32) {
+          const float vc = c == 0 ? v0 : xk[c];
+          const float nv = row[c] - fmaf(vr, fmaf(-K, vc, p[c]), wr * vc);
+          row[c] = nv;
+          if (c >= 2) s2 = fmaf(nv, nv, s2);
+        }
+        if (r == 0) {
+          s2 = warp_sumf(s2);
+          if (lane == 0) red[48] = s2;
+        }
+      }
+    } else {
+      // no reflection: the trailing block stays; the next sum of squares
+      // from its row 0 as it is (after every thread has read red[48])
+      __syncthreads();
+      if (warp == 0) {
+        float s2 = 0.0f;
+        for (int c = 2 + lane; c < m; c += 32) s2 = fmaf(A[c], A[c], s2);
+        s2 = warp_sumf(s2);
+        if (lane == 0) red[48] = s2;
       }
     }
-    for (int i = threadIdx.x; i < m; i += blockDim.x) HV[(long long)k * n + k + 1 + i] = v[i];
     __syncthreads();
   }
   if (threadIdx.x == 0) {
@@ -737,26 +880,54 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
       for (int i = 0; i < n; ++i)
         X[(long long)i * n + mbr] = 1.0f + 0.25f * (float)((i * 7919 + mbr * 104729) % 17) / 17.0f;
       for (int it = 0; it < 3; ++it) {
-        // x <- U^-1 L^-1 P x
-        for (int i = 0; i < n - 1; ++i) {
-          const long long q = (long long)i * n + j;
-          float xi = X[(long long)i * n + mbr], xn = X[(long long)(i + 1) * n + mbr];
-          if (PV[q] != 0.0f) {
-            const float t = xi;
-            xi = xn;
-            xn = t;
+        // x <- U^-1 L^-1 P x.  The factors of kAhead steps are loaded
+        // together (independent global loads, one L2 round trip per group)
+        // before the dependent recurrence consumes them.
+        constexpr int kAhead = 16;
+        for (int i0 = 0; i0 < n - 1; i0 += kAhead) {
+          float lf[kAhead], pf[kAhead];
+#pragma unroll
+          for (int t = 0; t < kAhead; ++t) {
+            const int i = min(i0 + t, n - 2);
+            lf[t] = Lm[(long long)i * n + j];
+            pf[t] = PV[(long long)i * n + j];
           }
-          X[(long long)i * n + mbr] = xi;
-          X[(long long)(i + 1) * n + mbr] = xn - Lm[q] * xi;
+#pragma unroll
+          for (int t = 0; t < kAhead; ++t) {
+            const int i = i0 + t;
+            if (i < n - 1) {
+              float xi = X[(long long)i * n + mbr], xn = X[(long long)(i + 1) * n + mbr];
+              if (pf[t] != 0.0f) {
+                const float tt = xi;
+                xi = xn;
+                xn = tt;
+              }
+              X[(long long)i * n + mbr] = xi;
+              X[(long long)(i + 1) * n + mbr] = xn - lf[t] * xi;
+            }
+          }
         }
         float x1 = 0.0f, x2 = 0.0f, amax = 0.0f;
-        for (int i = n - 1; i >= 0; --i) {
-          const long long q = (long long)i * n + j;
-          const float xi = __fdividef(X[(long long)i * n + mbr] - U1[q] * x1 - U2[q] * x2, U0[q]);
-          X[(long long)i * n + mbr] = xi;
-          x2 = x1;
-          x1 = xi;
-          amax = fmaxf(amax, fabsf(xi));
+        for (int i0 = n - 1; i0 >= 0; i0 -= kAhead) {
+          float f0[kAhead], f1[kAhead], f2[kAhead];
+#pragma unroll
+          for (int t = 0; t < kAhead; ++t) {
+            const long long q = (long long)max(i0 - t, 0) * n + j;
+            f0[t] = U0[q];
+            f1[t] = U1[q];
+            f2[t] = U2[q];
+          }
+#pragma unroll
+          for (int t = 0; t < kAhead; ++t) {
+            const int i = i0 - t;
+            if (i >= 0) {
+              const float xi = __fdividef(X[(long long)i * n + mbr] - f1[t] * x1 - f2[t] * x2, f0[t]);
+              X[(long long)i * n + mbr] = xi;
+              x2 = x1;
+              x1 = xi;
+              amax = fmaxf(amax, fabsf(xi));
+            }
+          }
         }
         // scale, orthogonalise against the cluster's earlier vectors, normalise
         const float sc = amax > 0.0f ? 1.0f / amax : 1.0f;
@@ -1323,8 +1494,18 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     // every matrix: FP64 factor and transformation, FP32 Jacobi with C in
     // shared memory and U^T in global memory, FP64 back-transformation
     float* U32 = reinterpret_cast<float*>(C64 + per);
-    cudaMemsetAsync(ok, 0, sizeof(int) * (size_t)batch, s);
-    chol64_kernel<<<batch, kThreads, 0, s>>>(n, As, Ss, L64, C64, ok);
+    chol_init_kernel<<<eb, 256, 0, s>>>(batch, n, As, Ss, C64, L64, ok);  // ok <- 3
+    for (int p0 = 0; p0 < n; p0 += kCholNb) {
+      chol_diag_kernel<<<batch, 128, 0, s>>>(n, p0, L64, ok);
+      const int rows = n - p0 - min(kCholNb, n - p0);
+      if (rows > 0) {
+        chol_panel_kernel<<<dim3((unsigned)((rows + 7) / 8), (unsigned)batch), 256, 0, s>>>(
+            n, p0, L64, ok);
+        const int T = (rows + kCholTile - 1) / kCholTile;
+        chol_update_kernel<<<dim3((unsigned)(T * (T + 1) / 2), (unsigned)batch),
+                             kCholTile * kCholTile, 0, s>>>(n, p0, L64, ok);
+      }
+    }
     const long long vecs = (long long)batch * n;
     const unsigned vb = (unsigned)((vecs + kVecWarps - 1) / kVecWarps);
     tri_fwd_kernel<<<vb, kVecWarps * 32, 0, s>>>(n, batch, L64, C64, ok, 0);  // C <- L^-1 C
