@@ -355,7 +355,12 @@ __global__ void __launch_bounds__(kThreads) eigh32_fp64factor_kernel(
 // Cholesky, 4 after the eigenvectors of C, 2 once X is formed.
 // ---------------------------------------------------------------------------
 constexpr int kVecWarps = 8;          // warps per CTA of the per-vector kernels
+// the FP64 per-vector kernels (two warps per CTA, spreading the vectors over
+// more SMs, ran 1.6x slower: the warps of a CTA share the triangle's rows in
+// L1)
+constexpr int kVec64Warps = 8;
 constexpr int kMaxLargeN = 240;       // vector staging in shared memory
+static_assert(kMaxLargeN <= 256, "tri_eig_kernel pairs threads j and j + 256");
 
 // ---------------------------------------------------------------------------
 // Blocked FP64 Cholesky S = L L^T over the GPU (right-looking, panels of
@@ -415,10 +420,14 @@ __global__ void __launch_bounds__(128) chol_diag_kernel(int n, int p0, double* _
     const double r = rsqrt64(dj), r2 = r * r;
     // column j of the factor; the trailing block loses D[:, j] D[:, j]^T / dj
     for (int i = j + threadIdx.x; i < w; i += blockDim.x) Lo[i][j] = D[i][j] * r;
+    // the trailing lower triangle, element e -> (i, l) with e = i (i + 1) / 2 + l
     const int m = w - j - 1;
-    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-      const int i = j + 1 + e / m, l = j + 1 + e % m;
-      if (l <= i) D[i][l] = fma(-D[i][j] * r2, D[l][j], D[i][l]);
+    for (int e = threadIdx.x; e < m * (m + 1) / 2; e += blockDim.x) {
+      int ti = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+      if ((ti + 1) * (ti + 2) / 2 <= e) ++ti;
+      if (ti * (ti + 1) / 2 > e) --ti;
+      const int i = j + 1 + ti, l = j + 1 + (e - ti * (ti + 1) / 2);
+      D[i][l] = fma(-D[i][j] * r2, D[l][j], D[i][l]);
     }
     __syncthreads();
   }
@@ -503,18 +512,43 @@ __device__ __forceinline__ double warp_sum64(double v) {
   return v;
 }
 
+// Lt = L^T (the lower triangle of L to the upper of Lt), 32 x 32 tiles through
+// shared memory, so that the back-transformation reads rows of L as columns
+// of Lt (see tri_fwd_kernel on why columns).
+__global__ void __launch_bounds__(256) lt_kernel(int n, const double* __restrict__ L64,
+                                                 double* __restrict__ Lt64,
+                                                 const int* __restrict__ ok) {
+  const int b = blockIdx.z;
+  if (ok[b] != 3) return;
+  __shared__ double tile[32][33];
+  const long long nn = (long long)n * n;
+  const double* L = L64 + b * nn;
+  double* Lt = Lt64 + b * nn;
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int r = ty; r < 32; r += 8) {
+    const int i = r0 + r, k = c0 + tx;
+    tile[r][tx] = (i < n && k < n && k <= i) ? L[(long long)i * n + k] : 0.0;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int i = c0 + r, k = r0 + tx;  // Lt[i][k] = L[k][i]
+    if (i < n && k < n) Lt[(long long)i * n + k] = tile[tx][r];
+  }
+}
+
 // Forward substitution v <- L^-1 v for every column (rows = 0) or every row
 // (rows = 1) of C64: C <- L^-1 C, then C <- C L^-T.  A warp per vector, the
 // vector staged in shared memory, the dot products split over the lanes.
-__global__ void __launch_bounds__(kVecWarps * 32) tri_fwd_kernel(int n, int batch,
+__global__ void __launch_bounds__(kVec64Warps * 32) tri_fwd_kernel(int n, int batch,
                                                                  const double* __restrict__ L64,
                                                                  double* __restrict__ C64,
                                                                  const int* __restrict__ ok,
                                                                  int rows) {
-  __shared__ double vec[kVecWarps][kMaxLargeN];
-  __shared__ double rdiag[kVecWarps][kMaxLargeN];
+  __shared__ double vec[kVec64Warps][kMaxLargeN];
+  __shared__ double rdiag[kVec64Warps][kMaxLargeN];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long gw = (long long)blockIdx.x * kVecWarps + w;
+  const long long gw = (long long)blockIdx.x * kVec64Warps + w;
   if (gw >= (long long)batch * n) return;
   const int b = (int)(gw / n), j = (int)(gw % n);
   if (ok[b] != 3) return;
@@ -531,7 +565,11 @@ __global__ void __launch_bounds__(kVecWarps * 32) tri_fwd_kernel(int n, int batc
   }
   __syncwarp();
   // column-oriented substitution: once x_i is known, the lanes update the
-  // remaining entries with column i of L (no reduction on the dependent chain)
+  // remaining entries with column i of L (no reduction on the dependent
+  // chain).  Column i is read across 32 rows, whose cache lines the next 15
+  // steps read again (L1 hits; rows of a transposed copy, new lines every
+  // step, ran 1.9x slower).  The loop runs exactly over the live entries: a
+  // predicated-off FP64 instruction costs as much as a live one.
   for (int i = 0; i < n; ++i) {
     const double x = v[i] * rd[i];
     for (int k = i + 1 + lane; k < n; k += 32) v[k] = fma(-L[(long long)k * n + i], x, v[k]);
@@ -593,6 +631,13 @@ __device__ inline float warp_sumf(float v) {
   return v;
 }
 
+// Row stride of C in tridiag_kernel's shared memory: rows 16-byte aligned.
+__host__ __device__ inline int tri_ld(int n) { return (n + 3) & ~3; }
+// Row parts of tridiag_kernel's product p = A v (kThreads = 64 x kTriParts:
+// 64 float4 column groups cover 256 columns).
+constexpr int kTriParts = 8;
+static_assert(kThreads == 64 * kTriParts, "tridiag_kernel thread layout");
+
 __global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* __restrict__ C64,
                                                            double* __restrict__ HVws,
                                                            double* __restrict__ TRIws,
@@ -601,9 +646,11 @@ __global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* 
   if (ok[b] != 3) return;
   extern __shared__ float sm[];
   const long long nn = (long long)n * n;
-  float* C = sm;
-  float* p = C + nn;  // p, then p2 (n floats each)
-  float* red = p + 2 * n;  // 64 floats
+  const int ld = tri_ld(n);
+  float* C = sm;                          // n rows of ld floats
+  float* p = C + (long long)n * ld;       // p (ld floats, indexed by absolute column)
+  float* pp = p + ld;                     // kTriParts partial sums of p (ld floats each)
+  float* red = pp + kTriParts * ld;       // 64 floats
   float* HV = reinterpret_cast<float*>(HVws + b * nn);
   float* d = reinterpret_cast<float*>(TRIws + b * nn);
   float* e = d + n;
@@ -612,37 +659,39 @@ __global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   // C in FP32, rows read coalesced, then symmetrised in shared memory
   for (int i = warp; i < n; i += nw)
-    for (int j = lane; j < n; j += 32) C[(long long)i * n + j] = (float)Cd[(long long)i * n + j];
+    for (int j = lane; j < ld; j += 32)
+      C[(long long)i * ld + j] = j < n ? (float)Cd[(long long)i * n + j] : 0.0f;
   __syncthreads();
   for (int i = warp; i < n; i += nw)
     for (int j = i + 1 + lane; j < n; j += 32) {
-      const float a = 0.5f * (C[(long long)i * n + j] + C[(long long)j * n + i]);
-      C[(long long)i * n + j] = a;
-      C[(long long)j * n + i] = a;
+      const float a = 0.5f * (C[(long long)i * ld + j] + C[(long long)j * ld + i]);
+      C[(long long)i * ld + j] = a;
+      C[(long long)j * ld + i] = a;
     }
+  if (n > 2 && warp == 0) {
+    float s0 = 0.0f;
+    for (int c = 2 + lane; c < n; c += 32) {
+      const float x = 0.5f * (Cd[c] + Cd[(long long)c * n]);
+      s0 = fmaf(x, x, s0);
+    }
+    s0 = warp_sumf(s0);
+    if (lane == 0) red[48] = s0;
+  }
   __syncthreads();
   // Three block barriers per step.  The reflector of step k is row k right of
   // the diagonal, x = C[k][k+1 ..], with its first entry replaced by
-  // v0 = x0 - alpha (read in place, never copied); the sum of squares of
-  // x[1 ..] comes from the previous step's update (red[48]).  Then: the
-  // product p = tau A v column by column (a thread per column, the rows in
-  // two halves, partial sums in p and p2) | p and v.p | the rank-2 update,
-  // which also sums the squares of the next step's x.
-  constexpr int kNw = kThreads / 32;
-  float* p2 = p + n;
-  if (n > 2) {
-    float s0 = 0.0f;
-    if (warp == 0)
-      for (int c = 2 + lane; c < n; c += 32) s0 = fmaf(C[c], C[c], s0);
-    s0 = warp_sumf(s0);
-    if (threadIdx.x == 0) red[48] = s0;
-  }
-  __syncthreads();
+  // v0 = x0 - alpha (read in place); the sum of squares of x[1 ..] comes from
+  // the previous step's update (red[48]).  Then: p = tau A v, a thread per
+  // column over half of the rows (partial sums in p and p2) | p and v.p | the
+  // rank-2 update, a warp per row with float4 column groups whose v and
+  // w = p - K v each lane keeps in registers (columns outside the trailing
+  // block have v = w = 0 and are left unchanged); the warp of the next row
+  // also sums the squares of its new entries for the next step's norm.
   for (int k = 0; k < n - 2; ++k) {
     const int m = n - k - 1;
-    const float* xk = C + (long long)k * n + k + 1;
+    const float* rk = C + (long long)k * ld;  // row k; x = rk[k + 1 ..]
     const float sq = red[48];
-    const float x0 = xk[0];
+    const float x0 = rk[k + 1];
     float alpha = x0, t = 0.0f;
     if (sq > 0.0f) {
       const float nrm = sqrtf(fmaf(x0, x0, sq));
@@ -652,71 +701,110 @@ __global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* 
     }
     const float v0 = (t != 0.0f) ? x0 - alpha : 1.0f;
     if (threadIdx.x == 0) {
-      d[k] = C[(long long)k * n + k];
+      d[k] = rk[k];
       e[k] = alpha;
       tau[k] = t;
     }
     for (int i = threadIdx.x; i < m; i += blockDim.x)
-      HV[(long long)k * n + k + 1 + i] = i == 0 ? v0 : xk[i];
-    float* A = C + (long long)(k + 1) * n + k + 1;  // trailing block, row stride n
+      HV[(long long)k * n + k + 1 + i] = i == 0 ? v0 : rk[k + 1 + i];
     if (t != 0.0f) {
       {
-        const int c = threadIdx.x & 255, h = threadIdx.x >> 8;
-        const int half = (m + 1) >> 1, r0 = h * half, r1 = min(m, r0 + half);
-        if (c < m) {
-          float a0 = 0.0f, a1 = 0.0f;
-          int r = r0;
-          if (r == 0) {
-            a0 = A[c] * v0;
-            r = 1;
+        // p = A v over the trailing block: a thread per float4 column group
+        // (from the one holding column k + 1) and part of the rows; the
+        // dead columns left of k + 1 in the first group are never used
+        const int g0 = (k + 1) >> 2, G = ld >> 2;
+        const int g = g0 + (threadIdx.x & 63), part = threadIdx.x >> 6;
+        if (g < G) {
+          const int rp = (m + kTriParts - 1) / kTriParts;
+          const int i0 = k + 1 + part * rp, i1 = min(n, i0 + rp);
+          float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          const float4* col = reinterpret_cast<const float4*>(C) + g;
+          for (int i = i0; i < i1; ++i) {
+            const float vi = i == k + 1 ? v0 : rk[i];
+            const float4 a4 = col[(long long)i * (ld >> 2)];
+            acc.x = fmaf(a4.x, vi, acc.x);
+            acc.y = fmaf(a4.y, vi, acc.y);
+            acc.z = fmaf(a4.z, vi, acc.z);
+            acc.w = fmaf(a4.w, vi, acc.w);
           }
-          for (; r + 1 < r1; r += 2) {
-            a0 = fmaf(A[(long long)r * n + c], xk[r], a0);
-            a1 = fmaf(A[(long long)(r + 1) * n + c], xk[r + 1], a1);
-          }
-          if (r < r1) a0 = fmaf(A[(long long)r * n + c], xk[r], a0);
-          (h ? p2 : p)[c] = a0 + a1;
+          reinterpret_cast<float4*>(pp + part * ld)[g] = acc;
         }
       }
       __syncthreads();
       float vp = 0.0f;
       if (threadIdx.x < m) {
-        const int c = threadIdx.x;
-        const float pc = t * (p[c] + p2[c]);
-        p[c] = pc;
-        vp = (c == 0 ? v0 : xk[c]) * pc;
+        const int j = k + 1 + threadIdx.x;
+        float sum = 0.0f;
+#pragma unroll
+        for (int q = 0; q < kTriParts; ++q) sum += pp[q * ld + j];
+        const float pc = t * sum;
+        p[j] = pc;
+        vp = (threadIdx.x == 0 ? v0 : rk[j]) * pc;
       }
       vp = warp_sumf(vp);
       if (lane == 0) red[32 + warp] = vp;
       __syncthreads();
       float q = 0.0f;
 #pragma unroll
-      for (int w = 0; w < kNw; ++w) q += red[32 + w];
+      for (int w = 0; w < kThreads / 32; ++w) q += red[32 + w];
       const float K = 0.5f * t * q;
-      // A <- A - v w^T - w v^T with w = p - K v formed on the fly; the warp
-      // of row 0 also sums the squares of its new entries 2 .. (next step)
-      for (int r = warp; r < m; r += nw) {
-        float* row = A + (long long)r * n;
-        const float vr = r == 0 ? v0 : xk[r], wr = fmaf(-K, vr, p[r]);
-        float s2 = 0.0f;
-        for (int c = lane; c < m; c += 32) {
-          const float vc = c == 0 ? v0 : xk[c];
-          const float nv = row[c] - fmaf(vr, fmaf(-K, vc, p[c]), wr * vc);
-          row[c] = nv;
-          if (c >= 2) s2 = fmaf(nv, nv, s2);
+      // this lane's column groups g = g0 + lane + 32 u (columns 4g .. 4g+3)
+      const int g0 = (k + 1) >> 2, G = ld >> 2;
+      float4 vc[2], wc[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int g = g0 + lane + 32 * u;
+        float vv[4] = {0.0f, 0.0f, 0.0f, 0.0f}, ww[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (g < G) {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int j = 4 * g + c;
+            if (j > k && j < n) {
+              vv[c] = j == k + 1 ? v0 : rk[j];
+              ww[c] = fmaf(-K, vv[c], p[j]);
+            }
+          }
         }
-        if (r == 0) {
+        vc[u] = make_float4(vv[0], vv[1], vv[2], vv[3]);
+        wc[u] = make_float4(ww[0], ww[1], ww[2], ww[3]);
+      }
+      for (int i = k + 1 + warp; i < n; i += nw) {
+        const float vr = i == k + 1 ? v0 : rk[i];
+        const float wr = fmaf(-K, vr, p[i]);
+        float s2 = 0.0f;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int g = g0 + lane + 32 * u;
+          if (g < G) {
+            float4* ap = reinterpret_cast<float4*>(C + (long long)i * ld) + g;
+            float4 a = *ap;
+            a.x = fmaf(-vr, wc[u].x, fmaf(-wr, vc[u].x, a.x));
+            a.y = fmaf(-vr, wc[u].y, fmaf(-wr, vc[u].y, a.y));
+            a.z = fmaf(-vr, wc[u].z, fmaf(-wr, vc[u].z, a.z));
+            a.w = fmaf(-vr, wc[u].w, fmaf(-wr, vc[u].w, a.w));
+            *ap = a;
+            if (i == k + 1) {
+              const int j = 4 * g;
+              if (j + 0 >= k + 3 && j + 0 < n) s2 = fmaf(a.x, a.x, s2);
+              if (j + 1 >= k + 3 && j + 1 < n) s2 = fmaf(a.y, a.y, s2);
+              if (j + 2 >= k + 3 && j + 2 < n) s2 = fmaf(a.z, a.z, s2);
+              if (j + 3 >= k + 3 && j + 3 < n) s2 = fmaf(a.w, a.w, s2);
+            }
+          }
+        }
+        if (i == k + 1) {
           s2 = warp_sumf(s2);
           if (lane == 0) red[48] = s2;
         }
       }
     } else {
       // no reflection: the trailing block stays; the next sum of squares
-      // from its row 0 as it is (after every thread has read red[48])
+      // from row k + 1 as it is (after every thread has read red[48])
       __syncthreads();
       if (warp == 0) {
         float s2 = 0.0f;
-        for (int c = 2 + lane; c < m; c += 32) s2 = fmaf(A[c], A[c], s2);
+        const float* r1 = C + (long long)(k + 1) * ld;
+        for (int c = k + 3 + lane; c < n; c += 32) s2 = fmaf(r1[c], r1[c], s2);
         s2 = warp_sumf(s2);
         if (lane == 0) red[48] = s2;
       }
@@ -725,11 +813,11 @@ __global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* 
   }
   if (threadIdx.x == 0) {
     if (n >= 2) {
-      d[n - 2] = C[(long long)(n - 2) * n + n - 2];
-      e[n - 2] = C[(long long)(n - 1) * n + n - 2];
+      d[n - 2] = C[(long long)(n - 2) * ld + n - 2];
+      e[n - 2] = C[(long long)(n - 1) * ld + n - 2];
       tau[n - 2] = 0.0f;
     }
-    d[n - 1] = C[(long long)(n - 1) * n + n - 1];
+    d[n - 1] = C[(long long)(n - 1) * ld + n - 1];
     e[n - 1] = 0.0f;
     tau[n - 1] = 0.0f;
   }
@@ -738,15 +826,41 @@ __global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* 
 // Number of eigenvalues of T below sigma (signs of the L D L^T pivots).
 __device__ inline int sturm_count32(int n, const float* d, const float* e2, float sigma,
                                     float pivmin) {
-  float q = d[0] - sigma;
-  if (fabsf(q) < pivmin) q = -pivmin;
-  int c = q < 0.0f;
+  float qv = d[0] - sigma;
+  if (fabsf(qv) < pivmin) qv = -pivmin;
+  int c = qv < 0.0f;
   for (int i = 1; i < n; ++i) {
-    q = d[i] - sigma - __fdividef(e2[i - 1], q);
-    if (fabsf(q) < pivmin) q = -pivmin;
-    c += q < 0.0f;
+    qv = d[i] - sigma - __fdividef(e2[i - 1], qv);
+    if (fabsf(qv) < pivmin) qv = -pivmin;
+    c += qv < 0.0f;
   }
   return c;
+}
+
+// Numbers of eigenvalues of T below three shifts, their recurrences
+// interleaved.
+__device__ inline void sturm_count32x3(int n, const float* d, const float* e2, float s0, float s1,
+                                       float s2, float pivmin, int& c0, int& c1, int& c2) {
+  float q0 = d[0] - s0, q1 = d[0] - s1, q2 = d[0] - s2;
+  if (fabsf(q0) < pivmin) q0 = -pivmin;
+  if (fabsf(q1) < pivmin) q1 = -pivmin;
+  if (fabsf(q2) < pivmin) q2 = -pivmin;
+  int k0 = q0 < 0.0f, k1 = q1 < 0.0f, k2 = q2 < 0.0f;
+  for (int i = 1; i < n; ++i) {
+    const float di = d[i], ei = e2[i - 1];
+    q0 = di - s0 - __fdividef(ei, q0);
+    q1 = di - s1 - __fdividef(ei, q1);
+    q2 = di - s2 - __fdividef(ei, q2);
+    if (fabsf(q0) < pivmin) q0 = -pivmin;
+    if (fabsf(q1) < pivmin) q1 = -pivmin;
+    if (fabsf(q2) < pivmin) q2 = -pivmin;
+    k0 += q0 < 0.0f;
+    k1 += q1 < 0.0f;
+    k2 += q2 < 0.0f;
+  }
+  c0 = k0;
+  c1 = k1;
+  c2 = k2;
 }
 
 // kSmemX: the vectors under inverse iteration live in shared memory (every
@@ -764,7 +878,7 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
   const float* e = d + n;
   float* W = reinterpret_cast<float*>(INVws + b * (long long)ks * nn);
   float* Lm = W;                 // multipliers
-  float* U0 = W + nn;            // U diagonal, first and second superdiagonals
+  float* U0 = W + nn;            // 1 / (U diagonal); U first and second superdiagonals
   float* U1 = W + 2 * nn;
   float* U2 = W + 3 * nn;
   float* PV = W + 4 * nn;        // 1 where rows i and i+1 were swapped
@@ -814,21 +928,59 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
   const float span = fmaxf(hi - lo, nrm * 1e-6f);
   lo -= 2.0f * FLT_EPSILON * span + pivmin;
   hi += 2.0f * FLT_EPSILON * span + pivmin;
-  // eigenvalue j by bisection (ascending)
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    float a = lo, c = hi;
-    for (int it = 0; it < 80; ++it) {
-      const float mid = 0.5f * (a + c);
-      if (mid <= a || mid >= c || c - a <= 2.0f * FLT_EPSILON * fmaxf(fabsf(a), fabsf(c)) + pivmin)
-        break;
-      if (sturm_count32(n, ds, e2, mid, pivmin) > j) {
-        c = mid;
+  // Eigenvalue j (ascending) on threads j and j + 256 (n <= 256).  One pass of
+  // counts at kThreads evenly spaced shifts (a thread each) brackets every
+  // eigenvalue to (hi - lo) / kThreads; then octasection, the pair's six
+  // interior shifts per pass (three each, their recurrences interleaved), to
+  // an absolute width of 4 eps |T| (the shifts of the inverse iteration need
+  // no more; the FP64 refinement recomputes the eigenvalues).
+  __shared__ int hist[kThreads];
+  __shared__ int oct[256][6];
+  const float atol = 4.0f * FLT_EPSILON * nrm + pivmin;
+  const float bw = (hi - lo) / (float)kThreads;
+  hist[threadIdx.x] = sturm_count32(
+      n, ds, e2, threadIdx.x + 1 == kThreads ? hi : fmaf(bw, (float)(threadIdx.x + 1), lo),
+      pivmin);
+  __syncthreads();
+  const int jj = threadIdx.x & 255, q = threadIdx.x >> 8;
+  float a = lo, c = hi;
+  if (jj < n) {
+    int l0 = 0, h0 = kThreads - 1;  // the smallest t with hist[t] > jj
+    while (l0 < h0) {
+      const int mid = (l0 + h0) >> 1;
+      if (hist[mid] > jj) {
+        h0 = mid;
       } else {
-        a = mid;
+        l0 = mid + 1;
       }
     }
-    lam[j] = 0.5f * (a + c);
+    a = l0 == 0 ? lo : fmaf(bw, (float)l0, lo);
+    c = l0 + 1 == kThreads ? hi : fmaf(bw, (float)(l0 + 1), lo);
   }
+  int passes = 0;
+  for (float wd = bw; wd > atol && passes < 16; wd *= 0.125f) ++passes;
+  for (int it = 0; it < passes; ++it) {
+    const float h = (c - a) * (1.0f / 7.0f);
+    if (jj < n) {
+      int n0, n1, n2;
+      sturm_count32x3(n, ds, e2, fmaf(h, (float)(1 + 3 * q), a), fmaf(h, (float)(2 + 3 * q), a),
+                      fmaf(h, (float)(3 + 3 * q), a), pivmin, n0, n1, n2);
+      oct[jj][3 * q] = n0;
+      oct[jj][3 * q + 1] = n1;
+      oct[jj][3 * q + 2] = n2;
+    }
+    __syncthreads();
+    if (jj < n) {
+      // both threads of the pair take the same sub-interval
+      int mm = 1;
+      while (mm <= 6 && oct[jj][mm - 1] <= jj) ++mm;
+      const float na = mm == 1 ? a : fmaf(h, (float)(mm - 1), a);
+      if (mm <= 6) c = fmaf(h, (float)mm, a);
+      a = na;
+    }
+    __syncthreads();
+  }
+  if (jj < n && q == 0) lam[jj] = 0.5f * (a + c);
   __syncthreads();
   // inverse iteration; a cluster's first thread computes its vectors in turn
   const float ctol = 1e-5f * nrm;
@@ -850,7 +1002,7 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
         const long long q = (long long)i * n + j;
         if (fabsf(ci) > fabsf(ra)) {
           const float l = __fdividef(ra, ci);
-          U0[q] = ci;
+          U0[q] = __frcp_rn(ci);
           U1[q] = an;
           U2[q] = bn;
           Lm[q] = l;
@@ -860,7 +1012,7 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
         } else {
           const float piv = fabsf(ra) < tiny ? copysignf(tiny, ra) : ra;
           const float l = __fdividef(ci, piv);
-          U0[q] = piv;
+          U0[q] = __frcp_rn(piv);
           U1[q] = rb;
           U2[q] = rc;
           Lm[q] = l;
@@ -872,7 +1024,7 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
       }
       {
         const long long q = (long long)(n - 1) * n + j;
-        U0[q] = fabsf(ra) < tiny ? copysignf(tiny, ra) : ra;
+        U0[q] = __frcp_rn(fabsf(ra) < tiny ? copysignf(tiny, ra) : ra);
         U1[q] = 0.0f;
         U2[q] = 0.0f;
       }
@@ -884,6 +1036,7 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
         // together (independent global loads, one L2 round trip per group)
         // before the dependent recurrence consumes them.
         constexpr int kAhead = 16;
+        float cur = X[mbr];
         for (int i0 = 0; i0 < n - 1; i0 += kAhead) {
           float lf[kAhead], pf[kAhead];
 #pragma unroll
@@ -896,17 +1049,19 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
           for (int t = 0; t < kAhead; ++t) {
             const int i = i0 + t;
             if (i < n - 1) {
-              float xi = X[(long long)i * n + mbr], xn = X[(long long)(i + 1) * n + mbr];
+              // cur: entry i as updated by step i - 1 (carried in a register)
+              float xi = cur, xn = X[(long long)(i + 1) * n + mbr];
               if (pf[t] != 0.0f) {
                 const float tt = xi;
                 xi = xn;
                 xn = tt;
               }
               X[(long long)i * n + mbr] = xi;
-              X[(long long)(i + 1) * n + mbr] = xn - lf[t] * xi;
+              cur = xn - lf[t] * xi;
             }
           }
         }
+        X[(long long)(n - 1) * n + mbr] = cur;
         float x1 = 0.0f, x2 = 0.0f, amax = 0.0f;
         for (int i0 = n - 1; i0 >= 0; i0 -= kAhead) {
           float f0[kAhead], f1[kAhead], f2[kAhead];
@@ -921,7 +1076,7 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
           for (int t = 0; t < kAhead; ++t) {
             const int i = i0 - t;
             if (i >= 0) {
-              const float xi = __fdividef(X[(long long)i * n + mbr] - f1[t] * x1 - f2[t] * x2, f0[t]);
+              const float xi = (X[(long long)i * n + mbr] - f1[t] * x1 - f2[t] * x2) * f0[t];
               X[(long long)i * n + mbr] = xi;
               x2 = x1;
               x1 = xi;
@@ -964,7 +1119,6 @@ __global__ void __launch_bounds__(kVecWarps * 32) tri_back_kernel32(int n, int b
                                                                     int ks,
                                                                     float* __restrict__ U32,
                                                                     const int* __restrict__ ok) {
-  __shared__ float z[kVecWarps][kMaxLargeN];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long gw = (long long)blockIdx.x * kVecWarps + w;
   if (gw >= (long long)batch * n) return;
@@ -974,21 +1128,53 @@ __global__ void __launch_bounds__(kVecWarps * 32) tri_back_kernel32(int n, int b
   const float* HV = reinterpret_cast<const float*>(HVws + b * nn);
   const float* tau = reinterpret_cast<const float*>(TRIws + b * nn) + 2 * n;
   const float* X = reinterpret_cast<const float*>(INVws + b * (long long)ks * nn) + 5 * nn;
-  float* zz = z[w];
-  for (int i = lane; i < n; i += 32) zz[i] = X[(long long)i * n + j];
-  __syncwarp();
+  // z in registers (entry lane + 32 t), the reflectors read one step ahead
+  constexpr int kPer = (kMaxLargeN + 31) / 32;
+  float zr[kPer], cv[kPer], nv[kPer];
+#pragma unroll
+  for (int t = 0; t < kPer; ++t) {
+    const int i = lane + 32 * t;
+    zr[t] = i < n ? X[(long long)i * n + j] : 0.0f;
+  }
+  if (n < 3) {
+    float* u = U32 + b * nn + (long long)j * n;
+#pragma unroll
+    for (int t = 0; t < kPer; ++t)
+      if (lane + 32 * t < n) u[lane + 32 * t] = zr[t];
+    return;
+  }
+  float ct = tau[n - 3], nt = 0.0f;
+#pragma unroll
+  for (int t = 0; t < kPer; ++t) {
+    const int i = lane + 32 * t;
+    cv[t] = (i > n - 3 && i < n) ? HV[(long long)(n - 3) * n + i] : 0.0f;
+  }
   for (int k = n - 3; k >= 0; --k) {
-    const float t = tau[k];
-    if (t == 0.0f) continue;
-    const float* v = HV + (long long)k * n;
-    float a = 0.0f;
-    for (int i = k + 1 + lane; i < n; i += 32) a = fmaf(v[i], zz[i], a);
-    a = t * warp_sumf(a);
-    for (int i = k + 1 + lane; i < n; i += 32) zz[i] = fmaf(-a, v[i], zz[i]);
-    __syncwarp();
+    if (k > 0) {
+      const float* vn = HV + (long long)(k - 1) * n;
+      nt = tau[k - 1];
+#pragma unroll
+      for (int t = 0; t < kPer; ++t) {
+        const int i = lane + 32 * t;
+        nv[t] = (i > k - 1 && i < n) ? vn[i] : 0.0f;
+      }
+    }
+    if (ct != 0.0f) {
+      float a = 0.0f;
+#pragma unroll
+      for (int t = 0; t < kPer; ++t) a = fmaf(cv[t], zr[t], a);
+      a = ct * warp_sumf(a);
+#pragma unroll
+      for (int t = 0; t < kPer; ++t) zr[t] = fmaf(-a, cv[t], zr[t]);
+    }
+    ct = nt;
+#pragma unroll
+    for (int t = 0; t < kPer; ++t) cv[t] = nv[t];
   }
   float* u = U32 + b * nn + (long long)j * n;
-  for (int i = lane; i < n; i += 32) u[i] = zz[i];
+#pragma unroll
+  for (int t = 0; t < kPer; ++t)
+    if (lane + 32 * t < n) u[lane + 32 * t] = zr[t];
 }
 
 __global__ void stage_done_kernel(int batch, int* __restrict__ ok, int from, int to) {
@@ -997,34 +1183,34 @@ __global__ void stage_done_kernel(int batch, int* __restrict__ ok, int from, int
 }
 
 // X[:, j] = L^-T u_j (backward substitution, FP64), u_j = row j of U^T.
-__global__ void __launch_bounds__(kVecWarps * 32) tri_back_kernel(int n, int batch,
-                                                                  const double* __restrict__ L64,
+__global__ void __launch_bounds__(kVec64Warps * 32) tri_back_kernel(int n, int batch,
+                                                                  const double* __restrict__ Lt64,
                                                                   const float* __restrict__ U32,
                                                                   double* __restrict__ X,
                                                                   const int* __restrict__ ok) {
-  __shared__ double vec[kVecWarps][kMaxLargeN];
-  __shared__ double rdiag[kVecWarps][kMaxLargeN];
+  __shared__ double vec[kVec64Warps][kMaxLargeN];
+  __shared__ double rdiag[kVec64Warps][kMaxLargeN];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long gw = (long long)blockIdx.x * kVecWarps + w;
+  const long long gw = (long long)blockIdx.x * kVec64Warps + w;
   if (gw >= (long long)batch * n) return;
   const int b = (int)(gw / n), j = (int)(gw % n);
   if (ok[b] != 4) return;
   const long long nn = (long long)n * n;
-  const double* L = L64 + b * nn;
+  const double* Lt = Lt64 + b * nn;
   const float* u = U32 + b * nn + (long long)j * n;
   double* v = vec[w];
   double* rd = rdiag[w];
   for (int i = lane; i < n; i += 32) {
     v[i] = (double)u[i];
-    rd[i] = 1.0 / L[(long long)i * n + i];
+    rd[i] = 1.0 / Lt[(long long)i * n + i];
   }
   __syncwarp();
   // L^T x = u from the bottom: once x_i is known, the lanes update the
-  // entries above it with row i of L (contiguous)
+  // entries above it with row i of L, read as column i of Lt = L^T (32 rows
+  // of Lt whose cache lines the next steps read again)
   for (int i = n - 1; i >= 0; --i) {
     const double x = v[i] * rd[i];
-    const double* Li = L + (long long)i * n;
-    for (int k = lane; k < i; k += 32) v[k] = fma(-Li[k], x, v[k]);
+    for (int k = lane; k < i; k += 32) v[k] = fma(-Lt[(long long)k * n + i], x, v[k]);
     __syncwarp();
     if (lane == 0) v[i] = x;
     __syncwarp();
@@ -1040,15 +1226,24 @@ __global__ void large_done_kernel(int batch, int* __restrict__ ok) {
 
 // Batched split-K FP64 GEMM partials: P[b][kc] = op(A_b)[:, kc chunk] B_b[kc chunk, :]
 // (n x n, op = transpose with kTA).  grid (tiles, tiles, batch * ksplit).
+// Early acceptance: a step whose check passes (X accurate to ~1e-7) sets
+// kDoneNext; that step's update X' = X + X E still runs (it brings X to the
+// FP64 floor, as the last step does), then kDone replaces kDoneNext and the
+// remaining steps skip the matrix (their update X' = X + X E copies X).
+constexpr int kDone = 16;
+constexpr int kDoneNext = 32;
+
 template <bool kTA>
 __global__ void __launch_bounds__(kGThreads) gemm_part_kernel(int n, int ksplit,
                                                               const double* __restrict__ A,
                                                               const double* __restrict__ B,
-                                                              double* __restrict__ P) {
+                                                              double* __restrict__ P,
+                                                              const int* __restrict__ skip) {
   __shared__ double As[kKC][kT + 1];
   __shared__ double Bs[kKC][kT + 1];
   const long long nn = (long long)n * n;
   const int b = blockIdx.z / ksplit, kc = blockIdx.z % ksplit;
+  if (skip && (skip[b] & kDone)) return;
   const int r0 = blockIdx.y * kT, c0 = blockIdx.x * kT;
   const int k0 = kc * kKC;
   const double* Ab = A + b * nn;
@@ -1090,11 +1285,16 @@ __global__ void __launch_bounds__(kGThreads) gemm_part_kernel(int n, int ksplit,
 // C_b = base + sign * sum_kc P[b][kc] (fixed order).  base: kIdentity -> I,
 // else the matrix `base` (may be null: 0).
 __global__ void gemm_sum_kernel(int batch, int n, int ksplit, const double* __restrict__ P,
-                                const double* base, bool identity, double sign, double* C) {
+                                const double* base, bool identity, double sign, double* C,
+                                const int* __restrict__ skip) {
   const long long nn = (long long)n * n;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < batch * nn;
        e += (long long)gridDim.x * blockDim.x) {
     const long long b = e / nn, o = e % nn;
+    if (skip && (skip[b] & kDone)) {
+      if (base && !identity) C[e] = base[e];
+      continue;
+    }
     double s = 0.0;
     for (int kc = 0; kc < ksplit; ++kc) s += P[(b * ksplit + kc) * nn + o];
     double v = identity ? ((o / n == o % n) ? 1.0 : 0.0) : (base ? base[e] : 0.0);
@@ -1116,6 +1316,12 @@ __global__ void sym_kernel(int batch, int n, const double* __restrict__ A,
   }
 }
 
+// kDoneNext -> kDone once the accepting step's update has run.
+__global__ void done_next_kernel(int batch, int* __restrict__ ok) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < batch && (ok[b] & kDoneNext)) ok[b] = (ok[b] & ~kDoneNext) | kDone;
+}
+
 // Refinement step, part 1: per 8-row block of every matrix (grid (row blocks,
 // matrices), a warp per row) lambda_i = t_ii / (1 - r_ii) and the block's
 // partial sums of |T - D|_F^2, |A|_F^2 and |R|_F^2 (in `part`, 4 doubles per
@@ -1124,9 +1330,11 @@ __global__ void __launch_bounds__(256) refine_partials_kernel(int n, const doubl
                                                               const double* __restrict__ R,
                                                               const double* __restrict__ T,
                                                               double* __restrict__ lam,
-                                                              double* __restrict__ part) {
+                                                              double* __restrict__ part,
+                                                              const int* __restrict__ ok) {
   __shared__ double red[3][8];
   const int b = blockIdx.y, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (ok[b] & kDone) return;
   const int i = blockIdx.x * 8 + warp;
   const long long nn = (long long)n * n;
   double od = 0.0, an = 0.0, rn = 0.0;
@@ -1166,9 +1374,11 @@ __global__ void __launch_bounds__(256) refine_partials_kernel(int n, const doubl
 // t_ij^2 / (d + sqrt(d^2 + t_ij^2)), d = |lambda_j - lambda_i| / 2 (slot 3).
 __global__ void __launch_bounds__(256) refine_pairs_kernel(int n, const double* __restrict__ T,
                                                            const double* __restrict__ lam,
-                                                           double* __restrict__ part) {
+                                                           double* __restrict__ part,
+                                                           const int* __restrict__ ok) {
   __shared__ double red[8];
   const int b = blockIdx.y, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (ok[b] & kDone) return;
   const int i = blockIdx.x * 8 + warp;
   const long long nn = (long long)n * n;
   double pe = 0.0;
@@ -1200,7 +1410,7 @@ __global__ void refine_final_kernel(int batch, int blocks, const double* __restr
                                     double* __restrict__ delta_out, int* __restrict__ ok,
                                     int check) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= batch) return;
+  if (b >= batch || (ok[b] & kDone)) return;
   double od = 0.0, an = 0.0, rn = 0.0, pe = 0.0;
   for (int k = 0; k < blocks; ++k) {
     const double* q = part + ((long long)b * blocks + k) * 4;
@@ -1219,11 +1429,14 @@ __global__ void refine_final_kernel(int batch, int blocks, const double* __restr
   // pair leaves both off by ~T_ij^2 / gap although |T - D|_F is small).
   // Check 1: this step decides; 2 and 3: the last two steps, either passing
   // suffices (at the FP64 floor of an ill-conditioned S, |R| fluctuates from
-  // step to step by orders of magnitude).
+  // step to step by orders of magnitude); 4: a step before those, where
+  // passing ends the matrix's refinement after this step's update.
   if (check && ok[b] != 0) {
     const bool pass = rn <= 1e-14 && od <= 1e-14 * an && (check < 2 || pe <= 1e-12 * sqrt(an));
     if (check == 1) {
       if (!pass) ok[b] = 0;
+    } else if (check == 4) {
+      if (pass) ok[b] |= kDoneNext;
     } else if (check == 2) {
       if (!pass) ok[b] |= 8;
     } else if (pass) {
@@ -1240,10 +1453,11 @@ __global__ void __launch_bounds__(256) refine_e_kernel(int n, const double* __re
                                                        const double* __restrict__ T,
                                                        const double* __restrict__ lam,
                                                        const double* __restrict__ delta,
-                                                       double* __restrict__ E) {
+                                                       double* __restrict__ E,
+                                                       const int* __restrict__ ok) {
   const int b = blockIdx.y;
   const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (i >= n) return;
+  if (i >= n || (ok[b] & kDone)) return;
   const long long nn = (long long)n * n;
   const double* rr = R + b * nn + (long long)i * n;
   const double* tr = T + b * nn + (long long)i * n;
@@ -1263,7 +1477,7 @@ __global__ void __launch_bounds__(256) refine_e_kernel(int n, const double* __re
 }
 
 // Rayleigh-Ritz on strongly mixed pairs: T = X^T A X of a nearly
-// S-orthonormal X; the pairs (i, j) with |t_ij| > 1e-3 |t_ii - t_jj| (a mixing
+// S-orthonormal X; the pairs (i, j) with |t_ij| > 2^-10 |t_ii - t_jj| (a mixing
 // angle above ~1e-3) are rotated by FP64 Jacobi rotations (three sweeps over
 // the pair list, in a fixed order) applied to T and to the columns of X.  The
 // FP32 start cannot resolve pairs closer than ~1e-7 |C|; their first-order
@@ -1284,10 +1498,18 @@ __global__ void __launch_bounds__(kThreads) cluster_jacobi_kernel(int n, double*
   const long long nn = (long long)n * n;
   double* Tb = T + b * nn;
   double* Xb = X + b * nn;
-  // pair list in (i, j) order: counts per row, prefix, fill (n <= kThreads)
+  // pair list in (i, j) order: counts per row, prefix, fill (n <= kThreads).
+  // The test |t_ij| > 2^-10 |t_ii - t_jj| runs on the bit patterns (the
+  // magnitudes of doubles order as their bits; 2^-10 lowers the exponent),
+  // with one FP64 subtraction per pair.
+  __shared__ double diag[kThreads];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) diag[i] = Tb[(long long)i * n + i];
+  __syncthreads();
   auto mixed = [&](int i, int j) {
-    return fabs(Tb[(long long)i * n + j]) >
-           1e-3 * fabs(Tb[(long long)i * n + i] - Tb[(long long)j * n + j]);
+    const long long a = __double_as_longlong(Tb[(long long)i * n + j]) & 0x7fffffffffffffffLL;
+    const long long d = __double_as_longlong(diag[i] - diag[j]) & 0x7fffffffffffffffLL;
+    constexpr long long kShift = 10LL << 52;
+    return a > (d > kShift ? d - kShift : 0LL);
   };
   const int i0 = threadIdx.x;
   int c = 0;
@@ -1321,13 +1543,22 @@ __global__ void __launch_bounds__(kThreads) cluster_jacobi_kernel(int n, double*
     for (int q = 0; q < np; ++q) {
       const int i = pi[q], j = pj[q];
       if (threadIdx.x == 0) {
+        // the angle in FP32 from the FP64 difference (the pass only has to
+        // bring the pair into the refinement's convergence region), then
+        // (c, s) normalised in FP64 so that the rotation stays orthogonal:
+        // a dozen dependent FP64 operations instead of two divides and two
+        // square roots on the serial path
         const double tij = Tb[(long long)i * n + j];
         double cc = 1.0, ss = 0.0;
-        if (tij != 0.0) {
-          const double tau = (Tb[(long long)j * n + j] - Tb[(long long)i * n + i]) / (2.0 * tij);
-          const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(fma(tau, tau, 1.0)));
-          cc = 1.0 / sqrt(fma(t, t, 1.0));
-          ss = t * cc;
+        const float tf = (float)tij;
+        if (tf != 0.0f && isfinite(tf)) {
+          const float tau = (float)(Tb[(long long)j * n + j] - Tb[(long long)i * n + i]) /
+                            (2.0f * tf);
+          const float t = (tau >= 0.0f ? 1.0f : -1.0f) / (fabsf(tau) + sqrtf(fmaf(tau, tau, 1.0f)));
+          const double c0 = (double)rsqrtf(fmaf(t, t, 1.0f)), s0 = (double)t * c0;
+          const double r = rsqrt64(fma(c0, c0, s0 * s0));
+          cc = c0 * r;
+          ss = s0 * r;
         }
         rot[0] = cc;
         rot[1] = ss;
@@ -1360,22 +1591,34 @@ __global__ void sort_out_kernel(int n, const double* __restrict__ lam,
                                 const double* __restrict__ X, const int* __restrict__ ok,
                                 double* __restrict__ w, double* __restrict__ V,
                                 int32_t* __restrict__ status) {
-  extern __shared__ int rank[];
+  extern __shared__ long long key[];  // n order-preserving integer keys, then n ranks
+  int* rank = reinterpret_cast<int*>(key + n);
   const int b = blockIdx.x;
   if (!ok[b]) return;
   const long long nn = (long long)n * n;
   const double* lb = lam + (long long)b * n;
+  // the integer image of a double that orders as the double does (negative
+  // values: all bits but the sign flipped), so that the ranks need no FP64
+  // compares
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double li = lb[i];
-    int r = 0;
-    for (int j = 0; j < n; ++j) r += (lb[j] < li) || (lb[j] == li && j < i);
-    rank[i] = r;
-    w[(long long)b * n + r] = li;
+    const long long kb = __double_as_longlong(lb[i]);
+    key[i] = kb >= 0 ? kb : kb ^ 0x7fffffffffffffffLL;
   }
   __syncthreads();
-  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
-    const int i = (int)(e / n), j = (int)(e % n);
-    V[b * nn + (long long)i * n + rank[j]] = X[b * nn + e];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const long long ki = key[i];
+    int r = 0;
+    for (int j = 0; j < n; ++j) r += (key[j] < ki) || (key[j] == ki && j < i);
+    rank[i] = r;
+    w[(long long)b * n + r] = lb[i];
+  }
+  __syncthreads();
+  // a warp per row: coalesced reads, writes permuted within the row
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int i = warp; i < n; i += nw) {
+    const double* xr = X + b * nn + (long long)i * n;
+    double* vr = V + b * nn + (long long)i * n;
+    for (int j = lane; j < n; j += 32) vr[rank[j]] = xr[j];
   }
   if (threadIdx.x == 0 && status) status[b] = 0;
 }
@@ -1419,7 +1662,7 @@ size_t smem_factor64_large(int n) {
 }
 
 size_t smem_tridiag(int n) {
-  return sizeof(float) * ((size_t)n * n + 2 * (size_t)n + 64);
+  return sizeof(float) * ((size_t)n * tri_ld(n) + (1 + kTriParts) * (size_t)tri_ld(n) + 64);
 }
 
 size_t smem32(int n) {
@@ -1428,18 +1671,19 @@ size_t smem32(int n) {
 }
 
 void gemm(cudaStream_t s, int batch, int n, bool ta, const double* A, const double* B, double* P,
-          const double* base, bool identity, double sign, double* C) {
+          const double* base, bool identity, double sign, double* C,
+          const int* skip = nullptr) {
   const int ks = ksplit_of(n);
   const int tiles = (n + kT - 1) / kT;
   const dim3 grid(tiles, tiles, (unsigned)(batch * ks));
   if (ta) {
-    gemm_part_kernel<true><<<grid, kGThreads, 0, s>>>(n, ks, A, B, P);
+    gemm_part_kernel<true><<<grid, kGThreads, 0, s>>>(n, ks, A, B, P, skip);
   } else {
-    gemm_part_kernel<false><<<grid, kGThreads, 0, s>>>(n, ks, A, B, P);
+    gemm_part_kernel<false><<<grid, kGThreads, 0, s>>>(n, ks, A, B, P, skip);
   }
   const long long work = (long long)batch * n * n;
   const int blocks = (int)((work + 255) / 256 < 4096 ? (work + 255) / 256 : 4096);
-  gemm_sum_kernel<<<blocks, 256, 0, s>>>(batch, n, ks, P, base, identity, sign, C);
+  gemm_sum_kernel<<<blocks, 256, 0, s>>>(batch, n, ks, P, base, identity, sign, C, skip);
 }
 
 }  // namespace qex_mp_host
@@ -1508,8 +1752,14 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     }
     const long long vecs = (long long)batch * n;
     const unsigned vb = (unsigned)((vecs + kVecWarps - 1) / kVecWarps);
-    tri_fwd_kernel<<<vb, kVecWarps * 32, 0, s>>>(n, batch, L64, C64, ok, 0);  // C <- L^-1 C
-    tri_fwd_kernel<<<vb, kVecWarps * 32, 0, s>>>(n, batch, L64, C64, ok, 1);  // C <- C L^-T
+    {
+      // L^T into E (idle until the refinement) for the back-transformation
+      const unsigned tl = (unsigned)((n + 31) / 32);
+      lt_kernel<<<dim3(tl, tl, (unsigned)batch), 256, 0, s>>>(n, L64, E, ok);
+    }
+    const unsigned vb64 = (unsigned)((vecs + kVec64Warps - 1) / kVec64Warps);
+    tri_fwd_kernel<<<vb64, kVec64Warps * 32, 0, s>>>(n, batch, L64, C64, ok, 0);  // C <- L^-1 C
+    tri_fwd_kernel<<<vb64, kVec64Warps * 32, 0, s>>>(n, batch, L64, C64, ok, 1);  // C <- C L^-T
     // eigenvectors of C in FP32: Householder tridiagonalisation, bisection and
     // inverse iteration, back-transformation (scratch: T, R and P, idle until
     // the refinement)
@@ -1518,7 +1768,7 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     tridiag_kernel<<<batch, kThreads, smt, s>>>(n, C64, T, R, ok);
     const int ks = ksplit_of(n);
     const size_t smx = sizeof(float) * (size_t)n * n;
-    if (smx + 8192 <= (size_t)max_optin &&
+    if (smx + 16384 <= (size_t)max_optin &&  // + the kernel's static shared memory
         cudaFuncSetAttribute(tri_eig_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smx) == cudaSuccess) {
       tri_eig_kernel<true><<<batch, kThreads, smx, s>>>(n, R, P, ks, ok);
@@ -1527,40 +1777,47 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     }
     tri_back_kernel32<<<vb, kVecWarps * 32, 0, s>>>(n, batch, T, R, P, ks, U32, ok);
     stage_done_kernel<<<(batch + 255) / 256, 256, 0, s>>>(batch, ok, 3, 4);
-    tri_back_kernel<<<vb, kVecWarps * 32, 0, s>>>(n, batch, L64, U32, X, ok);
+    tri_back_kernel<<<vb64, kVec64Warps * 32, 0, s>>>(n, batch, E, U32, X, ok);
     large_done_kernel<<<(batch + 255) / 256, 256, 0, s>>>(batch, ok);
   }
-  // four steps; beyond the shared-memory solver six, with a Rayleigh-Ritz
-  // pass on strongly mixed pairs after the first and the last two checked
-  // (either passing suffices)
+  // four steps; beyond the shared-memory solver up to six, with a
+  // Rayleigh-Ritz pass on strongly mixed pairs after the first, the third
+  // and fourth accepting X early when it passes the check (after that step's
+  // update the remaining steps skip the matrix; accepting after the second
+  // left near-degenerate pairs mixed at ~1e-7, 3e-7 Ha in an SCF energy), and
+  // the last two checked (either passing suffices)
   const int steps = large ? kRefineSteps + 2 : kRefineSteps;
+  const int* skip = large ? ok : nullptr;
   for (int it = 0; it < steps; ++it) {
     if (large && it == 1) {
       gemm(s, batch, n, false, As, X, P, nullptr, false, 1.0, T);  // T = A X
       gemm(s, batch, n, true, X, T, P, nullptr, false, 1.0, E);    // E <- X^T A X
       cluster_jacobi_kernel<<<batch, kThreads, 0, s>>>(n, E, X, ok);
     }
-    gemm(s, batch, n, false, Ss, X, P, nullptr, false, 1.0, T);   // T = S X
-    gemm(s, batch, n, true, X, T, P, nullptr, true, -1.0, R);     // R = I - X^T S X
-    gemm(s, batch, n, false, As, X, P, nullptr, false, 1.0, T);   // T = A X
-    gemm(s, batch, n, true, X, T, P, nullptr, false, 1.0, E);     // E <- X^T A X
+    gemm(s, batch, n, false, Ss, X, P, nullptr, false, 1.0, T, skip);   // T = S X
+    gemm(s, batch, n, true, X, T, P, nullptr, true, -1.0, R, skip);     // R = I - X^T S X
+    gemm(s, batch, n, false, As, X, P, nullptr, false, 1.0, T, skip);   // T = A X
+    gemm(s, batch, n, true, X, T, P, nullptr, false, 1.0, E, skip);     // E <- X^T A X
     // move X^T A X into T and build the correction in E
     cudaMemcpyAsync(T, E, sizeof(double) * per, cudaMemcpyDeviceToDevice, s);
     const int check = !large ? (it == steps - 1 ? 1 : 0)
-                             : (it == steps - 2 ? 2 : (it == steps - 1 ? 3 : 0));
+                             : (it == steps - 2 ? 2
+                                                : (it == steps - 1 ? 3 : (it >= 2 ? 4 : 0)));
     const dim3 rgrid((unsigned)((n + 7) / 8), (unsigned)batch);
-    refine_partials_kernel<<<rgrid, 256, 0, s>>>(n, As, R, T, lam, part);
-    if (check >= 2) refine_pairs_kernel<<<rgrid, 256, 0, s>>>(n, T, lam, part);
+    refine_partials_kernel<<<rgrid, 256, 0, s>>>(n, As, R, T, lam, part, ok);
+    if (check >= 2) refine_pairs_kernel<<<rgrid, 256, 0, s>>>(n, T, lam, part, ok);
     refine_final_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, (n + 7) / 8, part, dlt, ok,
                                                             check);
     refine_e_kernel<<<dim3((unsigned)((n + 7) / 8), (unsigned)batch), 256, 0, s>>>(n, R, T, lam, dlt,
-                                                                                  E);
-    gemm(s, batch, n, false, X, E, P, X, false, 1.0, X2);         // X' = X + X E
+                                                                                  E, ok);
+    gemm(s, batch, n, false, X, E, P, X, false, 1.0, X2, skip);         // X' = X + X E
+    if (large && it >= 2) done_next_kernel<<<(batch + 255) / 256, 256, 0, s>>>(batch, ok);
     double* t = X;
     X = X2;
     X2 = t;
   }
-  sort_out_kernel<<<batch, 256, sizeof(int) * n, s>>>(n, lam, X, ok, w, V, status);
+  sort_out_kernel<<<batch, 256, (sizeof(long long) + sizeof(int)) * n, s>>>(n, lam, X, ok, w, V,
+                                                                             status);
   return true;
 }
 
