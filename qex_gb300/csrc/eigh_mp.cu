@@ -512,31 +512,6 @@ __device__ __forceinline__ double warp_sum64(double v) {
   return v;
 }
 
-// Lt = L^T (the lower triangle of L to the upper of Lt), 32 x 32 tiles through
-// shared memory, so that the back-transformation reads rows of L as columns
-// of Lt (see tri_fwd_kernel on why columns).
-__global__ void __launch_bounds__(256) lt_kernel(int n, const double* __restrict__ L64,
-                                                 double* __restrict__ Lt64,
-                                                 const int* __restrict__ ok) {
-  const int b = blockIdx.z;
-  if (ok[b] != 3) return;
-  __shared__ double tile[32][33];
-  const long long nn = (long long)n * n;
-  const double* L = L64 + b * nn;
-  double* Lt = Lt64 + b * nn;
-  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  for (int r = ty; r < 32; r += 8) {
-    const int i = r0 + r, k = c0 + tx;
-    tile[r][tx] = (i < n && k < n && k <= i) ? L[(long long)i * n + k] : 0.0;
-  }
-  __syncthreads();
-  for (int r = ty; r < 32; r += 8) {
-    const int i = c0 + r, k = r0 + tx;  // Lt[i][k] = L[k][i]
-    if (i < n && k < n) Lt[(long long)i * n + k] = tile[tx][r];
-  }
-}
-
 // Forward substitution v <- L^-1 v for every column (rows = 0) or every row
 // (rows = 1) of C64: C <- L^-1 C, then C <- C L^-T.  A warp per vector, the
 // vector staged in shared memory, the dot products split over the lanes.
@@ -568,8 +543,8 @@ __global__ void __launch_bounds__(kVec64Warps * 32) tri_fwd_kernel(int n, int ba
   // remaining entries with column i of L (no reduction on the dependent
   // chain).  Column i is read across 32 rows, whose cache lines the next 15
   // steps read again (L1 hits; rows of a transposed copy, new lines every
-  // step, ran 1.9x slower).  The loop runs exactly over the live entries: a
-  // predicated-off FP64 instruction costs as much as a live one.
+  // step, ran 1.9x slower, and loading the next column into registers ahead
+  // of the step's __syncwarp 1.25x slower).
   for (int i = 0; i < n; ++i) {
     const double x = v[i] * rd[i];
     for (int k = i + 1 + lane; k < n; k += 32) v[k] = fma(-L[(long long)k * n + i], x, v[k]);
@@ -718,10 +693,19 @@ __global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* 
           const int rp = (m + kTriParts - 1) / kTriParts;
           const int i0 = k + 1 + part * rp, i1 = min(n, i0 + rp);
           float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-          const float4* col = reinterpret_cast<const float4*>(C) + g;
-          for (int i = i0; i < i1; ++i) {
-            const float vi = i == k + 1 ? v0 : rk[i];
-            const float4 a4 = col[(long long)i * (ld >> 2)];
+          const int l4 = ld >> 2;
+          const float4* col = reinterpret_cast<const float4*>(C) + g + i0 * l4;
+          int i = i0;
+          if (i == k + 1 && i < i1) {  // the reflector's first entry is v0
+            const float4 a4 = *col;
+            acc = make_float4(a4.x * v0, a4.y * v0, a4.z * v0, a4.w * v0);
+            ++i;
+            col += l4;
+          }
+#pragma unroll 2
+          for (; i < i1; ++i, col += l4) {
+            const float vi = rk[i];
+            const float4 a4 = *col;
             acc.x = fmaf(a4.x, vi, acc.x);
             acc.y = fmaf(a4.y, vi, acc.y);
             acc.z = fmaf(a4.z, vi, acc.z);
@@ -768,34 +752,46 @@ __global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* 
         vc[u] = make_float4(vv[0], vv[1], vv[2], vv[3]);
         wc[u] = make_float4(ww[0], ww[1], ww[2], ww[3]);
       }
-      for (int i = k + 1 + warp; i < n; i += nw) {
-        const float vr = i == k + 1 ? v0 : rk[i];
-        const float wr = fmaf(-K, vr, p[i]);
+      const bool on0 = g0 + lane < G, on1 = g0 + lane + 32 < G;
+      const int l4 = ld >> 2;
+      float4* c0p = reinterpret_cast<float4*>(C) + g0 + lane;  // column groups, row 0
+      auto upd = [&](float4* ap, int u, float vr, float wr) {
+        float4 a = *ap;
+        a.x = fmaf(-vr, wc[u].x, fmaf(-wr, vc[u].x, a.x));
+        a.y = fmaf(-vr, wc[u].y, fmaf(-wr, vc[u].y, a.y));
+        a.z = fmaf(-vr, wc[u].z, fmaf(-wr, vc[u].z, a.z));
+        a.w = fmaf(-vr, wc[u].w, fmaf(-wr, vc[u].w, a.w));
+        *ap = a;
+        return a;
+      };
+      int i = k + 1 + warp;
+      if (warp == 0) {
+        // row k + 1 (v0): also the squares of its new entries k + 3 .. for
+        // the next step's norm
+        const float wr = fmaf(-K, v0, p[i]);
         float s2 = 0.0f;
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-          const int g = g0 + lane + 32 * u;
-          if (g < G) {
-            float4* ap = reinterpret_cast<float4*>(C + (long long)i * ld) + g;
-            float4 a = *ap;
-            a.x = fmaf(-vr, wc[u].x, fmaf(-wr, vc[u].x, a.x));
-            a.y = fmaf(-vr, wc[u].y, fmaf(-wr, vc[u].y, a.y));
-            a.z = fmaf(-vr, wc[u].z, fmaf(-wr, vc[u].z, a.z));
-            a.w = fmaf(-vr, wc[u].w, fmaf(-wr, vc[u].w, a.w));
-            *ap = a;
-            if (i == k + 1) {
-              const int j = 4 * g;
-              if (j + 0 >= k + 3 && j + 0 < n) s2 = fmaf(a.x, a.x, s2);
-              if (j + 1 >= k + 3 && j + 1 < n) s2 = fmaf(a.y, a.y, s2);
-              if (j + 2 >= k + 3 && j + 2 < n) s2 = fmaf(a.z, a.z, s2);
-              if (j + 3 >= k + 3 && j + 3 < n) s2 = fmaf(a.w, a.w, s2);
-            }
+          if (u == 0 ? on0 : on1) {
+            const float4 a = upd(c0p + i * l4 + 32 * u, u, v0, wr);
+            const int j = 4 * (g0 + lane + 32 * u);
+            if (j + 0 >= k + 3 && j + 0 < n) s2 = fmaf(a.x, a.x, s2);
+            if (j + 1 >= k + 3 && j + 1 < n) s2 = fmaf(a.y, a.y, s2);
+            if (j + 2 >= k + 3 && j + 2 < n) s2 = fmaf(a.z, a.z, s2);
+            if (j + 3 >= k + 3 && j + 3 < n) s2 = fmaf(a.w, a.w, s2);
           }
         }
-        if (i == k + 1) {
-          s2 = warp_sumf(s2);
-          if (lane == 0) red[48] = s2;
-        }
+        s2 = warp_sumf(s2);
+        if (lane == 0) red[48] = s2;
+        i += nw;
+      }
+#pragma unroll 2
+      for (; i < n; i += nw) {
+        const float vr = rk[i];
+        const float wr = fmaf(-K, vr, p[i]);
+        float4* ap = c0p + i * l4;
+        if (on0) upd(ap, 0, vr, wr);
+        if (on1) upd(ap + 32, 1, vr, wr);
       }
     } else {
       // no reflection: the trailing block stays; the next sum of squares
@@ -1143,20 +1139,23 @@ __global__ void __launch_bounds__(kVecWarps * 32) tri_back_kernel32(int n, int b
       if (lane + 32 * t < n) u[lane + 32 * t] = zr[t];
     return;
   }
-  float ct = tau[n - 3], nt = 0.0f;
+  // reflectors k (cv), k - 1 (nv) in registers, k - 2 loaded during step k
+  float n2[kPer];
+  float ct = tau[n - 3], nt = n >= 4 ? tau[n - 4] : 0.0f, t2 = 0.0f;
 #pragma unroll
   for (int t = 0; t < kPer; ++t) {
     const int i = lane + 32 * t;
     cv[t] = (i > n - 3 && i < n) ? HV[(long long)(n - 3) * n + i] : 0.0f;
+    nv[t] = (n >= 4 && i > n - 4 && i < n) ? HV[(long long)(n - 4) * n + i] : 0.0f;
   }
   for (int k = n - 3; k >= 0; --k) {
-    if (k > 0) {
-      const float* vn = HV + (long long)(k - 1) * n;
-      nt = tau[k - 1];
+    if (k > 1) {
+      const float* vn = HV + (long long)(k - 2) * n;
+      t2 = tau[k - 2];
 #pragma unroll
       for (int t = 0; t < kPer; ++t) {
         const int i = lane + 32 * t;
-        nv[t] = (i > k - 1 && i < n) ? vn[i] : 0.0f;
+        n2[t] = (i > k - 2 && i < n) ? vn[i] : 0.0f;
       }
     }
     if (ct != 0.0f) {
@@ -1168,8 +1167,12 @@ __global__ void __launch_bounds__(kVecWarps * 32) tri_back_kernel32(int n, int b
       for (int t = 0; t < kPer; ++t) zr[t] = fmaf(-a, cv[t], zr[t]);
     }
     ct = nt;
+    nt = t2;
 #pragma unroll
-    for (int t = 0; t < kPer; ++t) cv[t] = nv[t];
+    for (int t = 0; t < kPer; ++t) {
+      cv[t] = nv[t];
+      nv[t] = n2[t];
+    }
   }
   float* u = U32 + b * nn + (long long)j * n;
 #pragma unroll
@@ -1184,7 +1187,7 @@ __global__ void stage_done_kernel(int batch, int* __restrict__ ok, int from, int
 
 // X[:, j] = L^-T u_j (backward substitution, FP64), u_j = row j of U^T.
 __global__ void __launch_bounds__(kVec64Warps * 32) tri_back_kernel(int n, int batch,
-                                                                  const double* __restrict__ Lt64,
+                                                                  const double* __restrict__ L64,
                                                                   const float* __restrict__ U32,
                                                                   double* __restrict__ X,
                                                                   const int* __restrict__ ok) {
@@ -1196,21 +1199,21 @@ __global__ void __launch_bounds__(kVec64Warps * 32) tri_back_kernel(int n, int b
   const int b = (int)(gw / n), j = (int)(gw % n);
   if (ok[b] != 4) return;
   const long long nn = (long long)n * n;
-  const double* Lt = Lt64 + b * nn;
+  const double* L = L64 + b * nn;
   const float* u = U32 + b * nn + (long long)j * n;
   double* v = vec[w];
   double* rd = rdiag[w];
   for (int i = lane; i < n; i += 32) {
     v[i] = (double)u[i];
-    rd[i] = 1.0 / Lt[(long long)i * n + i];
+    rd[i] = 1.0 / L[(long long)i * n + i];
   }
   __syncwarp();
   // L^T x = u from the bottom: once x_i is known, the lanes update the
-  // entries above it with row i of L, read as column i of Lt = L^T (32 rows
-  // of Lt whose cache lines the next steps read again)
+  // entries above it with row i of L (contiguous)
   for (int i = n - 1; i >= 0; --i) {
     const double x = v[i] * rd[i];
-    for (int k = lane; k < i; k += 32) v[k] = fma(-Lt[(long long)k * n + i], x, v[k]);
+    const double* Li = L + (long long)i * n;
+    for (int k = lane; k < i; k += 32) v[k] = fma(-Li[k], x, v[k]);
     __syncwarp();
     if (lane == 0) v[i] = x;
     __syncwarp();
@@ -1752,11 +1755,6 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     }
     const long long vecs = (long long)batch * n;
     const unsigned vb = (unsigned)((vecs + kVecWarps - 1) / kVecWarps);
-    {
-      // L^T into E (idle until the refinement) for the back-transformation
-      const unsigned tl = (unsigned)((n + 31) / 32);
-      lt_kernel<<<dim3(tl, tl, (unsigned)batch), 256, 0, s>>>(n, L64, E, ok);
-    }
     const unsigned vb64 = (unsigned)((vecs + kVec64Warps - 1) / kVec64Warps);
     tri_fwd_kernel<<<vb64, kVec64Warps * 32, 0, s>>>(n, batch, L64, C64, ok, 0);  // C <- L^-1 C
     tri_fwd_kernel<<<vb64, kVec64Warps * 32, 0, s>>>(n, batch, L64, C64, ok, 1);  // C <- C L^-T
@@ -1777,7 +1775,7 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     }
     tri_back_kernel32<<<vb, kVecWarps * 32, 0, s>>>(n, batch, T, R, P, ks, U32, ok);
     stage_done_kernel<<<(batch + 255) / 256, 256, 0, s>>>(batch, ok, 3, 4);
-    tri_back_kernel<<<vb64, kVec64Warps * 32, 0, s>>>(n, batch, E, U32, X, ok);
+    tri_back_kernel<<<vb64, kVec64Warps * 32, 0, s>>>(n, batch, L64, U32, X, ok);
     large_done_kernel<<<(batch + 255) / 256, 256, 0, s>>>(batch, ok);
   }
   // four steps; beyond the shared-memory solver up to six, with a
