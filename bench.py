@@ -776,8 +776,10 @@ def run_ours(args, rank, world):
     plan = next(iter(engine.tuner.cache.values()), None) if engine.tuner else None
     plan_desc = (None if plan is None else
                  {"bucketed": plan.bucketed, "solve_planes": plan.planes,
-                  "candidate_ms": {f"{'runs' if b else 'one'}/planes{p}": round(t, 3)
-                                   for (b, p), t in next(iter(engine.tuner.timings.values())).items()}})
+                  "ring_chunk": plan.chunk or 32,
+                  "candidate_ms": {f"{'runs' if b else 'one'}/planes{p}/chunk{c or 32}": round(t, 3)
+                                   for (b, p, c), t in
+                                   next(iter(engine.tuner.timings.values())).items()}})
     energy = out["energy"].cpu().numpy()
     status = out["status"].cpu().numpy()
     iters_run = out["iterations_run"].cpu().numpy()

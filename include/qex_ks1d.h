@@ -160,6 +160,8 @@ typedef struct qex_ks1d_options {
                            one wave of resident warps), 1 resident in shared memory,
                            2 streamed through a shared-memory ring (more warps per SM;
                            for large batches, or several batches launched concurrently) */
+  int32_t solve_chunk;  /* points per chunk of the streamed planes' ring: 0 (default 32),
+                           16, 32 or 64 (a tile shape the launch-plan autotuner picks) */
 } qex_ks1d_options;
 
 /* Molecule descriptors: all device arrays of length num_molecules (nuclei:

@@ -95,6 +95,7 @@ class Ks1dOptions(ctypes.Structure):
         ("max_num_electrons", ctypes.c_int32),
         ("max_nuclei", ctypes.c_int32),
         ("solve_planes", ctypes.c_int32),
+        ("solve_chunk", ctypes.c_int32),
     ]
 
 

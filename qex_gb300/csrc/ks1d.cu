@@ -109,6 +109,7 @@ struct Params {
   long long stride;  // doubles per molecule
   long long ruw_doubles;  // leading streamed-solve area of a molecule's workspace
   int planes;             // qex_ks1d_options.solve_planes
+  int chunk;              // qex_ks1d_options.solve_chunk (points per ring chunk)
   int* counter;
   MlpParams mlp;
   // window MLP in FP64 (a checking mode): 577 doubles in global memory, and
@@ -136,7 +137,7 @@ struct SmemLayout {
 
 // Rows of the streamed-solve area (whole chunks) and its size in doubles.
 __host__ __device__ inline long long ruw_rows(int nmax) {
-  return (long long)(nmax + kChunk - 1) / kChunk * kChunk;
+  return (long long)(nmax + kMaxChunk - 1) / kMaxChunk * kMaxChunk;  // whole chunks of any size
 }
 __host__ __device__ inline long long ruw_doubles(int nmax, int kmax) {
   return ruw_rows(nmax) * kmax * 3 / 2;  // a float2 and a float per point and eigenpair
@@ -145,7 +146,8 @@ __host__ __device__ inline long long ruw_doubles(int nmax, int kmax) {
 // resident: the FP32 solve planes live in shared memory (small batches, where
 // occupancy is not limited by shared memory) instead of streaming through the ring.
 __host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax, bool adjoint = false,
-                                                  bool resident = false, int nn_floats = 0) {
+                                                  bool resident = false, int nn_floats = 0,
+                                                  int chunk = kChunk) {
   SmemLayout L;
   L.nstr = ((nmax + 31) / 32) * 32 + 1;
   size_t off = 0;
@@ -164,7 +166,7 @@ __host__ __device__ inline SmemLayout smem_layout(int nmax, int kmax, bool adjoi
   // FP32 diagonal, then the ring of the streamed solves (16-byte aligned)
   const size_t ring_off = ((size_t)L.nstr + 3) / 4 * 4;
   L.ring = L.f32 + sizeof(float) * ring_off;
-  size_t eig_floats = ring_off + (size_t)(resident ? ruw_rows(nmax) : kRing * kChunk) * kmax * 3;
+  size_t eig_floats = ring_off + (size_t)(resident ? ruw_rows(nmax) : kRing * chunk) * kmax * 3;
   size_t f = xc_floats > eig_floats ? xc_floats : eig_floats;
   if (hart_floats > f) f = hart_floats;
   if (adjoint) {
@@ -681,7 +683,7 @@ __device__ inline float ldl_solve(int N, float b2, const float* R, const float* 
 // Streamed FP32 solves.  The factors and iterates of the K shifted systems live
 // in global workspace in two planes with point-major rows of kmax entries: RU
 // (float2 {r = 1/d_i, u_i}) and W (the right-hand side / solution w_i).  They
-// pass through a ring of kRing chunks of kChunk points in shared memory
+// pass through a ring of kRing chunks of `chunk` points in shared memory
 // (cp.async, kRing - 1 chunks in flight), so that the shared-memory footprint
 // of a warp does not grow with N * K.
 // ---------------------------------------------------------------------------
@@ -691,6 +693,7 @@ struct SolveArea {
   float2* ru;
   float* w;
   int kmax;
+  int chunk;  // points per chunk of the ring (streamed planes)
   __device__ float& at(int i, int j) const { return w[(size_t)i * kmax + j]; }
 };
 
@@ -718,8 +721,9 @@ __device__ __noinline__ Step ring_sweep(SolveArea g, int N, bool act, float4* ri
     __syncwarp();
     return step;
   }
-  const int nc = (N + kChunk - 1) / kChunk;
-  const int per = kChunk * kmax;            // entries per chunk
+  const int chunk = g.chunk;
+  const int nc = (N + chunk - 1) / chunk;
+  const int per = chunk * kmax;             // entries per chunk
   const int ru16 = per / 2, w16 = per / 4;  // 16-byte pieces per chunk and plane
   float2* rring = reinterpret_cast<float2*>(ring);
   float* wring = reinterpret_cast<float*>(rring + (size_t)kRing * per);
@@ -750,8 +754,8 @@ __device__ __noinline__ Step ring_sweep(SolveArea g, int N, bool act, float4* ri
     float2* rs = rring + (size_t)s * per + lane;
     float* ws = wring + (size_t)s * per + lane;
     const int c = kFwd ? k : nc - 1 - k;
-    const int i0 = c * kChunk;
-    const int n = min(kChunk, N - i0);
+    const int i0 = c * chunk;
+    const int n = min(chunk, N - i0);
     if (act) {
       if (kFwd) {
 #pragma unroll 4
@@ -782,11 +786,12 @@ __device__ __noinline__ Step ring_sweep(SolveArea g, int N, bool act, float4* ri
   return step;
 }
 
-__device__ inline SolveArea solve_area(double* base, int nmax, int kmax) {
+__device__ inline SolveArea solve_area(double* base, int nmax, int kmax, int chunk) {
   SolveArea a;
   a.ru = reinterpret_cast<float2*>(base);
   a.w = reinterpret_cast<float*>(a.ru + ruw_rows(nmax) * kmax);
   a.kmax = kmax;
+  a.chunk = chunk;
   return a;
 }
 
@@ -1482,7 +1487,7 @@ template <int kBand, bool kRes, bool kKsr>
 __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__ Params p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x;
-  const SmemLayout L = smem_layout(p.nmax, p.kmax, false, kRes, p.nn_floats);
+  const SmemLayout L = smem_layout(p.nmax, p.kmax, false, kRes, p.nn_floats, p.chunk);
   Smem sm = carve(smem_raw, L);
   if (p.xc_kind == QEX_XC_WINDOW_MLP) stage_mlp_weights(p.mlp, sm.mlpw, lane, kWarp);
   __syncwarp();
@@ -1506,8 +1511,9 @@ __global__ void __launch_bounds__(kWarp, 12) ks1d_kernel(const __grid_constant__
       continue;
     }
     double* const slot_base = p.ws + (long long)slot * p.stride;
-    const SolveArea ruw = kRes ? solve_area(reinterpret_cast<double*>(sm.ring), p.nmax, p.kmax)
-                               : solve_area(slot_base, p.nmax, p.kmax);  // FP32 solve planes
+    const SolveArea ruw = kRes ? solve_area(reinterpret_cast<double*>(sm.ring), p.nmax, p.kmax,
+                                            p.chunk)
+                               : solve_area(slot_base, p.nmax, p.kmax, p.chunk);  // FP32 solve planes
     double* ws = slot_base + p.ruw_doubles;
     double* vn = ws + (long long)VN * p.nmax;
     double* vext = ws + (long long)VEXT * p.nmax;
@@ -1998,7 +2004,7 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
   using T = typename std::conditional<kNet64, double, float>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x;
-  const SmemLayout L = smem_layout(p.nmax, p.kmax, true, false, p.nn_floats);
+  const SmemLayout L = smem_layout(p.nmax, p.kmax, true, false, p.nn_floats, p.chunk);
   Smem sm = carve(smem_raw, L);
   stage_mlp_weights(p.mlp, sm.mlpw, lane, kWarp);
   __syncwarp();
@@ -2020,7 +2026,7 @@ __global__ void __launch_bounds__(kWarp, 8) ks1d_adjoint_kernel(const __grid_con
       continue;
     }
     double* const slot_base = p.ws + (long long)slot * p.stride;
-    const SolveArea ruw = solve_area(slot_base, p.nmax, p.kmax);  // streamed FP32 solves
+    const SolveArea ruw = solve_area(slot_base, p.nmax, p.kmax, p.chunk);  // streamed FP32 solves
     double* ws = slot_base + p.ruw_doubles;
     double* vn = ws + (long long)VN * p.nmax;
     double* vext = ws + (long long)VEXT * p.nmax;
@@ -2210,6 +2216,9 @@ int check_options(const qex_ks1d_options* o) {
   if (o->max_num_electrons / 2 + 1 > QEX_KS1D_MAX_EIGENPAIRS) return QEX_BAD_ARG;
   if (o->num_mixing_iterations < 1) return QEX_BAD_ARG;
   if (o->solve_planes < 0 || o->solve_planes > 2) return QEX_BAD_ARG;
+  if (o->solve_chunk != 0 && o->solve_chunk != 16 && o->solve_chunk != 32 &&
+      o->solve_chunk != kMaxChunk)
+    return QEX_BAD_ARG;
   return QEX_OK;
 }
 
@@ -2340,6 +2349,7 @@ int fill_params(Params& P, int mode, const qex_ks1d_batch* b, const qex_ks1d_opt
   P.stride = stride_doubles(o);
   P.ruw_doubles = ruw_doubles(o->max_num_grids, o->max_num_electrons / 2 + 1);
   P.planes = o->solve_planes;
+  P.chunk = o->solve_chunk ? o->solve_chunk : kChunk;
   if (num_molecules < 0) return QEX_BAD_ARG;
   if (num_molecules > 0) {
     if (!b->num_grids || !b->grid_offsets || !b->grid_start || !b->grid_spacing ||
@@ -2400,7 +2410,7 @@ int launch_adjoint_variant(const Params& P, cudaStream_t stream, size_t smem, in
 int launch_adjoint(const Params& P, cudaStream_t stream) {
   g_last_launches = 0;
   if (P.num_molecules == 0) return QEX_OK;
-  const SmemLayout L = smem_layout(P.nmax, P.kmax, true, false, P.nn_floats);
+  const SmemLayout L = smem_layout(P.nmax, P.kmax, true, false, P.nn_floats, P.chunk);
   const size_t smem = L.total;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return QEX_CUDA_ERROR;
@@ -2478,8 +2488,8 @@ int launch(const Params& P, cudaStream_t stream) {
   int sms = 0, max_optin = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t smem_s = smem_layout(P.nmax, P.kmax, false, false, P.nn_floats).total;
-  const size_t smem_r = smem_layout(P.nmax, P.kmax, false, true, P.nn_floats).total;
+  const size_t smem_s = smem_layout(P.nmax, P.kmax, false, false, P.nn_floats, P.chunk).total;
+  const size_t smem_r = smem_layout(P.nmax, P.kmax, false, true, P.nn_floats, P.chunk).total;
   const bool band2 = (P.stencil == 5);
   if (P.xc_kind == QEX_XC_KSR) {
     // the KSR instantiation streams its solve planes (one variant per stencil)

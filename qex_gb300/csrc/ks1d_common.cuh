@@ -20,7 +20,8 @@ constexpr int kPhases = 16;  // phase timers per molecule
 // Warm route when |dv_KS| < kFastGap * (smallest gap): below 1/2 the Weyl
 // intervals of neighbouring eigenvalues are disjoint, which the check needs.
 constexpr double kFastGap = 0.45;
-constexpr int kChunk = 32;   // points per chunk of the streamed FP32 solves
+constexpr int kChunk = 32;   // points per chunk of the streamed FP32 solves (default)
+constexpr int kMaxChunk = 64;  // the largest chunk (qex_ks1d_options.solve_chunk: 16, 32, 64)
 constexpr int kRing = 4;     // chunks in the shared-memory ring (kRing - 1 in flight)
 constexpr int kPad64 = 2;   // zero padding either side of the FP64 staging vector
 constexpr int kPadMlp = 8;  // half window

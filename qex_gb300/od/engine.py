@@ -280,14 +280,17 @@ class Ks1dEngine:
         return o
 
     def solve(self, batch: PackedBatch, xc, cfg: SolveConfig, records=RECORD_ALL, out=None,
-              initial_density=None, bucketed=True, planes=None, tune=True, defer_ksr=True):
+              initial_density=None, bucketed=True, planes=None, tune=True, defer_ksr=True,
+              chunk=None):
         """Run the full SCF for every molecule of ``batch``.
 
         With ``bucketed`` the batch is split into runs of equal eigenpair count
         (shared memory per warp scales with it), launched concurrently on
         forked streams; otherwise one launch covers the whole batch.
         ``planes`` overrides the placement of the FP32 solve planes
-        (``qex_ks1d_options.solve_planes``: 1 resident, 2 streamed).
+        (``qex_ks1d_options.solve_planes``: 1 resident, 2 streamed) and
+        ``chunk`` the points per chunk of the streamed planes' ring
+        (``qex_ks1d_options.solve_chunk``: 16, 32 or 64).
         ``defer_ksr``: with a KSR functional, size the workspace so that the
         network's energies on the output densities run as one batched launch
         after the SCF (``qex_ks1d_workspace_size_xc``).
@@ -296,7 +299,7 @@ class Ks1dEngine:
         functional, params = resolve(xc)
         if self.tuner is not None and tune and planes is None and bucketed:
             plan = self.tuner.plan(self, batch, xc, cfg, functional.kind)
-            bucketed, planes = plan.bucketed, plan.planes
+            bucketed, planes, chunk = plan.bucketed, plan.planes, plan.chunk
         vext_given = batch.external_potential is not None
         spec, keep = functional.spec(params, _convention(cfg))
         if out is None:
@@ -316,6 +319,7 @@ class Ks1dEngine:
             opts.max_num_electrons = max(ne_max, 1)
             opts.max_num_grids = max(ng_max, 5)
             opts.solve_planes = planes
+            opts.solve_chunk = int(chunk or 0)
             nbytes = ctypes.c_size_t()
             if defer_ksr or functional.kind in (N.QEX_XC_LOCAL_MLP, N.QEX_XC_GLOBAL_MLP):
                 N.check(self.lib.qex_ks1d_workspace_size_xc(ctypes.byref(opts), ctypes.byref(spec),

@@ -373,11 +373,15 @@ def test_resident_and_streamed_planes_agree(qx, stencil):
     batch = od.PackedBatch(ms)
     cfg = od.SolveConfig(num_iterations=8, convention="local", stencil=stencil)
     eng = od.engine.default_engine()
-    res = [eng.solve(batch, qex.LDAExpCoulomb(), cfg, planes=pl) for pl in (1, 2)]
-    np.testing.assert_allclose(res[0]["energy"].cpu().numpy(), res[1]["energy"].cpu().numpy(),
-                               rtol=0, atol=1e-11)
-    np.testing.assert_allclose(res[0]["final_density"].cpu().numpy(),
-                               res[1]["final_density"].cpu().numpy(), rtol=0, atol=1e-11)
+    # resident planes, then streamed through rings of 16-, 32- and 64-point
+    # chunks (the tile shapes the autotuner chooses from): data movement only
+    res = [eng.solve(batch, qex.LDAExpCoulomb(), cfg, planes=pl, chunk=c)
+           for pl, c in ((1, 0), (2, 16), (2, 32), (2, 64))]
+    for r in res[1:]:
+        np.testing.assert_allclose(res[0]["energy"].cpu().numpy(), r["energy"].cpu().numpy(),
+                                   rtol=0, atol=1e-11)
+        np.testing.assert_allclose(res[0]["final_density"].cpu().numpy(),
+                                   r["final_density"].cpu().numpy(), rtol=0, atol=1e-11)
 
 
 def test_xc_eval_known_answer_on_gpu(qx):

@@ -50,6 +50,17 @@ def test_version_and_workspace_size_without_gpu():
     o.stencil = 5
     o.max_num_electrons = 40  # more eigenpairs than the kernel supports
     assert lib.qex_ks1d_workspace_size(ctypes.byref(o), 4, ctypes.byref(nb)) == N.QEX_BAD_ARG
+    o.max_num_electrons = 12
+    # the ring's tile: 16, 32 or 64 points per chunk (0: the default); the
+    # workspace holds whole chunks of any of them
+    sizes = set()
+    for chunk in (0, 16, 32, 64):
+        o.solve_chunk = chunk
+        assert lib.qex_ks1d_workspace_size(ctypes.byref(o), 8, ctypes.byref(nb)) == 0
+        sizes.add(nb.value)
+    assert len(sizes) == 1
+    o.solve_chunk = 48
+    assert lib.qex_ks1d_workspace_size(ctypes.byref(o), 8, ctypes.byref(nb)) == N.QEX_BAD_ARG
 
 
 def test_ksr_workspace_adds_deferred_energy_rows_without_gpu():
