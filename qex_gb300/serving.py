@@ -13,7 +13,8 @@ molecule that is not resident is admitted by building it first (grid, AO
 values and integrals on the GPU, then the captured graph), and that set-up is
 part of its latency.  The streams split into a 1D share and a 3D share
 (``max_inflight3d``), so that neither kind of backlog holds back the other,
-and at most one new 3D molecule is built per pass of the loop.  Admission is
+and a new 3D molecule is set up one stage per pass of the loop (one molecule
+at a time), so that 1D batches launch between its stages.  Admission is
 by device memory: a batch is admitted only
 while its estimated bytes fit the free HBM the driver reports
 (``cudaMemGetInfo``, through ``torch.cuda.mem_get_info``, plus the memory the
@@ -134,6 +135,7 @@ class ScfServer:
         self.max_cycle3d = max_cycle3d
         self.margin = hbm_margin_bytes
         self.built3d = 0
+        self._building = None  # (key, graph, remaining stages) of a molecule being set up
 
     def _fits(self, nbytes: int) -> bool:
         """Admission test: the fixed budget when given, else the free HBM."""
@@ -147,13 +149,30 @@ class ScfServer:
         """Make the molecule of a 3D request resident (build + capture) if needed."""
         if key in self.graphs3d:
             return
+        self._start_build(key)
+        while self._building is not None:
+            self._advance_build()
+
+    def _start_build(self, key):
+        """First stage of a new molecule's set-up (the builder: grid, AO
+        values, integrals); the rest runs one stage per pass of the loop."""
         from .td.graph import CapturedScf
 
         mol = self.builder3d(key)
-        g = CapturedScf(mol, max_cycle=self.max_cycle3d)
-        self.graphs3d[key] = g
-        self.resident += g.nbytes
-        self.built3d += 1
+        g = CapturedScf.__new__(CapturedScf)
+        self._building = (key, g, g.build_stages(mol, max_cycle=self.max_cycle3d))
+
+    def _advance_build(self):
+        """One more stage of the molecule being set up (eigensolver autotune,
+        warm-up SCF, capture); the molecule is resident after the last."""
+        key, g, stages = self._building
+        try:
+            next(stages)
+        except StopIteration:
+            self.graphs3d[key] = g
+            self.resident += g.nbytes
+            self.built3d += 1
+            self._building = None
 
     def _bytes_for(self, batch: PackedBatch, opts) -> int:
         nb = ctypes.c_size_t()
@@ -279,26 +298,28 @@ class ScfServer:
                     inflight.remove(L)
                     (free3d if L.graph3d is not None else free).append(L.stream)
             self._launch1d(pending1d, free, inflight, now)
+            # A new 3D molecule is set up one stage per pass (each stage waits
+            # for the GPU), so the 1D batches that arrive meanwhile launch
+            # between its stages; one molecule is set up at a time.
+            if self._building is not None:
+                self._advance_build()
+                now = time.perf_counter() - t0
             # 3D requests: a replay of the molecule's graph on a free 3D stream
             # (one replay of a graph at a time: its results are static tensors);
-            # the molecule whose oldest request arrived first goes first.  At
-            # most one new molecule is built per pass (a build takes a while):
-            # the 1D requests that arrived meanwhile launch at the next pass.
+            # the molecule whose oldest request arrived first goes first.
             if pending3d and free3d:
                 order = sorted((q[0].arrival, k) for k, q in pending3d.items()
                                if k not in self.busy3d)
-                built = False
                 for _, key in order:
                     if not free3d:
                         break
                     if key not in self.graphs3d:
                         if self.builder3d is None:
                             raise KeyError(f"3D molecule {key!r} is not resident")
-                        if built:
-                            continue
-                        self._ensure3d(key)  # set-up inside this request's latency
-                        built = True
-                        now = time.perf_counter() - t0
+                        if self._building is None:
+                            self._start_build(key)  # set-up inside this request's latency
+                            now = time.perf_counter() - t0
+                        continue
                     q = pending3d[key]
                     r = q.popleft()
                     if not q:

@@ -53,6 +53,14 @@ class CapturedScf:
     """One molecule's ``run_scf(max_cycle)`` captured as a CUDA graph."""
 
     def __init__(self, mol, max_cycle: int = 30, xc="LDA", tune_eigh: bool = True):
+        for _ in self.build_stages(mol, max_cycle, xc, tune_eigh):
+            pass
+
+    def build_stages(self, mol, max_cycle: int = 30, xc="LDA", tune_eigh: bool = True):
+        """The set-up as a generator: it yields between its stages (the
+        eigensolver autotune, the warm-up SCF, the capture), each of which
+        waits for the GPU, so that a caller such as the server can launch
+        other work between them.  Exhausting it leaves the object ready."""
         torch = N.require_cuda()
         self.max_cycle = max_cycle
         self.mol = mol if isinstance(mol, DeviceMolecule3D) else DeviceMolecule3D.from_host(mol)
@@ -61,6 +69,7 @@ class CapturedScf:
             from .eigh import tune_path
 
             self.eigh_path = tune_path(self.mol.h1e, self.mol.s1e)
+            yield
         before = torch.cuda.memory_allocated()
         # warm-up outside the capture: kernel attributes, allocator pools
         side = torch.cuda.Stream()
@@ -69,6 +78,7 @@ class CapturedScf:
             run_scf(self.mol, max_cycle, xc=xc)
         torch.cuda.current_stream().wait_stream(side)
         torch.cuda.synchronize()
+        yield
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             self.result: ScfResult = run_scf(self.mol, max_cycle, xc=xc)
