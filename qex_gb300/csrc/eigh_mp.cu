@@ -23,6 +23,7 @@
 // check of the last refinement step rejects, keep the FP64 Jacobi path of
 // td.cu, which applies the reference's shift
 // (qedft/train/td/generalized_eigensolver.py:264-330).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -831,6 +832,167 @@ __device__ inline int sturm_count32(int n, const float* d, const float* e2, floa
     c += qv < 0.0f;
   }
   return c;
+}
+
+// The Householder reduction over a thread-block cluster of kCl CTAs (one
+// cluster per matrix): CTA q holds rows [q R, q R + R) of C (R = ceil(n / kCl))
+// in its shared memory.  Per step k two cluster barriers: (1) the owner of
+// row k forms the reflector and writes v and tau into every CTA's shared
+// memory (distributed shared memory); (2) every CTA forms p = tau A v for its
+// rows (a warp per row) and writes its part of p and of v.p into every CTA;
+// then each CTA updates its rows, A <- A - v w^T - w v^T with w = p - K v.
+// The buffers written remotely alternate between two copies by step parity:
+// a CTA writes step k + 1's copy only after every CTA has passed step k's
+// first barrier, so nobody still reads it.  Output as tridiag_kernel's.
+constexpr int kCl = 8;
+constexpr int kClThreads = 256;
+__host__ __device__ inline int cl_rows(int n) { return (n + kCl - 1) / kCl; }
+
+__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kClThreads)
+    tridiag_cluster_kernel(int n, const double* __restrict__ C64, double* __restrict__ HVws,
+                           double* __restrict__ TRIws, const int* __restrict__ ok) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int q = (int)cluster.block_rank();
+  const int b = blockIdx.x / kCl;
+  if (ok[b] != 3) return;  // the same for the whole cluster (one matrix)
+  extern __shared__ float4 smraw[];
+  float* sm = reinterpret_cast<float*>(smraw);
+  const int R = cl_rows(n), ld = tri_ld(n);
+  float* A = sm;                  // R rows of ld floats: rows r0 .. r1 - 1 of C
+  float* vbuf = A + R * ld;       // [2][n] the reflector v (absolute column index)
+  float* pbuf = vbuf + 2 * n;     // [2][n] p
+  float* vpbuf = pbuf + 2 * n;    // [2][kCl] the CTAs' parts of v.p
+  float* scal = vpbuf + 2 * kCl;  // [2][4] tau
+  float* red = scal + 8;          // 64
+  const long long nn = (long long)n * n;
+  float* HV = reinterpret_cast<float*>(HVws + b * nn);
+  float* d = reinterpret_cast<float*>(TRIws + b * nn);
+  float* e = d + n;
+  float* tau = e + n;
+  const double* Cd = C64 + b * nn;
+  const int r0 = q * R, r1 = min(n, r0 + R);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int nw = kClThreads / 32;
+  for (int r = r0 + warp; r < r1; r += nw)
+    for (int c = lane; c < ld; c += 32)
+      A[(r - r0) * ld + c] =
+          c < n ? (float)(0.5 * (Cd[(long long)r * n + c] + Cd[(long long)c * n + r])) : 0.0f;
+  // red[48]: the sum of squares of x[1 ..] of the next reflector, kept by
+  // the owner of its row (summed during the previous step's update)
+  if (q == 0 && warp == 0) {
+    float s0 = 0.0f;
+    for (int c = 2 + lane; c < n; c += 32) s0 = fmaf(A[c], A[c], s0);
+    s0 = warp_sumf(s0);
+    if (lane == 0) red[48] = s0;
+  }
+  __syncthreads();
+  cluster.sync();  // every CTA of the cluster runs before any remote access
+  for (int k = 0; k < n - 2; ++k) {
+    const int par = k & 1;
+    float* vb = vbuf + par * n;
+    float* pb = pbuf + par * n;
+    float* vpb = vpbuf + par * kCl;
+    float* sc = scal + par * 4;
+    if (q == k / R) {
+      // (1) the owner of row k: the reflector of x = C[k][k+1 ..]
+      const float* rk = A + (k - r0) * ld;
+      if (threadIdx.x == 0) {
+        const float sq = red[48];
+        const float x0 = rk[k + 1];
+        float alpha = x0, t = 0.0f;
+        if (sq > 0.0f) {
+          const float nrm = sqrtf(fmaf(x0, x0, sq));
+          alpha = x0 >= 0.0f ? -nrm : nrm;
+          const float u0 = x0 - alpha;
+          t = 2.0f / fmaf(u0, u0, sq);
+        }
+        red[32] = t;
+        red[33] = (t != 0.0f) ? x0 - alpha : 1.0f;
+        d[k] = rk[k];
+        e[k] = alpha;
+        tau[k] = t;
+      }
+      __syncthreads();
+      const float t = red[32], v0 = red[33];
+      for (int c = k + 1 + threadIdx.x; c < n; c += kClThreads) {
+        const float val = c == k + 1 ? v0 : rk[c];
+        HV[(long long)k * n + c] = val;
+#pragma unroll
+        for (int t2 = 0; t2 < kCl; ++t2) cluster.map_shared_rank(vb, t2)[c] = val;
+      }
+      if (threadIdx.x < kCl) cluster.map_shared_rank(sc, (int)threadIdx.x)[0] = t;
+    }
+    cluster.sync();
+    // (2) p = tau A v for this CTA's rows beyond k (four rows at a time per
+    // warp, their sums and reductions interleaved), and their part of v.p
+    const float t = sc[0];
+    float vp = 0.0f;
+    for (int rb = max(k + 1, r0) + 4 * warp; rb < r1; rb += 4 * nw) {
+      float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      const float* ar = A + (rb - r0) * ld;
+      for (int c = k + 1 + lane; c < n; c += 32) {
+        const float vc = vb[c];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (rb + u < r1) a[u] = fmaf(ar[u * ld + c], vc, a[u]);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) a[u] += __shfl_xor_sync(0xffffffffu, a[u], o);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (rb + u < r1) {
+          const float pr = t * a[u];
+          if (lane < kCl) cluster.map_shared_rank(pb, lane)[rb + u] = pr;
+          vp = fmaf(vb[rb + u], pr, vp);
+        }
+      }
+    }
+    if (lane == 0) red[40 + warp] = vp;
+    __syncthreads();
+    if (threadIdx.x < kCl) {
+      float s = 0.0f;
+#pragma unroll
+      for (int w = 0; w < nw; ++w) s += red[40 + w];
+      cluster.map_shared_rank(vpb, (int)threadIdx.x)[q] = s;
+    }
+    cluster.sync();
+    // the rank-2 update of this CTA's rows (local only)
+    float qs = 0.0f;
+#pragma unroll
+    for (int t2 = 0; t2 < kCl; ++t2) qs += vpb[t2];
+    const float K = 0.5f * t * qs;
+    for (int r = max(k + 1, r0) + warp; r < r1; r += nw) {
+      float* ar = A + (r - r0) * ld;
+      const float vr = vb[r], wr = fmaf(-K, vr, pb[r]);
+      float s2 = 0.0f;
+      for (int c = k + 1 + lane; c < n; c += 32) {
+        const float vc = vb[c];
+        const float nv = ar[c] - fmaf(vr, fmaf(-K, vc, pb[c]), wr * vc);
+        ar[c] = nv;
+        if (c >= k + 3) s2 = fmaf(nv, nv, s2);
+      }
+      if (r == k + 1) {  // the next reflector's row: its norm for the next step
+        s2 = warp_sumf(s2);
+        if (lane == 0) red[48] = s2;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (n - 2 >= r0 && n - 2 < r1) {
+      d[n - 2] = A[(n - 2 - r0) * ld + n - 2];
+      tau[n - 2] = 0.0f;
+    }
+    if (n - 1 >= r0 && n - 1 < r1) {
+      e[n - 2] = A[(n - 1 - r0) * ld + n - 2];
+      d[n - 1] = A[(n - 1 - r0) * ld + n - 1];
+      e[n - 1] = 0.0f;
+      tau[n - 1] = 0.0f;
+    }
+  }
 }
 
 // Numbers of eigenvalues of T below three shifts, their recurrences
@@ -1664,6 +1826,10 @@ size_t smem_factor64_large(int n) {
   return sizeof(float) * ((size_t)n * n + 2 * (size_t)m + 33);
 }
 
+size_t smem_tridiag_cluster(int n) {
+  return sizeof(float) * ((size_t)cl_rows(n) * tri_ld(n) + 4 * (size_t)n + 2 * kCl + 8 + 64);
+}
+
 size_t smem_tridiag(int n) {
   return sizeof(float) * ((size_t)n * tri_ld(n) + (1 + kTriParts) * (size_t)tri_ld(n) + 64);
 }
@@ -1707,7 +1873,7 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (smem_factor64_large(n) + 64 > (size_t)max_optin) return false;  // + static shared
-    if (smem_tridiag(n) + 64 > (size_t)max_optin) return false;
+    if (smem_tridiag_cluster(n) + 64 > (size_t)max_optin) return false;
   }
   const long long nn = (long long)n * n;
   const long long per = (long long)batch * nn;
@@ -1761,9 +1927,10 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
     // eigenvectors of C in FP32: Householder tridiagonalisation, bisection and
     // inverse iteration, back-transformation (scratch: T, R and P, idle until
     // the refinement)
-    const size_t smt = smem_tridiag(n);
-    cudaFuncSetAttribute(tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
-    tridiag_kernel<<<batch, kThreads, smt, s>>>(n, C64, T, R, ok);
+    const size_t smt = smem_tridiag_cluster(n);
+    cudaFuncSetAttribute(tridiag_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smt);
+    tridiag_cluster_kernel<<<batch * kCl, kClThreads, smt, s>>>(n, C64, T, R, ok);
     const int ks = ksplit_of(n);
     const size_t smx = sizeof(float) * (size_t)n * n;
     if (smx + 16384 <= (size_t)max_optin &&  // + the kernel's static shared memory
