@@ -587,10 +587,11 @@ __global__ void __launch_bounds__(kThreads) jacobi_large_kernel(int n,
 // FP32 eigenvectors of C beyond kMaxSmemN by tridiagonal reduction (in place
 // of the one-CTA Jacobi, whose n - 1 synchronised rounds per sweep made it the
 // bulk of a solve at nao 150-240):
-//   tridiag_kernel: Householder reduction C = Q T Q^T in shared memory (one
-//     CTA per matrix; the reflectors v_k go to HV row k, d / e / tau to tri);
-//   tri_eig_kernel: all eigenvalues of T by Sturm bisection (a thread per
-//     eigenvalue) and its eigenvectors by inverse iteration with partial
+//   tridiag_cluster_kernel: Householder reduction C = Q T Q^T over a
+//     thread-block cluster (the reflectors v_k go to HV row k, d / e / tau to
+//     tri);
+//   tri_eig_kernel: all eigenvalues of T by Sturm counts (a counting pass,
+//     then octasection) and its eigenvectors by inverse iteration with partial
 //     pivoting, the vectors of a cluster (gaps below 1e-5 |T|) computed by one
 //     thread in turn and orthogonalised against each other (Gram-Schmidt),
 //     LAPACK stein's scheme;
@@ -607,218 +608,11 @@ __device__ inline float warp_sumf(float v) {
   return v;
 }
 
-// Row stride of C in tridiag_kernel's shared memory: rows 16-byte aligned.
+// Row stride of C in the Householder reduction's shared memory: rows 16-byte
+// aligned.
 __host__ __device__ inline int tri_ld(int n) { return (n + 3) & ~3; }
-// Row parts of tridiag_kernel's product p = A v (kThreads = 64 x kTriParts:
-// 64 float4 column groups cover 256 columns).
-constexpr int kTriParts = 8;
-static_assert(kThreads == 64 * kTriParts, "tridiag_kernel thread layout");
 
-__global__ void __launch_bounds__(kThreads) tridiag_kernel(int n, const double* __restrict__ C64,
-                                                           double* __restrict__ HVws,
-                                                           double* __restrict__ TRIws,
-                                                           const int* __restrict__ ok) {
-  const int b = blockIdx.x;
-  if (ok[b] != 3) return;
-  extern __shared__ float sm[];
-  const long long nn = (long long)n * n;
-  const int ld = tri_ld(n);
-  float* C = sm;                          // n rows of ld floats
-  float* p = C + (long long)n * ld;       // p (ld floats, indexed by absolute column)
-  float* pp = p + ld;                     // kTriParts partial sums of p (ld floats each)
-  float* red = pp + kTriParts * ld;       // 64 floats
-  float* HV = reinterpret_cast<float*>(HVws + b * nn);
-  float* d = reinterpret_cast<float*>(TRIws + b * nn);
-  float* e = d + n;
-  float* tau = e + n;
-  const double* Cd = C64 + b * nn;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  // C in FP32, rows read coalesced, then symmetrised in shared memory
-  for (int i = warp; i < n; i += nw)
-    for (int j = lane; j < ld; j += 32)
-      C[(long long)i * ld + j] = j < n ? (float)Cd[(long long)i * n + j] : 0.0f;
-  __syncthreads();
-  for (int i = warp; i < n; i += nw)
-    for (int j = i + 1 + lane; j < n; j += 32) {
-      const float a = 0.5f * (C[(long long)i * ld + j] + C[(long long)j * ld + i]);
-      C[(long long)i * ld + j] = a;
-      C[(long long)j * ld + i] = a;
-    }
-  if (n > 2 && warp == 0) {
-    float s0 = 0.0f;
-    for (int c = 2 + lane; c < n; c += 32) {
-      const float x = 0.5f * (Cd[c] + Cd[(long long)c * n]);
-      s0 = fmaf(x, x, s0);
-    }
-    s0 = warp_sumf(s0);
-    if (lane == 0) red[48] = s0;
-  }
-  __syncthreads();
-  // Three block barriers per step.  The reflector of step k is row k right of
-  // the diagonal, x = C[k][k+1 ..], with its first entry replaced by
-  // v0 = x0 - alpha (read in place); the sum of squares of x[1 ..] comes from
-  // the previous step's update (red[48]).  Then: p = tau A v, a thread per
-  // column over half of the rows (partial sums in p and p2) | p and v.p | the
-  // rank-2 update, a warp per row with float4 column groups whose v and
-  // w = p - K v each lane keeps in registers (columns outside the trailing
-  // block have v = w = 0 and are left unchanged); the warp of the next row
-  // also sums the squares of its new entries for the next step's norm.
-  for (int k = 0; k < n - 2; ++k) {
-    const int m = n - k - 1;
-    const float* rk = C + (long long)k * ld;  // row k; x = rk[k + 1 ..]
-    const float sq = red[48];
-    const float x0 = rk[k + 1];
-    float alpha = x0, t = 0.0f;
-    if (sq > 0.0f) {
-      const float nrm = sqrtf(fmaf(x0, x0, sq));
-      alpha = x0 >= 0.0f ? -nrm : nrm;
-      const float u0 = x0 - alpha;
-      t = 2.0f / fmaf(u0, u0, sq);
-    }
-    const float v0 = (t != 0.0f) ? x0 - alpha : 1.0f;
-    if (threadIdx.x == 0) {
-      d[k] = rk[k];
-      e[k] = alpha;
-      tau[k] = t;
-    }
-    for (int i = threadIdx.x; i < m; i += blockDim.x)
-      HV[(long long)k * n + k + 1 + i] = i == 0 ? v0 : rk[k + 1 + i];
-    if (t != 0.0f) {
-      {
-        // p = A v over the trailing block: a thread per float4 column group
-        // (from the one holding column k + 1) and part of the rows; the
-        // dead columns left of k + 1 in the first group are never used
-        const int g0 = (k + 1) >> 2, G = ld >> 2;
-        const int g = g0 + (threadIdx.x & 63), part = threadIdx.x >> 6;
-        if (g < G) {
-          const int rp = (m + kTriParts - 1) / kTriParts;
-          const int i0 = k + 1 + part * rp, i1 = min(n, i0 + rp);
-          float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-          const int l4 = ld >> 2;
-          const float4* col = reinterpret_cast<const float4*>(C) + g + i0 * l4;
-          int i = i0;
-          if (i == k + 1 && i < i1) {  // the reflector's first entry is v0
-            const float4 a4 = *col;
-            acc = make_float4(a4.x * v0, a4.y * v0, a4.z * v0, a4.w * v0);
-            ++i;
-            col += l4;
-          }
-#pragma unroll 2
-          for (; i < i1; ++i, col += l4) {
-            const float vi = rk[i];
-            const float4 a4 = *col;
-            acc.x = fmaf(a4.x, vi, acc.x);
-            acc.y = fmaf(a4.y, vi, acc.y);
-            acc.z = fmaf(a4.z, vi, acc.z);
-            acc.w = fmaf(a4.w, vi, acc.w);
-          }
-          reinterpret_cast<float4*>(pp + part * ld)[g] = acc;
-        }
-      }
-      __syncthreads();
-      float vp = 0.0f;
-      if (threadIdx.x < m) {
-        const int j = k + 1 + threadIdx.x;
-        float sum = 0.0f;
-#pragma unroll
-        for (int q = 0; q < kTriParts; ++q) sum += pp[q * ld + j];
-        const float pc = t * sum;
-        p[j] = pc;
-        vp = (threadIdx.x == 0 ? v0 : rk[j]) * pc;
-      }
-      vp = warp_sumf(vp);
-      if (lane == 0) red[32 + warp] = vp;
-      __syncthreads();
-      float q = 0.0f;
-#pragma unroll
-      for (int w = 0; w < kThreads / 32; ++w) q += red[32 + w];
-      const float K = 0.5f * t * q;
-      // this lane's column groups g = g0 + lane + 32 u (columns 4g .. 4g+3)
-      const int g0 = (k + 1) >> 2, G = ld >> 2;
-      float4 vc[2], wc[2];
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int g = g0 + lane + 32 * u;
-        float vv[4] = {0.0f, 0.0f, 0.0f, 0.0f}, ww[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        if (g < G) {
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            const int j = 4 * g + c;
-            if (j > k && j < n) {
-              vv[c] = j == k + 1 ? v0 : rk[j];
-              ww[c] = fmaf(-K, vv[c], p[j]);
-            }
-          }
-        }
-        vc[u] = make_float4(vv[0], vv[1], vv[2], vv[3]);
-        wc[u] = make_float4(ww[0], ww[1], ww[2], ww[3]);
-      }
-      const bool on0 = g0 + lane < G, on1 = g0 + lane + 32 < G;
-      const int l4 = ld >> 2;
-      float4* c0p = reinterpret_cast<float4*>(C) + g0 + lane;  // column groups, row 0
-      auto upd = [&](float4* ap, int u, float vr, float wr) {
-        float4 a = *ap;
-        a.x = fmaf(-vr, wc[u].x, fmaf(-wr, vc[u].x, a.x));
-        a.y = fmaf(-vr, wc[u].y, fmaf(-wr, vc[u].y, a.y));
-        a.z = fmaf(-vr, wc[u].z, fmaf(-wr, vc[u].z, a.z));
-        a.w = fmaf(-vr, wc[u].w, fmaf(-wr, vc[u].w, a.w));
-        *ap = a;
-        return a;
-      };
-      int i = k + 1 + warp;
-      if (warp == 0) {
-        // row k + 1 (v0): also the squares of its new entries k + 3 .. for
-        // the next step's norm
-        const float wr = fmaf(-K, v0, p[i]);
-        float s2 = 0.0f;
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          if (u == 0 ? on0 : on1) {
-            const float4 a = upd(c0p + i * l4 + 32 * u, u, v0, wr);
-            const int j = 4 * (g0 + lane + 32 * u);
-            if (j + 0 >= k + 3 && j + 0 < n) s2 = fmaf(a.x, a.x, s2);
-            if (j + 1 >= k + 3 && j + 1 < n) s2 = fmaf(a.y, a.y, s2);
-            if (j + 2 >= k + 3 && j + 2 < n) s2 = fmaf(a.z, a.z, s2);
-            if (j + 3 >= k + 3 && j + 3 < n) s2 = fmaf(a.w, a.w, s2);
-          }
-        }
-        s2 = warp_sumf(s2);
-        if (lane == 0) red[48] = s2;
-        i += nw;
-      }
-#pragma unroll 2
-      for (; i < n; i += nw) {
-        const float vr = rk[i];
-        const float wr = fmaf(-K, vr, p[i]);
-        float4* ap = c0p + i * l4;
-        if (on0) upd(ap, 0, vr, wr);
-        if (on1) upd(ap + 32, 1, vr, wr);
-      }
-    } else {
-      // no reflection: the trailing block stays; the next sum of squares
-      // from row k + 1 as it is (after every thread has read red[48])
-      __syncthreads();
-      if (warp == 0) {
-        float s2 = 0.0f;
-        const float* r1 = C + (long long)(k + 1) * ld;
-        for (int c = k + 3 + lane; c < n; c += 32) s2 = fmaf(r1[c], r1[c], s2);
-        s2 = warp_sumf(s2);
-        if (lane == 0) red[48] = s2;
-      }
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    if (n >= 2) {
-      d[n - 2] = C[(long long)(n - 2) * ld + n - 2];
-      e[n - 2] = C[(long long)(n - 1) * ld + n - 2];
-      tau[n - 2] = 0.0f;
-    }
-    d[n - 1] = C[(long long)(n - 1) * ld + n - 1];
-    e[n - 1] = 0.0f;
-    tau[n - 1] = 0.0f;
-  }
-}
+
 
 // Number of eigenvalues of T below sigma (signs of the L D L^T pivots).
 __device__ inline int sturm_count32(int n, const float* d, const float* e2, float sigma,
@@ -839,11 +633,13 @@ __device__ inline int sturm_count32(int n, const float* d, const float* e2, floa
 // in its shared memory.  Per step k two cluster barriers: (1) the owner of
 // row k forms the reflector and writes v and tau into every CTA's shared
 // memory (distributed shared memory); (2) every CTA forms p = tau A v for its
-// rows (a warp per row) and writes its part of p and of v.p into every CTA;
+// rows (a warp per four rows) and writes its part of p and of v.p into every
+// CTA;
 // then each CTA updates its rows, A <- A - v w^T - w v^T with w = p - K v.
 // The buffers written remotely alternate between two copies by step parity:
 // a CTA writes step k + 1's copy only after every CTA has passed step k's
-// first barrier, so nobody still reads it.  Output as tridiag_kernel's.
+// first barrier, so nobody still reads it.  The norm of the next reflector is
+// summed by its row's owner during the update.
 constexpr int kCl = 8;
 constexpr int kClThreads = 256;
 __host__ __device__ inline int cl_rows(int n) { return (n + kCl - 1) / kCl; }
@@ -1828,10 +1624,6 @@ size_t smem_factor64_large(int n) {
 
 size_t smem_tridiag_cluster(int n) {
   return sizeof(float) * ((size_t)cl_rows(n) * tri_ld(n) + 4 * (size_t)n + 2 * kCl + 8 + 64);
-}
-
-size_t smem_tridiag(int n) {
-  return sizeof(float) * ((size_t)n * tri_ld(n) + (1 + kTriParts) * (size_t)tri_ld(n) + 64);
 }
 
 size_t smem32(int n) {
