@@ -1658,7 +1658,11 @@ bool qex_mp_gen_eigh(int batch, int n, const double* A, const double* S, double*
   using namespace qex_mp_host;
   if (n > kMaxN) return false;
   const int path = g_path[n].load(std::memory_order_relaxed);
-  const bool large = (path == 2 || n > kMaxSmemN) && !(path == 1 && n <= kMaxSmemN);
+  // the tridiagonal path needs n >= 8 (its reduction leaves a 2 x 2 block and
+  // splits the rows over kCl CTAs); smaller matrices always take the
+  // shared-memory solve
+  const bool large =
+      n >= kCl && (path == 2 || n > kMaxSmemN) && !(path == 1 && n <= kMaxSmemN);
   int max_optin = 0;
   if (large) {
     int dev = 0;

@@ -86,11 +86,12 @@ def test_generalized_eigh(td, n):
         np.testing.assert_allclose(A[b] @ V[b], S[b] @ V[b] * w[b][None, :], atol=1e-9)
 
 
-@pytest.mark.parametrize("n", [4, 17, 64, 103])
+@pytest.mark.parametrize("n", [8, 17, 64, 103])
 def test_tridiagonal_path_at_small_sizes(td, n):
     """The FP64-factor + tridiagonal path selected for sizes the shared-memory
-    solver covers by default (the eigensolver autotuner's other candidate):
-    the same accuracy against the oracle, including a degenerate spectrum."""
+    solver covers by default (the eigensolver autotuner's other candidate;
+    from n = 8, below which the shared-memory solve always runs): the same
+    accuracy against the oracle, including a degenerate spectrum."""
     torch, eigh, numint, scf, W = td
     rng = np.random.default_rng(100 + n)
     q = np.linalg.qr(rng.normal(size=(n, n)))[0]
