@@ -936,19 +936,24 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
   }
   if (jj < n && q == 0) lam[jj] = 0.5f * (a + c);
   __syncthreads();
-  // inverse iteration; a cluster's first thread computes its vectors in turn
+  // inverse iteration, every eigenvector on its own thread (the members of a
+  // cluster in parallel too, with shifts separated by sep in member order);
+  // the clusters' vectors are orthogonalised after the iterations
   const float ctol = 1e-5f * nrm;
   const float sep = 10.0f * FLT_EPSILON * nrm;
   const float tiny = FLT_EPSILON * nrm;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    if (j > 0 && lam[j] - lam[j - 1] <= ctol) continue;  // not the first of its cluster
-    int end = j;
-    while (end + 1 < n && lam[end + 1] - lam[end] <= ctol) ++end;
+    int lead = j;  // the first member of j's cluster
+    while (lead > 0 && lam[lead] - lam[lead - 1] <= ctol) --lead;
     float lprev = -3.0e38f;
-    for (int mbr = j; mbr <= end; ++mbr) {
-      float lm = lam[mbr];
-      if (mbr > j && lm - lprev < sep) lm = lprev + sep;
-      lprev = lm;
+    for (int m2 = lead; m2 <= j; ++m2) {
+      float l2 = lam[m2];
+      if (m2 > lead && l2 - lprev < sep) l2 = lprev + sep;
+      lprev = l2;
+    }
+    {
+      const int mbr = j;
+      const float lm = lprev;
       // T - lm I = P L U (partial pivoting); column j of the factor arrays
       float ra = ds[0] - lm, rb = n > 1 ? es[0] : 0.0f, rc = 0.0f;
       for (int i = 0; i < n - 1; ++i) {
@@ -1038,16 +1043,9 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
             }
           }
         }
-        // scale, orthogonalise against the cluster's earlier vectors, normalise
+        // scale, normalise
         const float sc = amax > 0.0f ? 1.0f / amax : 1.0f;
         for (int i = 0; i < n; ++i) X[(long long)i * n + mbr] *= sc;
-        for (int o = j; o < mbr; ++o) {
-          float dot = 0.0f;
-          for (int i = 0; i < n; ++i)
-            dot = fmaf(X[(long long)i * n + o], X[(long long)i * n + mbr], dot);
-          for (int i = 0; i < n; ++i)
-            X[(long long)i * n + mbr] = fmaf(-dot, X[(long long)i * n + o], X[(long long)i * n + mbr]);
-        }
         float ss = 0.0f;
         for (int i = 0; i < n; ++i) {
           const float xi = X[(long long)i * n + mbr];
@@ -1056,6 +1054,32 @@ __global__ void __launch_bounds__(kThreads) tri_eig_kernel(int n, double* __rest
         const float inv = ss > 0.0f ? rsqrtf(ss) : 0.0f;
         for (int i = 0; i < n; ++i) X[(long long)i * n + mbr] *= inv;
       }
+    }
+  }
+  __syncthreads();
+  // modified Gram-Schmidt inside each cluster, by its first thread in member
+  // order (the vectors of a cluster span its invariant subspace to FP32
+  // accuracy; the FP64 refinement and its Rayleigh-Ritz pass resolve the
+  // pairs inside it)
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    if (j > 0 && lam[j] - lam[j - 1] <= ctol) continue;
+    int end = j;
+    while (end + 1 < n && lam[end + 1] - lam[end] <= ctol) ++end;
+    for (int mbr = j + 1; mbr <= end; ++mbr) {
+      for (int o = j; o < mbr; ++o) {
+        float dot = 0.0f;
+        for (int i = 0; i < n; ++i)
+          dot = fmaf(X[(long long)i * n + o], X[(long long)i * n + mbr], dot);
+        for (int i = 0; i < n; ++i)
+          X[(long long)i * n + mbr] = fmaf(-dot, X[(long long)i * n + o], X[(long long)i * n + mbr]);
+      }
+      float ss = 0.0f;
+      for (int i = 0; i < n; ++i) {
+        const float xi = X[(long long)i * n + mbr];
+        ss = fmaf(xi, xi, ss);
+      }
+      const float inv = ss > 0.0f ? rsqrtf(ss) : 0.0f;
+      for (int i = 0; i < n; ++i) X[(long long)i * n + mbr] *= inv;
     }
   }
   if (kSmemX) {
