@@ -147,6 +147,8 @@ class ScfServer:
 
     def _ensure3d(self, key):
         """Make the molecule of a 3D request resident (build + capture) if needed."""
+        while self._building is not None:  # finish a set-up in progress first
+            self._advance_build()
         if key in self.graphs3d:
             return
         self._start_build(key)
@@ -173,6 +175,9 @@ class ScfServer:
             self.resident += g.nbytes
             self.built3d += 1
             self._building = None
+        except BaseException:
+            self._building = None  # a failed set-up leaves nothing half-built behind
+            raise
 
     def _bytes_for(self, batch: PackedBatch, opts) -> int:
         nb = ctypes.c_size_t()

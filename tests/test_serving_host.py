@@ -108,3 +108,47 @@ def test_plan_tuner_key_is_the_shape_histogram():
     assert PlanTuner.key(a, 3, dataclasses.replace(cfg, stencil=3)) != ka
     c = B([513, 257, 513], [M(4), M(3), M(2)])  # one molecule moves to K = 3
     assert PlanTuner.key(c, 3, cfg) != ka
+
+
+def test_staged_molecule_setup_state_machine():
+    """A new 3D molecule's set-up advances one stage per call; the molecule
+    becomes resident after the last stage, and a stage that fails leaves no
+    half-built molecule behind (host logic only, no GPU)."""
+    import pytest
+
+    from qex_gb300.serving import ScfServer
+
+    srv = ScfServer.__new__(ScfServer)
+    srv.graphs3d, srv.resident, srv.built3d, srv._building = {}, 0, 0, None
+
+    class Graph:
+        nbytes = 10
+
+    done = []
+
+    def stages():
+        done.append(1)
+        yield
+        done.append(2)
+        yield
+        done.append(3)
+
+    g = Graph()
+    srv._building = ("a", g, stages())
+    srv._advance_build()
+    assert srv._building is not None and done == [1]
+    srv._advance_build()
+    assert done == [1, 2] and "a" not in srv.graphs3d
+    srv._advance_build()
+    assert srv._building is None and srv.graphs3d == {"a": g}
+    assert srv.resident == 10 and srv.built3d == 1
+
+    def failing():
+        yield
+        raise RuntimeError("out of device memory")
+
+    srv._building = ("b", Graph(), failing())
+    srv._advance_build()
+    with pytest.raises(RuntimeError):
+        srv._advance_build()
+    assert srv._building is None and "b" not in srv.graphs3d and srv.built3d == 1
