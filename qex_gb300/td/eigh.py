@@ -28,7 +28,7 @@ def generalized_eigh(A, B, *, eps: float = 1.0e-12, return_status: bool = False)
     batch, n, _ = A.shape
     w = torch.empty((batch, n), dtype=torch.float64, device="cuda")
     V = torch.empty((batch, n, n), dtype=torch.float64, device="cuda")
-    st = torch.zeros(batch, dtype=torch.int32, device="cuda")
+    st = torch.empty(batch, dtype=torch.int32, device="cuda")  # every entry written by the solver
     ws = torch.empty(L.qex_td_gen_eigh_workspace_size(batch, n), dtype=torch.uint8, device="cuda")
     N.check(L.qex_td_gen_eigh(batch, n, _lib.p(A), _lib.p(B), _lib.p(w), _lib.p(V), _lib.p(st),
                               _lib.p(ws), ws.numel(), _lib.stream()), "qex_td_gen_eigh")
