@@ -681,6 +681,55 @@ def run_eigh_eval(args):
     return {"workload": "generalized eigensolve, core Hamiltonian and overlap", **out}
 
 
+# phase timers of ks1d_kernel (clock64 cycles per molecule; write_stats)
+# (3 contains 8-10, 4 contains 11-13 and 15, 5 contains 14)
+PHASES = {0: "Hartree on the input density", 1: "XC on the input density (network forward "
+          "and backward) and v_KS", 2: "Sturm multisection", 3: "cold route: start vectors "
+          "and inverse iteration", 4: "FP64 refinement, Rayleigh-Ritz, normalisation",
+          5: "density, Hartree and XC energies on the output density", 6: "mixing and "
+          "outputs", 7: "whole molecule", 8: "start vectors", 9: "first factorisation and "
+          "solve", 10: "inverse-iteration rounds", 11: "Rayleigh quotients",
+          12: "FP32 correction solves", 13: "vector updates",
+          14: "XC energy on the output density (network forward)", 15: "final normalisation"}
+
+
+def run_phase_eval(args):
+    """The batched configuration (the headline's molecules, MLP, iterations and
+    launch plan) with the kernel's per-phase clock64 timers: each phase's
+    share of the summed per-molecule cycles (phase 7), and the step time."""
+    import torch
+
+    from qex_gb300 import Partial
+    from qex_gb300.od import engine as eng
+
+    mols = workload(args.batch, args.seed)
+    params, xc_fn = mlp_params(0)
+    xc = Partial(xc_fn, params=params)
+    cfg = eng.SolveConfig(num_iterations=args.iters, alpha=0.5, alpha_decay=0.9,
+                          num_mixing_iterations=1, convention="local", stencil=5)
+    engine = eng.Ks1dEngine(autotune=True)
+    batch = eng.PackedBatch(mols)
+    out = engine.allocate_outputs(batch, cfg, ("energy",))
+    for _ in range(max(args.warmup, 1)):
+        engine.solve(batch, xc, cfg, out=out)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(max(args.steps, 1)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        engine.solve(batch, xc, cfg, out=out)
+        e1.record()
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    pc = out["phase_cycles"].cpu().numpy().astype(np.float64)
+    total = pc[:, 7].sum()
+    return {"workload": f"{args.batch} molecules, window-17 MLP, {args.iters} iterations, "
+                        f"5-point kinetic (the headline configuration)",
+            "ms_per_step": float(np.median(ts)),
+            "share_of_molecule_cycles": {f"{k} {PHASES[k]}": round(float(pc[:, k].sum() / total), 4)
+                                         for k in range(16)}}
+
+
 def run_ints_eval(args):
     """Analytic one-electron integrals and density-fitting factors (int3c2e,
     int2c2e, Cholesky, substitution) for seeded synthetic molecules of 8 and
@@ -1093,6 +1142,8 @@ def main():
                     help="restrict --eigh-eval to the molecules of these atom counts")
     ap.add_argument("--eigh-eval", action="store_true",
                     help="time the 3D generalized eigensolver at the configuration's basis sizes")
+    ap.add_argument("--phase-eval", action="store_true",
+                    help="the batched 1D step's time by phase (the kernel's clock64 timers)")
     ap.add_argument("--probe", action="store_true",
                     help="measure the FP64/FP32 FMA and FP64 tensor-core (DMMA) throughput")
     ap.add_argument("--ints-eval", action="store_true",
@@ -1143,6 +1194,12 @@ def main():
 
         _native.load()
         print(json.dumps({"eigh_eval": run_eigh_eval(args)}), flush=True)
+        return
+    if args.phase_eval:
+        from qex_gb300 import _native
+
+        _native.load()
+        print(json.dumps({"phase_eval": run_phase_eval(args)}), flush=True)
         return
     if args.ints_eval:
         from qex_gb300 import _native
